@@ -1,0 +1,174 @@
+/*
+ * rc_api.h -- C ABI of the GB300 radiance-cache frame loop.
+ *
+ * The reference (falcon123212/render_engine, bench B) is a single CUDA program,
+ * cuda/poc_gpu.cu, with no library boundary: its "operators" are the structs DevState /
+ * Cache / Params handed by value to the kernels (poc_gpu.cu:222-237, 394-422), the
+ * scene loader load() (poc_gpu.cu:751-801), the frame driver Runner::run
+ * (poc_gpu.cu:809-1017) and the method record Method (poc_gpu.cu:803-805).  Each entry
+ * point below names the piece of that program it replaces.  Plain C types only: no CUDA
+ * or torch types appear in a signature (a stream is passed as void*).
+ *
+ * Conventions
+ *  - Every call returns RC_OK or an error status and never exits the process; the
+ *    reference exits on any error (CK macro, poc_gpu.cu:44-45).  rc_last_error() gives
+ *    the message of the last failing call on a context.
+ *  - The context owns every device buffer.  One context is used by one host thread at a
+ *    time.  Work is issued on the context's stream; calls that return data to the host
+ *    synchronise that stream.
+ *  - There is no CPU fallback: rc_create fails with RC_ERR_CUDA when no usable GPU is
+ *    present.
+ */
+#ifndef RC_API_H
+#define RC_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RC_ABI_VERSION 1
+
+typedef struct rc_ctx rc_ctx;
+
+typedef enum rc_status {
+    RC_OK = 0,
+    RC_ERR_ARG = 1,         /* bad argument (null pointer, index out of range, ...) */
+    RC_ERR_IO = 2,          /* file cannot be read */
+    RC_ERR_FORMAT = 3,      /* scene file malformed or truncated */
+    RC_ERR_CUDA = 4,        /* CUDA runtime error (message in rc_last_error) */
+    RC_ERR_NOMEM = 5,       /* device or host allocation failed */
+    RC_ERR_STATE = 6,       /* call out of order (no scene, no run begun, ...) */
+    RC_ERR_DEVICE = 7,      /* a device-side bound check or iteration limit tripped */
+    RC_ERR_UNSUPPORTED = 8, /* configuration outside what this build supports */
+    RC_ERR_LIGHTS = 9       /* scene light count differs from the expected count */
+} rc_status;
+
+/* Context configuration.  Zero-initialised fields take the defaults noted. */
+typedef struct rc_config {
+    int grid[3];        /* transit voxel grid VX,VY,VZ (product a multiple of 128);
+                           default 8,4,4 = the -DGX=8 -DGY=4 -DGZ=4 of cuda/build.sh:12 */
+    int device;         /* CUDA device ordinal (default 0) */
+    void* stream;       /* cudaStream_t to issue on; NULL = the context creates its own */
+    unsigned flags;     /* RC_FLAG_* */
+    int expect_lights;  /* >0: scenes must have exactly this many lights, as the reference
+                           binaries compiled with -DNLIGHTS=3/8 require (poc_gpu.cu:755) */
+} rc_config;
+
+#define RC_FLAG_BRUTE_FORCE 1u  /* test every dynamic triangle (no plane culling) */
+#define RC_FLAG_CHECK_TRACE 2u  /* trace both ways and count disagreements (slow; tests) */
+
+/* Reference Method (poc_gpu.cu:803-805) plus the BENCH_RAYONS multiplier (poc_gpu.cu:69). */
+typedef struct rc_method {
+    int mode;           /* 0 fixed budget, 1 adaptive allocation */
+    float nmax;
+    float budget;
+    int deps, verify, oracle, track_every, rescale, resp_mask;
+    float nmax_resp;
+    int ddgi;
+    float ddgi_h, ddgi_thr;
+    int ddgi_clamp;
+    int memory, ramp, wake_verify, snaps, proj, snap_verify;
+    float rays;         /* rays per point and frame (BENCH_RAYONS, default 1) */
+} rc_method;
+
+/* Reference Timers (poc_gpu.cu:807): milliseconds summed over frames / events. */
+typedef struct rc_timers {
+    double trace, decide, update, swap, event;
+    int frames, events;
+} rc_timers;
+
+typedef struct rc_scene_info {
+    int np, nq, nt, ns, nl, nr, has_ref, fmt, nw, nst, nnodes, hsize;
+    double scene_bytes;  /* device bytes held by the scene */
+    double cache_bytes;  /* device bytes held by the cache buffers */
+} rc_scene_info;
+
+typedef struct rc_device_info {
+    char name[256];
+    int sm_count, cc_major, cc_minor;
+    double mem_used_mb, mem_total_mb;
+} rc_device_info;
+
+/* Per-ray record of rc_probe_rays. */
+typedef struct rc_ray_rec {
+    int point, ray;
+    int q;       /* quad id (>=0), -2-j for static triangle j, -1 no hit */
+    int pi;      /* cache point of the hit (the tracing point when the hit does not count) */
+    int back;    /* 1 when the hit does not count (no hit, back face, cell absent) */
+    float t;     /* hit distance (+inf when no hit) */
+} rc_ray_rec;
+
+/* Arrays of the run state (rc_array_*).  Layouts follow the reference Cache
+ * (poc_gpu.cu:394-409): per-light arrays are point-major NL floats per point; masks are
+ * word-major (word w of point i at w*Np+i). */
+enum {
+    RC_A_LC = 0, RC_A_LC2, RC_A_M, RC_A_N, RC_A_C0, RC_A_KK, RC_A_PENDING, RC_A_CUR, RC_A_PREV,
+    RC_A_STALE, RC_A_AGE, RC_A_SNAP, RC_A_NEQ, RC_A_COEF, RC_A_RSTAT, RC_A_DSTAT, RC_A_SUMPR,
+    RC_A_NPEND, RC_A_COUNT
+};
+/* Host scalars of the run (rc_scalar_*): Runner::run locals, poc_gpu.cu:839-850. */
+enum { RC_S_PEND_LEFT = 0, RC_S_DORMANT, RC_S_PROJ_LEFT, RC_S_FRAME, RC_S_NSLOTS, RC_S_LAST_EVENT, RC_S_PROJK, RC_S_COUNT };
+/* Per-state scene arrays (rc_state_array_copy): the k_build outputs and the references. */
+enum { RC_SA_EDIR = 0, RC_SA_SV, RC_SA_REF, RC_SA_VALID, RC_SA_PW };
+
+int rc_abi_version(void);
+const char* rc_status_string(rc_status s);
+
+/* Create / destroy a context (replaces the process-level setup of main(),
+ * poc_gpu.cu:1286-1313).  Fails with RC_ERR_CUDA when no GPU is usable. */
+rc_status rc_create(const rc_config* cfg, rc_ctx** out);
+void rc_destroy(rc_ctx* ctx);
+const char* rc_last_error(const rc_ctx* ctx);
+/* GPU name and memory in use (the reference prints the name and cudaMemGetInfo deltas,
+ * poc_gpu.cu:42, 1315-1323). */
+rc_status rc_device_info_get(rc_ctx* ctx, rc_device_info* out);
+
+/* Load a scene, formats 2 and 3, and build every state's direct light and shadow-voxel
+ * masks on the GPU.  Replaces load() + k_build (poc_gpu.cu:751-801, 369-391).  The memory
+ * variant takes the same bytes from a host buffer. */
+rc_status rc_scene_load(rc_ctx* ctx, const char* path);
+rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes);
+rc_status rc_scene_info_get(const rc_ctx* ctx, rc_scene_info* out);
+/* Light intensities of a state (the per-state `in` block of the scene file, poc_gpu.cu:774). */
+rc_status rc_state_lights(const rc_ctx* ctx, int state, float* inten, int nl);
+
+/* Start a run: warm start and cache reset of Runner::run (poc_gpu.cu:826-850). */
+rc_status rc_run_begin(rc_ctx* ctx, const rc_method* m, int first_state, uint32_t seed);
+/* One frame in `state`: event handling when the state changed, then the frame kernels
+ * (poc_gpu.cu:851-1011).  Asynchronous unless the method's projection solve falls on this
+ * frame.  With want_err and a scene with references, the frame's error is recorded. */
+rc_status rc_frame(rc_ctx* ctx, int state, int want_err);
+/* Errors recorded so far in this run (synchronises). */
+rc_status rc_errors(rc_ctx* ctx, float* out, int max, int* n);
+/* Whole run over a state sequence (Runner::run, poc_gpu.cu:826-1016).  errs may be NULL;
+ * when tm is given each frame is timed with events like the reference's timing mode
+ * (one synchronisation per frame). */
+rc_status rc_run(rc_ctx* ctx, const rc_method* m, const int* seq, int nframes, uint32_t seed,
+                 int want_err, float* errs, rc_timers* tm);
+rc_status rc_sync(rc_ctx* ctx);
+
+/* Run-state access for parity harnesses: size and device pointer of an array, and a copy
+ * between the array and a host buffer of exactly `nbytes` (to_device=0: device to host,
+ * to_device=1: host to device).  Arrays use the reference layouts listed above. */
+rc_status rc_array_info(rc_ctx* ctx, int which, size_t* nbytes, void** dev_ptr);
+rc_status rc_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, int to_device);
+rc_status rc_scalar_get(rc_ctx* ctx, int which, int* value);
+rc_status rc_scalar_set(rc_ctx* ctx, int which, int value);
+rc_status rc_state_array_copy(rc_ctx* ctx, int state, int which, void* host, size_t nbytes);
+
+/* Trace the rays that the next frame would trace for the listed points, without changing
+ * the run, and return one record per ray. */
+rc_status rc_probe_rays(rc_ctx* ctx, int state, const int* points, int npoints,
+                        rc_ray_rec* out, int maxrec, int* nrec);
+/* Disagreements counted by RC_FLAG_CHECK_TRACE since the last call (then reset). */
+rc_status rc_trace_check_count(rc_ctx* ctx, long long* mismatches, long long* rays);
+/* Device-side guard flags raised since the last call (then reset); 0 = none. */
+rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RC_API_H */

@@ -1,0 +1,171 @@
+"""ctypes front end of the CPU oracle (oracle/rc_oracle.c) — TEST INFRASTRUCTURE ONLY.
+
+Used by the test suite, the smoke check and the CPU-baseline leg of the benchmark as the
+checker.  It is never imported by the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+SRC = os.path.join(HERE, "rc_oracle.c")
+
+A_LC, A_LC2, A_M, A_N, A_C0, A_KK, A_PENDING, A_CUR, A_PREV, A_STALE, A_AGE, A_SNAP, A_NEQ, A_COEF, \
+    A_RSTAT, A_DSTAT, A_SUMPR, A_NPEND = range(18)
+_DT = {A_LC: np.float32, A_LC2: np.float32, A_M: np.float32, A_N: np.float32, A_C0: np.float32,
+       A_KK: np.int32, A_PENDING: np.uint8, A_CUR: np.uint32, A_PREV: np.uint32, A_STALE: np.uint32,
+       A_AGE: np.float32, A_SNAP: np.float32, A_NEQ: np.float32, A_COEF: np.float32, A_RSTAT: np.float32,
+       A_DSTAT: np.float32, A_SUMPR: np.float32, A_NPEND: np.int32}
+
+
+class RayRec(ctypes.Structure):
+    _fields_ = [("point", ctypes.c_int), ("ray", ctypes.c_int), ("q", ctypes.c_int), ("pi", ctypes.c_int),
+                ("back", ctypes.c_int), ("t", ctypes.c_float)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (-O3, OpenMP, no FP contraction so x86 and Arm agree)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "rc_oracle.h"))):
+        tmp = LIB + ".%d.tmp" % os.getpid()
+        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+                               SRC, "-o", tmp, "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.osc_load_file.restype = ctypes.c_void_p
+        L.osc_load_file.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+        L.osc_load_mem.restype = ctypes.c_void_p
+        L.osc_load_mem.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+        L.osc_free.argtypes = [ctypes.c_void_p]
+        L.osc_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.osc_build.argtypes = [ctypes.c_void_p]
+        L.osc_state_array.restype = ctypes.c_void_p
+        L.osc_state_array.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+        L.osc_event_list.restype = ctypes.POINTER(ctypes.c_int)
+        L.osc_event_list.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.osc_run_new.restype = ctypes.c_void_p
+        L.osc_run_new.argtypes = [ctypes.c_void_p]
+        L.osc_run_free.argtypes = [ctypes.c_void_p]
+        L.osc_run_begin.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32]
+        L.osc_frame.restype = ctypes.c_int
+        L.osc_frame.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float)]
+        L.osc_run_array.restype = ctypes.c_void_p
+        L.osc_run_array.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+        L.osc_run_scalar.restype = ctypes.c_int
+        L.osc_run_scalar.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.osc_set_threads.argtypes = [ctypes.c_int]
+        L.osc_probe_rays.restype = ctypes.c_int
+        L.osc_probe_rays.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                     ctypes.POINTER(RayRec), ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    lib().osc_set_threads(int(n))
+
+
+class Scene:
+    def __init__(self, path: str | None = None, data: bytes | None = None, grid=(8, 4, 4)):
+        L = lib()
+        err = ctypes.create_string_buffer(256)
+        if data is not None:
+            self._buf = ctypes.create_string_buffer(data, len(data))
+            p = L.osc_load_mem(self._buf, len(data), grid[0], grid[1], grid[2], err, 256)
+        else:
+            p = L.osc_load_file(path.encode(), grid[0], grid[1], grid[2], err, 256)
+        if not p:
+            raise ValueError("oracle: " + err.value.decode())
+        self.p = p
+        info = (ctypes.c_int * 10)()
+        L.osc_info(p, info)
+        (self.Np, self.Nq, self.Nt, self.NS, self.NL, self.NR, self.has_ref, self.fmt, self.NW, self.nst) = list(info)
+        self.grid = tuple(grid)
+        self.built = False
+
+    def build(self):
+        lib().osc_build(self.p)
+        self.built = True
+
+    def state_array(self, state: int, which: int) -> np.ndarray:
+        nb = ctypes.c_size_t()
+        ptr = lib().osc_state_array(self.p, state, which, ctypes.byref(nb))
+        dt = {0: np.float32, 1: np.uint32, 2: np.float32, 3: np.uint8, 4: np.float32}[which]
+        if not ptr or nb.value == 0:
+            return np.zeros(0, dt)
+        return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)), (nb.value,)).view(dt).copy()
+
+    def event_list(self, pair: int, kind: int) -> np.ndarray:
+        n = ctypes.c_int()
+        ptr = lib().osc_event_list(self.p, pair, kind, ctypes.byref(n))
+        return np.array([ptr[i] for i in range(n.value)], np.int32)
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            lib().osc_free(self.p)
+            self.p = None
+
+
+class Run:
+    def __init__(self, scene: Scene):
+        if not scene.built:
+            scene.build()
+        self.scene = scene
+        self.p = lib().osc_run_new(scene.p)
+
+    def begin(self, method, s0: int, seed: int):
+        from render_engine_gb300.methods import to_c
+        self._cm = to_c(method)
+        lib().osc_run_begin(self.p, ctypes.byref(self._cm), s0, seed & 0xFFFFFFFF)
+
+    def frame(self, state: int, want_err: bool = False):
+        e3 = (ctypes.c_double * 3)()
+        ev = ctypes.c_float()
+        have = lib().osc_frame(self.p, state, 1 if want_err else 0, e3, ctypes.byref(ev))
+        if have < 0:
+            raise ValueError("bad state")
+        return (float(ev.value), tuple(e3)) if have else (None, None)
+
+    def run(self, method, seq, seed, want_err=True):
+        self.begin(method, seq[0], seed)
+        errs = []
+        for s in seq:
+            e, _ = self.frame(s, want_err)
+            if e is not None:
+                errs.append(e)
+        return errs
+
+    def array(self, which: int) -> np.ndarray:
+        nb = ctypes.c_size_t()
+        ptr = lib().osc_run_array(self.p, which, ctypes.byref(nb))
+        return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)), (nb.value,)).view(_DT[which])
+
+    def scalar(self, which: int) -> int:
+        return lib().osc_run_scalar(self.p, which)
+
+    def probe(self, state: int, points) -> list[tuple]:
+        pts = (ctypes.c_int * len(points))(*[int(x) for x in points])
+        cap = 64 * len(points) + 64
+        out = (RayRec * cap)()
+        n = lib().osc_probe_rays(self.p, state, pts, len(points), out, cap)
+        return [(r.point, r.ray, r.q, r.pi, r.back, r.t) for r in out[:n]]
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            lib().osc_run_free(self.p)
+            self.p = None

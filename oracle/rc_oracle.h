@@ -1,0 +1,85 @@
+/*
+ * CPU oracle for the radiance-cache frame loop — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's bench-B hot path (cuda/poc_gpu.cu of
+ * falcon123212/render_engine): scene loading (formats 2 and 3), the per-state build
+ * of direct light and shadow-voxel masks, the per-frame trace / decide / update
+ * kernels, the event handling of Runner::run and the error metric.  Every function
+ * cites the reference file:line it follows.  Floating-point work is FP32 in the same
+ * operation order as the reference; FP64 only where the reference uses double
+ * (k_error sums, the projection solve).
+ *
+ * Only the test suite, the smoke check and the CPU-baseline leg of the benchmark use
+ * this library.  It is never linked into the product library.
+ */
+#ifndef RC_ORACLE_H
+#define RC_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct osc_scene osc_scene;
+typedef struct osc_run osc_run;
+
+/* Same field list as rc_method in include/rc_api.h (reference Method, poc_gpu.cu:803-805). */
+typedef struct {
+    int mode;          /* 0 = fixed budget, 1 = adaptive allocation */
+    float nmax;        /* history cap in frames (scaled by rays) */
+    float budget;      /* rays per point per frame in mode 0 */
+    int deps;          /* dependency tracking */
+    int verify;        /* occluder events -> verification */
+    int oracle;        /* reference-driven invalidation (upper bound) */
+    int track_every;   /* track dependencies one frame in N */
+    int rescale;       /* per-light storage + linear rescale on intensity change */
+    int resp_mask;     /* SHaRC responsive lights (bit l) */
+    float nmax_resp;
+    int ddgi;
+    float ddgi_h, ddgi_thr;
+    int ddgi_clamp;
+    int memory, ramp, wake_verify, snaps, proj, snap_verify;
+    float rays;        /* BENCH_RAYONS multiplier */
+} osc_method;
+
+/* Load a scene file (formats 2 and 3), transit grid vx*vy*vz (multiple of 128 voxels). */
+osc_scene* osc_load_file(const char* path, int vx, int vy, int vz, char* err, int errlen);
+osc_scene* osc_load_mem(const void* buf, size_t n, int vx, int vy, int vz, char* err, int errlen);
+void osc_free(osc_scene* s);
+/* Np, Nq, Nt, NS, NL, NR, has_ref, fmt, NW, nst */
+void osc_info(const osc_scene* s, int out[10]);
+/* k_build for every state (direct light + static shadow-voxel masks). */
+void osc_build(osc_scene* s);
+/* Host arrays of a state: 0 Edir (float NL*Np), 1 SV (u32 NW*Np), 2 ref, 3 valid, 4 Pw. */
+void* osc_state_array(osc_scene* s, int state, int which, size_t* nbytes);
+/* Transit-grid voxel list of an event (pair e -> s): kind 0 = occluder list, 1.. = light l-1. */
+const int* osc_event_list(const osc_scene* s, int pair, int kind, int* n);
+
+osc_run* osc_run_new(osc_scene* s);
+void osc_run_free(osc_run* r);
+void osc_run_begin(osc_run* r, const osc_method* m, int s0, uint32_t seed);
+/* One frame in state si (events handled when si differs from the previous frame's state).
+ * When want_err and the scene has references, err3 receives the three FP64 sums. */
+int osc_frame(osc_run* r, int si, int want_err, double err3[3], float* err);
+/* Run arrays (see OSC_A_*). */
+void* osc_run_array(osc_run* r, int which, size_t* nbytes);
+/* Scalars: 0 pend_left, 1 dormant, 2 proj_left, 3 frame, 4 nslots, 5 last_event_f, 6 projK */
+int osc_run_scalar(osc_run* r, int which);
+void osc_set_threads(int n);
+
+/* One-frame trace probe: rays of the listed points for (state, seed, frame) with the
+ * current run state, writing per ray {point, ray, q, pi, back, t} records. */
+typedef struct { int point, ray, q, pi, back; float t; } osc_ray_rec;
+int osc_probe_rays(osc_run* r, int si, const int* pts, int npts, osc_ray_rec* out, int maxrec);
+
+enum {
+    OSC_A_LC = 0, OSC_A_LC2, OSC_A_M, OSC_A_N, OSC_A_C0, OSC_A_KK, OSC_A_PENDING, OSC_A_CUR, OSC_A_PREV,
+    OSC_A_STALE, OSC_A_AGE, OSC_A_SNAP, OSC_A_NEQ, OSC_A_COEF, OSC_A_RSTAT, OSC_A_DSTAT, OSC_A_SUMPR,
+    OSC_A_NPEND, OSC_A_COUNT
+};
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,147 @@
+// Device-side building blocks of the radiance-cache frame loop (sm_103a).
+//
+// The arithmetic of every function that decides a hit, a cache point or a voxel bit is
+// written expression by expression like the reference (cuda/poc_gpu.cu of
+// falcon123212/render_engine), so that the GPU results are bit-identical to the
+// reference kernels built with the same compiler: hit primitive ids, cache-point ids,
+// dependency masks and invalidation sets are integer results of that arithmetic.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rc {
+
+constexpr int KSNAP = 6;
+constexpr int NEQ = 28;
+constexpr int BLOCK = 256;          // points per block; also the fixed reduction tree
+constexpr int MAX_GROUPS = 64;      // plane-culling groups per state (64-bit candidate mask)
+constexpr int MAX_EV_OPS = 40;
+
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ f3 xyz(float4 a) { return {a.x, a.y, a.z}; }
+
+// poc_gpu.cu:127-135
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float rnd(uint32_t& s) {
+    s = s * 747796405u + 2891336453u;
+    uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+    w = (w >> 22u) ^ w;
+    return (w >> 8) * (1.0f / 16777216.0f);
+}
+// poc_gpu.cu:260-262, 251-259
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ull; x ^= x >> 27; x *= 0x94d049bb133111ebull; x ^= x >> 31;
+    return x;
+}
+__device__ __forceinline__ int normal_bucket(float nx, float ny, float nz) {
+    float ax = fabsf(nx), ay = fabsf(ny), az = fabsf(nz);
+    if (ax >= ay && ax >= az) return nx > 0.f ? 0 : 1;
+    if (ay >= az) return ny > 0.f ? 2 : 3;
+    return nz > 0.f ? 4 : 5;
+}
+__device__ __forceinline__ unsigned long long cell_key(int cx, int cy, int cz, int b) {
+    unsigned long long k = (unsigned long long)(cx & 0xFFFFF);
+    k = (k << 20) | (unsigned long long)(cy & 0xFFFFF);
+    k = (k << 20) | (unsigned long long)(cz & 0xFFFFF);
+    return ((k << 3) | (unsigned long long)b) + 1ull;
+}
+
+// Transit voxel grid: bounds and resolution (the reference keeps them in __constant__
+// c_lo/c_ext and compile-time VX/VY/VZ, poc_gpu.cu:98-114).
+struct Grid {
+    float lo[3], ext[3];
+    int vx, vy, vz;
+};
+
+// poc_gpu.cu:137-142
+__device__ __forceinline__ int vox_of(const Grid& g, f3 p) {
+    int i = min(max(int((p.x - g.lo[0]) / g.ext[0] * g.vx), 0), g.vx - 1);
+    int j = min(max(int((p.y - g.lo[1]) / g.ext[1] * g.vy), 0), g.vy - 1);
+    int k = min(max(int((p.z - g.lo[2]) / g.ext[2] * g.vz), 0), g.vz - 1);
+    return (k * g.vy + j) * g.vx + i;
+}
+
+template <int NW>
+__device__ __forceinline__ void set_bit(uint32_t (&m)[NW], int v) {
+    const uint32_t bit = 1u << (v & 31);
+    const int w0 = v >> 5;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) m[w] |= (w == w0) ? bit : 0u;
+}
+
+// Amanatides-Woo walk of segment a->b over the transit grid, same float sequence as
+// dda_reg (poc_gpu.cu:171-190).  The loop bound vx+vy+vz is the reference's.
+template <int NW>
+__device__ __forceinline__ void dda_walk(const Grid& g, f3 a, f3 b, uint32_t (&m)[NW]) {
+    const int VX = g.vx, VY = g.vy, VZ = g.vz;
+    const float sx = VX / g.ext[0], sy = VY / g.ext[1], sz = VZ / g.ext[2];
+    float ax = (a.x - g.lo[0]) * sx, ay = (a.y - g.lo[1]) * sy, az = (a.z - g.lo[2]) * sz;
+    float bx = (b.x - g.lo[0]) * sx, by = (b.y - g.lo[1]) * sy, bz = (b.z - g.lo[2]) * sz;
+    int ix = min(max(int(ax), 0), VX - 1), iy = min(max(int(ay), 0), VY - 1), iz = min(max(int(az), 0), VZ - 1);
+    int ex = min(max(int(bx), 0), VX - 1), ey = min(max(int(by), 0), VY - 1), ez = min(max(int(bz), 0), VZ - 1);
+    float dx = bx - ax, dy = by - ay, dz = bz - az;
+    int stx = dx > 0 ? 1 : -1, sty = dy > 0 ? 1 : -1, stz = dz > 0 ? 1 : -1;
+    float tdx = dx != 0 ? fabsf(1.f / dx) : 1e30f, tdy = dy != 0 ? fabsf(1.f / dy) : 1e30f, tdz = dz != 0 ? fabsf(1.f / dz) : 1e30f;
+    float tmx = dx != 0 ? ((dx > 0 ? (ix + 1 - ax) : (ax - ix)) * tdx) : 1e30f;
+    float tmy = dy != 0 ? ((dy > 0 ? (iy + 1 - ay) : (ay - iy)) * tdy) : 1e30f;
+    float tmz = dz != 0 ? ((dz > 0 ? (iz + 1 - az) : (az - iz)) * tdz) : 1e30f;
+    const int steps = VX + VY + VZ;
+    for (int s = 0; s < steps; ++s) {
+        set_bit<NW>(m, (iz * VY + iy) * VX + ix);
+        if (ix == ex && iy == ey && iz == ez) break;
+        if (tmx < tmy && tmx < tmz) { ix += stx; tmx += tdx; if (ix < 0 || ix >= VX) break; }
+        else if (tmy < tmz) { iy += sty; tmy += tdy; if (iy < 0 || iy >= VY) break; }
+        else { iz += stz; tmz += tdz; if (iz < 0 || iz >= VZ) break; }
+    }
+}
+
+// poc_gpu.cu:360-366
+__device__ __forceinline__ f3 cosine_dir(f3 N, float u1, float u2) {
+    float r = sqrtf(u1), phi = 6.28318530718f * u2;
+    f3 a = fabsf(N.x) > 0.9f ? mk(0, 1, 0) : mk(1, 0, 0);
+    f3 T = cross(N, a); T = T * rsqrtf(dot(T, T));
+    f3 B = cross(N, T);
+    return T * (r * cosf(phi)) + B * (r * sinf(phi)) + N * sqrtf(fmaxf(0.f, 1.f - u1));
+}
+
+// ---------------------------------------------------------------------------- triangles
+// Dynamic triangles live in shared memory as 3 float4 each: (v0, quad id bits), (e1, 0), (e2, 0).
+//
+// Möller-Trumbore of one triangle, the reference's expression order (poc_gpu.cu:203-217).
+// Accepts when t is smaller, or equal with a smaller triangle index: over any visiting order
+// this selects what the reference's in-order scan selects.
+__device__ __forceinline__ void mt_tri(const float4* __restrict__ tri, int j, f3 o, f3 d,
+                                       float& tmin, int& q, int& jbest) {
+    const float4 A = tri[3 * j], B = tri[3 * j + 1], C = tri[3 * j + 2];
+    const f3 v0 = xyz(A), e1 = xyz(B), e2 = xyz(C);
+    f3 p = cross(d, e2);
+    float det = dot(e1, p);
+    if (fabsf(det) <= 1e-9f) return;
+    float inv = 1.f / det;
+    f3 tv = o - v0;
+    float u = dot(tv, p) * inv;
+    if (u < 0.f) return;
+    f3 qv = cross(tv, e1);
+    float v = dot(d, qv) * inv;
+    if (v < 0.f || u + v > 1.f) return;
+    float t = dot(e2, qv) * inv;
+    if (t > 1e-4f && (t < tmin || (t == tmin && j < jbest))) { tmin = t; q = __float_as_int(A.w); jbest = j; }
+}
+
+// Plane-culling group: an axis-aligned rectangle made of two triangles of one quad, or a
+// single axis-aligned triangle.  3 float4: (c, lo_a, hi_a, lo_b) (hi_b, ilo_a, ihi_a, ilo_b)
+// (ihi_b, j0 bits, cnt bits, rect bits); the outer box is grown and the inner box shrunk by a
+// margin far above the rounding error of the exact test, so the filter never drops the
+// triangle the exact scan would pick.
+struct GroupRanges { int g0[4]; };  // groups of axis 0 in [g0[0], g0[1]), axis 1 [g0[1], g0[2]), axis 2 [g0[2], g0[3])
+
+}  // namespace rc

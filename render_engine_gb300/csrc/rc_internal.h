@@ -1,0 +1,151 @@
+// Structures shared by the host runtime and the kernels (plain data, passed by value).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rc_device.cuh"
+
+namespace rc {
+
+// Per-state scene data on the device.
+struct DState {
+    const float4* P4;          // point position (xyz, 0)
+    const float4* N4;          // point normal (xyz, 0)
+    const float4* AE;          // gather record per point: A, Edir[0..NL-1], zero padded to AES floats
+    const uint32_t* SV;        // static shadow-voxel mask, NW words per point
+    const float* Q;            // quads: o, u, v, n (12 floats each)
+    const int* dims;           // nu, nv per quad
+    const int* off;            // first point of each quad
+    const float4* tri;         // dynamic triangles, 3 float4 each (v0 + quad id bits, e1, e2)
+    const float4* grp;         // plane-culling groups, 3 float4 each
+    const int* misc;           // dynamic triangles outside any group (always tested exactly)
+    const float* ref;          // converged reference per point (scenes with references)
+    const uint8_t* valid;
+    int nt, ng, nmisc;
+    GroupRanges gr;
+};
+
+// State-independent scene data (format 3 static mesh and spatial hash, per-point albedo/regions).
+struct DStatic {
+    const float* ST;           // static triangles v0, e1, e2
+    const float4* STN;         // geometric normal + flags (w bit 0 = double sided)
+    const float4* BN;          // BVH nodes, 2 float4 each
+    const unsigned long long* HK;
+    const int* HV;
+    const int* region;
+    const float* A;            // albedo per point
+    unsigned hmask;
+    float hcell;
+    int has_bvh;
+    int nnodes;
+    int max_visits;            // traversal guard (4 x nodes)
+};
+
+struct DevCache {
+    float* Lc;                 // LCS floats per point
+    float* Lc2;
+    float* m;                  // LCS floats per point (trace output on split frames)
+    float* n;
+    float* c0;
+    int* kk;
+    uint8_t* pending;
+    uint32_t* cur;             // word-major masks
+    uint32_t* prev;
+    uint32_t* stale;
+    float* age;
+    float* snap;               // KSNAP x Np x LCS
+    float* neq;                // NR x NEQ
+    float* coef;               // NR x KSNAP
+    float* rstat;              // NR x 4
+    float* dstat;              // NR x 3
+    float* sumpr;              // 2 slots
+    int* npend;                // [0] current, [1] accumulator
+    double* err;               // 3 doubles per frame of the run
+    float* partf;              // block partials (float)
+    double* partd;             // block partials (3 doubles per block)
+    int* parti;                // block partials (int)
+    unsigned* ticket;          // last-block counters [4]
+    unsigned* flags;           // device guard flags
+    unsigned long long* check; // [0] trace disagreements, [1] rays checked
+};
+
+enum MaskOp { MASK_NONE = 0, MASK_OR = 1, MASK_FRESH = 2, MASK_ZERO = 3 };
+enum DevFlag { FLAG_BVH_VISITS = 1u, FLAG_BAD_INDEX = 2u };
+
+struct FrameParams {
+    int Np, NR, mode;
+    float budget, nmax;
+    uint32_t seed, frame;
+    int pend_left, dormant, resp_mask;
+    float nmax_resp;
+    int ddgi;
+    float ddgi_h, ddgi_thr;
+    int ddgi_clamp, ramp, proj_left, projK;
+    int slot[KSNAP];
+    float rays;
+    int mask_op;
+    int want_err, err_frame;   // error sums of this frame go to err[3*err_frame]
+    int sum_in, sum_out;       // sumpr slots read / written
+    int decide;                // split update: run the verification decision first
+    int brute, check;          // trace options
+};
+
+// Event program: the per-point kernels of one event of Runner::run, in launch order.
+enum EvKind { EV_SNAP_SAVE = 0, EV_ORACLE, EV_RESCALE, EV_WAKE, EV_TOUCHED, EV_SNAP_RESTORE, EV_RESTORED };
+struct EvOp {
+    int kind;
+    int a;            // slot / light / touched kind / verify
+    int b;            // verify (wake) / list length (touched)
+    int count;        // pending count of this op reaches npend
+    int dormant;      // host dormant mask when the reference launches the op
+    float x;          // rescale ratio
+    const int* list;  // touched voxel list
+    const float* r0;  // oracle: reference before / after
+    const float* r1;
+};
+struct EvProgram {
+    int nops;
+    int npend_mode;   // 0 keep, 1 publish the counted ops, 2 set to zero
+    int zero_rstat, zero_neq;
+    int want_sumpr;   // mode 1: recompute Sum 1/(n+1) into sumpr[sum_slot]
+    int sum_slot;
+    float nmax;       // restored history
+    int Np, NR;
+    EvOp ops[MAX_EV_OPS];
+};
+
+// Launch wrappers (rc_kernels.cu), one instantiation per light count, each compiled in its
+// own translation unit (-DRC_NL_ONE=n) so the build runs in parallel.
+template <int NL>
+struct Ops {
+    static cudaError_t build(int NW, const DState& s, const DStatic& g, const Grid& grid, const float* L, const float* inten,
+                             float4* AE, uint32_t* SV, int Np, unsigned* flags, cudaStream_t st);
+    static cudaError_t frame(int NW, bool deps, bool fused, const DState& s, const DStatic& g, const Grid& grid,
+                             const DevCache& c, const FrameParams& p, cudaStream_t st);
+    static cudaError_t update(const DState& s, const DStatic& g, const DevCache& c, const FrameParams& p, cudaStream_t st);
+    static cudaError_t event(const EvProgram& ev, const DevCache& c, cudaStream_t st);
+    static cudaError_t error(const DState& s, const DevCache& c, const FrameParams& p, cudaStream_t st);
+    static cudaError_t proj_apply(const DevCache& c, const DStatic& g, const FrameParams& p, cudaStream_t st);
+    static cudaError_t probe(int NW, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                             const int* pts, int npts, void* recs, int maxrec, int* nrec, cudaStream_t st);
+};
+// Light counts and mask widths with compiled kernels.
+#define RC_NL_VALUES(X) X(1) X(2) X(3) X(4) X(8) X(16) X(32)
+inline bool supported_nl_nw(int NL, int NW) {
+    bool nl = false;
+#define X(n) nl = nl || NL == n;
+    RC_NL_VALUES(X)
+#undef X
+    return nl && (NW == 4 || NW == 24);
+}
+#define X(n) extern template struct Ops<n>;
+RC_NL_VALUES(X)
+#undef X
+inline size_t frame_smem_bytes(const DState& s) {
+    return sizeof(float4) * (3 * (size_t)s.nt + 3 * (size_t)s.ng) + sizeof(int) * (size_t)s.nmisc + 16;
+}
+__host__ __device__ constexpr int lcs_of(int NL) { return (NL + 3) / 4 * 4; }
+__host__ __device__ constexpr int aes_of(int NL) { return (NL + 1 + 3) / 4 * 4; }
+
+}  // namespace rc

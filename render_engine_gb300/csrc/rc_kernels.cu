@@ -1,0 +1,965 @@
+// Kernels of the radiance-cache frame loop for sm_103a.
+//
+// One thread per cache point, 256 points per block, like the reference's k_trace2 /
+// k_update (cuda/poc_gpu.cu:433-602).  What differs is how the work is organised:
+//  * a frame without verification, projection or DDGI is ONE kernel: trace + blend +
+//    history + Sum 1/(n+1) + error sums, so the per-point rays' result never goes through
+//    HBM (the reference writes kk and m, then k_update reads them back);
+//  * dynamic triangles are culled by a plane filter over axis-aligned rectangles before the
+//    exact Möller-Trumbore test; the exact test runs only on the few rectangles that can
+//    hold the closest hit, so hit ids and distances are those of the reference's full scan;
+//  * per-point gathers at the hit point are 16-byte vectors (albedo + direct light in one
+//    record, the cache padded to 4 lights);
+//  * reductions use a fixed tree (warp butterfly, warps in order, block partials reduced by
+//    the last block) so that runs are reproducible bit for bit;
+//  * an event is one kernel applying the reference's per-point event kernels in order.
+#include <cstdio>
+
+#include "rc_internal.h"
+
+namespace rc {
+
+// ------------------------------------------------------------------ fixed-order reductions
+template <typename T>
+__device__ __forceinline__ T warp_tree(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+// Block partial of one value per thread; the result is valid in thread 0.
+template <typename T>
+__device__ __forceinline__ T block_tree(T v, T* sh) {
+    v = warp_tree(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    T s = T(0);
+    if (threadIdx.x == 0) {
+        s = sh[0];
+#pragma unroll
+        for (int k = 1; k < BLOCK / 32; ++k) s = s + sh[k];
+    }
+    __syncthreads();
+    return s;
+}
+// Second level over G block partials (stride BLOCK per slot, then the block tree).
+template <typename T>
+__device__ __forceinline__ T final_tree(const T* part, int G, int stride, int comp, T* sh) {
+    T x = T(0);
+    const int t = threadIdx.x;
+    if (t < G) x = __ldcg(part + (size_t)t * stride + comp);
+    for (int b = t + BLOCK; b < G; b += BLOCK) x = x + __ldcg(part + (size_t)b * stride + comp);
+    return block_tree(x, sh);
+}
+
+// ------------------------------------------------------------------ tracing
+struct TraceSmem {
+    const float4* tri;
+    const float4* grp;
+    const int* misc;
+};
+
+__device__ __forceinline__ void filter_group(const float4* __restrict__ grp, int g, float ok, float idk, float oa, float da,
+                                             float ob, float db, unsigned long long& mask, float& tcert) {
+    const float4 G0 = grp[3 * g], G1 = grp[3 * g + 1];
+    const float tk = (G0.x - ok) * idk;
+    const float xa = oa + tk * da, xb = ob + tk * db;
+    if (tk > 5e-5f && xa >= G0.y && xa <= G0.z && xb >= G0.w && xb <= G1.x) {
+        mask |= 1ull << g;
+        const float4 G2 = grp[3 * g + 2];
+        if (tk > 2e-4f && xa >= G1.y && xa <= G1.z && xb >= G1.w && xb <= G2.x) tcert = fminf(tcert, tk);
+    }
+}
+
+// Closest dynamic-triangle hit, equal to the reference's in-order scan (poc_gpu.cu:199-220).
+__device__ __forceinline__ void trace_dyn(const TraceSmem& sm, const DState& s, bool brute, f3 o, f3 d, float& tmin, int& q,
+                                          int& jb) {
+    tmin = __int_as_float(0x7f800000);
+    q = -1;
+    jb = 0x7fffffff;
+    if (brute || s.ng == 0) {
+        for (int j = 0; j < s.nt; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
+        return;
+    }
+    for (int k = 0; k < s.nmisc; ++k) mt_tri(sm.tri, sm.misc[k], o, d, tmin, q, jb);
+    float tcert = tmin;
+    unsigned long long mask = 0ull;
+    const float idx = 1.f / d.x, idy = 1.f / d.y, idz = 1.f / d.z;
+    for (int g = s.gr.g0[0]; g < s.gr.g0[1]; ++g) filter_group(sm.grp, g, o.x, idx, o.y, d.y, o.z, d.z, mask, tcert);
+    for (int g = s.gr.g0[1]; g < s.gr.g0[2]; ++g) filter_group(sm.grp, g, o.y, idy, o.x, d.x, o.z, d.z, mask, tcert);
+    for (int g = s.gr.g0[2]; g < s.gr.g0[3]; ++g) filter_group(sm.grp, g, o.z, idz, o.x, d.x, o.y, d.y, mask, tcert);
+    const float thr = tcert * 1.0001f + 1e-5f;
+    while (mask) {
+        const int g = __ffsll((long long)mask) - 1;
+        mask &= mask - 1ull;
+        const float4 G0 = sm.grp[3 * g], G2 = sm.grp[3 * g + 2];
+        const float ok = g < s.gr.g0[1] ? o.x : (g < s.gr.g0[2] ? o.y : o.z);
+        const float idk = g < s.gr.g0[1] ? idx : (g < s.gr.g0[2] ? idy : idz);
+        const float tk = (G0.x - ok) * idk;
+        if (tk <= thr) {
+            const int j0 = __float_as_int(G2.y), cnt = __float_as_int(G2.z);
+            for (int j = j0; j < j0 + cnt; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
+        }
+    }
+}
+
+// poc_gpu.cu:288-295
+__device__ __forceinline__ float aabb_enter(float4 a, float4 b, f3 o, f3 inv, float tmax) {
+    float tx1 = (a.x - o.x) * inv.x, tx2 = (b.x - o.x) * inv.x;
+    float ty1 = (a.y - o.y) * inv.y, ty2 = (b.y - o.y) * inv.y;
+    float tz1 = (a.z - o.z) * inv.z, tz2 = (b.z - o.z) * inv.z;
+    float tn = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fmaxf(fminf(tz1, tz2), 0.f));
+    float tf = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fminf(fmaxf(tz1, tz2), tmax));
+    return tn <= tf ? tn : 1e30f;
+}
+// Static-mesh traversal, the reference's stack algorithm (poc_gpu.cu:297-338), with a visit
+// guard against malformed node links.
+static __device__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int& q, unsigned* flags) {
+    f3 inv = mk(fabsf(d.x) > 1e-12f ? 1.f / d.x : copysignf(1e30f, d.x),
+                fabsf(d.y) > 1e-12f ? 1.f / d.y : copysignf(1e30f, d.y),
+                fabsf(d.z) > 1e-12f ? 1.f / d.z : copysignf(1e30f, d.z));
+    int stack[64];
+    int sp = 0, node = 0, visits = 0;
+    while (true) {
+        if (++visits > g.max_visits) { atomicOr(flags, (unsigned)FLAG_BVH_VISITS); break; }
+        float4 a = __ldg(g.BN + 2 * node), b = __ldg(g.BN + 2 * node + 1);
+        int lf = __float_as_int(a.w), cnt = __float_as_int(b.w);
+        if (cnt > 0) {
+            for (int j = lf; j < lf + cnt; ++j) {
+                const float* T = g.ST + 9 * (size_t)j;
+                f3 v0 = mk(__ldg(T), __ldg(T + 1), __ldg(T + 2));
+                f3 e1 = mk(__ldg(T + 3), __ldg(T + 4), __ldg(T + 5));
+                f3 e2 = mk(__ldg(T + 6), __ldg(T + 7), __ldg(T + 8));
+                f3 p = cross(d, e2);
+                float det = dot(e1, p);
+                if (fabsf(det) <= 1e-12f) continue;
+                float iv = 1.f / det;
+                f3 tv = o - v0;
+                float u = dot(tv, p) * iv;
+                if (u < 0.f || u > 1.f) continue;
+                f3 qv = cross(tv, e1);
+                float v = dot(d, qv) * iv;
+                if (v < 0.f || u + v > 1.f) continue;
+                float t = dot(e2, qv) * iv;
+                if (t > 1e-4f && t < tmin) { tmin = t; q = -2 - j; }
+            }
+        } else {
+            float4 la = __ldg(g.BN + 2 * lf), lb = __ldg(g.BN + 2 * lf + 1);
+            float4 ra = __ldg(g.BN + 2 * lf + 2), rb = __ldg(g.BN + 2 * lf + 3);
+            float tl = aabb_enter(la, lb, o, inv, tmin), tr = aabb_enter(ra, rb, o, inv, tmin);
+            int first = lf, second = lf + 1;
+            if (tr < tl) { float x = tl; tl = tr; tr = x; first = lf + 1; second = lf; }
+            if (tl < 1e30f) {
+                if (tr < 1e30f && sp < 64) stack[sp++] = second;
+                node = first;
+                continue;
+            }
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+}
+
+// poc_gpu.cu:239-246
+__device__ __forceinline__ int point_index(const DState& s, f3 H, int q) {
+    const float* Q = s.Q + 12 * q;
+    f3 o = mk(__ldg(Q), __ldg(Q + 1), __ldg(Q + 2)), u = mk(__ldg(Q + 3), __ldg(Q + 4), __ldg(Q + 5));
+    f3 v = mk(__ldg(Q + 6), __ldg(Q + 7), __ldg(Q + 8));
+    f3 dd = H - o;
+    float a = dot(dd, u) / dot(u, u), b = dot(dd, v) / dot(v, v);
+    int nu = __ldg(s.dims + 2 * q), nv = __ldg(s.dims + 2 * q + 1);
+    int iu = min(max(int(a * nu), 0), nu - 1), iv = min(max(int(b * nv), 0), nv - 1);
+    return __ldg(s.off + q) + iv * nu + iu;
+}
+// poc_gpu.cu:263-287
+__device__ __forceinline__ int hash_find(const DStatic& g, unsigned long long key) {
+    unsigned h = (unsigned)mix64(key) & g.hmask;
+    for (int probe = 0; probe < 64; ++probe) {
+        unsigned long long k = __ldg(g.HK + h);
+        if (k == key) return __ldg(g.HV + h);
+        if (k == 0ull) return -1;
+        h = (h + 1) & g.hmask;
+    }
+    return -1;
+}
+static __device__ int hash_point(const DStatic& g, const Grid& grid, f3 H, f3 n) {
+    int b = normal_bucket(n.x, n.y, n.z);
+    float ih = 1.f / g.hcell;
+    int cx = (int)floorf((H.x - grid.lo[0]) * ih), cy = (int)floorf((H.y - grid.lo[1]) * ih), cz = (int)floorf((H.z - grid.lo[2]) * ih);
+    int p = hash_find(g, cell_key(cx, cy, cz, b));
+    if (p >= 0) return p;
+    for (int dd = 0; dd < 27; ++dd) {
+        int dz = dd / 9 - 1, dy = (dd / 3) % 3 - 1, dx = dd % 3 - 1;
+        if (dx == 0 && dy == 0 && dz == 0) continue;
+        p = hash_find(g, cell_key(cx + dx, cy + dy, cz + dz, b));
+        if (p >= 0) return p;
+    }
+    return -1;
+}
+
+struct Hit {
+    float t;
+    int q;
+    int pi;
+    bool back;
+    f3 H;
+};
+
+// Trace one ray and resolve its cache point (poc_gpu.cu:340-358, 466-469).
+__device__ __forceinline__ Hit trace_resolve(const TraceSmem& sm, const DState& s, const DStatic& g, const Grid& grid,
+                                             const FrameParams& p, const DevCache& c, f3 O, f3 D, int i) {
+    Hit h;
+    int jb;
+    trace_dyn(sm, s, p.brute != 0, O, D, h.t, h.q, jb);
+    if (p.check) {
+        float tb; int qb, jbb;
+        trace_dyn(sm, s, true, O, D, tb, qb, jbb);
+        atomicAdd(c.check + 1, 1ull);
+        if (qb != h.q || __float_as_int(tb) != __float_as_int(h.t)) atomicAdd(c.check, 1ull);
+    }
+    if (g.has_bvh) trace_bvh(g, O, D, h.t, h.q, c.flags);
+    const bool hit = h.q != -1;
+    h.H = hit ? O + D * h.t : O;
+    if (!hit) { h.pi = i; h.back = true; return h; }
+    if (h.q >= 0) {
+        h.pi = point_index(s, h.H, h.q);
+        const float* Q = s.Q + 12 * h.q;
+        h.back = dot(mk(__ldg(Q + 9), __ldg(Q + 10), __ldg(Q + 11)), D) > 0.f;
+        return h;
+    }
+    float4 n4 = __ldg(g.STN + (-2 - h.q));
+    f3 n = mk(n4.x, n4.y, n4.z);
+    if (dot(n, D) > 0.f) {
+        if (!(__float_as_int(n4.w) & 1)) { h.pi = i; h.back = true; return h; }
+        n = n * -1.f;
+    }
+    h.pi = hash_point(g, grid, h.H, n);
+    h.back = false;
+    if (h.pi < 0) { h.pi = i; h.back = true; }
+    return h;
+}
+
+__device__ __forceinline__ void stage_smem(float4* sm, const DState& s) {
+    float4* st = sm;
+    float4* sg = sm + 3 * s.nt;
+    int* smi = (int*)(sg + 3 * s.ng);
+    for (int j = threadIdx.x; j < 3 * s.nt; j += blockDim.x) st[j] = s.tri[j];
+    for (int j = threadIdx.x; j < 3 * s.ng; j += blockDim.x) sg[j] = s.grp[j];
+    for (int j = threadIdx.x; j < s.nmisc; j += blockDim.x) smi[j] = s.misc[j];
+}
+__device__ __forceinline__ TraceSmem smem_view(float4* sm, const DState& s) {
+    TraceSmem t;
+    t.tri = sm;
+    t.grp = sm + 3 * s.nt;
+    t.misc = (const int*)(sm + 3 * s.nt + 3 * s.ng);
+    return t;
+}
+
+template <int N>
+__device__ __forceinline__ float comp(const float4 (&v)[N], int k) {
+    const float4 x = v[k >> 2];
+    const int r = k & 3;
+    return r == 0 ? x.x : (r == 1 ? x.y : (r == 2 ? x.z : x.w));
+}
+
+// Ray count of a point this frame (poc_gpu.cu:442-454).
+__device__ __forceinline__ int ray_count(const FrameParams& p, const DevCache& c, float n_i, bool pend, float sumpr_cur,
+                                         int npend_cur, uint32_t& rs) {
+    if (p.mode == 0) {
+        float kb = floorf(p.budget);
+        return int(kb) + (rnd(rs) < p.budget - kb ? 1 : 0);
+    }
+    float pr = 1.f / (n_i + 1.f);
+    float rrest = float(p.Np - npend_cur);
+    float e = rrest * (0.5f / p.Np + 0.5f * pr / sumpr_cur) * p.rays;
+    float eb = floorf(e);
+    return (pend ? 1 : 0) + int(eb) + (rnd(rs) < e - eb ? 1 : 0);
+}
+
+// ------------------------------------------------------------------ state build
+// poc_gpu.cu:369-391: per point and light, a shadow ray gives the direct light; 20 samples
+// along each shadow segment give the static voxel mask.
+template <int NL, int NW>
+__global__ void __launch_bounds__(BLOCK) k_build(const DState s, const DStatic g, const Grid grid, const float* __restrict__ L,
+                                                 const float* __restrict__ inten, float4* __restrict__ AE,
+                                                 uint32_t* __restrict__ SV, int Np, unsigned* flags) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= Np) return;
+    constexpr int AES = aes_of(NL);
+    const float4 P4 = s.P4[i], N4 = s.N4[i];
+    const f3 P = xyz(P4), N = xyz(N4), O = P + N * 1e-3f;
+    uint32_t m[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) m[w] = 0u;
+    float rec[AES];
+#pragma unroll
+    for (int k = 0; k < AES; ++k) rec[k] = 0.f;
+    rec[0] = g.A[i];
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+        f3 d = mk(L[3 * l], L[3 * l + 1], L[3 * l + 2]) - P;
+        float r = sqrtf(dot(d, d));
+        f3 D = d * (1.f / r);
+        float cc = dot(N, D), t;
+        int q, jb;
+        trace_dyn(tsm, s, false, O, D, t, q, jb);
+        if (g.has_bvh) trace_bvh(g, O, D, t, q, flags);
+        bool vis = t >= r - 1e-3f;
+        float rr = fmaxf(r, 0.05f);
+        rec[1 + l] = inten[l] * fmaxf(cc, 0.f) / (rr * rr) * (vis ? 1.f : 0.f);
+        f3 a = O, b = O + D * fminf(t, r);
+        for (int k = 0; k < 20; ++k) set_bit<NW>(m, vox_of(grid, a + (b - a) * (k / 19.f)));
+    }
+#pragma unroll
+    for (int k = 0; k < AES / 4; ++k) AE[(size_t)i * (AES / 4) + k] = make_float4(rec[4 * k], rec[4 * k + 1], rec[4 * k + 2], rec[4 * k + 3]);
+#pragma unroll
+    for (int w = 0; w < NW; ++w) SV[(size_t)NW * i + w] = m[w];
+}
+
+// ------------------------------------------------------------------ frame kernel
+// FUSED: trace + update + reductions (frames without verification, projection or DDGI).
+// !FUSED: trace only, writing kk / m and the region statistics (poc_gpu.cu:492-529).
+template <int NL, int NW, bool DEPS, bool FUSED>
+__global__ void __launch_bounds__(BLOCK, 2) k_frame(const DState s, const DStatic g, const Grid grid, const DevCache c,
+                                                 const FrameParams p) {
+    extern __shared__ float4 sm[];
+    __shared__ float shf[BLOCK / 32];
+    __shared__ double shd[BLOCK / 32];
+    __shared__ bool last;
+    constexpr int LCS = lcs_of(NL), AES = aes_of(NL);
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    float pr_out = 0.f;
+    double e_d2 = 0.0, e_rs = 0.0, e_cn = 0.0;
+    if (i < p.Np) {
+        uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
+        const bool pend = !FUSED && p.pend_left > 0 && c.pending[i];
+        const float n_i = c.n[i];
+        const int k = ray_count(p, c, n_i, pend, c.sumpr[p.sum_in], c.npend[0], rs);
+        const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
+        float acc[NL];
+#pragma unroll
+        for (int l = 0; l < NL; ++l) acc[l] = 0.f;
+        uint32_t m[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) m[w] = 0u;
+        const float c0 = pend ? c.c0[i] : 0.f;
+        float sd = 0.f, sq = 0.f;
+        for (int r = 0; r < k; ++r) {
+            const float u1 = rnd(rs);
+            const float u2 = rnd(rs);
+            const f3 D = cosine_dir(N, u1, u2);
+            const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+            float val = 0.f;
+            if (!h.back) {
+                float4 ae[AES / 4], lc[LCS / 4];
+                const float4* aep = s.AE + (size_t)h.pi * (AES / 4);
+                const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)h.pi * (LCS / 4);
+#pragma unroll
+                for (int k4 = 0; k4 < AES / 4; ++k4) ae[k4] = __ldg(aep + k4);
+#pragma unroll
+                for (int k4 = 0; k4 < LCS / 4; ++k4) lc[k4] = __ldcg(lcp + k4);
+                const float A = ae[0].x;
+#pragma unroll
+                for (int l = 0; l < NL; ++l) {
+                    const float lcv = ((p.dormant >> l) & 1) ? 0.f : comp(lc, l);
+                    const float v = A * (comp(ae, l + 1) + lcv);
+                    acc[l] += v;
+                    val += v;
+                }
+            }
+            if (DEPS) {
+                const int src = h.back ? i : h.pi;
+                const uint4* sv = reinterpret_cast<const uint4*>(s.SV + (size_t)NW * src);
+#pragma unroll
+                for (int w = 0; w < NW / 4; ++w) {
+                    const uint4 x = __ldg(sv + w);
+                    m[4 * w] |= x.x; m[4 * w + 1] |= x.y; m[4 * w + 2] |= x.z; m[4 * w + 3] |= x.w;
+                }
+                dda_walk<NW>(grid, O, h.H, m);
+            }
+            if (pend) { float dv = val - c0; sd += dv; sq += dv * dv; }
+        }
+        const float ik = k > 0 ? 1.f / k : 0.f;
+        if (!FUSED) {
+            const int rg = g.region[i];
+            if (pend && k > 0) {
+                atomicAdd(&c.rstat[4 * rg + 0], sd);
+                atomicAdd(&c.rstat[4 * rg + 1], sq);
+                atomicAdd(&c.rstat[4 * rg + 2], c0 * k);
+                atomicAdd(&c.rstat[4 * rg + 3], float(k));
+            }
+            if (p.proj_left > 0 && k > 0) {
+                float T[KSNAP];
+                for (int a = 0; a < p.projK; ++a) {
+                    const float* sp = c.snap + ((size_t)p.slot[a] * p.Np + i) * LCS;
+                    float t = 0.f;
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) t += sp[l];
+                    T[a] = t;
+                }
+                float sv = 0.f;
+#pragma unroll
+                for (int l = 0; l < NL; ++l) sv += acc[l];
+                float* qn = c.neq + (size_t)rg * NEQ;
+                int ix = 0;
+                for (int a = 0; a < p.projK; ++a)
+                    for (int b = a; b < p.projK; ++b) atomicAdd(&qn[ix++], k * T[a] * T[b]);
+                for (int a = 0; a < p.projK; ++a) atomicAdd(&qn[21 + a], sv * T[a]);
+                atomicAdd(&qn[27], float(k));
+            }
+            c.kk[i] = k;
+            float mo[LCS];
+#pragma unroll
+            for (int l = 0; l < LCS; ++l) mo[l] = l < NL ? acc[l] * ik : 0.f;
+            float4* mp = reinterpret_cast<float4*>(c.m) + (size_t)i * (LCS / 4);
+#pragma unroll
+            for (int k4 = 0; k4 < LCS / 4; ++k4) mp[k4] = make_float4(mo[4 * k4], mo[4 * k4 + 1], mo[4 * k4 + 2], mo[4 * k4 + 3]);
+            if (p.ddgi && k > 0) {
+                float sa = 0.f;
+#pragma unroll
+                for (int l = 0; l < NL; ++l) sa += acc[l];
+                float est = 0.f;
+#pragma unroll
+                for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) est += c.Lc[(size_t)LCS * i + l];
+                atomicAdd(&c.dstat[3 * rg + 0], sa * ik);
+                atomicAdd(&c.dstat[3 * rg + 1], est);
+                atomicAdd(&c.dstat[3 * rg + 2], 1.f);
+            }
+        } else {
+            // k_update (poc_gpu.cu:562-602) on the point's own history.
+            float4 lc[LCS / 4];
+            const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)i * (LCS / 4);
+#pragma unroll
+            for (int k4 = 0; k4 < LCS / 4; ++k4) lc[k4] = __ldcg(lcp + k4);
+            float nn = n_i + k;
+            float nmx = p.nmax;
+            if (p.ramp) {
+                float a = c.age[i];
+                nmx = fminf(p.nmax, (4.f + 0.5f * a) * p.rays);
+                c.age[i] = fminf(a + 1.f, 1e4f);
+            }
+            const float alpha = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), nmx), 1.f) : 0.f;
+            const float alpha_r = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), p.nmax_resp), 1.f) : 0.f;
+            float out[LCS];
+            float est = 0.f;
+#pragma unroll
+            for (int l = 0; l < LCS; ++l) {
+                if (l < NL) {
+                    const float a = comp(lc, l);
+                    float al = ((p.resp_mask >> l) & 1) ? alpha_r : alpha;
+                    if ((p.dormant >> l) & 1) al = 0.f;
+                    out[l] = a + al * (acc[l] * ik - a);
+                    if (!((p.dormant >> l) & 1)) est += out[l];
+                } else {
+                    out[l] = 0.f;
+                }
+            }
+            float4* op = reinterpret_cast<float4*>(c.Lc2) + (size_t)i * (LCS / 4);
+#pragma unroll
+            for (int k4 = 0; k4 < LCS / 4; ++k4) op[k4] = make_float4(out[4 * k4], out[4 * k4 + 1], out[4 * k4 + 2], out[4 * k4 + 3]);
+            const float nf = fminf(nn, nmx);
+            c.n[i] = nf;
+            pr_out = 1.f / (nf + 1.f);
+            if (p.want_err && s.valid[i]) {
+                const float e = est - s.ref[i];
+                e_d2 = double(e) * e;
+                e_rs = s.ref[i];
+                e_cn = 1.0;
+            }
+        }
+        if (p.mask_op == MASK_OR) {
+            if (DEPS && k > 0) {
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    const uint32_t old = c.cur[(size_t)w * p.Np + i];
+                    if ((old | m[w]) != old) c.cur[(size_t)w * p.Np + i] = old | m[w];
+                }
+            }
+        } else if (p.mask_op == MASK_FRESH || p.mask_op == MASK_ZERO) {
+#pragma unroll
+            for (int w = 0; w < NW; ++w) c.cur[(size_t)w * p.Np + i] = (DEPS && p.mask_op == MASK_FRESH && k > 0) ? m[w] : 0u;
+        }
+    }
+    if (FUSED) {
+        const float bpr = block_tree(pr_out, shf);
+        double b0 = 0, b1 = 0, b2 = 0;
+        if (p.want_err) { b0 = block_tree(e_d2, shd); b1 = block_tree(e_rs, shd); b2 = block_tree(e_cn, shd); }
+        if (threadIdx.x == 0) {
+            c.partf[blockIdx.x] = bpr;
+            if (p.want_err) { c.partd[3 * blockIdx.x] = b0; c.partd[3 * blockIdx.x + 1] = b1; c.partd[3 * blockIdx.x + 2] = b2; }
+            __threadfence();
+            last = atomicAdd(c.ticket, 1u) == gridDim.x - 1;
+        }
+        __syncthreads();
+        if (last) {
+            __threadfence();
+            const float tot = final_tree(c.partf, gridDim.x, 1, 0, shf);
+            double t0 = 0, t1 = 0, t2 = 0;
+            if (p.want_err) {
+                t0 = final_tree(c.partd, gridDim.x, 3, 0, shd);
+                t1 = final_tree(c.partd, gridDim.x, 3, 1, shd);
+                t2 = final_tree(c.partd, gridDim.x, 3, 2, shd);
+            }
+            if (threadIdx.x == 0) {
+                c.sumpr[p.sum_out] = tot;
+                if (p.want_err) { c.err[3 * p.err_frame] = t0; c.err[3 * p.err_frame + 1] = t1; c.err[3 * p.err_frame + 2] = t2; }
+                *c.ticket = 0u;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ split update
+// k_decide + k_update (poc_gpu.cu:532-602) for one point, then Sum 1/(n+1), the error sums
+// and the pending count, reduced by the last block.
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_update(const DState s, const DStatic g, const DevCache c, const FrameParams p) {
+    __shared__ float shf[BLOCK / 32];
+    __shared__ double shd[BLOCK / 32];
+    __shared__ int shi[BLOCK / 32];
+    __shared__ bool last;
+    constexpr int LCS = lcs_of(NL);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    float pr_out = 0.f;
+    double e_d2 = 0.0, e_rs = 0.0, e_cn = 0.0;
+    int cnt = 0;
+    if (i < p.Np) {
+        const int rg = g.region[i];
+        if (p.decide && c.pending[i]) {
+            const float* r4 = c.rstat + 4 * rg;
+            const float cn = r4[3];
+            bool done = false;
+            if (cn >= 8.f) {
+                float mean = r4[0] / cn;
+                float se = sqrtf(fmaxf(r4[1] / cn - mean * mean, 0.f) / cn);
+                float base = r4[2] / cn;
+                float rel = mean / base;
+                if (fabsf(mean) > 2.f * se && fabsf(rel) > 0.03f) {
+                    float tgt = fminf(fmaxf(0.5f / fabsf(rel), 1.f) * p.rays, p.nmax);
+                    c.n[i] = fminf(c.n[i], tgt);
+                    c.pending[i] = 0;
+                    done = true;
+                }
+            }
+            if (!done) {
+                if (p.pend_left <= 1) c.pending[i] = 0;
+                else cnt = 1;
+            }
+        }
+        const int k = c.kk[i];
+        float n = c.n[i], nn = n + k;
+        float nmx = p.nmax;
+        if (p.ramp) {
+            float a = c.age[i];
+            nmx = fminf(p.nmax, (4.f + 0.5f * a) * p.rays);
+            c.age[i] = fminf(a + 1.f, 1e4f);
+        }
+        const float alpha = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), nmx), 1.f) : 0.f;
+        const float* lci = c.Lc + (size_t)LCS * i;
+        const float* mi = c.m + (size_t)LCS * i;
+        float* lo = c.Lc2 + (size_t)LCS * i;
+        float est = 0.f;
+        if (p.ddgi) {
+            const float* d3 = c.dstat + 3 * rg;
+            float scale = 1.f, h = p.ddgi_h;
+            if (d3[2] > 0.f) {
+                float mn = d3[0] / d3[2], mc = d3[1] / d3[2];
+                float rel = fabsf(mn - mc) / fmaxf(mc, 1e-3f);
+                if (rel > p.ddgi_thr) h = fmaxf(0.f, h - 0.75f);
+                if (p.ddgi_clamp && rel > 0.10f) scale = 0.25f;
+            }
+            const float w = k > 0 ? (1.f - h) * scale : 0.f;
+#pragma unroll
+            for (int l = 0; l < NL; ++l) {
+                const float a = lci[l];
+                lo[l] = ((p.dormant >> l) & 1) ? a : a + w * (mi[l] - a);
+                if (!((p.dormant >> l) & 1)) est += lo[l];
+            }
+        } else {
+            const float alpha_r = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), p.nmax_resp), 1.f) : 0.f;
+#pragma unroll
+            for (int l = 0; l < NL; ++l) {
+                const float a = lci[l];
+                float al = ((p.resp_mask >> l) & 1) ? alpha_r : alpha;
+                if ((p.dormant >> l) & 1) al = 0.f;
+                lo[l] = a + al * (mi[l] - a);
+                if (!((p.dormant >> l) & 1)) est += lo[l];
+            }
+        }
+#pragma unroll
+        for (int l = NL; l < LCS; ++l) lo[l] = 0.f;
+        n = fminf(nn, nmx);
+        c.n[i] = n;
+        pr_out = 1.f / (n + 1.f);
+        if (p.want_err && s.valid[i]) {
+            const float e = est - s.ref[i];
+            e_d2 = double(e) * e;
+            e_rs = s.ref[i];
+            e_cn = 1.0;
+        }
+    }
+    const float bpr = block_tree(pr_out, shf);
+    double b0 = 0, b1 = 0, b2 = 0;
+    if (p.want_err) { b0 = block_tree(e_d2, shd); b1 = block_tree(e_rs, shd); b2 = block_tree(e_cn, shd); }
+    int bc = 0;
+    if (p.decide) bc = block_tree(cnt, shi);
+    if (threadIdx.x == 0) {
+        c.partf[blockIdx.x] = bpr;
+        if (p.want_err) { c.partd[3 * blockIdx.x] = b0; c.partd[3 * blockIdx.x + 1] = b1; c.partd[3 * blockIdx.x + 2] = b2; }
+        if (p.decide) c.parti[blockIdx.x] = bc;
+        __threadfence();
+        last = atomicAdd(c.ticket + 1, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        const float tot = final_tree(c.partf, gridDim.x, 1, 0, shf);
+        double t0 = 0, t1 = 0, t2 = 0;
+        if (p.want_err) {
+            t0 = final_tree(c.partd, gridDim.x, 3, 0, shd);
+            t1 = final_tree(c.partd, gridDim.x, 3, 1, shd);
+            t2 = final_tree(c.partd, gridDim.x, 3, 2, shd);
+        }
+        int ct = 0;
+        if (p.decide) ct = final_tree(c.parti, gridDim.x, 1, 0, shi);
+        if (threadIdx.x == 0) {
+            c.sumpr[p.sum_out] = tot;
+            if (p.want_err) { c.err[3 * p.err_frame] = t0; c.err[3 * p.err_frame + 1] = t1; c.err[3 * p.err_frame + 2] = t2; }
+            if (p.decide) { c.npend[0] = ct; c.npend[1] = ct; }
+            *(c.ticket + 1) = 0u;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ events
+template <int NL>
+__device__ __forceinline__ float est_point(const float* lc, int dormant) {
+    float e = 0.f;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) if (!((dormant >> l) & 1)) e += lc[l];
+    return e;
+}
+
+// The per-point kernels of one event (poc_gpu.cu:612-681), applied in launch order to each
+// point; then the pending count and, in adaptive mode, Sum 1/(n+1) (poc_gpu.cu:938-941).
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_event(const __grid_constant__ EvProgram ev, const DevCache c) {
+    __shared__ float shf[BLOCK / 32];
+    __shared__ int shi[BLOCK / 32];
+    __shared__ bool last;
+    constexpr int LCS = lcs_of(NL);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    const int Np = ev.Np;
+    if (ev.zero_rstat)
+        for (int x = i; x < 4 * ev.NR; x += gridDim.x * BLOCK) c.rstat[x] = 0.f;
+    if (ev.zero_neq)
+        for (int x = i; x < NEQ * ev.NR; x += gridDim.x * BLOCK) c.neq[x] = 0.f;
+    int cnt = 0;
+    float pr = 0.f;
+    if (i < Np) {
+        float* lc = c.Lc + (size_t)LCS * i;
+        for (int o = 0; o < ev.nops; ++o) {
+            const EvOp& op = ev.ops[o];
+            switch (op.kind) {
+                case EV_SNAP_SAVE: {
+                    float* sp = c.snap + ((size_t)op.a * Np + i) * LCS;
+#pragma unroll
+                    for (int l = 0; l < LCS; ++l) sp[l] = lc[l];
+                } break;
+                case EV_SNAP_RESTORE: {
+                    const float* sp = c.snap + ((size_t)op.a * Np + i) * LCS;
+#pragma unroll
+                    for (int l = 0; l < LCS; ++l) lc[l] = sp[l];
+                } break;
+                case EV_ORACLE: {
+                    float rel = fabsf(op.r1[i] - op.r0[i]) / (op.r0[i] + 1e-2f);
+                    c.n[i] *= 1.f - fminf(fmaxf(4.f * rel, 0.f), 1.f);
+                } break;
+                case EV_RESCALE:
+                    lc[op.a] *= op.x;
+                    break;
+                case EV_WAKE:
+                    if ((c.stale[i] >> op.a) & 1u) {
+                        if (op.b) {
+                            c.pending[i] = 1;
+                            c.c0[i] = est_point<NL>(lc, op.dormant);
+                            if (op.count) cnt++;
+                        } else {
+                            lc[op.a] = 0.f;
+                            c.n[i] = 0.f;
+                            c.age[i] = 0.f;
+                        }
+                        c.stale[i] &= ~(1u << op.a);
+                    }
+                    break;
+                case EV_TOUCHED: {
+                    bool t = false;
+                    for (int j = 0; j < op.b && !t; ++j) {
+                        const int v = op.list[j];
+                        const size_t oo = (size_t)(v >> 5) * Np + i;
+                        t = ((c.cur[oo] | c.prev[oo]) >> (v & 31)) & 1u;
+                    }
+                    if (t) {
+                        if (op.a == 0) { c.n[i] = 0.f; c.age[i] = 0.f; }
+                        else if (op.a == 1) {
+                            c.pending[i] = 1;
+                            c.c0[i] = est_point<NL>(lc, op.dormant);
+                            if (op.count) cnt++;
+                        }
+                        if (op.a >= 1 && op.dormant) c.stale[i] |= (uint32_t)op.dormant;
+                    }
+                } break;
+                case EV_RESTORED:
+                    c.n[i] = ev.nmax;
+                    c.age[i] = 1e4f;
+                    c.pending[i] = 0;
+                    if (op.a) {
+                        c.pending[i] = 1;
+                        c.c0[i] = est_point<NL>(lc, op.dormant);
+                        if (op.count) cnt++;
+                    }
+                    break;
+            }
+        }
+        pr = 1.f / (c.n[i] + 1.f);
+    }
+    if (!ev.want_sumpr && ev.npend_mode != 1) {
+        if (ev.npend_mode == 2 && blockIdx.x == 0 && threadIdx.x == 0) { c.npend[0] = 0; c.npend[1] = 0; }
+        return;
+    }
+    const float bpr = ev.want_sumpr ? block_tree(pr, shf) : 0.f;
+    const int bc = ev.npend_mode == 1 ? block_tree(cnt, shi) : 0;
+    if (threadIdx.x == 0) {
+        c.partf[blockIdx.x] = bpr;
+        c.parti[blockIdx.x] = bc;
+        __threadfence();
+        last = atomicAdd(c.ticket + 2, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        const float tot = ev.want_sumpr ? final_tree(c.partf, gridDim.x, 1, 0, shf) : 0.f;
+        const int ct = ev.npend_mode == 1 ? final_tree(c.parti, gridDim.x, 1, 0, shi) : 0;
+        if (threadIdx.x == 0) {
+            if (ev.want_sumpr) c.sumpr[ev.sum_slot] = tot;
+            if (ev.npend_mode == 1) { c.npend[0] = ct; c.npend[1] = ct; }
+            if (ev.npend_mode == 2) { c.npend[0] = 0; c.npend[1] = 0; }
+            *(c.ticket + 2) = 0u;
+        }
+    }
+}
+
+// poc_gpu.cu:620-635 + the pending-count reset / publish around it (poc_gpu.cu:990-993).
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_proj_apply(const DevCache c, const DStatic g, const FrameParams p) {
+    __shared__ int shi[BLOCK / 32];
+    __shared__ bool last;
+    constexpr int LCS = lcs_of(NL);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    for (int x = i; x < 4 * p.NR; x += gridDim.x * BLOCK) c.rstat[x] = 0.f;
+    int cnt = 0;
+    if (i < p.Np && !(c.n[i] >= 16.f)) {
+        const float* cf = c.coef + (size_t)g.region[i] * KSNAP;
+        if (!isnan(cf[0])) {
+            float* lc = c.Lc + (size_t)LCS * i;
+            for (int l = 0; l < NL; ++l) {
+                if ((p.dormant >> l) & 1) continue;
+                float v = 0.f;
+                for (int a = 0; a < p.projK; ++a) v += cf[a] * c.snap[((size_t)p.slot[a] * p.Np + i) * LCS + l];
+                lc[l] = fmaxf(v, 0.f);
+            }
+            c.n[i] = 8.f * p.rays;
+            c.age[i] = 8.f;
+            c.pending[i] = 1;
+            c.c0[i] = est_point<NL>(lc, p.dormant);
+            cnt = 1;
+        }
+    }
+    const int bc = block_tree(cnt, shi);
+    if (threadIdx.x == 0) {
+        c.parti[blockIdx.x] = bc;
+        __threadfence();
+        last = atomicAdd(c.ticket + 3, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        const int ct = final_tree(c.parti, gridDim.x, 1, 0, shi);
+        if (threadIdx.x == 0) { c.npend[0] = ct; c.npend[1] = ct; *(c.ticket + 3) = 0u; }
+    }
+}
+
+// poc_gpu.cu:683-696: FP64 error sums of the current cache over valid points (used on
+// frames whose cache changes after the update, i.e. when the projection is applied).
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_error(const DState s, const DevCache c, const FrameParams p) {
+    __shared__ double shd[BLOCK / 32];
+    __shared__ bool last;
+    constexpr int LCS = lcs_of(NL);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    double d2 = 0.0, rs = 0.0, cn = 0.0;
+    if (i < p.Np && s.valid[i]) {
+        const float e = est_point<NL>(c.Lc + (size_t)LCS * i, p.dormant) - s.ref[i];
+        d2 = double(e) * e;
+        rs = s.ref[i];
+        cn = 1.0;
+    }
+    const double b0 = block_tree(d2, shd), b1 = block_tree(rs, shd), b2 = block_tree(cn, shd);
+    if (threadIdx.x == 0) {
+        c.partd[3 * blockIdx.x] = b0; c.partd[3 * blockIdx.x + 1] = b1; c.partd[3 * blockIdx.x + 2] = b2;
+        __threadfence();
+        last = atomicAdd(c.ticket + 3, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        const double t0 = final_tree(c.partd, gridDim.x, 3, 0, shd);
+        const double t1 = final_tree(c.partd, gridDim.x, 3, 1, shd);
+        const double t2 = final_tree(c.partd, gridDim.x, 3, 2, shd);
+        if (threadIdx.x == 0) {
+            c.err[3 * p.err_frame] = t0; c.err[3 * p.err_frame + 1] = t1; c.err[3 * p.err_frame + 2] = t2;
+            *(c.ticket + 3) = 0u;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ probe
+struct RayRecD { int point, ray, q, pi, back; float t; };
+
+template <int NL, int NW>
+__global__ void __launch_bounds__(BLOCK) k_probe(const DState s, const DStatic g, const Grid grid, const DevCache c,
+                                                 const FrameParams p, const int* __restrict__ pts, int npts,
+                                                 RayRecD* __restrict__ out, int maxrec, int* __restrict__ nrec) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int t = blockIdx.x * BLOCK + threadIdx.x;
+    if (t >= npts) return;
+    const int i = pts[t];
+    if (i < 0 || i >= p.Np) return;
+    uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
+    const bool pend = p.pend_left > 0 && c.pending[i];
+    const int k = ray_count(p, c, c.n[i], pend, c.sumpr[p.sum_in], c.npend[0], rs);
+    const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
+    for (int r = 0; r < k; ++r) {
+        const float u1 = rnd(rs);
+        const float u2 = rnd(rs);
+        const f3 D = cosine_dir(N, u1, u2);
+        const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+        const int slot = atomicAdd(nrec, 1);
+        if (slot < maxrec) {
+            RayRecD x;
+            x.point = i; x.ray = r; x.q = h.q; x.pi = h.pi; x.back = h.back ? 1 : 0;
+            x.t = h.q != -1 ? h.t : __int_as_float(0x7f800000);
+            out[slot] = x;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ launch wrappers
+
+static int grid_of(int Np) { return (Np + BLOCK - 1) / BLOCK; }
+
+template <typename K>
+static cudaError_t prep_smem(K kern, size_t smem) {
+    if (smem > 48 * 1024) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+// Mask widths built for every light count (NW = voxels / 32 of the transit grid).
+#define RC_NW_LIST(X) X(4) X(24)
+
+template <int NL>
+cudaError_t Ops<NL>::build(int NW, const DState& s, const DStatic& g, const Grid& grid, const float* L, const float* inten,
+                           float4* AE, uint32_t* SV, int Np, unsigned* flags, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+#define X(W)                                                                                     \
+    if (NW == W) {                                                                               \
+        cudaError_t e = prep_smem(k_build<NL, W>, smem);                                         \
+        if (e != cudaSuccess) return e;                                                          \
+        k_build<NL, W><<<grid_of(Np), BLOCK, smem, st>>>(s, g, grid, L, inten, AE, SV, Np, flags); \
+        return cudaGetLastError();                                                               \
+    }
+    RC_NW_LIST(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+template <int NL, int NW, bool DEPS, bool FUSED>
+static cudaError_t frame_t(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                           cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+    cudaError_t e = prep_smem(k_frame<NL, NW, DEPS, FUSED>, smem);
+    if (e != cudaSuccess) return e;
+    k_frame<NL, NW, DEPS, FUSED><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::frame(int NW, bool deps, bool fused, const DState& s, const DStatic& g, const Grid& grid,
+                           const DevCache& c, const FrameParams& p, cudaStream_t st) {
+#define X(W)                                                                        \
+    if (NW == W) {                                                                  \
+        if (deps) return fused ? frame_t<NL, W, true, true>(s, g, grid, c, p, st)   \
+                               : frame_t<NL, W, true, false>(s, g, grid, c, p, st); \
+        return fused ? frame_t<NL, W, false, true>(s, g, grid, c, p, st)            \
+                     : frame_t<NL, W, false, false>(s, g, grid, c, p, st);          \
+    }
+    RC_NW_LIST(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+template <int NL>
+cudaError_t Ops<NL>::update(const DState& s, const DStatic& g, const DevCache& c, const FrameParams& p, cudaStream_t st) {
+    k_update<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(s, g, c, p);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::event(const EvProgram& ev, const DevCache& c, cudaStream_t st) {
+    k_event<NL><<<grid_of(ev.Np), BLOCK, 0, st>>>(ev, c);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::error(const DState& s, const DevCache& c, const FrameParams& p, cudaStream_t st) {
+    k_error<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(s, c, p);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::proj_apply(const DevCache& c, const DStatic& g, const FrameParams& p, cudaStream_t st) {
+    k_proj_apply<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(c, g, p);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::probe(int NW, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                           const int* pts, int npts, void* recs, int maxrec, int* nrec, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+#define X(W)                                                                                                   \
+    if (NW == W) {                                                                                             \
+        cudaError_t e = prep_smem(k_probe<NL, W>, smem);                                                       \
+        if (e != cudaSuccess) return e;                                                                        \
+        k_probe<NL, W><<<grid_of(npts), BLOCK, smem, st>>>(s, g, grid, c, p, pts, npts, (RayRecD*)recs, maxrec, nrec); \
+        return cudaGetLastError();                                                                             \
+    }
+    RC_NW_LIST(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+#ifdef RC_NL_ONE
+template struct Ops<RC_NL_ONE>;
+#endif
+
+}  // namespace rc

@@ -1,0 +1,1203 @@
+// Host runtime behind include/rc_api.h: scene loading, device buffers, and the frame driver.
+//
+// The frame driver follows Runner::run of the reference (cuda/poc_gpu.cu:826-1016) step by
+// step — the same event rules, the same order of operations on the cache — but issues the
+// work differently: one kernel per ordinary frame, one kernel per event, no host
+// synchronisation except where the reference's projection solve needs the region sums on
+// the host, and no per-frame memsets or device-to-device copies (counters and sums live in
+// ping-pong slots written by the kernels' last block).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rc_api.h"
+#include "rc_internal.h"
+
+using namespace rc;
+
+// Dispatch on the light count to the per-count kernel instantiations.
+#define RC_DISPATCH(NL, call)                       \
+    [&]() -> cudaError_t {                          \
+        switch (NL) {                               \
+            case 1: return Ops<1>::call;            \
+            case 2: return Ops<2>::call;            \
+            case 3: return Ops<3>::call;            \
+            case 4: return Ops<4>::call;            \
+            case 8: return Ops<8>::call;            \
+            case 16: return Ops<16>::call;          \
+            case 32: return Ops<32>::call;          \
+        }                                           \
+        return cudaErrorInvalidValue;               \
+    }()
+
+namespace {
+
+constexpr int VERIF_FRAMES = 4;   // poc_gpu.cu:115
+constexpr int PROJ_FRAMES = 4;    // poc_gpu.cu:424
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+};
+
+struct HostState {
+    std::vector<float> inten;
+    std::vector<float> ref;         // host copy of the reference
+    const float* pw = nullptr;      // device warm start (padded cache layout)
+    DState d{};
+};
+
+struct Scene {
+    int Np = 0, Nq = 0, Nt = 0, NS = 0, NL = 0, NR = 0, has_ref = 0, fmt = 2;
+    int nst = 0, nnodes = 0, hsize = 0, npst = 0;
+    float hcell = 0.f;
+    Grid grid{};
+    std::vector<HostState> st;
+    DStatic g{};
+    // events: [pair * (1 + NL) + 0] = occluder voxels, [.. + 1 + l] = voxels of light l
+    std::vector<std::vector<int>> ev;
+    std::vector<const int*> ev_dev;
+    double scene_bytes = 0;
+};
+
+struct Run {
+    bool active = false;
+    rc_method M{};
+    FrameParams p{};
+    int dormant = 0;
+    float ilearn[32] = {0};
+    int pend_left = 0, nslots = 0, slot_state[KSNAP], slot_next = 0, last_event_f = 0, proj_left = 0, projK = 0;
+    int slot[KSNAP] = {0};
+    int prev_state = 0, f = 0, sum_cur = 0, nerr = 0;
+    float nmax = 0.f;
+};
+
+}  // namespace
+
+struct rc_ctx {
+    rc_config cfg{};
+    int NW = 4;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    std::vector<DevBuf> scene_bufs, cache_bufs;
+    Scene S;
+    bool have_scene = false;
+    DevCache c{};
+    size_t err_cap = 0;         // frames of error sums allocated
+    Run run;
+    double cache_bytes = 0;
+    unsigned* flags_dev = nullptr;
+    cudaEvent_t ev[8] = {};
+};
+
+namespace {
+
+rc_status fail(rc_ctx* ctx, rc_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list a;
+    va_start(a, fmt);
+    vsnprintf(buf, sizeof buf, fmt, a);
+    va_end(a);
+    if (ctx) ctx->err = buf;
+    return s;
+}
+#define CKR(x)                                                                                          \
+    do {                                                                                                \
+        cudaError_t e_ = (x);                                                                           \
+        if (e_ != cudaSuccess) return fail(ctx, RC_ERR_CUDA, "CUDA %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+template <class T>
+rc_status dalloc(rc_ctx* ctx, std::vector<DevBuf>& pool, T** out, size_t n) {
+    void* p = nullptr;
+    size_t bytes = n * sizeof(T) + 16;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return fail(ctx, RC_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    pool.push_back({p, bytes});
+    *out = (T*)p;
+    return RC_OK;
+}
+template <class T>
+rc_status dput(rc_ctx* ctx, std::vector<DevBuf>& pool, const T** out, const std::vector<T>& v) {
+    T* p = nullptr;
+    rc_status s = dalloc(ctx, pool, &p, v.size());
+    if (s != RC_OK) return s;
+    if (!v.empty()) CKR(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    *out = p;
+    return RC_OK;
+}
+void free_pool(std::vector<DevBuf>& pool) {
+    for (auto& b : pool) cudaFree(b.p);
+    pool.clear();
+}
+
+struct Reader {
+    const uint8_t* p;
+    size_t n, off = 0;
+    bool bad = false;
+    template <class T>
+    void get(T* dst, size_t cnt) {
+        size_t b = cnt * sizeof(T);
+        if (bad || b / sizeof(T) != cnt || off + b > n) { bad = true; return; }
+        if (b) memcpy(dst, p + off, b);
+        off += b;
+    }
+    template <class T>
+    std::vector<T> vec(size_t cnt) {
+        if (bad || cnt > (n - off) / sizeof(T)) { bad = true; return {}; }
+        std::vector<T> v(cnt);
+        get(v.data(), cnt);
+        return v;
+    }
+};
+
+// poc_gpu.cu:720-735: fine event grid (16 x 8 x 6 over the 8 x 4 x 3 m box) -> transit grid.
+std::vector<int> to_grid(const std::vector<int>& fine, int VX, int VY, int VZ) {
+    const int FX = 16, FY = 8, FZ = 6;
+    const float X1 = 8.f, Y1 = 4.f, Z1 = 3.f;
+    std::vector<char> mark((size_t)VX * VY * VZ, 0);
+    for (int v : fine) {
+        int i = v % FX, j = (v / FX) % FY, k = v / (FX * FY);
+        float x0 = i * X1 / FX, x1 = (i + 1) * X1 / FX, y0 = j * Y1 / FY, y1 = (j + 1) * Y1 / FY;
+        float z0 = k * Z1 / FZ, z1 = (k + 1) * Z1 / FZ;
+        int a0 = std::min(int(x0 / X1 * VX + 1e-4f), VX - 1), a1 = std::min(int(x1 / X1 * VX - 1e-4f), VX - 1);
+        int b0 = std::min(int(y0 / Y1 * VY + 1e-4f), VY - 1), b1 = std::min(int(y1 / Y1 * VY - 1e-4f), VY - 1);
+        int c0 = std::min(int(z0 / Z1 * VZ + 1e-4f), VZ - 1), c1 = std::min(int(z1 / Z1 * VZ - 1e-4f), VZ - 1);
+        for (int a = a0; a <= a1; ++a)
+            for (int b = b0; b <= b1; ++b)
+                for (int c = c0; c <= c1; ++c) mark[((size_t)c * VY + b) * VX + a] = 1;
+    }
+    std::vector<int> out;
+    for (size_t v = 0; v < mark.size(); ++v)
+        if (mark[v]) out.push_back((int)v);
+    return out;
+}
+
+// Plane-culling groups of one state's dynamic triangles.  A group is a pair of consecutive
+// triangles of the same quad lying in one axis-aligned plane (or a lone such triangle); its
+// outer box (grown by a margin) must contain every point the exact test can accept, its inner
+// box (shrunk) only points the exact test surely accepts — only full rectangles get one.
+struct Groups {
+    std::vector<float4> grp;
+    std::vector<int> misc;
+    GroupRanges gr{};
+};
+Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int nt) {
+    struct G { int axis, j0, cnt; bool rect; float c, lo[2], hi[2]; };
+    std::vector<G> gs;
+    std::vector<int> misc;
+    auto axis_of = [&](int j) {
+        const float* t = &T[9 * (size_t)j];
+        for (int k = 0; k < 3; ++k)
+            if (t[3 + k] == 0.f && t[6 + k] == 0.f) return k;
+        return -1;
+    };
+    auto box = [&](int j, int k, float lo[2], float hi[2]) {
+        const float* t = &T[9 * (size_t)j];
+        int a = (k + 1) % 3, b = (k + 2) % 3;
+        if (k == 1) { a = 0; b = 2; }
+        if (k == 0) { a = 1; b = 2; }
+        if (k == 2) { a = 0; b = 1; }
+        const int ax[2] = {a, b};
+        for (int u = 0; u < 2; ++u) {
+            float v0 = t[ax[u]], v1 = t[ax[u]] + t[3 + ax[u]], v2 = t[ax[u]] + t[6 + ax[u]];
+            lo[u] = std::min(v0, std::min(v1, v2));
+            hi[u] = std::max(v0, std::max(v1, v2));
+        }
+    };
+    int j = 0;
+    while (j < nt) {
+        int k = axis_of(j);
+        if (k < 0) { misc.push_back(j); ++j; continue; }
+        G g{};
+        g.axis = k;
+        g.j0 = j;
+        g.c = T[9 * (size_t)j + k];
+        box(j, k, g.lo, g.hi);
+        g.cnt = 1;
+        g.rect = false;
+        if (j + 1 < nt && TQ[j + 1] == TQ[j] && axis_of(j + 1) == k && T[9 * (size_t)(j + 1) + k] == g.c) {
+            float lo2[2], hi2[2];
+            box(j + 1, k, lo2, hi2);
+            const float* a = &T[9 * (size_t)j];
+            const float* b = &T[9 * (size_t)(j + 1)];
+            // second triangle = (v0 + e1 + e2, -e1, -e2) and edges along the two in-plane axes:
+            // the pair tiles the rectangle that is its bounding box
+            bool tiles = true;
+            for (int x = 0; x < 3; ++x)
+                if (b[x] != a[x] + a[3 + x] + a[6 + x] || b[3 + x] != -a[3 + x] || b[6 + x] != -a[6 + x]) tiles = false;
+            int nz1 = 0, nz2 = 0;
+            for (int x = 0; x < 3; ++x) { nz1 += a[3 + x] != 0.f; nz2 += a[6 + x] != 0.f; }
+            bool axis_edges = nz1 == 1 && nz2 == 1;
+            for (int u = 0; u < 2; ++u) { g.lo[u] = std::min(g.lo[u], lo2[u]); g.hi[u] = std::max(g.hi[u], hi2[u]); }
+            g.cnt = 2;
+            g.rect = tiles && axis_edges;
+        }
+        gs.push_back(g);
+        j += g.cnt;
+    }
+    Groups out;
+    if ((int)gs.size() > MAX_GROUPS) {
+        std::stable_sort(gs.begin(), gs.end(), [](const G& a, const G& b) {
+            return (a.hi[0] - a.lo[0]) * (a.hi[1] - a.lo[1]) > (b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]);
+        });
+        for (size_t x = MAX_GROUPS; x < gs.size(); ++x)
+            for (int t = 0; t < gs[x].cnt; ++t) misc.push_back(gs[x].j0 + t);
+        gs.resize(MAX_GROUPS);
+    }
+    std::stable_sort(gs.begin(), gs.end(), [](const G& a, const G& b) { return a.axis < b.axis; });
+    int cnt[3] = {0, 0, 0};
+    for (auto& g : gs) cnt[g.axis]++;
+    out.gr.g0[0] = 0;
+    out.gr.g0[1] = cnt[0];
+    out.gr.g0[2] = cnt[0] + cnt[1];
+    out.gr.g0[3] = cnt[0] + cnt[1] + cnt[2];
+    for (auto& g : gs) {
+        float m[2], olo[2], ohi[2], ilo[2], ihi[2];
+        for (int u = 0; u < 2; ++u) {
+            m[u] = 2e-3f + 1e-4f * (g.hi[u] - g.lo[u]) + 1e-6f * (fabsf(g.lo[u]) + fabsf(g.hi[u]));
+            olo[u] = g.lo[u] - m[u];
+            ohi[u] = g.hi[u] + m[u];
+            if (g.rect) { ilo[u] = g.lo[u] + m[u]; ihi[u] = g.hi[u] - m[u]; }
+            else { ilo[u] = 1.f; ihi[u] = -1.f; }
+        }
+        int j0 = g.j0, c = g.cnt, rect = g.rect ? 1 : 0;
+        float fj0, fc, fr;
+        memcpy(&fj0, &j0, 4); memcpy(&fc, &c, 4); memcpy(&fr, &rect, 4);
+        out.grp.push_back(make_float4(g.c, olo[0], ohi[0], olo[1]));
+        out.grp.push_back(make_float4(ohi[1], ilo[0], ihi[0], ilo[1]));
+        out.grp.push_back(make_float4(ihi[1], fj0, fc, fr));
+    }
+    std::sort(misc.begin(), misc.end());
+    out.misc = misc;
+    return out;
+}
+
+rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
+    Reader r{data, n};
+    int h[8];
+    r.get(h, 8);
+    if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated header");
+    if (h[7] != 2 && h[7] != 3) return fail(ctx, RC_ERR_FORMAT, "scene format %d not supported (2 or 3)", h[7]);
+    if (h[0] <= 0 || h[1] < 0 || h[2] < 0 || h[3] <= 0 || h[4] <= 0 || h[5] <= 0)
+        return fail(ctx, RC_ERR_FORMAT, "scene: bad header");
+    if (ctx->cfg.expect_lights > 0 && h[4] != ctx->cfg.expect_lights)
+        return fail(ctx, RC_ERR_LIGHTS, "scene has %d lights, this build expects %d", h[4], ctx->cfg.expect_lights);
+    if (!supported_nl_nw(h[4], ctx->NW)) return fail(ctx, RC_ERR_UNSUPPORTED, "%d lights with %d mask words not built", h[4], ctx->NW);
+    Scene S;
+    S.Np = h[0]; S.Nq = h[1]; S.Nt = h[2]; S.NS = h[3]; S.NL = h[4]; S.NR = h[5]; S.has_ref = h[6]; S.fmt = h[7];
+    const int NL = S.NL, NW = ctx->NW;
+    const size_t Np = (size_t)S.Np;
+    S.grid.lo[0] = S.grid.lo[1] = S.grid.lo[2] = 0.f;
+    S.grid.ext[0] = 8.f; S.grid.ext[1] = 4.f; S.grid.ext[2] = 3.f;
+    S.grid.vx = ctx->cfg.grid[0]; S.grid.vy = ctx->cfg.grid[1]; S.grid.vz = ctx->cfg.grid[2];
+    auto& pool = ctx->scene_bufs;
+    DStatic& g = S.g;
+    memset(&g, 0, sizeof g);
+    if (S.fmt == 3) {
+        int m[4];
+        r.get(S.grid.lo, 3); r.get(S.grid.ext, 3); r.get(&S.hcell, 1); r.get(m, 4);
+        if (r.bad || m[0] < 0 || m[1] <= 0 || m[2] <= 0 || (m[2] & (m[2] - 1)) || m[3] < 0)
+            return fail(ctx, RC_ERR_FORMAT, "scene: bad mesh block");
+        S.nst = m[0]; S.nnodes = m[1]; S.hsize = m[2]; S.npst = m[3];
+        auto ST = r.vec<float>(9 * (size_t)m[0]);
+        auto STN = r.vec<float>(4 * (size_t)m[0]);
+        auto BN = r.vec<float>(8 * (size_t)m[1]);
+        auto HK = r.vec<unsigned long long>((size_t)m[2]);
+        auto HV = r.vec<int>((size_t)m[2]);
+        if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated mesh block");
+        // every node link and leaf range must stay inside the arrays the traversal reads
+        for (int k = 0; k < m[1]; ++k) {
+            int lf, cnt;
+            memcpy(&lf, &BN[8 * (size_t)k + 3], 4);
+            memcpy(&cnt, &BN[8 * (size_t)k + 7], 4);
+            if (cnt > 0) { if (lf < 0 || (long long)lf + cnt > m[0]) return fail(ctx, RC_ERR_FORMAT, "BVH leaf %d out of range", k); }
+            else if (lf < 0 || lf + 1 >= m[1]) return fail(ctx, RC_ERR_FORMAT, "BVH node %d child out of range", k);
+        }
+        for (int v : HV) if (v < -1 || v >= S.Np) return fail(ctx, RC_ERR_FORMAT, "hash value out of range");
+        if (!(S.hcell > 0.f)) return fail(ctx, RC_ERR_FORMAT, "hash cell size");
+        rc_status s;
+        if ((s = dput(ctx, pool, &g.ST, ST)) || (s = dput(ctx, pool, (const float**)&g.STN, STN)) ||
+            (s = dput(ctx, pool, (const float**)&g.BN, BN)) || (s = dput(ctx, pool, &g.HK, HK)) || (s = dput(ctx, pool, &g.HV, HV)))
+            return s;
+        g.hmask = (unsigned)m[2] - 1u;
+        g.hcell = S.hcell;
+        g.has_bvh = 1;
+        g.nnodes = m[1];
+        g.max_visits = 4 * m[1] + 64;
+    }
+    auto L = r.vec<float>(3 * (size_t)NL);
+    auto A = r.vec<float>(Np);
+    auto region = r.vec<int>(Np);
+    if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated");
+    for (int v : region) if (v < 0 || v >= S.NR) return fail(ctx, RC_ERR_FORMAT, "region index out of range");
+    rc_status s;
+    const float* dL = nullptr;
+    if ((s = dput(ctx, pool, &dL, L)) || (s = dput(ctx, pool, &g.A, A)) || (s = dput(ctx, pool, &g.region, region))) return s;
+    S.st.resize(S.NS);
+    for (int k = 0; k < S.NS; ++k) {
+        HostState& hs = S.st[k];
+        hs.inten = r.vec<float>(NL);
+        auto P = r.vec<float>(3 * Np), N = r.vec<float>(3 * Np), Q = r.vec<float>(12 * (size_t)S.Nq);
+        auto dims = r.vec<int>(2 * (size_t)S.Nq), off = r.vec<int>((size_t)S.Nq);
+        auto T = r.vec<float>(9 * (size_t)S.Nt);
+        auto TQ = r.vec<int>((size_t)S.Nt);
+        std::vector<uint8_t> valid;
+        std::vector<float> Pw;
+        if (S.has_ref) { hs.ref = r.vec<float>(Np); valid = r.vec<uint8_t>(Np); Pw = r.vec<float>((size_t)NL * Np); }
+        if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated state %d", k);
+        for (int q = 0; q < S.Nq; ++q)
+            if (dims[2 * q] <= 0 || dims[2 * q + 1] <= 0 || off[q] < 0 ||
+                (long long)off[q] + (long long)dims[2 * q] * dims[2 * q + 1] > S.Np)
+                return fail(ctx, RC_ERR_FORMAT, "quad %d grid out of range", q);
+        for (int t : TQ) if (t < 0 || t >= S.Nq) return fail(ctx, RC_ERR_FORMAT, "triangle quad id out of range");
+        std::vector<float4> P4(Np), N4(Np), tri(3 * (size_t)S.Nt);
+        for (size_t i = 0; i < Np; ++i) {
+            P4[i] = make_float4(P[3 * i], P[3 * i + 1], P[3 * i + 2], 0.f);
+            N4[i] = make_float4(N[3 * i], N[3 * i + 1], N[3 * i + 2], 0.f);
+        }
+        for (int j = 0; j < S.Nt; ++j) {
+            float qb;
+            memcpy(&qb, &TQ[j], 4);
+            const float* t = &T[9 * (size_t)j];
+            tri[3 * j] = make_float4(t[0], t[1], t[2], qb);
+            tri[3 * j + 1] = make_float4(t[3], t[4], t[5], 0.f);
+            tri[3 * j + 2] = make_float4(t[6], t[7], t[8], 0.f);
+        }
+        Groups G = build_groups(T, TQ, S.Nt);
+        DState& d = hs.d;
+        memset(&d, 0, sizeof d);
+        if ((s = dput(ctx, pool, &d.P4, P4)) || (s = dput(ctx, pool, &d.N4, N4)) || (s = dput(ctx, pool, &d.Q, Q)) ||
+            (s = dput(ctx, pool, &d.dims, dims)) || (s = dput(ctx, pool, &d.off, off)) || (s = dput(ctx, pool, &d.tri, tri)) ||
+            (s = dput(ctx, pool, &d.grp, G.grp)) || (s = dput(ctx, pool, &d.misc, G.misc)))
+            return s;
+        if (S.has_ref) {
+            if ((s = dput(ctx, pool, &d.ref, hs.ref)) || (s = dput(ctx, pool, &d.valid, valid))) return s;
+            // warm start of every run beginning in this state (poc_gpu.cu:832), padded like the cache
+            std::vector<float> pw((size_t)lcs_of(NL) * Np, 0.f);
+            for (size_t i = 0; i < Np; ++i)
+                for (int l = 0; l < NL; ++l) pw[(size_t)lcs_of(NL) * i + l] = Pw[(size_t)NL * i + l];
+            if ((s = dput(ctx, pool, &hs.pw, pw))) return s;
+        }
+        d.nt = S.Nt;
+        d.ng = (int)G.grp.size() / 3;
+        d.nmisc = (int)G.misc.size();
+        d.gr = G.gr;
+        size_t smem = frame_smem_bytes(d);
+        if (smem > 200 * 1024) return fail(ctx, RC_ERR_UNSUPPORTED, "%d dynamic triangles exceed shared memory", S.Nt);
+        float4* AE = nullptr;
+        uint32_t* SV = nullptr;
+        if ((s = dalloc(ctx, pool, &AE, (size_t)aes_of(NL) / 4 * Np)) || (s = dalloc(ctx, pool, &SV, (size_t)NW * Np))) return s;
+        const float* dint = nullptr;
+        if ((s = dput(ctx, pool, &dint, hs.inten))) return s;
+        CKR(RC_DISPATCH(NL, build(NW, d, g, S.grid, dL, dint, AE, SV, S.Np, ctx->flags_dev, ctx->stream)));
+        d.AE = AE;
+        d.SV = SV;
+    }
+    const int npairs = S.NS * S.NS;
+    S.ev.resize((size_t)npairs * (1 + NL));
+    for (int e = 0; e < npairs; ++e) {
+        for (int kind = 0; kind <= NL; ++kind) {
+            int cnt = 0;
+            r.get(&cnt, 1);
+            if (r.bad || cnt < 0) return fail(ctx, RC_ERR_FORMAT, "scene: truncated event lists");
+            auto raw = r.vec<int>((size_t)cnt);
+            if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated event lists");
+            auto& dst = S.ev[(size_t)e * (1 + NL) + kind];
+            if (S.fmt == 3) dst = raw;
+            else {
+                for (int v : raw) if (v < 0 || v >= 16 * 8 * 6) return fail(ctx, RC_ERR_FORMAT, "event voxel out of range");
+                dst = to_grid(raw, S.grid.vx, S.grid.vy, S.grid.vz);
+            }
+            for (int v : dst) if (v < 0 || v >= S.grid.vx * S.grid.vy * S.grid.vz) return fail(ctx, RC_ERR_FORMAT, "event voxel out of range");
+        }
+    }
+    S.ev_dev.resize(S.ev.size());
+    for (size_t e = 0; e < S.ev.size(); ++e) {
+        if (S.ev[e].empty()) { S.ev_dev[e] = nullptr; continue; }
+        const int* p = nullptr;
+        if ((s = dput(ctx, pool, &p, S.ev[e]))) return s;
+        S.ev_dev[e] = p;
+    }
+    CKR(cudaStreamSynchronize(ctx->stream));
+    ctx->S = std::move(S);
+    return RC_OK;
+}
+
+}  // namespace
+
+namespace {
+
+rc_status alloc_cache(rc_ctx* ctx) {
+    free_pool(ctx->cache_bufs);
+    ctx->err_cap = 0;
+    const Scene& S = ctx->S;
+    const size_t Np = (size_t)S.Np, LCS = (size_t)lcs_of(S.NL), NW = (size_t)ctx->NW, NR = (size_t)S.NR;
+    const size_t G = (Np + BLOCK - 1) / BLOCK;
+    DevCache& c = ctx->c;
+    auto& pool = ctx->cache_bufs;
+    rc_status s;
+    if ((s = dalloc(ctx, pool, &c.Lc, LCS * Np)) || (s = dalloc(ctx, pool, &c.Lc2, LCS * Np)) ||
+        (s = dalloc(ctx, pool, &c.m, LCS * Np)) || (s = dalloc(ctx, pool, &c.n, Np)) || (s = dalloc(ctx, pool, &c.c0, Np)) ||
+        (s = dalloc(ctx, pool, &c.kk, Np)) || (s = dalloc(ctx, pool, &c.pending, Np)) || (s = dalloc(ctx, pool, &c.cur, NW * Np)) ||
+        (s = dalloc(ctx, pool, &c.prev, NW * Np)) || (s = dalloc(ctx, pool, &c.stale, Np)) || (s = dalloc(ctx, pool, &c.age, Np)) ||
+        (s = dalloc(ctx, pool, &c.snap, (size_t)KSNAP * Np * LCS)) || (s = dalloc(ctx, pool, &c.neq, NR * NEQ)) ||
+        (s = dalloc(ctx, pool, &c.coef, NR * KSNAP)) || (s = dalloc(ctx, pool, &c.rstat, 4 * NR)) ||
+        (s = dalloc(ctx, pool, &c.dstat, 3 * NR)) || (s = dalloc(ctx, pool, &c.sumpr, 2)) || (s = dalloc(ctx, pool, &c.npend, 2)) ||
+        (s = dalloc(ctx, pool, &c.partf, G)) || (s = dalloc(ctx, pool, &c.partd, 3 * G)) || (s = dalloc(ctx, pool, &c.parti, G)) ||
+        (s = dalloc(ctx, pool, &c.ticket, 4)) || (s = dalloc(ctx, pool, &c.check, 2)))
+        return s;
+    CKR(cudaMemsetAsync(c.ticket, 0, 16, ctx->stream));
+    CKR(cudaMemsetAsync(c.check, 0, 16, ctx->stream));
+    CKR(cudaMemsetAsync(c.snap, 0, (size_t)KSNAP * Np * LCS * 4, ctx->stream));
+    CKR(cudaMemsetAsync(c.m, 0, LCS * Np * 4, ctx->stream));
+    CKR(cudaMemsetAsync(c.kk, 0, Np * 4, ctx->stream));
+    CKR(cudaMemsetAsync(c.c0, 0, Np * 4, ctx->stream));
+    CKR(cudaMemsetAsync(c.neq, 0, NR * NEQ * 4, ctx->stream));
+    CKR(cudaMemsetAsync(c.coef, 0, NR * KSNAP * 4, ctx->stream));
+    CKR(cudaMemsetAsync(c.rstat, 0, 4 * NR * 4, ctx->stream));
+    CKR(cudaMemsetAsync(c.dstat, 0, 3 * NR * 4, ctx->stream));
+    c.flags = ctx->flags_dev;
+    c.err = nullptr;
+    double b = 0;
+    for (auto& x : pool) b += (double)x.n;
+    ctx->cache_bytes = b;
+    return RC_OK;
+}
+
+rc_status ensure_err(rc_ctx* ctx, size_t frames) {
+    if (frames <= ctx->err_cap) return RC_OK;
+    size_t cap = std::max<size_t>(1024, frames * 2);
+    double* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, cap * 3 * sizeof(double));
+    if (e != cudaSuccess) return fail(ctx, RC_ERR_NOMEM, "error buffer: %s", cudaGetErrorString(e));
+    if (ctx->c.err) {
+        CKR(cudaMemcpyAsync(p, ctx->c.err, ctx->err_cap * 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        CKR(cudaStreamSynchronize(ctx->stream));
+        for (auto it = ctx->cache_bufs.begin(); it != ctx->cache_bufs.end(); ++it)
+            if (it->p == ctx->c.err) { cudaFree(it->p); ctx->cache_bufs.erase(it); break; }
+    }
+    ctx->cache_bufs.push_back({p, cap * 3 * sizeof(double)});
+    ctx->c.err = p;
+    ctx->err_cap = cap;
+    return RC_OK;
+}
+
+// One event of Runner::run (poc_gpu.cu:856-943) as an event program for k_event.
+struct EvBuilder {
+    EvProgram ev{};
+    // pending-count bookkeeping of the reference: every verification step resets the count
+    // (cudaMemset of npend) and publishes its own count; a restore without verification
+    // leaves it at zero
+    int last_reset = -1;
+    bool any_count = false;
+    bool zero_after = false;
+    bool ok = true;
+    EvOp& add(int kind) {
+        if (ev.nops >= MAX_EV_OPS) { ok = false; return ev.ops[MAX_EV_OPS - 1]; }
+        EvOp& o = ev.ops[ev.nops++];
+        memset(&o, 0, sizeof o);
+        o.kind = kind;
+        return o;
+    }
+    void counting_op(EvOp& o) {
+        last_reset = ev.nops - 1;
+        any_count = true;
+        zero_after = false;
+        o.count = 1;
+    }
+    void finish() {
+        for (int k = 0; k < ev.nops; ++k)
+            if (ev.ops[k].count && k != last_reset) ev.ops[k].count = 0;
+        ev.npend_mode = zero_after ? 2 : (any_count ? 1 : 0);
+    }
+};
+
+rc_status do_event(rc_ctx* ctx, int e, int si) {
+    Scene& S = ctx->S;
+    Run& R = ctx->run;
+    const rc_method& M = R.M;
+    const int NL = S.NL, f = R.f;
+    const int pe = e * S.NS + si;
+    EvBuilder B;
+    B.ev.Np = S.Np;
+    B.ev.NR = S.NR;
+    B.ev.nmax = R.nmax;
+    if (M.snaps && f - R.last_event_f >= 20) {
+        int k = -1;
+        for (int a = 0; a < R.nslots; ++a) if (R.slot_state[a] == e) k = a;
+        if (k < 0) { if (R.nslots < KSNAP) k = R.nslots++; else { k = R.slot_next; R.slot_next = (R.slot_next + 1) % KSNAP; } }
+        R.slot_state[k] = e;
+        EvOp& o = B.add(EV_SNAP_SAVE);
+        o.a = k;
+    }
+    if (M.oracle && S.has_ref) {
+        EvOp& o = B.add(EV_ORACLE);
+        o.r0 = S.st[e].d.ref;
+        o.r1 = S.st[si].d.ref;
+    }
+    auto rescale = [&](int l, float ratio) {
+        EvOp& o = B.add(EV_RESCALE);
+        o.a = l;
+        o.x = ratio;
+    };
+    if (M.rescale && !M.deps) {
+        for (int l = 0; l < NL; ++l) {
+            float a = S.st[e].inten[l], b = S.st[si].inten[l];
+            if (a == b) continue;
+            if (M.memory && a > 0 && b == 0) { R.dormant |= 1 << l; R.ilearn[l] = a; }
+            else if (M.memory && a == 0 && b > 0 && ((R.dormant >> l) & 1)) { rescale(l, b / R.ilearn[l]); R.dormant &= ~(1 << l); }
+            else if (a > 0) rescale(l, b / a);
+        }
+    }
+    if (M.deps) {
+        int woke = 0;
+        for (int l = 0; l < NL; ++l) {
+            float a = S.st[e].inten[l], b = S.st[si].inten[l];
+            if (a == b) continue;
+            if (M.memory && a > 0 && b == 0) { R.dormant |= 1 << l; R.ilearn[l] = a; }
+            else if (M.memory && a == 0 && b > 0 && ((R.dormant >> l) & 1)) {
+                rescale(l, b / R.ilearn[l]);
+                R.dormant &= ~(1 << l);
+                woke |= 1 << l;
+                EvOp& o = B.add(EV_WAKE);
+                o.a = l;
+                o.b = M.wake_verify ? 1 : 0;
+                o.dormant = R.dormant;
+                if (M.wake_verify) {
+                    B.counting_op(o);
+                    B.ev.zero_rstat = 1;
+                    R.pend_left = VERIF_FRAMES;
+                }
+            } else if (a > 0) rescale(l, b / a);
+        }
+        for (int l = 0; l < NL; ++l) {
+            const auto& V = S.ev[(size_t)pe * (1 + NL) + 1 + l];
+            if (!V.empty() && !((woke >> l) & 1)) {
+                EvOp& o = B.add(EV_TOUCHED);
+                o.a = 0;
+                o.b = (int)V.size();
+                o.list = S.ev_dev[(size_t)pe * (1 + NL) + 1 + l];
+                o.dormant = R.dormant;
+            }
+        }
+        const auto& occ = S.ev[(size_t)pe * (1 + NL)];
+        if (!occ.empty()) {
+            if (M.verify) {
+                EvOp& o = B.add(EV_TOUCHED);
+                o.a = 1;
+                o.b = (int)occ.size();
+                o.list = S.ev_dev[(size_t)pe * (1 + NL)];
+                o.dormant = R.dormant;
+                B.counting_op(o);
+                B.ev.zero_rstat = 1;
+                R.pend_left = VERIF_FRAMES;
+            } else if (R.dormant) {
+                EvOp& o = B.add(EV_TOUCHED);
+                o.a = 2;
+                o.b = (int)occ.size();
+                o.list = S.ev_dev[(size_t)pe * (1 + NL)];
+                o.dormant = R.dormant;
+            }
+        }
+    }
+    if (M.snaps) {
+        int hit = -1;
+        for (int a = 0; a < R.nslots; ++a) if (R.slot_state[a] == si) hit = a;
+        if (hit >= 0) {
+            EvOp& o = B.add(EV_SNAP_RESTORE);
+            o.a = hit;
+            EvOp& r = B.add(EV_RESTORED);
+            r.a = M.snap_verify ? 1 : 0;
+            r.dormant = R.dormant;
+            if (M.snap_verify) {
+                B.counting_op(r);
+                B.ev.zero_rstat = 1;
+                R.pend_left = VERIF_FRAMES;
+            } else {
+                B.zero_after = true;
+                B.any_count = false;
+                B.last_reset = -1;
+                R.pend_left = 0;
+            }
+            R.proj_left = 0;
+        } else if (M.proj && R.nslots >= 2) {
+            R.projK = R.nslots;
+            for (int a = 0; a < R.nslots; ++a) R.slot[a] = a;
+            B.ev.zero_neq = 1;
+            R.proj_left = PROJ_FRAMES;
+        }
+    }
+    R.last_event_f = f;
+    B.ev.want_sumpr = M.mode == 1 ? 1 : 0;
+    B.ev.sum_slot = R.sum_cur;
+    B.finish();
+    if (!B.ok) return fail(ctx, RC_ERR_UNSUPPORTED, "event needs more than %d kernel steps", MAX_EV_OPS);
+    if (B.ev.nops == 0 && !B.ev.want_sumpr && B.ev.npend_mode == 0 && !B.ev.zero_rstat && !B.ev.zero_neq) return RC_OK;
+    CKR(RC_DISPATCH(NL, event(B.ev, ctx->c, ctx->stream)));
+    return RC_OK;
+}
+
+// poc_gpu.cu:966-988: per-region FP64 least squares of the snapshot projection (host).
+void proj_solve(const std::vector<float>& q, std::vector<float>& cf, int NR, int K) {
+    for (int r = 0; r < NR; ++r) {
+        const float* Q = &q[(size_t)r * NEQ];
+        if (Q[27] < 24.f) continue;
+        double A[KSNAP][KSNAP + 1];
+        int ix = 0;
+        double tr = 0;
+        for (int a = 0; a < K; ++a) for (int b = a; b < K; ++b) { A[a][b] = A[b][a] = Q[ix++]; }
+        for (int a = 0; a < K; ++a) { A[a][K] = Q[21 + a]; tr += A[a][a]; }
+        for (int a = 0; a < K; ++a) A[a][a] += 1e-3 * tr / K + 1e-9;
+        bool ok = true;
+        for (int a = 0; a < K && ok; ++a) {
+            int pv = a;
+            for (int b = a + 1; b < K; ++b) if (fabs(A[b][a]) > fabs(A[pv][a])) pv = b;
+            if (fabs(A[pv][a]) < 1e-12) { ok = false; break; }
+            for (int t = 0; t <= K; ++t) std::swap(A[a][t], A[pv][t]);
+            for (int b = 0; b < K; ++b)
+                if (b != a) { double m = A[b][a] / A[a][a]; for (int t = a; t <= K; ++t) A[b][t] -= m * A[a][t]; }
+        }
+        if (!ok) continue;
+        bool sane = true;
+        double x[KSNAP];
+        for (int a = 0; a < K; ++a) { x[a] = A[a][K] / A[a][a]; if (!std::isfinite(x[a]) || fabs(x[a]) > 4.0) sane = false; }
+        if (sane) for (int a = 0; a < K; ++a) cf[(size_t)r * KSNAP + a] = (float)x[a];
+    }
+}
+
+FrameParams base_params(rc_ctx* ctx) {
+    const Run& R = ctx->run;
+    const rc_method& M = R.M;
+    FrameParams p{};
+    p.Np = ctx->S.Np;
+    p.NR = ctx->S.NR;
+    p.mode = M.mode;
+    p.budget = M.budget * M.rays;
+    p.nmax = R.nmax;
+    p.seed = R.p.seed;
+    p.frame = (uint32_t)R.f;
+    p.pend_left = R.pend_left;
+    p.dormant = R.dormant;
+    p.resp_mask = M.resp_mask;
+    p.nmax_resp = M.nmax_resp * M.rays;
+    p.ddgi = M.ddgi ? 1 : 0;
+    p.ddgi_h = M.ddgi_h;
+    p.ddgi_thr = M.ddgi_thr;
+    p.ddgi_clamp = M.ddgi_clamp ? 1 : 0;
+    p.ramp = M.ramp ? 1 : 0;
+    p.proj_left = R.proj_left;
+    p.projK = R.projK;
+    for (int a = 0; a < KSNAP; ++a) p.slot[a] = R.slot[a];
+    p.rays = M.rays;
+    p.sum_in = R.sum_cur;
+    p.sum_out = 1 - R.sum_cur;
+    p.brute = (ctx->cfg.flags & RC_FLAG_BRUTE_FORCE) ? 1 : 0;
+    p.check = (ctx->cfg.flags & RC_FLAG_CHECK_TRACE) ? 1 : 0;
+    return p;
+}
+
+rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
+    Scene& S = ctx->S;
+    Run& R = ctx->run;
+    const rc_method& M = R.M;
+    const int f = R.f;
+    cudaStream_t st = ctx->stream;
+    rc_status s;
+    if (f > 0 && R.prev_state != si) {
+        if (tm) CKR(cudaEventRecord(ctx->ev[4], st));
+        if ((s = do_event(ctx, R.prev_state, si)) != RC_OK) return s;
+        if (tm) {
+            CKR(cudaEventRecord(ctx->ev[5], st));
+            CKR(cudaEventSynchronize(ctx->ev[5]));
+            float ms;
+            cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+            tm->event += ms;
+            tm->events++;
+        }
+    }
+    R.prev_state = si;
+    const DState& d = S.st[si].d;
+    FrameParams p = base_params(ctx);
+    const bool rec_err = want_err && S.has_ref;
+    if (rec_err && (s = ensure_err(ctx, (size_t)R.nerr + 1)) != RC_OK) return s;
+    p.want_err = rec_err ? 1 : 0;
+    p.err_frame = R.nerr;
+    if (M.ddgi) CKR(cudaMemsetAsync(ctx->c.dstat, 0, 3 * (size_t)S.NR * 4, st));
+    if (tm) CKR(cudaEventRecord(ctx->ev[0], st));
+    const bool track = M.deps && (f % (M.track_every > 0 ? M.track_every : 1) == 0);
+    if (M.deps && f % 32 == 0) {
+        std::swap(ctx->c.cur, ctx->c.prev);
+        p.mask_op = track ? MASK_FRESH : MASK_ZERO;
+    } else {
+        p.mask_op = track ? MASK_OR : MASK_NONE;
+    }
+    if (tm) CKR(cudaEventRecord(ctx->ev[1], st));
+    const bool proj_apply_now = R.proj_left == 1;
+    const bool fused = R.pend_left == 0 && R.proj_left == 0 && !M.ddgi;
+    if (fused) {
+        CKR(RC_DISPATCH(S.NL, frame(ctx->NW, track, true, d, S.g, S.grid, ctx->c, p, st)));
+        if (tm) { CKR(cudaEventRecord(ctx->ev[2], st)); CKR(cudaEventRecord(ctx->ev[3], st)); }
+    } else {
+        CKR(RC_DISPATCH(S.NL, frame(ctx->NW, track, false, d, S.g, S.grid, ctx->c, p, st)));
+        if (tm) CKR(cudaEventRecord(ctx->ev[2], st));
+        FrameParams pu = p;
+        pu.decide = R.pend_left > 0 ? 1 : 0;
+        if (tm) CKR(cudaEventRecord(ctx->ev[3], st));
+        if (proj_apply_now) pu.want_err = 0;
+        CKR(RC_DISPATCH(S.NL, update(d, S.g, ctx->c, pu, st)));
+        if (R.pend_left > 0) R.pend_left--;
+    }
+    R.sum_cur = 1 - R.sum_cur;
+    std::swap(ctx->c.Lc, ctx->c.Lc2);
+    if (R.proj_left > 0 && --R.proj_left == 0) {
+        const size_t nq = (size_t)S.NR * NEQ;
+        std::vector<float> q(nq), cf((size_t)S.NR * KSNAP, NAN);
+        CKR(cudaMemcpyAsync(q.data(), ctx->c.neq, nq * 4, cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));
+        proj_solve(q, cf, S.NR, R.projK);
+        CKR(cudaMemcpyAsync(ctx->c.coef, cf.data(), cf.size() * 4, cudaMemcpyHostToDevice, st));
+        FrameParams pp = base_params(ctx);
+        CKR(RC_DISPATCH(S.NL, proj_apply(ctx->c, S.g, pp, st)));
+        CKR(cudaStreamSynchronize(st));   // cf lives on this stack frame
+        R.pend_left = VERIF_FRAMES;
+        if (rec_err) {
+            FrameParams pe = base_params(ctx);
+            pe.err_frame = R.nerr;
+            CKR(RC_DISPATCH(S.NL, error(d, ctx->c, pe, st)));
+        }
+    }
+    if (tm) {
+        CKR(cudaEventRecord(ctx->ev[6], st));
+        CKR(cudaEventSynchronize(ctx->ev[6]));
+        float a, b, dd, u;
+        cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&dd, ctx->ev[2], ctx->ev[3]);
+        cudaEventElapsedTime(&u, ctx->ev[3], ctx->ev[6]);
+        tm->swap += a; tm->trace += b; tm->decide += dd; tm->update += u;
+        tm->frames++;
+    }
+    if (rec_err) R.nerr++;
+    R.f = f + 1;
+    return RC_OK;
+}
+
+}  // namespace
+
+// ============================================================================ C ABI
+extern "C" {
+
+int rc_abi_version(void) { return RC_ABI_VERSION; }
+
+const char* rc_status_string(rc_status s) {
+    switch (s) {
+        case RC_OK: return "ok";
+        case RC_ERR_ARG: return "bad argument";
+        case RC_ERR_IO: return "i/o error";
+        case RC_ERR_FORMAT: return "bad scene format";
+        case RC_ERR_CUDA: return "CUDA error";
+        case RC_ERR_NOMEM: return "out of memory";
+        case RC_ERR_STATE: return "call out of order";
+        case RC_ERR_DEVICE: return "device guard tripped";
+        case RC_ERR_UNSUPPORTED: return "unsupported configuration";
+        case RC_ERR_LIGHTS: return "light count mismatch";
+    }
+    return "unknown status";
+}
+
+rc_status rc_create(const rc_config* cfg, rc_ctx** out) {
+    if (!out) return RC_ERR_ARG;
+    *out = nullptr;
+    rc_ctx* ctx = new rc_ctx();
+    if (cfg) ctx->cfg = *cfg;
+    if (ctx->cfg.grid[0] <= 0 || ctx->cfg.grid[1] <= 0 || ctx->cfg.grid[2] <= 0) {
+        ctx->cfg.grid[0] = 8; ctx->cfg.grid[1] = 4; ctx->cfg.grid[2] = 4;
+    }
+    const int nv = ctx->cfg.grid[0] * ctx->cfg.grid[1] * ctx->cfg.grid[2];
+    if (nv % 128 != 0 || nv > 32 * 128) { delete ctx; return RC_ERR_UNSUPPORTED; }
+    ctx->NW = nv / 32;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= ctx->cfg.device || ctx->cfg.device < 0) {
+        cudaGetLastError();
+        delete ctx;
+        return RC_ERR_CUDA;
+    }
+    if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) { delete ctx; return RC_ERR_CUDA; }
+    if (ctx->cfg.stream) ctx->stream = (cudaStream_t)ctx->cfg.stream;
+    else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return RC_ERR_CUDA; }
+        ctx->own_stream = true;
+    }
+    for (auto& e : ctx->ev) cudaEventCreate(&e);
+    if (cudaMalloc(&ctx->flags_dev, 16) != cudaSuccess || cudaMemset(ctx->flags_dev, 0, 16) != cudaSuccess) {
+        rc_destroy(ctx);
+        return RC_ERR_CUDA;
+    }
+    *out = ctx;
+    return RC_OK;
+}
+
+void rc_destroy(rc_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_pool(ctx->cache_bufs);
+    free_pool(ctx->scene_bufs);
+    if (ctx->flags_dev) cudaFree(ctx->flags_dev);
+    for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* rc_last_error(const rc_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+rc_status rc_device_info_get(rc_ctx* ctx, rc_device_info* out) {
+    if (!ctx || !out) return RC_ERR_ARG;
+    cudaDeviceProp pr;
+    CKR(cudaGetDeviceProperties(&pr, ctx->cfg.device));
+    memset(out, 0, sizeof *out);
+    strncpy(out->name, pr.name, sizeof out->name - 1);
+    out->sm_count = pr.multiProcessorCount;
+    out->cc_major = pr.major;
+    out->cc_minor = pr.minor;
+    size_t fr = 0, tot = 0;
+    CKR(cudaMemGetInfo(&fr, &tot));
+    out->mem_used_mb = (double)(tot - fr) / 1048576.0;
+    out->mem_total_mb = (double)tot / 1048576.0;
+    return RC_OK;
+}
+
+rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
+    if (!ctx || !data) return RC_ERR_ARG;
+    CKR(cudaSetDevice(ctx->cfg.device));
+    CKR(cudaStreamSynchronize(ctx->stream));
+    free_pool(ctx->cache_bufs);
+    free_pool(ctx->scene_bufs);
+    ctx->have_scene = false;
+    ctx->run.active = false;
+    ctx->c = DevCache{};
+    ctx->err_cap = 0;
+    rc_status s = load_scene(ctx, (const uint8_t*)data, nbytes);
+    if (s != RC_OK) { free_pool(ctx->scene_bufs); return s; }
+    double b = 0;
+    for (auto& x : ctx->scene_bufs) b += (double)x.n;
+    ctx->S.scene_bytes = b;
+    if ((s = alloc_cache(ctx)) != RC_OK) return s;
+    CKR(cudaStreamSynchronize(ctx->stream));
+    ctx->have_scene = true;
+    return RC_OK;
+}
+
+rc_status rc_scene_load(rc_ctx* ctx, const char* path) {
+    if (!ctx || !path) return RC_ERR_ARG;
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(ctx, RC_ERR_IO, "cannot open scene file %s", path);
+    std::vector<uint8_t> buf;
+    fseek(f, 0, SEEK_END);
+    long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    if (n < 0) { fclose(f); return fail(ctx, RC_ERR_IO, "cannot size %s", path); }
+    buf.resize((size_t)n);
+    size_t got = n ? fread(buf.data(), 1, (size_t)n, f) : 0;
+    fclose(f);
+    if (got != (size_t)n) return fail(ctx, RC_ERR_IO, "short read on %s", path);
+    return rc_scene_load_memory(ctx, buf.data(), buf.size());
+}
+
+rc_status rc_scene_info_get(const rc_ctx* ctx, rc_scene_info* out) {
+    if (!ctx || !out) return RC_ERR_ARG;
+    if (!ctx->have_scene) return RC_ERR_STATE;
+    const Scene& S = ctx->S;
+    out->np = S.Np; out->nq = S.Nq; out->nt = S.Nt; out->ns = S.NS; out->nl = S.NL; out->nr = S.NR;
+    out->has_ref = S.has_ref; out->fmt = S.fmt; out->nw = ctx->NW; out->nst = S.nst; out->nnodes = S.nnodes; out->hsize = S.hsize;
+    out->scene_bytes = S.scene_bytes;
+    out->cache_bytes = ctx->cache_bytes;
+    return RC_OK;
+}
+
+rc_status rc_state_lights(const rc_ctx* ctx, int state, float* inten, int nl) {
+    if (!ctx || !inten) return RC_ERR_ARG;
+    if (!ctx->have_scene) return RC_ERR_STATE;
+    if (state < 0 || state >= ctx->S.NS || nl != ctx->S.NL) return RC_ERR_ARG;
+    memcpy(inten, ctx->S.st[state].inten.data(), sizeof(float) * (size_t)nl);
+    return RC_OK;
+}
+
+rc_status rc_run_begin(rc_ctx* ctx, const rc_method* m, int s0, uint32_t seed) {
+    if (!ctx || !m) return RC_ERR_ARG;
+    if (!ctx->have_scene) return fail(ctx, RC_ERR_STATE, "no scene loaded");
+    Scene& S = ctx->S;
+    if (s0 < 0 || s0 >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", s0);
+    if (!(m->rays > 0.f)) return fail(ctx, RC_ERR_ARG, "rays must be > 0");
+    Run& R = ctx->run;
+    R = Run{};
+    R.M = *m;
+    if (R.M.track_every <= 0) R.M.track_every = 1;
+    cudaStream_t st = ctx->stream;
+    const size_t Np = (size_t)S.Np, LCS = (size_t)lcs_of(S.NL);
+    DevCache& c = ctx->c;
+    // poc_gpu.cu:832-841
+    if (S.has_ref) CKR(cudaMemcpyAsync(c.Lc, S.st[s0].pw, LCS * Np * 4, cudaMemcpyDeviceToDevice, st));
+    else CKR(cudaMemsetAsync(c.Lc, 0, LCS * Np * 4, st));
+    R.nmax = m->nmax * m->rays;
+    {
+        std::vector<float> nm(Np, R.nmax), ag(Np, 1e4f);
+        CKR(cudaMemcpyAsync(c.n, nm.data(), Np * 4, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemcpyAsync(c.age, ag.data(), Np * 4, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemsetAsync(c.pending, 0, Np, st));
+        CKR(cudaMemsetAsync(c.cur, 0, (size_t)ctx->NW * Np * 4, st));
+        CKR(cudaMemsetAsync(c.prev, 0, (size_t)ctx->NW * Np * 4, st));
+        CKR(cudaMemsetAsync(c.stale, 0, Np * 4, st));
+        float sp[2] = {float(S.Np) / (R.nmax + 1.f), 0.f};
+        int z2[2] = {0, 0};
+        CKR(cudaMemcpyAsync(c.sumpr, sp, 8, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemcpyAsync(c.npend, z2, 8, cudaMemcpyHostToDevice, st));
+        CKR(cudaStreamSynchronize(st));   // host vectors above are about to go out of scope
+    }
+    R.p.seed = seed;
+    for (int k = 0; k < KSNAP; ++k) R.slot_state[k] = -1;
+    R.prev_state = s0;
+    R.active = true;
+    return RC_OK;
+}
+
+rc_status rc_frame(rc_ctx* ctx, int state, int want_err) {
+    if (!ctx) return RC_ERR_ARG;
+    if (!ctx->run.active) return fail(ctx, RC_ERR_STATE, "no run begun");
+    if (state < 0 || state >= ctx->S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", state);
+    return frame_impl(ctx, state, want_err, nullptr);
+}
+
+rc_status rc_errors(rc_ctx* ctx, float* out, int max, int* n) {
+    if (!ctx || !n) return RC_ERR_ARG;
+    const int k = ctx->run.nerr;
+    *n = k;
+    if (!out || k == 0) return RC_OK;
+    std::vector<double> h(3 * (size_t)k);
+    CKR(cudaMemcpyAsync(h.data(), ctx->c.err, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CKR(cudaStreamSynchronize(ctx->stream));
+    for (int f = 0; f < k && f < max; ++f) out[f] = float(sqrt(h[3 * f] / h[3 * f + 2]) / (h[3 * f + 1] / h[3 * f + 2]));
+    return RC_OK;
+}
+
+rc_status rc_run(rc_ctx* ctx, const rc_method* m, const int* seq, int nframes, uint32_t seed, int want_err, float* errs,
+                 rc_timers* tm) {
+    if (!ctx || !m || !seq || nframes <= 0) return RC_ERR_ARG;
+    for (int f = 0; f < nframes; ++f)
+        if (seq[f] < 0 || (ctx->have_scene && seq[f] >= ctx->S.NS)) return fail(ctx, RC_ERR_ARG, "state out of range");
+    rc_status s = rc_run_begin(ctx, m, seq[0], seed);
+    if (s != RC_OK) return s;
+    for (int f = 0; f < nframes; ++f)
+        if ((s = frame_impl(ctx, seq[f], want_err, tm)) != RC_OK) return s;
+    if (errs) {
+        int n = 0;
+        if ((s = rc_errors(ctx, errs, nframes, &n)) != RC_OK) return s;
+    }
+    CKR(cudaStreamSynchronize(ctx->stream));
+    return RC_OK;
+}
+
+rc_status rc_sync(rc_ctx* ctx) {
+    if (!ctx) return RC_ERR_ARG;
+    CKR(cudaStreamSynchronize(ctx->stream));
+    return RC_OK;
+}
+
+static bool array_geom(rc_ctx* ctx, int which, size_t* elem, size_t* count, size_t* src_stride, size_t* dst_stride, void** dev) {
+    const Scene& S = ctx->S;
+    const size_t Np = (size_t)S.Np, NL = (size_t)S.NL, LCS = (size_t)lcs_of(S.NL), NR = (size_t)S.NR, NW = (size_t)ctx->NW;
+    DevCache& c = ctx->c;
+    *src_stride = *dst_stride = 0;
+    switch (which) {
+        case RC_A_LC: *elem = 4; *count = NL * Np; *dev = c.Lc; *src_stride = LCS; *dst_stride = NL; return true;
+        case RC_A_LC2: *elem = 4; *count = NL * Np; *dev = c.Lc2; *src_stride = LCS; *dst_stride = NL; return true;
+        case RC_A_M: *elem = 4; *count = NL * Np; *dev = c.m; *src_stride = LCS; *dst_stride = NL; return true;
+        case RC_A_N: *elem = 4; *count = Np; *dev = c.n; return true;
+        case RC_A_C0: *elem = 4; *count = Np; *dev = c.c0; return true;
+        case RC_A_KK: *elem = 4; *count = Np; *dev = c.kk; return true;
+        case RC_A_PENDING: *elem = 1; *count = Np; *dev = c.pending; return true;
+        case RC_A_CUR: *elem = 4; *count = NW * Np; *dev = c.cur; return true;
+        case RC_A_PREV: *elem = 4; *count = NW * Np; *dev = c.prev; return true;
+        case RC_A_STALE: *elem = 4; *count = Np; *dev = c.stale; return true;
+        case RC_A_AGE: *elem = 4; *count = Np; *dev = c.age; return true;
+        case RC_A_SNAP: *elem = 4; *count = (size_t)KSNAP * Np * NL; *dev = c.snap; *src_stride = LCS; *dst_stride = NL; return true;
+        case RC_A_NEQ: *elem = 4; *count = NR * NEQ; *dev = c.neq; return true;
+        case RC_A_COEF: *elem = 4; *count = NR * KSNAP; *dev = c.coef; return true;
+        case RC_A_RSTAT: *elem = 4; *count = 4 * NR; *dev = c.rstat; return true;
+        case RC_A_DSTAT: *elem = 4; *count = 3 * NR; *dev = c.dstat; return true;
+        case RC_A_SUMPR: *elem = 4; *count = 2; *dev = c.sumpr; return true;
+        case RC_A_NPEND: *elem = 4; *count = 2; *dev = c.npend; return true;
+    }
+    return false;
+}
+
+rc_status rc_array_info(rc_ctx* ctx, int which, size_t* nbytes, void** dev_ptr) {
+    if (!ctx || !nbytes) return RC_ERR_ARG;
+    if (!ctx->have_scene) return RC_ERR_STATE;
+    size_t elem, count, ss, ds;
+    void* dev;
+    if (!array_geom(ctx, which, &elem, &count, &ss, &ds, &dev)) return RC_ERR_ARG;
+    *nbytes = elem * count;
+    if (dev_ptr) *dev_ptr = dev;
+    return RC_OK;
+}
+
+rc_status rc_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, int to_device) {
+    if (!ctx || !host) return RC_ERR_ARG;
+    if (!ctx->have_scene) return RC_ERR_STATE;
+    size_t elem, count, ss, ds;
+    void* dev;
+    if (!array_geom(ctx, which, &elem, &count, &ss, &ds, &dev)) return RC_ERR_ARG;
+    if (nbytes != elem * count) return fail(ctx, RC_ERR_ARG, "array %d is %zu bytes, not %zu", which, elem * count, nbytes);
+    if (which == RC_A_SUMPR && to_device) {
+        // logical slot 0 = the value the next frame reads
+        float v[2];
+        memcpy(v, host, 8);
+        float d[2];
+        d[ctx->run.sum_cur] = v[0];
+        d[1 - ctx->run.sum_cur] = v[1];
+        CKR(cudaMemcpyAsync(dev, d, 8, cudaMemcpyHostToDevice, ctx->stream));
+        CKR(cudaStreamSynchronize(ctx->stream));
+        return RC_OK;
+    }
+    if (ss) {
+        // padded device rows of ss elements, packed host rows of ds elements
+        const size_t rows = count / ds;
+        if (to_device) CKR(cudaMemcpy2DAsync(dev, ss * elem, host, ds * elem, ds * elem, rows, cudaMemcpyHostToDevice, ctx->stream));
+        else CKR(cudaMemcpy2DAsync(host, ds * elem, dev, ss * elem, ds * elem, rows, cudaMemcpyDeviceToHost, ctx->stream));
+    } else {
+        CKR(cudaMemcpyAsync(to_device ? dev : host, to_device ? host : dev, nbytes,
+                            to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CKR(cudaStreamSynchronize(ctx->stream));
+    if (which == RC_A_SUMPR && !to_device) {
+        float v[2];
+        memcpy(v, host, 8);
+        float o[2] = {v[ctx->run.sum_cur], v[1 - ctx->run.sum_cur]};
+        memcpy(host, o, 8);
+    }
+    return RC_OK;
+}
+
+rc_status rc_scalar_get(rc_ctx* ctx, int which, int* value) {
+    if (!ctx || !value) return RC_ERR_ARG;
+    const Run& R = ctx->run;
+    switch (which) {
+        case RC_S_PEND_LEFT: *value = R.pend_left; return RC_OK;
+        case RC_S_DORMANT: *value = R.dormant; return RC_OK;
+        case RC_S_PROJ_LEFT: *value = R.proj_left; return RC_OK;
+        case RC_S_FRAME: *value = R.f; return RC_OK;
+        case RC_S_NSLOTS: *value = R.nslots; return RC_OK;
+        case RC_S_LAST_EVENT: *value = R.last_event_f; return RC_OK;
+        case RC_S_PROJK: *value = R.projK; return RC_OK;
+    }
+    return RC_ERR_ARG;
+}
+
+rc_status rc_scalar_set(rc_ctx* ctx, int which, int value) {
+    if (!ctx) return RC_ERR_ARG;
+    Run& R = ctx->run;
+    switch (which) {
+        case RC_S_PEND_LEFT: R.pend_left = value; return RC_OK;
+        case RC_S_DORMANT: R.dormant = value; return RC_OK;
+        case RC_S_PROJ_LEFT: R.proj_left = value; return RC_OK;
+        case RC_S_FRAME: R.f = value; return RC_OK;
+        case RC_S_NSLOTS: R.nslots = value; return RC_OK;
+        case RC_S_LAST_EVENT: R.last_event_f = value; return RC_OK;
+        case RC_S_PROJK: R.projK = value; return RC_OK;
+    }
+    return RC_ERR_ARG;
+}
+
+rc_status rc_state_array_copy(rc_ctx* ctx, int state, int which, void* host, size_t nbytes) {
+    if (!ctx || !host) return RC_ERR_ARG;
+    if (!ctx->have_scene) return RC_ERR_STATE;
+    const Scene& S = ctx->S;
+    if (state < 0 || state >= S.NS) return RC_ERR_ARG;
+    const size_t Np = (size_t)S.Np, NL = (size_t)S.NL, AES = (size_t)aes_of(S.NL);
+    const DState& d = S.st[state].d;
+    cudaStream_t st = ctx->stream;
+    switch (which) {
+        case RC_SA_EDIR:
+            if (nbytes != 4 * NL * Np) return RC_ERR_ARG;
+            CKR(cudaMemcpy2DAsync(host, NL * 4, (const float*)d.AE + 1, AES * 4, NL * 4, Np, cudaMemcpyDeviceToHost, st));
+            break;
+        case RC_SA_SV:
+            if (nbytes != 4 * (size_t)ctx->NW * Np) return RC_ERR_ARG;
+            CKR(cudaMemcpyAsync(host, d.SV, nbytes, cudaMemcpyDeviceToHost, st));
+            break;
+        case RC_SA_REF:
+            if (!S.has_ref || nbytes != 4 * Np) return RC_ERR_ARG;
+            CKR(cudaMemcpyAsync(host, d.ref, nbytes, cudaMemcpyDeviceToHost, st));
+            break;
+        case RC_SA_VALID:
+            if (!S.has_ref || nbytes != Np) return RC_ERR_ARG;
+            CKR(cudaMemcpyAsync(host, d.valid, nbytes, cudaMemcpyDeviceToHost, st));
+            break;
+        case RC_SA_PW:
+            if (!S.has_ref || nbytes != 4 * NL * Np) return RC_ERR_ARG;
+            CKR(cudaMemcpy2DAsync(host, NL * 4, S.st[state].pw, (size_t)lcs_of(S.NL) * 4, NL * 4, Np, cudaMemcpyDeviceToHost, st));
+            break;
+        default:
+            return RC_ERR_ARG;
+    }
+    CKR(cudaStreamSynchronize(st));
+    return RC_OK;
+}
+
+rc_status rc_probe_rays(rc_ctx* ctx, int state, const int* points, int npoints, rc_ray_rec* out, int maxrec, int* nrec) {
+    if (!ctx || !points || !out || !nrec || npoints < 0 || maxrec < 0) return RC_ERR_ARG;
+    if (!ctx->run.active) return fail(ctx, RC_ERR_STATE, "no run begun");
+    const Scene& S = ctx->S;
+    if (state < 0 || state >= S.NS) return RC_ERR_ARG;
+    *nrec = 0;
+    if (npoints == 0) return RC_OK;
+    int* dpts = nullptr;
+    int* dn = nullptr;
+    void* drec = nullptr;
+    CKR(cudaMalloc(&dpts, sizeof(int) * (size_t)npoints));
+    CKR(cudaMalloc(&dn, sizeof(int)));
+    CKR(cudaMalloc(&drec, sizeof(rc_ray_rec) * (size_t)(maxrec > 0 ? maxrec : 1)));
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(dpts, points, sizeof(int) * (size_t)npoints, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(dn, 0, sizeof(int), st);
+    FrameParams p = base_params(ctx);
+    cudaError_t e = RC_DISPATCH(S.NL, probe(ctx->NW, S.st[state].d, S.g, S.grid, ctx->c, p, dpts, npoints, drec, maxrec, dn, st));
+    int n = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&n, dn, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && n > 0) e = cudaMemcpy(out, drec, sizeof(rc_ray_rec) * (size_t)std::min(n, maxrec), cudaMemcpyDeviceToHost);
+    cudaFree(dpts);
+    cudaFree(dn);
+    cudaFree(drec);
+    if (e != cudaSuccess) return fail(ctx, RC_ERR_CUDA, "probe: %s", cudaGetErrorString(e));
+    *nrec = std::min(n, maxrec);
+    return RC_OK;
+}
+
+rc_status rc_trace_check_count(rc_ctx* ctx, long long* mismatches, long long* rays) {
+    if (!ctx || !mismatches || !rays) return RC_ERR_ARG;
+    if (!ctx->have_scene) return RC_ERR_STATE;
+    unsigned long long h[2];
+    CKR(cudaMemcpyAsync(h, ctx->c.check, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CKR(cudaMemsetAsync(ctx->c.check, 0, 16, ctx->stream));
+    CKR(cudaStreamSynchronize(ctx->stream));
+    *mismatches = (long long)h[0];
+    *rays = (long long)h[1];
+    return RC_OK;
+}
+
+rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags) {
+    if (!ctx || !flags) return RC_ERR_ARG;
+    CKR(cudaMemcpyAsync(flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CKR(cudaMemsetAsync(ctx->flags_dev, 0, 4, ctx->stream));
+    CKR(cudaStreamSynchronize(ctx->stream));
+    return RC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,270 @@
+"""ctypes binding of the C ABI (include/rc_api.h) for Python callers, tests and the benchmark.
+
+The binding loads ``render_engine_gb300/_build/librc_gb300.so``; when the library is missing
+it raises instead of falling back to anything else.  Build it with
+``python -m render_engine_gb300.build`` (or ``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .methods import CMethod, Method, to_c
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "librc_gb300.so")
+
+RC_OK = 0
+STATUS = {0: "ok", 1: "bad argument", 2: "i/o error", 3: "bad scene format", 4: "CUDA error", 5: "out of memory",
+          6: "call out of order", 7: "device guard tripped", 8: "unsupported configuration", 9: "light count mismatch"}
+
+(A_LC, A_LC2, A_M, A_N, A_C0, A_KK, A_PENDING, A_CUR, A_PREV, A_STALE, A_AGE, A_SNAP, A_NEQ, A_COEF, A_RSTAT,
+ A_DSTAT, A_SUMPR, A_NPEND) = range(18)
+ARRAY_DTYPE = {A_LC: np.float32, A_LC2: np.float32, A_M: np.float32, A_N: np.float32, A_C0: np.float32,
+               A_KK: np.int32, A_PENDING: np.uint8, A_CUR: np.uint32, A_PREV: np.uint32, A_STALE: np.uint32,
+               A_AGE: np.float32, A_SNAP: np.float32, A_NEQ: np.float32, A_COEF: np.float32, A_RSTAT: np.float32,
+               A_DSTAT: np.float32, A_SUMPR: np.float32, A_NPEND: np.int32}
+(S_PEND_LEFT, S_DORMANT, S_PROJ_LEFT, S_FRAME, S_NSLOTS, S_LAST_EVENT, S_PROJK) = range(7)
+SA_EDIR, SA_SV, SA_REF, SA_VALID, SA_PW = range(5)
+FLAG_BRUTE_FORCE = 1
+FLAG_CHECK_TRACE = 2
+
+# Exported symbols, one per declaration of include/rc_api.h.
+EXPORTS = [
+    "rc_abi_version", "rc_status_string", "rc_create", "rc_destroy", "rc_last_error", "rc_device_info_get",
+    "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
+    "rc_errors", "rc_run", "rc_sync", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
+    "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_device_flags",
+]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("grid", ctypes.c_int * 3), ("device", ctypes.c_int), ("stream", ctypes.c_void_p),
+                ("flags", ctypes.c_uint), ("expect_lights", ctypes.c_int)]
+
+
+class Timers(ctypes.Structure):
+    _fields_ = [("trace", ctypes.c_double), ("decide", ctypes.c_double), ("update", ctypes.c_double),
+                ("swap", ctypes.c_double), ("event", ctypes.c_double), ("frames", ctypes.c_int), ("events", ctypes.c_int)]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("np", "nq", "nt", "ns", "nl", "nr", "has_ref", "fmt", "nw", "nst", "nnodes", "hsize")] + \
+               [("scene_bytes", ctypes.c_double), ("cache_bytes", ctypes.c_double)]
+
+
+class DeviceInfo(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 256), ("sm_count", ctypes.c_int), ("cc_major", ctypes.c_int),
+                ("cc_minor", ctypes.c_int), ("mem_used_mb", ctypes.c_double), ("mem_total_mb", ctypes.c_double)]
+
+
+class RayRec(ctypes.Structure):
+    _fields_ = [("point", ctypes.c_int), ("ray", ctypes.c_int), ("q", ctypes.c_int), ("pi", ctypes.c_int),
+                ("back", ctypes.c_int), ("t", ctypes.c_float)]
+
+
+_lib = None
+
+
+def load_library():
+    """Load the native library; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("render_engine_gb300: native library missing (%s); run the build first" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ip, i, u32, sz = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_uint32, ctypes.c_size_t
+    L.rc_abi_version.restype = i
+    L.rc_status_string.restype = ctypes.c_char_p
+    L.rc_status_string.argtypes = [i]
+    L.rc_create.restype = i
+    L.rc_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+    L.rc_destroy.argtypes = [vp]
+    L.rc_last_error.restype = ctypes.c_char_p
+    L.rc_last_error.argtypes = [vp]
+    L.rc_device_info_get.restype = i
+    L.rc_device_info_get.argtypes = [vp, ctypes.POINTER(DeviceInfo)]
+    L.rc_scene_load.restype = i
+    L.rc_scene_load.argtypes = [vp, ctypes.c_char_p]
+    L.rc_scene_load_memory.restype = i
+    L.rc_scene_load_memory.argtypes = [vp, vp, sz]
+    L.rc_scene_info_get.restype = i
+    L.rc_scene_info_get.argtypes = [vp, ctypes.POINTER(SceneInfo)]
+    L.rc_state_lights.restype = i
+    L.rc_state_lights.argtypes = [vp, i, ctypes.POINTER(ctypes.c_float), i]
+    L.rc_run_begin.restype = i
+    L.rc_run_begin.argtypes = [vp, ctypes.POINTER(CMethod), i, u32]
+    L.rc_frame.restype = i
+    L.rc_frame.argtypes = [vp, i, i]
+    L.rc_errors.restype = i
+    L.rc_errors.argtypes = [vp, ctypes.POINTER(ctypes.c_float), i, ip]
+    L.rc_run.restype = i
+    L.rc_run.argtypes = [vp, ctypes.POINTER(CMethod), ip, i, u32, i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(Timers)]
+    L.rc_sync.restype = i
+    L.rc_sync.argtypes = [vp]
+    L.rc_array_info.restype = i
+    L.rc_array_info.argtypes = [vp, i, ctypes.POINTER(sz), ctypes.POINTER(vp)]
+    L.rc_array_copy.restype = i
+    L.rc_array_copy.argtypes = [vp, i, vp, sz, i]
+    L.rc_scalar_get.restype = i
+    L.rc_scalar_get.argtypes = [vp, i, ip]
+    L.rc_scalar_set.restype = i
+    L.rc_scalar_set.argtypes = [vp, i, i]
+    L.rc_state_array_copy.restype = i
+    L.rc_state_array_copy.argtypes = [vp, i, i, vp, sz]
+    L.rc_probe_rays.restype = i
+    L.rc_probe_rays.argtypes = [vp, i, ip, i, ctypes.POINTER(RayRec), i, ip]
+    L.rc_trace_check_count.restype = i
+    L.rc_trace_check_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
+    L.rc_device_flags.restype = i
+    L.rc_device_flags.argtypes = [vp, ctypes.POINTER(ctypes.c_uint)]
+    _lib = L
+    return L
+
+
+class RCError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Context:
+    """One radiance-cache context on one GPU (rc_create / rc_destroy)."""
+
+    def __init__(self, grid=(8, 4, 4), device: int = 0, flags: int = 0, expect_lights: int = 0, stream: int | None = None):
+        self.L = load_library()
+        cfg = Config()
+        cfg.grid[0], cfg.grid[1], cfg.grid[2] = grid
+        cfg.device = device
+        cfg.flags = flags
+        cfg.expect_lights = expect_lights
+        cfg.stream = stream
+        h = ctypes.c_void_p()
+        st = self.L.rc_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != RC_OK:
+            raise RCError(st, "rc_create failed (is a GPU available?)")
+        self.h = h
+        self.grid = tuple(grid)
+
+    def _chk(self, st: int):
+        if st != RC_OK:
+            raise RCError(st, self.L.rc_last_error(self.h).decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.rc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def device_info(self) -> dict:
+        d = DeviceInfo()
+        self._chk(self.L.rc_device_info_get(self.h, ctypes.byref(d)))
+        return {"name": d.name.decode(), "sm_count": d.sm_count, "cc": (d.cc_major, d.cc_minor),
+                "mem_used_mb": d.mem_used_mb, "mem_total_mb": d.mem_total_mb}
+
+    def load(self, path: str):
+        self._chk(self.L.rc_scene_load(self.h, path.encode()))
+        return self.info()
+
+    def load_bytes(self, data):
+        buf = data if isinstance(data, np.ndarray) else np.frombuffer(data, np.uint8)
+        self._chk(self.L.rc_scene_load_memory(self.h, buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes))
+        return self.info()
+
+    def info(self) -> dict:
+        s = SceneInfo()
+        self._chk(self.L.rc_scene_info_get(self.h, ctypes.byref(s)))
+        self._info = {n: getattr(s, n) for n, _ in SceneInfo._fields_}
+        return self._info
+
+    def state_lights(self, state: int) -> np.ndarray:
+        nl = self._info["nl"]
+        out = (ctypes.c_float * nl)()
+        self._chk(self.L.rc_state_lights(self.h, state, out, nl))
+        return np.array(out[:], np.float32)
+
+    def begin(self, method: Method, s0: int, seed: int):
+        self._cm = to_c(method)
+        self._chk(self.L.rc_run_begin(self.h, ctypes.byref(self._cm), s0, seed & 0xFFFFFFFF))
+
+    def frame(self, state: int, want_err: bool = False):
+        self._chk(self.L.rc_frame(self.h, state, 1 if want_err else 0))
+
+    def errors(self) -> np.ndarray:
+        n = ctypes.c_int()
+        self._chk(self.L.rc_errors(self.h, None, 0, ctypes.byref(n)))
+        out = (ctypes.c_float * max(n.value, 1))()
+        self._chk(self.L.rc_errors(self.h, out, n.value, ctypes.byref(n)))
+        return np.array(out[: n.value], np.float32)
+
+    def run(self, method: Method, seq, seed: int, want_err: bool = True, timers: bool = False):
+        cm = to_c(method)
+        arr = (ctypes.c_int * len(seq))(*[int(x) for x in seq])
+        errs = (ctypes.c_float * len(seq))()
+        tm = Timers() if timers else None
+        self._chk(self.L.rc_run(self.h, ctypes.byref(cm), arr, len(seq), seed & 0xFFFFFFFF, 1 if want_err else 0,
+                                errs if want_err else None, ctypes.byref(tm) if timers else None))
+        out = np.array(errs[:], np.float32) if want_err else None
+        if timers:
+            return out, {n: getattr(tm, n) for n, _ in Timers._fields_}
+        return out
+
+    def sync(self):
+        self._chk(self.L.rc_sync(self.h))
+
+    def array(self, which: int) -> np.ndarray:
+        n = ctypes.c_size_t()
+        self._chk(self.L.rc_array_info(self.h, which, ctypes.byref(n), None))
+        a = np.empty(n.value // np.dtype(ARRAY_DTYPE[which]).itemsize, ARRAY_DTYPE[which])
+        self._chk(self.L.rc_array_copy(self.h, which, a.ctypes.data_as(ctypes.c_void_p), a.nbytes, 0))
+        return a
+
+    def set_array(self, which: int, a: np.ndarray):
+        a = np.ascontiguousarray(a, ARRAY_DTYPE[which])
+        self._chk(self.L.rc_array_copy(self.h, which, a.ctypes.data_as(ctypes.c_void_p), a.nbytes, 1))
+
+    def device_ptr(self, which: int) -> int:
+        n = ctypes.c_size_t()
+        p = ctypes.c_void_p()
+        self._chk(self.L.rc_array_info(self.h, which, ctypes.byref(n), ctypes.byref(p)))
+        return p.value
+
+    def scalar(self, which: int) -> int:
+        v = ctypes.c_int()
+        self._chk(self.L.rc_scalar_get(self.h, which, ctypes.byref(v)))
+        return v.value
+
+    def set_scalar(self, which: int, value: int):
+        self._chk(self.L.rc_scalar_set(self.h, which, int(value)))
+
+    def state_array(self, state: int, which: int) -> np.ndarray:
+        inf = self._info
+        np_, nl, nw = inf["np"], inf["nl"], inf["nw"]
+        shape, dt = {SA_EDIR: (nl * np_, np.float32), SA_SV: (nw * np_, np.uint32), SA_REF: (np_, np.float32),
+                     SA_VALID: (np_, np.uint8), SA_PW: (nl * np_, np.float32)}[which]
+        a = np.empty(shape, dt)
+        self._chk(self.L.rc_state_array_copy(self.h, state, which, a.ctypes.data_as(ctypes.c_void_p), a.nbytes))
+        return a
+
+    def probe(self, state: int, points) -> list[tuple]:
+        pts = (ctypes.c_int * len(points))(*[int(x) for x in points])
+        cap = 64 * len(points) + 64
+        out = (RayRec * cap)()
+        n = ctypes.c_int()
+        self._chk(self.L.rc_probe_rays(self.h, state, pts, len(points), out, cap, ctypes.byref(n)))
+        return sorted((r.point, r.ray, r.q, r.pi, r.back, r.t) for r in out[: n.value])
+
+    def check_count(self) -> tuple[int, int]:
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        self._chk(self.L.rc_trace_check_count(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def device_flags(self) -> int:
+        v = ctypes.c_uint()
+        self._chk(self.L.rc_device_flags(self.h, ctypes.byref(v)))
+        return v.value

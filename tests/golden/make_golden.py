@@ -1,0 +1,42 @@
+"""Regenerates the committed golden fixtures from a reference checkout.
+
+Reads, from the reference (falcon123212/render_engine):
+  cuda/scenes/scene_main.bin, cuda/scenes/scene_stress.bin     (its box-scene fixtures)
+  reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl    (its published RTX 4060
+      per-frame error curves: `poc_gpu_l3 scen scene_main.bin 10` and
+      `poc_gpu_l8 scenf scene_stress.bin 10 scenarios_stress.txt`)
+  cuda/scenes/scenarios_stress.txt
+and writes gzip copies of the scenes and the curves as JSON next to this script.
+
+Usage: python tests/golden/make_golden.py [reference checkout, default /root/reference]
+"""
+import gzip
+import json
+import os
+import shutil
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def curves(path):
+    out = []
+    for line in open(path):
+        if not line.startswith("{"):
+            continue
+        r = json.loads(line)
+        if r.get("type") == "scen":
+            out.append({k: r[k] for k in ("scen", "name", "pre", "post", "last", "curve")})
+    return out
+
+
+for name in ("scene_main.bin", "scene_stress.bin"):
+    with open(os.path.join(REF, "cuda", "scenes", name), "rb") as f, gzip.open(os.path.join(HERE, name + ".gz"), "wb", 9) as g:
+        shutil.copyfileobj(f, g)
+shutil.copy(os.path.join(REF, "cuda", "scenes", "scenarios_stress.txt"), os.path.join(HERE, "scenarios_stress.txt"))
+json.dump({"mode": "scen", "seed0": 2000, "nseeds": 10, "rows": curves(os.path.join(REF, "reference", "cuda_rtx4060", "scen_main.jsonl"))},
+          open(os.path.join(HERE, "golden_scen_main.json"), "w"))
+json.dump({"mode": "scenf", "seed0": 3000, "nseeds": 10, "rows": curves(os.path.join(REF, "reference", "cuda_rtx4060", "scen_stress.jsonl"))},
+          open(os.path.join(HERE, "golden_scen_stress.json"), "w"))
+print("golden fixtures written to", HERE)

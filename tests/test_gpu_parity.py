@@ -1,0 +1,182 @@
+"""GPU parity: the product kernels against the reference's own kernels and the CPU oracle.
+
+* Against the reference kernels (cuda/poc_gpu.cu compiled for sm_103a, driven by
+  oracle/refrun.cpp): the per-state build (direct light, shadow-voxel masks) and every frame
+  of full method runs are compared BIT FOR BIT, each frame starting from identical state
+  (the product's state is copied into the reference before the frame).  The only tolerated
+  differences come from region sums that both sides accumulate with float atomics (their
+  order is undefined), which can flip a verification decision at its threshold.
+* Against the CPU oracle: per-ray hit records (primitive id, cache point, distance) and
+  the 10-seed error curves published by the reference (RTX 4060).
+* The plane-culled trace against a brute-force trace of every triangle on the same rays:
+  zero disagreements.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from oracle import pyref
+from render_engine_gb300 import methods as M
+from render_engine_gb300 import native as N
+from render_engine_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+SYNC = [N.A_LC, N.A_N, N.A_C0, N.A_PENDING, N.A_CUR, N.A_PREV, N.A_STALE, N.A_AGE, N.A_SNAP, N.A_NEQ, N.A_COEF,
+        N.A_RSTAT, N.A_DSTAT, N.A_SUMPR, N.A_NPEND]
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built():
+    from render_engine_gb300 import build
+    build.build()
+    from oracle import build as ob
+    ob.build()
+
+
+def _ctx(data, **kw):
+    c = N.Context(**kw)
+    c.load_bytes(data)
+    return c
+
+
+def _sync_to_ref(ctx, ref):
+    for a in SYNC:
+        v = ctx.array(a)
+        if a == N.A_STALE:
+            v = v.astype(np.uint8)
+        ref.set_array(a, v)
+    for s in range(7):
+        ref.set_scalar(s, ctx.scalar(s))
+
+
+def test_state_build_bitexact_vs_reference(scene_main_bytes):
+    if not pyref.available(3):
+        pytest.skip("reference kernels not built")
+    ctx = _ctx(scene_main_bytes)
+    ref = pyref.RefRunner(3, scene_main_bytes)
+    for s in range(ctx.info()["ns"]):
+        assert np.array_equal(ctx.state_array(s, N.SA_EDIR).view(np.uint32), ref.state_array(s, 0).view(np.uint32))
+        assert np.array_equal(ctx.state_array(s, N.SA_SV), ref.state_array(s, 1))
+
+
+def _frames_vs_reference(data, nl, method, seq, seed, exact_frac=1.0):
+    ctx = _ctx(data)
+    ref = pyref.RefRunner(nl, data)
+    ctx.begin(method, seq[0], seed)
+    ref.begin(method, seq[0], seed)
+    worst = 1.0
+    for f, s in enumerate(seq):
+        _sync_to_ref(ctx, ref)
+        verifying = ctx.scalar(N.S_PEND_LEFT) > 0
+        ctx.frame(s)
+        ref.frame(s)
+        a, b = ctx.array(N.A_LC), ref.array(N.A_LC)
+        same = np.mean(a.view(np.uint32) == b.view(np.uint32))
+        na, nb = ctx.array(N.A_N), ref.array(N.A_N)
+        same_n = np.mean(na.view(np.uint32) == nb.view(np.uint32))
+        ca, cb = ctx.array(N.A_CUR), ref.array(N.A_CUR)
+        assert np.array_equal(ca, cb), (f, "dependency masks differ")
+        assert np.array_equal(ctx.array(N.A_PENDING), ref.array(N.A_PENDING)) or verifying, f
+        assert np.array_equal(ctx.array(N.A_STALE).astype(np.uint8), ref.array(N.A_STALE)), f
+        if not verifying and not method.ddgi and not method.proj:
+            assert same == 1.0 and same_n == 1.0, (f, same, same_n)
+        worst = min(worst, same, same_n)
+        assert np.allclose(a, b, rtol=1e-3, atol=1e-6), f
+    assert worst >= exact_frac, worst
+
+
+@pytest.mark.parametrize("name", ["Classique 1.0x", "SHaRC responsive 1.0x", "v3 complet", "v4-A2C suivi 1/4", "DDGI 1.0x"])
+def test_timing_methods_bitexact_vs_reference(scene_main_bytes, name):
+    if not pyref.available(3):
+        pytest.skip("reference kernels not built")
+    m = M.by_name(M.timing_methods(), name)
+    seq = [0] * 35 + [1] * 12 + [2] * 12 + [3] * 12 + [0] * 12
+    _frames_vs_reference(scene_main_bytes, 3, m, seq, 11, exact_frac=0.999)
+
+
+@pytest.mark.parametrize("name", ["v5-A instantanes verifies", "v5-AB instantanes+projection", "Oracle",
+                                  "SHaRC + memoire + instantanes, 1.57x", "v4-A2 memoire verifiee"])
+def test_event_methods_vs_reference(scene_main_bytes, name):
+    if not pyref.available(3):
+        pytest.skip("reference kernels not built")
+    m = M.by_name(M.scen_methods(), name)
+    seq = M.sequence([(0, 25), (1, 22), (2, 22), (3, 12), (0, 24), (1, 6)])
+    _frames_vs_reference(scene_main_bytes, 3, m, seq, 2001, exact_frac=0.99)
+
+
+def test_eight_lights_vs_reference(scene_stress_bytes):
+    if not pyref.available(8):
+        pytest.skip("reference kernels not built")
+    m = M.by_name(M.timing_methods(), "v4-A2C suivi 1/4")
+    seq = [0] * 25 + [3] * 10 + [0] * 10 + [2] * 10 + [4] * 8
+    _frames_vs_reference(scene_stress_bytes, 8, m, seq, 3, exact_frac=0.999)
+
+
+def test_large_generated_scene_vs_reference():
+    if not pyref.available(3):
+        pytest.skip("reference kernels not built")
+    data = S.write(S.box_room(points=300_000, seed=7))
+    m = M.by_name(M.timing_methods(), "v3 complet")
+    seq = [0] * 6 + [1] * 4 + [2] * 4 + [3] * 4
+    _frames_vs_reference(data, 3, m, seq, 12, exact_frac=0.999)
+
+
+def test_culled_trace_equals_brute_force(scene_main_bytes):
+    for data in (scene_main_bytes, S.write(S.box_room(points=200_000, seed=2))):
+        ctx = _ctx(data, flags=N.FLAG_CHECK_TRACE)
+        m = M.by_name(M.timing_methods(), "Classique 2.0x")
+        ctx.run(m, [0] * 8 + [2] * 8 + [4] * 8, 21, want_err=False)
+        bad, rays = ctx.check_count()
+        assert rays > 0 and bad == 0, (bad, rays)
+
+
+def test_probe_hits_vs_oracle(scene_main_bytes):
+    ctx = _ctx(scene_main_bytes)
+    orc = po.Scene(data=scene_main_bytes)
+    run = po.Run(orc)
+    m = M.by_name(M.timing_methods(), "Classique 2.0x")
+    ctx.begin(m, 0, 99)
+    run.begin(m, 0, 99)
+    pts = list(range(0, 10728, 3))
+    for state in (0, 2, 4):
+        a = ctx.probe(state, pts)
+        b = sorted(run.probe(state, pts))
+        assert len(a) == len(b)
+        ga = np.array([(r[0], r[1], r[2], r[3], r[4]) for r in a])
+        gb = np.array([(r[0], r[1], r[2], r[3], r[4]) for r in b])
+        same = np.all(ga == gb, axis=1)
+        assert same.mean() > 0.999, same.mean()
+        ta = np.array([r[5] for r in a])[same]
+        tb = np.array([r[5] for r in b])[same]
+        fin = np.isfinite(ta)
+        assert np.all(np.abs(ta[fin] - tb[fin]) <= 1e-5 * np.abs(tb[fin]) + 1e-7)
+
+
+@pytest.mark.parametrize("scen,method", [("R1 allumee-eteinte-rallumee", "Accumulation+parlampe N=32, 1.53x"),
+                                         ("R1 allumee-eteinte-rallumee", "v4-A2C memoire verifiee+rampe"),
+                                         ("R3 porte ouverte-fermee-rouverte", "v5-AB instantanes+projection")])
+def test_gpu_matches_rtx4060_curves(scene_main_bytes, golden_main, scen, method):
+    ctx = _ctx(scene_main_bytes)
+    seq = M.sequence(dict(M.SCEN_SCENARIOS)[scen])
+    m = M.by_name(M.scen_methods(), method)
+    curve = np.zeros(len(seq))
+    for sd in range(golden_main["nseeds"]):
+        curve += ctx.run(m, seq, golden_main["seed0"] + sd) / golden_main["nseeds"]
+    gold = [r for r in golden_main["rows"] if r["scen"] == scen and r["name"] == method][0]
+    g = np.asarray(gold["curve"])
+    rel = np.abs(curve - g) / g
+    assert rel.max() < 2e-3, rel.max()
+
+
+def test_million_point_scene_runs_clean():
+    data = S.write(S.box_room(points=1_082_802, seed=0))
+    ctx = _ctx(data)
+    info = ctx.info()
+    assert abs(info["np"] - 1_082_802) < 30_000
+    m = M.by_name(M.timing_methods(), "v4-A2C suivi 1/4")
+    seq = [s for s in range(5) for _ in range(12)]
+    ctx.run(m, seq, 11, want_err=False)
+    lc = ctx.array(N.A_LC)
+    assert np.isfinite(lc).all() and lc.max() > 0
+    assert ctx.device_flags() == 0

@@ -1,0 +1,97 @@
+"""The CPU oracle against the reference's published golden error curves.
+
+The reference ships, for its box scenes, the per-frame error curves that its own binary
+printed on an RTX 4060 (reference/cuda_rtx4060/scen_main.jsonl and scen_stress.jsonl, means
+over 10 seeds, 5 decimals).  The oracle restates the reference in C; it must reproduce those
+curves.  The only differences allowed are those of the C library's cosf/sinf/rsqrt against
+CUDA's (a few ulp on ray directions), which move the 10-seed means by less than 2e-3
+relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from render_engine_gb300 import methods as M
+
+TOL = 2e-3
+
+
+def _scenario(golden, name):
+    for r in golden["rows"]:
+        if r["scen"] == name:
+            return r
+    raise KeyError(name)
+
+
+def _curve(run, method, seq, seed0, nseeds):
+    acc = np.zeros(len(seq))
+    for sd in range(nseeds):
+        acc += np.asarray(run.run(method, seq, seed0 + sd)) / nseeds
+    return acc
+
+
+@pytest.fixture(scope="module")
+def main_run(scene_main_bytes):
+    sc = po.Scene(data=scene_main_bytes)
+    sc.build()
+    return po.Run(sc)
+
+
+CASES_MAIN = [
+    ("R1 allumee-eteinte-rallumee", "Accumulation+parlampe N=32, 1.53x"),
+    ("R1 allumee-eteinte-rallumee", "SHaRC N=64 resp=8, 1.57x"),
+    ("R1 allumee-eteinte-rallumee", "v4-A2C memoire verifiee+rampe"),
+    ("R2 allumee-eteinte-porte-rallumee", "v5-A instantanes verifies"),
+    ("R3 porte ouverte-fermee-rouverte", "v5-AB instantanes+projection"),
+    ("I3 lampe allumee 1re fois", "Oracle"),
+]
+
+
+@pytest.mark.parametrize("scen,method", CASES_MAIN)
+def test_oracle_matches_rtx4060_curves_main(main_run, golden_main, scen, method):
+    parts = dict(M.SCEN_SCENARIOS)[scen]
+    seq = M.sequence(parts)
+    m = M.by_name(M.scen_methods(), method)
+    gold = [r for r in golden_main["rows"] if r["scen"] == scen and r["name"] == method][0]
+    ours = _curve(main_run, m, seq, golden_main["seed0"], golden_main["nseeds"])
+    g = np.asarray(gold["curve"])
+    rel = np.abs(ours - g) / np.maximum(g, 1e-6)
+    assert rel.max() < TOL, (scen, method, rel.max())
+    last = gold["last"]
+    post = ours[last:last + 30].mean()
+    assert abs(post - gold["post"]) / gold["post"] < TOL
+
+
+def _stress_scenarios():
+    import os
+    out = {}
+    for line in open(os.path.join(os.path.dirname(__file__), "golden", "scenarios_stress.txt")):
+        line = line.strip()
+        if not line or line.startswith("#"):
+            continue
+        name, rest = line.split(";", 1)
+        out[name] = [tuple(int(x) for x in t.split(":")) for t in rest.split(",")]
+    return out
+
+
+@pytest.mark.parametrize("scen,method", [("G3 quatre objets deplaces", "v3"),
+                                         ("L2 quatre lampes eteintes puis rallumees", "SHaRC N=64 resp=8, 1.57x")])
+def test_oracle_matches_rtx4060_curves_stress(scene_stress_bytes, golden_stress, scen, method):
+    sc = po.Scene(data=scene_stress_bytes)
+    sc.build()
+    run = po.Run(sc)
+    inten = [sc_state for sc_state in range(sc.NS)]
+    from render_engine_gb300 import scene as S
+    parsed = S.read(scene_stress_bytes)
+    dyn = 0
+    for s in range(1, sc.NS):
+        for l in range(sc.NL):
+            if parsed.states[s].inten[l] != parsed.states[0].inten[l]:
+                dyn |= 1 << l
+    m = M.by_name(M.scenf_methods(dyn), method)
+    seq = M.sequence(_stress_scenarios()[scen])
+    gold = [r for r in golden_stress["rows"] if r["scen"] == scen and r["name"] == method][0]
+    ours = _curve(run, m, seq, golden_stress["seed0"], golden_stress["nseeds"])
+    g = np.asarray(gold["curve"])
+    rel = np.abs(ours - g) / np.maximum(g, 1e-6)
+    assert rel.max() < TOL, (scen, method, rel.max())

@@ -1,0 +1,68 @@
+"""Unit checks of the oracle's integer building blocks and loader (no GPU)."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from render_engine_gb300 import methods as M
+from render_engine_gb300 import scene as S
+
+
+def hash32(x):
+    x &= 0xFFFFFFFF
+    x ^= x >> 16; x = (x * 0x7FEB352D) & 0xFFFFFFFF
+    x ^= x >> 15; x = (x * 0x846CA68B) & 0xFFFFFFFF
+    x ^= x >> 16
+    return x
+
+
+def test_scene_roundtrip(scene_main_bytes):
+    sc = S.read(scene_main_bytes)
+    assert S.write(sc) == scene_main_bytes
+    assert sc.Np == 10728 and sc.NL == 3 and sc.NS == 5
+
+
+def test_truncated_scene_rejected(scene_main_bytes):
+    for cut in (10, 1000, len(scene_main_bytes) // 2, len(scene_main_bytes) - 3):
+        with pytest.raises(ValueError):
+            po.Scene(data=scene_main_bytes[:cut])
+
+
+def test_bad_region_rejected(scene_main_bytes):
+    sc = S.read(scene_main_bytes)
+    sc.region = sc.region.copy()
+    sc.region[5] = sc.NR + 3
+    with pytest.raises(ValueError):
+        po.Scene(data=S.write(sc))
+
+
+def test_generated_room_loads_and_builds():
+    sc = S.box_room(points=20000, seed=3)
+    data = S.write(sc)
+    o = po.Scene(data=data)
+    assert o.Np == sc.Np and o.NL == 3 and o.NS == 5
+    o.build()
+    ed = o.state_array(0, 0).reshape(-1, 3)
+    assert np.isfinite(ed).all() and (ed >= 0).all() and ed.max() > 0
+    # light 0 is off in state 1: its direct light vanishes, the others stay
+    ed1 = o.state_array(1, 0).reshape(-1, 3)
+    assert ed1[:, 0].max() == 0 and np.array_equal(ed1[:, 1:], ed[:, 1:])
+    # the box moves between states 1 and 2: occluder voxels listed for that pair
+    assert len(o.event_list(1 * 5 + 2, 0)) > 0
+    # light 0 comes on between 2 and 3: its voxel is listed
+    assert len(o.event_list(2 * 5 + 3, 1)) == 1
+
+
+def test_run_is_deterministic():
+    sc = po.Scene(data=S.write(S.box_room(points=8000, seed=1)))
+    run = po.Run(sc)
+    m = M.by_name(M.timing_methods(), "v4-A2C suivi 1/4")
+    seq = [0] * 12 + [1] * 12 + [2] * 12
+    run.begin(m, 0, 5)
+    for s in seq:
+        run.frame(s)
+    a = run.array(po.A_LC).copy()
+    run.begin(m, 0, 5)
+    for s in seq:
+        run.frame(s)
+    assert np.array_equal(a, run.array(po.A_LC))
+    assert np.isfinite(a).all()
