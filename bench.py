@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark of the dependency-tracked radiance cache on GB300.
+
+Workload: the reference's headline timing case (cuda/poc_gpu.cu `timing` mode, published as
+reference/cuda_rtx4060/timing_1M.jsonl) on a seeded stand-in for its 1,082,802-point box
+scene: an 8 x 4 x 3 m room with four static boxes and a movable one (31 quads, 62 triangles),
+3 point lights, 5 states switched every 60 frames (light off, box moved, light back on, ...),
+method "v4-A2C suivi 1/4" (adaptive ray allocation, dependency masks on a 8 x 4 x 4 transit
+grid tracked one frame in four, verified dormant-light memory, history ramp).
+
+One step = one frame of the whole cache (trace + update of every cache point, plus the
+event kernels when the state changes).  Timed frames are separated by an L2 flush (a 512 MB
+write) and timed with CUDA events on the stream the kernels run on.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference runs the reference's own kernels (the unmodified cuda/poc_gpu.cu compiled
+for sm_103a into oracle/_ref/, driven by oracle/refrun.cpp) on the same scene, method and
+frames, timed the same way.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s and Mrays/s at 1080p, 1M cache pts; 30-frame post-event luma err % vs FP64"
+POINTS = 1_082_802
+METHOD = "v4-A2C suivi 1/4"
+FRAMES_PER_STATE = 60
+PUBLISHED_FPS = 1000.0 / 1.44806   # timing_1M.jsonl:10 (RTX 4060): trace+decide+update+swap = 1.448 ms
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--points", type=int, default=POINTS)
+    ap.add_argument("--method", default=METHOD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-frames", type=int, default=12)
+    return ap.parse_args()
+
+
+def sequence(n: int, ns: int = 5) -> list[int]:
+    return [(f // FRAMES_PER_STATE) % ns for f in range(n)]
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (every 200 ms)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.p = None
+        self.device = device
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic() -> float | None:
+    """DRAM bytes per launch of the fused frame kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_frame_fused_room1m.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def algorithmic_bytes(np_: int, tracked: bool, ramp: bool) -> float:
+    """Bytes one fused frame kernel must move for Np points (each array touched once):
+    reads P 16, N 16, n 4, own cache 16, gathered albedo+direct light 16 and cache 16 at the
+    hit points; writes cache 16, n 4; ramp: age read+write 8; tracked frames: shadow-voxel
+    mask gather 16 and dependency-mask write 16."""
+    b = 16 + 16 + 4 + 16 + 16 + 16 + 16 + 4
+    if ramp:
+        b += 8
+    if tracked:
+        b += 32
+    return float(np_) * b
+
+
+def setup_dist(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return world, rank, local, dist
+
+
+def run_ours(args, world, rank, local, dist):
+    import torch
+
+    from render_engine_gb300 import methods as M
+    from render_engine_gb300 import native as N
+    from render_engine_gb300 import scene as S
+
+    torch.cuda.set_device(local)
+    # a dedicated stream: the library's kernels, the L2 flush and the timing events all go on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    data = S.write(S.box_room(points=args.points, seed=0))
+    method = M.by_name(M.timing_methods(), args.method)
+    ctx = N.Context(device=local, stream=stream.cuda_stream)
+    info = ctx.load_bytes(data)
+    seq = sequence(args.warmup + args.steps)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    ctx.begin(method, seq[0], 11)
+    for f in range(args.warmup):
+        ctx.frame(seq[f])
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    fused = []
+    tracked = []
+    l0 = ctx.stats()
+    r0 = l0["rays"]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        f = args.warmup + k
+        flush.zero_()
+        starts[k].record(stream)
+        ctx.frame(seq[f])
+        ends[k].record(stream)
+        fused.append(ctx.scalar(N.S_LAST_FRAME_FUSED) == 1 and ctx.scalar(N.S_LAST_FRAME_KERNELS) == 1)
+        tracked.append(f % method.track_every == 0)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    st = ctx.stats()
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    frames = args.steps * world
+    rays = st["rays"] - r0
+    np_ = info["np"]
+    # dominant kernel: frames that are exactly one fused launch
+    fk = [m for m, fu in zip(ms, fused) if fu]
+    fk_tr = [m for m, fu, tr in zip(ms, fused, tracked) if fu]
+    fk_bytes = [algorithmic_bytes(np_, tr, method.ramp) for fu, tr in zip(fused, tracked) if fu]
+    kern_ms = sum(fk) / max(len(fk), 1)
+    kern_bytes = sum(fk_bytes) / max(len(fk_bytes), 1)
+    peak, peak_kind = measured_peaks()
+    achieved = kern_bytes / (kern_ms * 1e-3) / 1e9 if fk else None
+    traffic = profile_traffic()
+    out = {
+        "frames_per_s": frames / (total_ms * 1e-3),
+        "ms_per_step": total_ms / args.steps,
+        "mrays_per_s": rays * world / (total_ms * 1e-3) / 1e6,
+        "cache_updates_per_s": np_ * frames / (total_ms * 1e-3),
+        "rays_per_frame": rays / args.steps,
+        "launches": st["launches"] - l0["launches"],
+        "wall_s": wall,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": traffic,
+                     "kernel": "rc::k_frame<3,4,DEPS,FUSED=true>", "kernel_ms": kern_ms, "kernel_launches": len(fk),
+                     "peak_source": peak_kind},
+        "np": np_,
+        "nt": info["nt"],
+    }
+    # end to end through the C ABI from host memory: scene upload + build, the frames, and the
+    # final cache read back
+    ctx2 = N.Context(device=local, stream=stream.cuda_stream)
+    host = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    ctx2.load_bytes(host.numpy())
+    ctx2.begin(method, seq[0], 11)
+    for f in range(args.steps):
+        ctx2.frame(seq[f])
+    lc = ctx2.array(N.A_LC)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    out["e2e"] = {"value": args.steps * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": len(data) / args.steps,
+                  "d2h_bytes_per_step": lc.nbytes / args.steps,
+                  "includes": "scene upload + per-state build + %d frames + final cache download" % args.steps}
+    ctx2.close()
+    ctx.close()
+    return out, data, method
+
+
+def cpu_baseline(args, data, method):
+    from oracle import pyoracle as po
+    cores = os.cpu_count() or 1
+    po.set_threads(cores)
+    sc = po.Scene(data=data)
+    t = time.perf_counter()
+    sc.build()
+    run = po.Run(sc)
+    seq = sequence(args.cpu_frames)
+    run.begin(method, seq[0], 11)
+    t = time.perf_counter()
+    for s in seq:
+        run.frame(s)
+    dt = time.perf_counter() - t
+    return {"value": args.cpu_frames / dt, "unit": "frames/s", "cores": cores, "kind": "port",
+            "sample": "frames 0-%d of the same sequence at full size (%d points), C restatement with OpenMP" % (args.cpu_frames - 1, sc.Np)}
+
+
+def run_reference(args, world, rank, local, dist):
+    import torch
+
+    from oracle import pyref
+    from render_engine_gb300 import methods as M
+    from render_engine_gb300 import scene as S
+
+    if not pyref.available(3):
+        return None, "reference kernels not built (oracle/_ref/ref_l3.cubin missing: needs the reference checkout at build time)"
+    torch.cuda.set_device(local)
+    torch.cuda.init()
+    data = S.write(S.box_room(points=args.points, seed=0))
+    method = M.by_name(M.timing_methods(), args.method)
+    ref = pyref.RefRunner(3, data)
+    seq = sequence(args.warmup + args.steps)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    ref.begin(method, seq[0], 11)
+    for f in range(args.warmup):
+        ref.frame(seq[f])
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = Clocks(local)
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        ref.frame(seq[args.warmup + k])
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(ms)
+    # the reference's own timing-mode figures (per-frame events, one sync per frame)
+    import numpy as np
+    tm = np.zeros(5)
+    ref.begin(method, seq[0], 12)
+    for f in range(min(args.steps, 5 * FRAMES_PER_STATE)):
+        ref.frame(seq[f], timers=tm)
+    nf = min(args.steps, 5 * FRAMES_PER_STATE)
+    ref.close()
+    return {"frames_per_s": args.steps / (total_ms * 1e-3), "ms_per_step": total_ms / args.steps, "clocks": clk,
+            "timing_mode": {"trace": tm[1] / nf, "decide": tm[2] / nf, "update": tm[3] / nf, "swap": tm[0] / nf,
+                            "event_total": tm[4]}}, None
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = setup_dist(args)
+    config = {"workload": "dependency-tracked radiance cache, %s, seeded box room (%d cache points, 62 triangles, 3 point lights, "
+                          "5 states x %d frames with events), one frame per step" % (args.method, args.points, FRAMES_PER_STATE),
+              "method": args.method, "cache_points": args.points, "transit_grid": "8x4x4 (128-bit dependency masks)",
+              "l2": "flushed between timed frames (512 MB write); per-frame working set ~140 MB",
+              "scene": "synthetic stand-in for the reference's scene_scale_1M.bin (same room, size and light count)",
+              "parallelism": "replicas" if world > 1 else "single GPU"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        res, why = run_reference(args, 1, 0, local, None)
+        if res is None:
+            print(json.dumps({"impl": "reference", "unavailable": why}))
+            return
+        line = {"metric": METRIC, "value": res["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
+                "impl": "reference", "clocks": res["clocks"], "reference_timing_mode_ms": res["timing_mode"],
+                "cpu_baseline": {"value": res["frames_per_s"], "unit": "frames/s", "cores": 1, "kind": "reference",
+                                 "sample": "the reference's own kernels (cuda/poc_gpu.cu for sm_103a) on the GB300, driven by one host thread; "
+                                           "the reference has no CPU implementation of this path"},
+                "e2e": {"value": res["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    res, data, method = run_ours(args, world, rank, local, dist)
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, data, method)
+    line = {"metric": METRIC, "value": res["frames_per_s"], "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
+            "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
+            "rays_per_frame": res["rays_per_frame"], "clocks": res["clocks"], "e2e": res["e2e"],
+            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -92,6 +92,16 @@ typedef struct rc_device_info {
     double mem_used_mb, mem_total_mb;
 } rc_device_info;
 
+/* Counters of the current run (rc_run_stats_get). */
+typedef struct rc_run_stats {
+    long long frames;        /* frames run since rc_run_begin */
+    long long rays;          /* rays traced since rc_run_begin (sum of per-point ray counts) */
+    long long launches;      /* kernels launched by the context since it was created */
+    int last_frame_kernels;  /* kernels launched by the last frame, event included */
+    int last_frame_fused;    /* 1 when the last frame was the single fused trace+update kernel */
+    int last_frame_event;    /* 1 when the last frame started with an event */
+} rc_run_stats;
+
 /* Per-ray record of rc_probe_rays. */
 typedef struct rc_ray_rec {
     int point, ray;
@@ -110,7 +120,8 @@ enum {
     RC_A_NPEND, RC_A_COUNT
 };
 /* Host scalars of the run (rc_scalar_*): Runner::run locals, poc_gpu.cu:839-850. */
-enum { RC_S_PEND_LEFT = 0, RC_S_DORMANT, RC_S_PROJ_LEFT, RC_S_FRAME, RC_S_NSLOTS, RC_S_LAST_EVENT, RC_S_PROJK, RC_S_COUNT };
+enum { RC_S_PEND_LEFT = 0, RC_S_DORMANT, RC_S_PROJ_LEFT, RC_S_FRAME, RC_S_NSLOTS, RC_S_LAST_EVENT, RC_S_PROJK,
+       RC_S_LAST_FRAME_KERNELS, RC_S_LAST_FRAME_FUSED, RC_S_COUNT };   /* the last two are read-only */
 /* Per-state scene arrays (rc_state_array_copy): the k_build outputs and the references. */
 enum { RC_SA_EDIR = 0, RC_SA_SV, RC_SA_REF, RC_SA_VALID, RC_SA_PW };
 
@@ -165,6 +176,8 @@ rc_status rc_probe_rays(rc_ctx* ctx, int state, const int* points, int npoints,
                         rc_ray_rec* out, int maxrec, int* nrec);
 /* Disagreements counted by RC_FLAG_CHECK_TRACE since the last call (then reset). */
 rc_status rc_trace_check_count(rc_ctx* ctx, long long* mismatches, long long* rays);
+/* Run counters (synchronises to read the ray count). */
+rc_status rc_run_stats_get(rc_ctx* ctx, rc_run_stats* out);
 /* Device-side guard flags raised since the last call (then reset); 0 = none. */
 rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags);
 

@@ -7,10 +7,9 @@
  *    versions differ by a few ulp, so ray directions match the GPU to ~1e-7 relative;
  *  - build with -ffp-contract=off: no fused multiply-add, identical results on x86 and Arm;
  *  - region sums (rstat, neq, dstat) are accumulated in point order (the reference uses
- *    float atomics, whose order is not defined); Sum 1/(n+1) and the FP64 error sums use
- *    the fixed reduction tree of the product kernels (warp butterfly of 32, then warps of a
- *    256-point block in order, then blocks in order), so those sums are exact copies of
- *    what the product computes;
+ *    float atomics, whose order is not defined); Sum 1/(n+1) is computed exactly (64-bit
+ *    fixed point, one final rounding) and the FP64 error sums use the fixed reduction tree of
+ *    the product kernels, so those sums are exact copies of what the product computes;
  *  - the per-point "stale" set of dormant lights is 32 bits wide (the reference stores it
  *    in 8 bits, which only differs for scenes with more than 8 lights).
  */
@@ -572,29 +571,6 @@ int osc_run_scalar(osc_run* r, int which) {
         }                                                                              \
         out = blk;                                                                     \
     }
-static float tree_sum_f(const float* v, long n) {
-    long G = (n + BLK - 1) / BLK;
-    float* part = (float*)malloc(sizeof(float) * (size_t)(G ? G : 1));
-    for (long b = 0; b < G; ++b) {
-        float out;
-#define GETF(k) ((b * BLK + (k)) < n ? v[b * BLK + (k)] : 0.f)
-        TREE_BLOCK(float, GETF)
-#undef GETF
-        part[b] = out;
-    }
-    float slot[BLK];
-    for (long t = 0; t < BLK; ++t) {
-        float x = t < G ? part[t] : 0.f;
-        for (long b = t + BLK; b < G; b += BLK) x = x + part[b];
-        slot[t] = x;
-    }
-    free(part);
-    float out;
-#define GETS(k) (slot[(k)])
-    TREE_BLOCK(float, GETS)
-#undef GETS
-    return out;
-}
 static double tree_sum_d(const double* v, long n) {
     long G = (n + BLK - 1) / BLK;
     double* part = (double*)malloc(sizeof(double) * (size_t)(G ? G : 1));
@@ -626,13 +602,17 @@ static inline float est_of(const osc_run* r, int i, int dormant) {
     return e;
 }
 
-/* poc_gpu.cu:604-609 (sum in the fixed tree order) */
+/* poc_gpu.cu:604-609.  The sum is exact: each 1/(n+1) is an integer number of 2^-40 units
+ * (exact for terms >= 2^-16), the integers are added, and the total is rounded once to float,
+ * as the product kernels do. */
 static void sumpr_into(osc_run* r, int slot) {
     long Np = r->S->Np;
-    float* pr = (float*)malloc(sizeof(float) * (size_t)Np);
-    for (long i = 0; i < Np; ++i) pr[i] = 1.f / (r->n[i] + 1.f);
-    r->sumpr[slot] = tree_sum_f(pr, Np);
-    free(pr);
+    uint64_t tot = 0;
+    for (long i = 0; i < Np; ++i) {
+        float pr = 1.f / (r->n[i] + 1.f);
+        tot += (uint64_t)llrintf(pr * 1099511627776.0f);
+    }
+    r->sumpr[slot] = (float)tot * (1.0f / 1099511627776.0f);
 }
 
 void osc_run_begin(osc_run* r, const osc_method* m, int s0, uint32_t seed) {

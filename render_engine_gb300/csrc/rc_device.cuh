@@ -98,9 +98,18 @@ __device__ __forceinline__ void dda_walk(const Grid& g, f3 a, f3 b, uint32_t (&m
     for (int s = 0; s < steps; ++s) {
         set_bit<NW>(m, (iz * VY + iy) * VX + ix);
         if (ix == ex && iy == ey && iz == ez) break;
-        if (tmx < tmy && tmx < tmz) { ix += stx; tmx += tdx; if (ix < 0 || ix >= VX) break; }
-        else if (tmy < tmz) { iy += sty; tmy += tdy; if (iy < 0 || iy >= VY) break; }
-        else { iz += stz; tmz += tdz; if (iz < 0 || iz >= VZ) break; }
+        // one axis steps per iteration, chosen like the reference's if / else-if chain; written
+        // with selects so the lanes of a warp do not split three ways
+        const bool sx = tmx < tmy && tmx < tmz;
+        const bool sy = !sx && tmy < tmz;
+        const bool sz = !sx && !sy;
+        ix += sx ? stx : 0;
+        iy += sy ? sty : 0;
+        iz += sz ? stz : 0;
+        tmx = sx ? tmx + tdx : tmx;
+        tmy = sy ? tmy + tdy : tmy;
+        tmz = sz ? tmz + tdz : tmz;
+        if ((unsigned)ix >= (unsigned)VX || (unsigned)iy >= (unsigned)VY || (unsigned)iz >= (unsigned)VZ) break;
     }
 }
 
@@ -137,10 +146,10 @@ __device__ __forceinline__ void mt_tri(const float4* __restrict__ tri, int j, f3
     if (t > 1e-4f && (t < tmin || (t == tmin && j < jbest))) { tmin = t; q = __float_as_int(A.w); jbest = j; }
 }
 
-// Plane-culling group: an axis-aligned rectangle made of two triangles of one quad, or a
-// single axis-aligned triangle.  3 float4: (c, lo_a, hi_a, lo_b) (hi_b, ilo_a, ihi_a, ilo_b)
-// (ihi_b, j0 bits, cnt bits, rect bits); the outer box is grown and the inner box shrunk by a
-// margin far above the rounding error of the exact test, so the filter never drops the
+// Plane-culling group: the axis-aligned triangles of one quad lying in one plane k = c.
+// 2 float4: (c, lo_a, hi_a, lo_b) (hi_b, first triangle bits, count bits, 0), where a, b are
+// the two other axes in increasing order and the box is the triangles' bounding box grown by
+// a margin far above the rounding error of the exact test, so the filter never drops the
 // triangle the exact scan would pick.
 struct GroupRanges { int g0[4]; };  // groups of axis 0 in [g0[0], g0[1]), axis 1 [g0[1], g0[2]), axis 2 [g0[2], g0[3])
 

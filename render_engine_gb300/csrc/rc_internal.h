@@ -18,7 +18,7 @@ struct DState {
     const int* dims;           // nu, nv per quad
     const int* off;            // first point of each quad
     const float4* tri;         // dynamic triangles, 3 float4 each (v0 + quad id bits, e1, e2)
-    const float4* grp;         // plane-culling groups, 3 float4 each
+    const float4* grp;         // plane-culling groups, 2 float4 each
     const int* misc;           // dynamic triangles outside any group (always tested exactly)
     const float* ref;          // converged reference per point (scenes with references)
     const uint8_t* valid;
@@ -65,9 +65,12 @@ struct DevCache {
     float* partf;              // block partials (float)
     double* partd;             // block partials (3 doubles per block)
     int* parti;                // block partials (int)
-    unsigned* ticket;          // last-block counters [4]
+    unsigned* ticket;          // last-block counters: [0] Sum 1/(n+1), [1] error sums, [2] pending count
     unsigned* flags;           // device guard flags
     unsigned long long* check; // [0] trace disagreements, [1] rays checked
+    unsigned long long* rays;  // rays traced since the run began
+    unsigned long long* pracc; // fixed-point accumulator of Sum 1/(n+1) (zero between kernels)
+    unsigned long long* npacc; // pending-count accumulator (zero between kernels)
 };
 
 enum MaskOp { MASK_NONE = 0, MASK_OR = 1, MASK_FRESH = 2, MASK_ZERO = 3 };
@@ -143,7 +146,7 @@ inline bool supported_nl_nw(int NL, int NW) {
 RC_NL_VALUES(X)
 #undef X
 inline size_t frame_smem_bytes(const DState& s) {
-    return sizeof(float4) * (3 * (size_t)s.nt + 3 * (size_t)s.ng) + sizeof(int) * (size_t)s.nmisc + 16;
+    return sizeof(float4) * (3 * (size_t)s.nt + 2 * (size_t)s.ng) + sizeof(int) * (size_t)s.nmisc + 16;
 }
 __host__ __device__ constexpr int lcs_of(int NL) { return (NL + 3) / 4 * 4; }
 __host__ __device__ constexpr int aes_of(int NL) { return (NL + 1 + 3) / 4 * 4; }

@@ -10,8 +10,9 @@
 //    hold the closest hit, so hit ids and distances are those of the reference's full scan;
 //  * per-point gathers at the hit point are 16-byte vectors (albedo + direct light in one
 //    record, the cache padded to 4 lights);
-//  * reductions use a fixed tree (warp butterfly, warps in order, block partials reduced by
-//    the last block) so that runs are reproducible bit for bit;
+//  * reductions are order-free or fixed-order (Sum 1/(n+1) exactly in 64-bit fixed point,
+//    error sums in a fixed tree) and need no block-wide barrier, so runs are reproducible bit
+//    for bit and no warp waits for its block's slowest warp;
 //  * an event is one kernel applying the reference's per-point event kernels in order.
 #include <cstdio>
 
@@ -26,30 +27,115 @@ __device__ __forceinline__ T warp_tree(T v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
-// Block partial of one value per thread; the result is valid in thread 0.
-template <typename T>
-__device__ __forceinline__ T block_tree(T v, T* sh) {
-    v = warp_tree(v);
+// Fixed-order float sum over the grid without a block-wide barrier.  Level 1, per block of 256
+// values: each warp's butterfly sum (lane l += lane l+off, off = 16..1) goes to shared memory
+// and the last warp of the block to arrive adds the 8 sums in warp order.  Level 2, done by
+// the grid's last such warp over the G block partials: slot t = lane + 32 j sums partials
+// t, t+256, ... in order, each group of 32 slots goes through the butterfly and the 8 group
+// sums are added in order.  The CPU oracle restates this order exactly.
+template <typename T, int NV>
+struct WarpTail {
+    T sh[NV][BLOCK / 32];
+    unsigned arrived;
+    int last_block;
+};
+
+template <typename T, int NV>
+__device__ __forceinline__ bool warp_tail_reduce(const T (&v)[NV], WarpTail<T, NV>& wt, T* part, unsigned* ticket,
+                                                 T (&total)[NV]) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    T s = T(0);
-    if (threadIdx.x == 0) {
-        s = sh[0];
+    T r[NV];
 #pragma unroll
-        for (int k = 1; k < BLOCK / 32; ++k) s = s + sh[k];
+    for (int k = 0; k < NV; ++k) r[k] = warp_tree(v[k]);
+    unsigned arrived = 0;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) wt.sh[k][w] = r[k];
+        __threadfence_block();
+        arrived = atomicAdd(&wt.arrived, 1u);
     }
-    __syncthreads();
-    return s;
+    arrived = __shfl_sync(0xffffffffu, arrived, 0);
+    if (arrived != BLOCK / 32 - 1) return false;
+    __threadfence_block();
+    unsigned tk = 0;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const volatile T* sv = wt.sh[k];
+            T s = sv[0];
+#pragma unroll
+            for (int j = 1; j < BLOCK / 32; ++j) s = s + sv[j];
+            part[(size_t)blockIdx.x * NV + k] = s;
+        }
+        __threadfence();
+        tk = atomicAdd(ticket, 1u);
+    }
+    tk = __shfl_sync(0xffffffffu, tk, 0);
+    if (tk != gridDim.x - 1) return false;
+    __threadfence();
+    const int G = gridDim.x;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        T acc = T(0);
+        for (int j = 0; j < BLOCK / 32; ++j) {
+            const int t = lane + 32 * j;
+            T x = T(0);
+            if (t < G) x = __ldcg(part + (size_t)t * NV + k);
+            for (int b = t + BLOCK; b < G; b += BLOCK) x = x + __ldcg(part + (size_t)b * NV + k);
+            x = warp_tree(x);
+            acc = j == 0 ? x : acc + x;
+        }
+        total[k] = acc;
+    }
+    if (lane == 0) *ticket = 0u;
+    return lane == 0;
 }
-// Second level over G block partials (stride BLOCK per slot, then the block tree).
-template <typename T>
-__device__ __forceinline__ T final_tree(const T* part, int G, int stride, int comp, T* sh) {
-    T x = T(0);
-    const int t = threadIdx.x;
-    if (t < G) x = __ldcg(part + (size_t)t * stride + comp);
-    for (int b = t + BLOCK; b < G; b += BLOCK) x = x + __ldcg(part + (size_t)b * stride + comp);
-    return block_tree(x, sh);
+
+// Sum 1/(n+1) over the points, exactly: every term is a float in (0, 1] held as an integer
+// number of 2^-40 units (exact for terms >= 2^-16, i.e. histories below 65535 frames), the
+// integers are added with 64-bit atomics (order-free, so the sum is reproducible), and the
+// total is rounded once to float.  Per block: warp sums into a shared accumulator, the last
+// warp to arrive adds it to the global accumulator; the grid's last block converts it.
+__device__ __forceinline__ unsigned long long pr_fixed(float pr) { return __float2ull_rn(pr * 1099511627776.0f); }
+
+__device__ __forceinline__ float fixed_to_float(unsigned long long tot) {
+    return __ull2float_rn(tot) * (1.0f / 1099511627776.0f);
+}
+
+// Order-free integer total over the grid (pending counts, fixed-point sums): warp sums into a
+// shared accumulator, the block's last warp adds it to `gacc`, the grid's last block reads and
+// clears it.  Returns true in the one thread that holds the total.
+struct U64Tail {
+    unsigned long long acc;
+    unsigned arrived;
+};
+__device__ __forceinline__ bool u64_tail_reduce(unsigned long long v, U64Tail& t, unsigned long long* gacc, unsigned* ticket,
+                                                unsigned long long& total) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    unsigned arrived = 0;
+    if (lane == 0) {
+        if (v) atomicAdd(&t.acc, v);
+        __threadfence_block();
+        arrived = atomicAdd(&t.arrived, 1u);
+    }
+    arrived = __shfl_sync(0xffffffffu, arrived, 0);
+    if (arrived != BLOCK / 32 - 1) return false;
+    unsigned tk = 0;
+    if (lane == 0) {
+        __threadfence_block();
+        const unsigned long long b = atomicAdd(&t.acc, 0ull);
+        if (b) atomicAdd(gacc, b);
+        __threadfence();
+        tk = atomicAdd(ticket, 1u);
+    }
+    tk = __shfl_sync(0xffffffffu, tk, 0);
+    if (tk != gridDim.x - 1 || lane != 0) return false;
+    __threadfence();
+    total = atomicExch(gacc, 0ull);
+    *ticket = 0u;
+    return true;
 }
 
 // ------------------------------------------------------------------ tracing
@@ -59,19 +145,22 @@ struct TraceSmem {
     const int* misc;
 };
 
+// Plane filter of one group: the ray's crossing of the group's plane (t = (c - o_k) / d_k)
+// is a candidate when it lies ahead of the origin and inside the group's outer box.
 __device__ __forceinline__ void filter_group(const float4* __restrict__ grp, int g, float ok, float idk, float oa, float da,
-                                             float ob, float db, unsigned long long& mask, float& tcert) {
-    const float4 G0 = grp[3 * g], G1 = grp[3 * g + 1];
+                                             float ob, float db, unsigned long long& mask) {
+    const float4 G0 = grp[2 * g];
+    const float hb = grp[2 * g + 1].x;
     const float tk = (G0.x - ok) * idk;
     const float xa = oa + tk * da, xb = ob + tk * db;
-    if (tk > 5e-5f && xa >= G0.y && xa <= G0.z && xb >= G0.w && xb <= G1.x) {
-        mask |= 1ull << g;
-        const float4 G2 = grp[3 * g + 2];
-        if (tk > 2e-4f && xa >= G1.y && xa <= G1.z && xb >= G1.w && xb <= G2.x) tcert = fminf(tcert, tk);
-    }
+    const bool in = tk > 5e-5f && xa >= G0.y && xa <= G0.z && xb >= G0.w && xb <= hb;
+    mask |= in ? (1ull << g) : 0ull;
 }
 
 // Closest dynamic-triangle hit, equal to the reference's in-order scan (poc_gpu.cu:199-220).
+// Pass 1 marks the groups whose plane crossing falls in their outer box; pass 2 visits the
+// marked groups nearest first, runs the exact Möller-Trumbore on their triangles, and stops
+// once the next crossing lies beyond the best exact hit by more than the filter's error.
 __device__ __forceinline__ void trace_dyn(const TraceSmem& sm, const DState& s, bool brute, f3 o, f3 d, float& tmin, int& q,
                                           int& jb) {
     tmin = __int_as_float(0x7f800000);
@@ -82,24 +171,31 @@ __device__ __forceinline__ void trace_dyn(const TraceSmem& sm, const DState& s, 
         return;
     }
     for (int k = 0; k < s.nmisc; ++k) mt_tri(sm.tri, sm.misc[k], o, d, tmin, q, jb);
-    float tcert = tmin;
     unsigned long long mask = 0ull;
     const float idx = 1.f / d.x, idy = 1.f / d.y, idz = 1.f / d.z;
-    for (int g = s.gr.g0[0]; g < s.gr.g0[1]; ++g) filter_group(sm.grp, g, o.x, idx, o.y, d.y, o.z, d.z, mask, tcert);
-    for (int g = s.gr.g0[1]; g < s.gr.g0[2]; ++g) filter_group(sm.grp, g, o.y, idy, o.x, d.x, o.z, d.z, mask, tcert);
-    for (int g = s.gr.g0[2]; g < s.gr.g0[3]; ++g) filter_group(sm.grp, g, o.z, idz, o.x, d.x, o.y, d.y, mask, tcert);
-    const float thr = tcert * 1.0001f + 1e-5f;
+#pragma unroll 4
+    for (int g = s.gr.g0[0]; g < s.gr.g0[1]; ++g) filter_group(sm.grp, g, o.x, idx, o.y, d.y, o.z, d.z, mask);
+#pragma unroll 4
+    for (int g = s.gr.g0[1]; g < s.gr.g0[2]; ++g) filter_group(sm.grp, g, o.y, idy, o.x, d.x, o.z, d.z, mask);
+#pragma unroll 4
+    for (int g = s.gr.g0[2]; g < s.gr.g0[3]; ++g) filter_group(sm.grp, g, o.z, idz, o.x, d.x, o.y, d.y, mask);
+    float thr = tmin * 1.0001f + 1e-5f;
     while (mask) {
-        const int g = __ffsll((long long)mask) - 1;
-        mask &= mask - 1ull;
-        const float4 G0 = sm.grp[3 * g], G2 = sm.grp[3 * g + 2];
-        const float ok = g < s.gr.g0[1] ? o.x : (g < s.gr.g0[2] ? o.y : o.z);
-        const float idk = g < s.gr.g0[1] ? idx : (g < s.gr.g0[2] ? idy : idz);
-        const float tk = (G0.x - ok) * idk;
-        if (tk <= thr) {
-            const int j0 = __float_as_int(G2.y), cnt = __float_as_int(G2.z);
-            for (int j = j0; j < j0 + cnt; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
+        float best = __int_as_float(0x7f800000);
+        int bg = 0;
+        for (unsigned long long m = mask; m; m &= m - 1ull) {
+            const int g = __ffsll((long long)m) - 1;
+            const float ok = g < s.gr.g0[1] ? o.x : (g < s.gr.g0[2] ? o.y : o.z);
+            const float idk = g < s.gr.g0[1] ? idx : (g < s.gr.g0[2] ? idy : idz);
+            const float tk = (sm.grp[2 * g].x - ok) * idk;
+            if (tk < best) { best = tk; bg = g; }
         }
+        if (!(best <= thr)) break;
+        mask &= ~(1ull << bg);
+        const float4 G1 = sm.grp[2 * bg + 1];
+        const int j0 = __float_as_int(G1.y), cnt = __float_as_int(G1.z);
+        for (int j = j0; j < j0 + cnt; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
+        thr = tmin * 1.0001f + 1e-5f;
     }
 }
 
@@ -242,16 +338,16 @@ __device__ __forceinline__ Hit trace_resolve(const TraceSmem& sm, const DState& 
 __device__ __forceinline__ void stage_smem(float4* sm, const DState& s) {
     float4* st = sm;
     float4* sg = sm + 3 * s.nt;
-    int* smi = (int*)(sg + 3 * s.ng);
+    int* smi = (int*)(sg + 2 * s.ng);
     for (int j = threadIdx.x; j < 3 * s.nt; j += blockDim.x) st[j] = s.tri[j];
-    for (int j = threadIdx.x; j < 3 * s.ng; j += blockDim.x) sg[j] = s.grp[j];
+    for (int j = threadIdx.x; j < 2 * s.ng; j += blockDim.x) sg[j] = s.grp[j];
     for (int j = threadIdx.x; j < s.nmisc; j += blockDim.x) smi[j] = s.misc[j];
 }
 __device__ __forceinline__ TraceSmem smem_view(float4* sm, const DState& s) {
     TraceSmem t;
     t.tri = sm;
     t.grp = sm + 3 * s.nt;
-    t.misc = (const int*)(sm + 3 * s.nt + 3 * s.ng);
+    t.misc = (const int*)(sm + 3 * s.nt + 2 * s.ng);
     return t;
 }
 
@@ -323,25 +419,31 @@ __global__ void __launch_bounds__(BLOCK) k_build(const DState s, const DStatic g
 // ------------------------------------------------------------------ frame kernel
 // FUSED: trace + update + reductions (frames without verification, projection or DDGI).
 // !FUSED: trace only, writing kk / m and the region statistics (poc_gpu.cu:492-529).
+#ifndef RC_FRAME_MINB
+#define RC_FRAME_MINB 4
+#endif
+
 template <int NL, int NW, bool DEPS, bool FUSED>
-__global__ void __launch_bounds__(BLOCK, 2) k_frame(const DState s, const DStatic g, const Grid grid, const DevCache c,
+__global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, const DStatic g, const Grid grid, const DevCache c,
                                                  const FrameParams p) {
     extern __shared__ float4 sm[];
-    __shared__ float shf[BLOCK / 32];
-    __shared__ double shd[BLOCK / 32];
-    __shared__ bool last;
+    __shared__ U64Tail prt;
+    __shared__ WarpTail<double, 3> taild;
     constexpr int LCS = lcs_of(NL), AES = aes_of(NL);
     stage_smem(sm, s);
+    if (threadIdx.x == 0) { prt.acc = 0ull; prt.arrived = 0u; taild.arrived = 0u; }
     __syncthreads();
     const TraceSmem tsm = smem_view(sm, s);
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     float pr_out = 0.f;
     double e_d2 = 0.0, e_rs = 0.0, e_cn = 0.0;
+    int k_rays = 0;
     if (i < p.Np) {
         uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
         const bool pend = !FUSED && p.pend_left > 0 && c.pending[i];
         const float n_i = c.n[i];
         const int k = ray_count(p, c, n_i, pend, c.sumpr[p.sum_in], c.npend[0], rs);
+        k_rays = k;
         const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
         float acc[NL];
 #pragma unroll
@@ -487,30 +589,21 @@ __global__ void __launch_bounds__(BLOCK, 2) k_frame(const DState s, const DStati
             for (int w = 0; w < NW; ++w) c.cur[(size_t)w * p.Np + i] = (DEPS && p.mask_op == MASK_FRESH && k > 0) ? m[w] : 0u;
         }
     }
+    {
+        // ray count of the frame: warp sum, one 64-bit atomic per warp
+        const unsigned wk = __reduce_add_sync(0xffffffffu, (unsigned)k_rays);
+        if ((threadIdx.x & 31) == 0 && wk) atomicAdd(c.rays, (unsigned long long)wk);
+    }
     if (FUSED) {
-        const float bpr = block_tree(pr_out, shf);
-        double b0 = 0, b1 = 0, b2 = 0;
-        if (p.want_err) { b0 = block_tree(e_d2, shd); b1 = block_tree(e_rs, shd); b2 = block_tree(e_cn, shd); }
-        if (threadIdx.x == 0) {
-            c.partf[blockIdx.x] = bpr;
-            if (p.want_err) { c.partd[3 * blockIdx.x] = b0; c.partd[3 * blockIdx.x + 1] = b1; c.partd[3 * blockIdx.x + 2] = b2; }
-            __threadfence();
-            last = atomicAdd(c.ticket, 1u) == gridDim.x - 1;
-        }
-        __syncthreads();
-        if (last) {
-            __threadfence();
-            const float tot = final_tree(c.partf, gridDim.x, 1, 0, shf);
-            double t0 = 0, t1 = 0, t2 = 0;
-            if (p.want_err) {
-                t0 = final_tree(c.partd, gridDim.x, 3, 0, shd);
-                t1 = final_tree(c.partd, gridDim.x, 3, 1, shd);
-                t2 = final_tree(c.partd, gridDim.x, 3, 2, shd);
-            }
-            if (threadIdx.x == 0) {
-                c.sumpr[p.sum_out] = tot;
-                if (p.want_err) { c.err[3 * p.err_frame] = t0; c.err[3 * p.err_frame + 1] = t1; c.err[3 * p.err_frame + 2] = t2; }
-                *c.ticket = 0u;
+        unsigned long long tot;
+        if (u64_tail_reduce(pr_fixed(pr_out), prt, c.pracc, c.ticket, tot)) c.sumpr[p.sum_out] = fixed_to_float(tot);
+        if (p.want_err) {
+            const double vd[3] = {e_d2, e_rs, e_cn};
+            double totd[3];
+            if (warp_tail_reduce<double, 3>(vd, taild, c.partd, c.ticket + 1, totd)) {
+                c.err[3 * p.err_frame] = totd[0];
+                c.err[3 * p.err_frame + 1] = totd[1];
+                c.err[3 * p.err_frame + 2] = totd[2];
             }
         }
     }
@@ -521,11 +614,11 @@ __global__ void __launch_bounds__(BLOCK, 2) k_frame(const DState s, const DStati
 // and the pending count, reduced by the last block.
 template <int NL>
 __global__ void __launch_bounds__(BLOCK) k_update(const DState s, const DStatic g, const DevCache c, const FrameParams p) {
-    __shared__ float shf[BLOCK / 32];
-    __shared__ double shd[BLOCK / 32];
-    __shared__ int shi[BLOCK / 32];
-    __shared__ bool last;
+    __shared__ U64Tail prt, npt;
+    __shared__ WarpTail<double, 3> taild;
     constexpr int LCS = lcs_of(NL);
+    if (threadIdx.x == 0) { prt.acc = 0ull; prt.arrived = 0u; npt.acc = 0ull; npt.arrived = 0u; taild.arrived = 0u; }
+    __syncthreads();
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     float pr_out = 0.f;
     double e_d2 = 0.0, e_rs = 0.0, e_cn = 0.0;
@@ -605,36 +698,20 @@ __global__ void __launch_bounds__(BLOCK) k_update(const DState s, const DStatic 
             e_cn = 1.0;
         }
     }
-    const float bpr = block_tree(pr_out, shf);
-    double b0 = 0, b1 = 0, b2 = 0;
-    if (p.want_err) { b0 = block_tree(e_d2, shd); b1 = block_tree(e_rs, shd); b2 = block_tree(e_cn, shd); }
-    int bc = 0;
-    if (p.decide) bc = block_tree(cnt, shi);
-    if (threadIdx.x == 0) {
-        c.partf[blockIdx.x] = bpr;
-        if (p.want_err) { c.partd[3 * blockIdx.x] = b0; c.partd[3 * blockIdx.x + 1] = b1; c.partd[3 * blockIdx.x + 2] = b2; }
-        if (p.decide) c.parti[blockIdx.x] = bc;
-        __threadfence();
-        last = atomicAdd(c.ticket + 1, 1u) == gridDim.x - 1;
+    unsigned long long tot;
+    if (u64_tail_reduce(pr_fixed(pr_out), prt, c.pracc, c.ticket, tot)) c.sumpr[p.sum_out] = fixed_to_float(tot);
+    if (p.want_err) {
+        const double vd[3] = {e_d2, e_rs, e_cn};
+        double totd[3];
+        if (warp_tail_reduce<double, 3>(vd, taild, c.partd, c.ticket + 1, totd)) {
+            c.err[3 * p.err_frame] = totd[0];
+            c.err[3 * p.err_frame + 1] = totd[1];
+            c.err[3 * p.err_frame + 2] = totd[2];
+        }
     }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        const float tot = final_tree(c.partf, gridDim.x, 1, 0, shf);
-        double t0 = 0, t1 = 0, t2 = 0;
-        if (p.want_err) {
-            t0 = final_tree(c.partd, gridDim.x, 3, 0, shd);
-            t1 = final_tree(c.partd, gridDim.x, 3, 1, shd);
-            t2 = final_tree(c.partd, gridDim.x, 3, 2, shd);
-        }
-        int ct = 0;
-        if (p.decide) ct = final_tree(c.parti, gridDim.x, 1, 0, shi);
-        if (threadIdx.x == 0) {
-            c.sumpr[p.sum_out] = tot;
-            if (p.want_err) { c.err[3 * p.err_frame] = t0; c.err[3 * p.err_frame + 1] = t1; c.err[3 * p.err_frame + 2] = t2; }
-            if (p.decide) { c.npend[0] = ct; c.npend[1] = ct; }
-            *(c.ticket + 1) = 0u;
-        }
+    if (p.decide && u64_tail_reduce((unsigned long long)cnt, npt, c.npacc, c.ticket + 2, tot)) {
+        c.npend[0] = (int)tot;
+        c.npend[1] = (int)tot;
     }
 }
 
@@ -651,10 +728,10 @@ __device__ __forceinline__ float est_point(const float* lc, int dormant) {
 // point; then the pending count and, in adaptive mode, Sum 1/(n+1) (poc_gpu.cu:938-941).
 template <int NL>
 __global__ void __launch_bounds__(BLOCK) k_event(const __grid_constant__ EvProgram ev, const DevCache c) {
-    __shared__ float shf[BLOCK / 32];
-    __shared__ int shi[BLOCK / 32];
-    __shared__ bool last;
+    __shared__ U64Tail prt, npt;
     constexpr int LCS = lcs_of(NL);
+    if (threadIdx.x == 0) { prt.acc = 0ull; prt.arrived = 0u; npt.acc = 0ull; npt.arrived = 0u; }
+    __syncthreads();
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     const int Np = ev.Np;
     if (ev.zero_rstat)
@@ -734,34 +811,22 @@ __global__ void __launch_bounds__(BLOCK) k_event(const __grid_constant__ EvProgr
         if (ev.npend_mode == 2 && blockIdx.x == 0 && threadIdx.x == 0) { c.npend[0] = 0; c.npend[1] = 0; }
         return;
     }
-    const float bpr = ev.want_sumpr ? block_tree(pr, shf) : 0.f;
-    const int bc = ev.npend_mode == 1 ? block_tree(cnt, shi) : 0;
-    if (threadIdx.x == 0) {
-        c.partf[blockIdx.x] = bpr;
-        c.parti[blockIdx.x] = bc;
-        __threadfence();
-        last = atomicAdd(c.ticket + 2, 1u) == gridDim.x - 1;
+    unsigned long long tot;
+    if (ev.want_sumpr && u64_tail_reduce(pr_fixed(pr), prt, c.pracc, c.ticket, tot)) c.sumpr[ev.sum_slot] = fixed_to_float(tot);
+    if (ev.npend_mode == 1 && u64_tail_reduce((unsigned long long)cnt, npt, c.npacc, c.ticket + 2, tot)) {
+        c.npend[0] = (int)tot;
+        c.npend[1] = (int)tot;
     }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        const float tot = ev.want_sumpr ? final_tree(c.partf, gridDim.x, 1, 0, shf) : 0.f;
-        const int ct = ev.npend_mode == 1 ? final_tree(c.parti, gridDim.x, 1, 0, shi) : 0;
-        if (threadIdx.x == 0) {
-            if (ev.want_sumpr) c.sumpr[ev.sum_slot] = tot;
-            if (ev.npend_mode == 1) { c.npend[0] = ct; c.npend[1] = ct; }
-            if (ev.npend_mode == 2) { c.npend[0] = 0; c.npend[1] = 0; }
-            *(c.ticket + 2) = 0u;
-        }
-    }
+    if (ev.npend_mode == 2 && blockIdx.x == 0 && threadIdx.x == 0) { c.npend[0] = 0; c.npend[1] = 0; }
 }
 
 // poc_gpu.cu:620-635 + the pending-count reset / publish around it (poc_gpu.cu:990-993).
 template <int NL>
 __global__ void __launch_bounds__(BLOCK) k_proj_apply(const DevCache c, const DStatic g, const FrameParams p) {
-    __shared__ int shi[BLOCK / 32];
-    __shared__ bool last;
+    __shared__ U64Tail npt;
     constexpr int LCS = lcs_of(NL);
+    if (threadIdx.x == 0) { npt.acc = 0ull; npt.arrived = 0u; }
+    __syncthreads();
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     for (int x = i; x < 4 * p.NR; x += gridDim.x * BLOCK) c.rstat[x] = 0.f;
     int cnt = 0;
@@ -782,17 +847,10 @@ __global__ void __launch_bounds__(BLOCK) k_proj_apply(const DevCache c, const DS
             cnt = 1;
         }
     }
-    const int bc = block_tree(cnt, shi);
-    if (threadIdx.x == 0) {
-        c.parti[blockIdx.x] = bc;
-        __threadfence();
-        last = atomicAdd(c.ticket + 3, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        const int ct = final_tree(c.parti, gridDim.x, 1, 0, shi);
-        if (threadIdx.x == 0) { c.npend[0] = ct; c.npend[1] = ct; *(c.ticket + 3) = 0u; }
+    unsigned long long tot;
+    if (u64_tail_reduce((unsigned long long)cnt, npt, c.npacc, c.ticket + 2, tot)) {
+        c.npend[0] = (int)tot;
+        c.npend[1] = (int)tot;
     }
 }
 
@@ -800,9 +858,10 @@ __global__ void __launch_bounds__(BLOCK) k_proj_apply(const DevCache c, const DS
 // frames whose cache changes after the update, i.e. when the projection is applied).
 template <int NL>
 __global__ void __launch_bounds__(BLOCK) k_error(const DState s, const DevCache c, const FrameParams p) {
-    __shared__ double shd[BLOCK / 32];
-    __shared__ bool last;
+    __shared__ WarpTail<double, 3> taild;
     constexpr int LCS = lcs_of(NL);
+    if (threadIdx.x == 0) taild.arrived = 0u;
+    __syncthreads();
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     double d2 = 0.0, rs = 0.0, cn = 0.0;
     if (i < p.Np && s.valid[i]) {
@@ -811,22 +870,12 @@ __global__ void __launch_bounds__(BLOCK) k_error(const DState s, const DevCache 
         rs = s.ref[i];
         cn = 1.0;
     }
-    const double b0 = block_tree(d2, shd), b1 = block_tree(rs, shd), b2 = block_tree(cn, shd);
-    if (threadIdx.x == 0) {
-        c.partd[3 * blockIdx.x] = b0; c.partd[3 * blockIdx.x + 1] = b1; c.partd[3 * blockIdx.x + 2] = b2;
-        __threadfence();
-        last = atomicAdd(c.ticket + 3, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        const double t0 = final_tree(c.partd, gridDim.x, 3, 0, shd);
-        const double t1 = final_tree(c.partd, gridDim.x, 3, 1, shd);
-        const double t2 = final_tree(c.partd, gridDim.x, 3, 2, shd);
-        if (threadIdx.x == 0) {
-            c.err[3 * p.err_frame] = t0; c.err[3 * p.err_frame + 1] = t1; c.err[3 * p.err_frame + 2] = t2;
-            *(c.ticket + 3) = 0u;
-        }
+    const double vd[3] = {d2, rs, cn};
+    double totd[3];
+    if (warp_tail_reduce<double, 3>(vd, taild, c.partd, c.ticket + 1, totd)) {
+        c.err[3 * p.err_frame] = totd[0];
+        c.err[3 * p.err_frame + 1] = totd[1];
+        c.err[3 * p.err_frame + 2] = totd[2];
     }
 }
 

@@ -74,6 +74,7 @@ struct Run {
     int slot[KSNAP] = {0};
     int prev_state = 0, f = 0, sum_cur = 0, nerr = 0;
     float nmax = 0.f;
+    int last_kernels = 0, last_fused = 0, last_event = 0;
 };
 
 }  // namespace
@@ -91,6 +92,7 @@ struct rc_ctx {
     size_t err_cap = 0;         // frames of error sums allocated
     Run run;
     double cache_bytes = 0;
+    long long launches = 0;
     unsigned* flags_dev = nullptr;
     cudaEvent_t ev[8] = {};
 };
@@ -178,17 +180,17 @@ std::vector<int> to_grid(const std::vector<int>& fine, int VX, int VY, int VZ) {
     return out;
 }
 
-// Plane-culling groups of one state's dynamic triangles.  A group is a pair of consecutive
-// triangles of the same quad lying in one axis-aligned plane (or a lone such triangle); its
-// outer box (grown by a margin) must contain every point the exact test can accept, its inner
-// box (shrunk) only points the exact test surely accepts — only full rectangles get one.
+// Plane-culling groups of one state's dynamic triangles: consecutive triangles of one quad
+// lying in the same axis-aligned plane (a quad's two triangles) form a group whose box is
+// their bounding box grown by a margin; triangles that are not axis-aligned stay outside any
+// group and are always tested exactly.  Groups are ordered by plane axis.
 struct Groups {
     std::vector<float4> grp;
     std::vector<int> misc;
     GroupRanges gr{};
 };
 Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int nt) {
-    struct G { int axis, j0, cnt; bool rect; float c, lo[2], hi[2]; };
+    struct G { int axis, j0, cnt; float c, lo[2], hi[2]; };
     std::vector<G> gs;
     std::vector<int> misc;
     auto axis_of = [&](int j) {
@@ -197,13 +199,10 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
             if (t[3 + k] == 0.f && t[6 + k] == 0.f) return k;
         return -1;
     };
+    // in-plane axes in increasing order, as the kernel's filter reads them
     auto box = [&](int j, int k, float lo[2], float hi[2]) {
         const float* t = &T[9 * (size_t)j];
-        int a = (k + 1) % 3, b = (k + 2) % 3;
-        if (k == 1) { a = 0; b = 2; }
-        if (k == 0) { a = 1; b = 2; }
-        if (k == 2) { a = 0; b = 1; }
-        const int ax[2] = {a, b};
+        const int ax[2] = {k == 0 ? 1 : 0, k == 2 ? 1 : 2};
         for (int u = 0; u < 2; ++u) {
             float v0 = t[ax[u]], v1 = t[ax[u]] + t[3 + ax[u]], v2 = t[ax[u]] + t[6 + ax[u]];
             lo[u] = std::min(v0, std::min(v1, v2));
@@ -212,31 +211,19 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
     };
     int j = 0;
     while (j < nt) {
-        int k = axis_of(j);
+        const int k = axis_of(j);
         if (k < 0) { misc.push_back(j); ++j; continue; }
         G g{};
         g.axis = k;
         g.j0 = j;
         g.c = T[9 * (size_t)j + k];
-        box(j, k, g.lo, g.hi);
         g.cnt = 1;
-        g.rect = false;
+        box(j, k, g.lo, g.hi);
         if (j + 1 < nt && TQ[j + 1] == TQ[j] && axis_of(j + 1) == k && T[9 * (size_t)(j + 1) + k] == g.c) {
             float lo2[2], hi2[2];
             box(j + 1, k, lo2, hi2);
-            const float* a = &T[9 * (size_t)j];
-            const float* b = &T[9 * (size_t)(j + 1)];
-            // second triangle = (v0 + e1 + e2, -e1, -e2) and edges along the two in-plane axes:
-            // the pair tiles the rectangle that is its bounding box
-            bool tiles = true;
-            for (int x = 0; x < 3; ++x)
-                if (b[x] != a[x] + a[3 + x] + a[6 + x] || b[3 + x] != -a[3 + x] || b[6 + x] != -a[6 + x]) tiles = false;
-            int nz1 = 0, nz2 = 0;
-            for (int x = 0; x < 3; ++x) { nz1 += a[3 + x] != 0.f; nz2 += a[6 + x] != 0.f; }
-            bool axis_edges = nz1 == 1 && nz2 == 1;
             for (int u = 0; u < 2; ++u) { g.lo[u] = std::min(g.lo[u], lo2[u]); g.hi[u] = std::max(g.hi[u], hi2[u]); }
             g.cnt = 2;
-            g.rect = tiles && axis_edges;
         }
         gs.push_back(g);
         j += g.cnt;
@@ -250,7 +237,8 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
             for (int t = 0; t < gs[x].cnt; ++t) misc.push_back(gs[x].j0 + t);
         gs.resize(MAX_GROUPS);
     }
-    std::stable_sort(gs.begin(), gs.end(), [](const G& a, const G& b) { return a.axis < b.axis; });
+    std::stable_sort(gs.begin(), gs.end(), [](const G& a, const G& b) { return a.axis < b.axis; })
+    ;
     int cnt[3] = {0, 0, 0};
     for (auto& g : gs) cnt[g.axis]++;
     out.gr.g0[0] = 0;
@@ -258,20 +246,17 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
     out.gr.g0[2] = cnt[0] + cnt[1];
     out.gr.g0[3] = cnt[0] + cnt[1] + cnt[2];
     for (auto& g : gs) {
-        float m[2], olo[2], ohi[2], ilo[2], ihi[2];
+        float olo[2], ohi[2];
         for (int u = 0; u < 2; ++u) {
-            m[u] = 2e-3f + 1e-4f * (g.hi[u] - g.lo[u]) + 1e-6f * (fabsf(g.lo[u]) + fabsf(g.hi[u]));
-            olo[u] = g.lo[u] - m[u];
-            ohi[u] = g.hi[u] + m[u];
-            if (g.rect) { ilo[u] = g.lo[u] + m[u]; ihi[u] = g.hi[u] - m[u]; }
-            else { ilo[u] = 1.f; ihi[u] = -1.f; }
+            const float m = 2e-3f + 1e-4f * (g.hi[u] - g.lo[u]) + 1e-6f * (fabsf(g.lo[u]) + fabsf(g.hi[u]));
+            olo[u] = g.lo[u] - m;
+            ohi[u] = g.hi[u] + m;
         }
-        int j0 = g.j0, c = g.cnt, rect = g.rect ? 1 : 0;
-        float fj0, fc, fr;
-        memcpy(&fj0, &j0, 4); memcpy(&fc, &c, 4); memcpy(&fr, &rect, 4);
+        int j0 = g.j0, c = g.cnt, z = 0;
+        float fj0, fc, fz;
+        memcpy(&fj0, &j0, 4); memcpy(&fc, &c, 4); memcpy(&fz, &z, 4);
         out.grp.push_back(make_float4(g.c, olo[0], ohi[0], olo[1]));
-        out.grp.push_back(make_float4(ohi[1], ilo[0], ihi[0], ilo[1]));
-        out.grp.push_back(make_float4(ihi[1], fj0, fc, fr));
+        out.grp.push_back(make_float4(ohi[1], fj0, fc, fz));
     }
     std::sort(misc.begin(), misc.end());
     out.misc = misc;
@@ -385,7 +370,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
             if ((s = dput(ctx, pool, &hs.pw, pw))) return s;
         }
         d.nt = S.Nt;
-        d.ng = (int)G.grp.size() / 3;
+        d.ng = (int)G.grp.size() / 2;
         d.nmisc = (int)G.misc.size();
         d.gr = G.gr;
         size_t smem = frame_smem_bytes(d);
@@ -450,10 +435,13 @@ rc_status alloc_cache(rc_ctx* ctx) {
         (s = dalloc(ctx, pool, &c.coef, NR * KSNAP)) || (s = dalloc(ctx, pool, &c.rstat, 4 * NR)) ||
         (s = dalloc(ctx, pool, &c.dstat, 3 * NR)) || (s = dalloc(ctx, pool, &c.sumpr, 2)) || (s = dalloc(ctx, pool, &c.npend, 2)) ||
         (s = dalloc(ctx, pool, &c.partf, G)) || (s = dalloc(ctx, pool, &c.partd, 3 * G)) || (s = dalloc(ctx, pool, &c.parti, G)) ||
-        (s = dalloc(ctx, pool, &c.ticket, 4)) || (s = dalloc(ctx, pool, &c.check, 2)))
+        (s = dalloc(ctx, pool, &c.ticket, 4)) || (s = dalloc(ctx, pool, &c.check, 2)) || (s = dalloc(ctx, pool, &c.rays, 1)) ||
+        (s = dalloc(ctx, pool, &c.pracc, 1)) || (s = dalloc(ctx, pool, &c.npacc, 1)))
         return s;
     CKR(cudaMemsetAsync(c.ticket, 0, 16, ctx->stream));
     CKR(cudaMemsetAsync(c.check, 0, 16, ctx->stream));
+    CKR(cudaMemsetAsync(c.pracc, 0, 8, ctx->stream));
+    CKR(cudaMemsetAsync(c.npacc, 0, 8, ctx->stream));
     CKR(cudaMemsetAsync(c.snap, 0, (size_t)KSNAP * Np * LCS * 4, ctx->stream));
     CKR(cudaMemsetAsync(c.m, 0, LCS * Np * 4, ctx->stream));
     CKR(cudaMemsetAsync(c.kk, 0, Np * 4, ctx->stream));
@@ -640,6 +628,7 @@ rc_status do_event(rc_ctx* ctx, int e, int si) {
     if (!B.ok) return fail(ctx, RC_ERR_UNSUPPORTED, "event needs more than %d kernel steps", MAX_EV_OPS);
     if (B.ev.nops == 0 && !B.ev.want_sumpr && B.ev.npend_mode == 0 && !B.ev.zero_rstat && !B.ev.zero_neq) return RC_OK;
     CKR(RC_DISPATCH(NL, event(B.ev, ctx->c, ctx->stream)));
+    ctx->run.last_kernels++;
     return RC_OK;
 }
 
@@ -709,7 +698,10 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
     const int f = R.f;
     cudaStream_t st = ctx->stream;
     rc_status s;
+    R.last_kernels = 0;
+    R.last_event = 0;
     if (f > 0 && R.prev_state != si) {
+        R.last_event = 1;
         if (tm) CKR(cudaEventRecord(ctx->ev[4], st));
         if ((s = do_event(ctx, R.prev_state, si)) != RC_OK) return s;
         if (tm) {
@@ -742,6 +734,7 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
     const bool fused = R.pend_left == 0 && R.proj_left == 0 && !M.ddgi;
     if (fused) {
         CKR(RC_DISPATCH(S.NL, frame(ctx->NW, track, true, d, S.g, S.grid, ctx->c, p, st)));
+        R.last_kernels += 1;
         if (tm) { CKR(cudaEventRecord(ctx->ev[2], st)); CKR(cudaEventRecord(ctx->ev[3], st)); }
     } else {
         CKR(RC_DISPATCH(S.NL, frame(ctx->NW, track, false, d, S.g, S.grid, ctx->c, p, st)));
@@ -751,6 +744,7 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
         if (tm) CKR(cudaEventRecord(ctx->ev[3], st));
         if (proj_apply_now) pu.want_err = 0;
         CKR(RC_DISPATCH(S.NL, update(d, S.g, ctx->c, pu, st)));
+        R.last_kernels += 2;
         if (R.pend_left > 0) R.pend_left--;
     }
     R.sum_cur = 1 - R.sum_cur;
@@ -764,12 +758,14 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
         CKR(cudaMemcpyAsync(ctx->c.coef, cf.data(), cf.size() * 4, cudaMemcpyHostToDevice, st));
         FrameParams pp = base_params(ctx);
         CKR(RC_DISPATCH(S.NL, proj_apply(ctx->c, S.g, pp, st)));
+        R.last_kernels += 1;
         CKR(cudaStreamSynchronize(st));   // cf lives on this stack frame
         R.pend_left = VERIF_FRAMES;
         if (rec_err) {
             FrameParams pe = base_params(ctx);
             pe.err_frame = R.nerr;
             CKR(RC_DISPATCH(S.NL, error(d, ctx->c, pe, st)));
+            R.last_kernels += 1;
         }
     }
     if (tm) {
@@ -784,6 +780,8 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
         tm->frames++;
     }
     if (rec_err) R.nerr++;
+    R.last_fused = fused ? 1 : 0;
+    ctx->launches += R.last_kernels;
     R.f = f + 1;
     return RC_OK;
 }
@@ -957,6 +955,7 @@ rc_status rc_run_begin(rc_ctx* ctx, const rc_method* m, int s0, uint32_t seed) {
         int z2[2] = {0, 0};
         CKR(cudaMemcpyAsync(c.sumpr, sp, 8, cudaMemcpyHostToDevice, st));
         CKR(cudaMemcpyAsync(c.npend, z2, 8, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemsetAsync(c.rays, 0, 8, st));
         CKR(cudaStreamSynchronize(st));   // host vectors above are about to go out of scope
     }
     R.p.seed = seed;
@@ -1095,6 +1094,8 @@ rc_status rc_scalar_get(rc_ctx* ctx, int which, int* value) {
         case RC_S_NSLOTS: *value = R.nslots; return RC_OK;
         case RC_S_LAST_EVENT: *value = R.last_event_f; return RC_OK;
         case RC_S_PROJK: *value = R.projK; return RC_OK;
+        case RC_S_LAST_FRAME_KERNELS: *value = R.last_kernels; return RC_OK;
+        case RC_S_LAST_FRAME_FUSED: *value = R.last_fused; return RC_OK;
     }
     return RC_ERR_ARG;
 }
@@ -1189,6 +1190,22 @@ rc_status rc_trace_check_count(rc_ctx* ctx, long long* mismatches, long long* ra
     CKR(cudaStreamSynchronize(ctx->stream));
     *mismatches = (long long)h[0];
     *rays = (long long)h[1];
+    return RC_OK;
+}
+
+rc_status rc_run_stats_get(rc_ctx* ctx, rc_run_stats* out) {
+    if (!ctx || !out) return RC_ERR_ARG;
+    memset(out, 0, sizeof *out);
+    out->launches = ctx->launches;
+    if (!ctx->have_scene) return RC_OK;
+    unsigned long long r = 0;
+    CKR(cudaMemcpyAsync(&r, ctx->c.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CKR(cudaStreamSynchronize(ctx->stream));
+    out->rays = (long long)r;
+    out->frames = ctx->run.f;
+    out->last_frame_kernels = ctx->run.last_kernels;
+    out->last_frame_fused = ctx->run.last_fused;
+    out->last_frame_event = ctx->run.last_event;
     return RC_OK;
 }
 

@@ -26,7 +26,8 @@ ARRAY_DTYPE = {A_LC: np.float32, A_LC2: np.float32, A_M: np.float32, A_N: np.flo
                A_KK: np.int32, A_PENDING: np.uint8, A_CUR: np.uint32, A_PREV: np.uint32, A_STALE: np.uint32,
                A_AGE: np.float32, A_SNAP: np.float32, A_NEQ: np.float32, A_COEF: np.float32, A_RSTAT: np.float32,
                A_DSTAT: np.float32, A_SUMPR: np.float32, A_NPEND: np.int32}
-(S_PEND_LEFT, S_DORMANT, S_PROJ_LEFT, S_FRAME, S_NSLOTS, S_LAST_EVENT, S_PROJK) = range(7)
+(S_PEND_LEFT, S_DORMANT, S_PROJ_LEFT, S_FRAME, S_NSLOTS, S_LAST_EVENT, S_PROJK, S_LAST_FRAME_KERNELS,
+ S_LAST_FRAME_FUSED) = range(9)
 SA_EDIR, SA_SV, SA_REF, SA_VALID, SA_PW = range(5)
 FLAG_BRUTE_FORCE = 1
 FLAG_CHECK_TRACE = 2
@@ -36,7 +37,7 @@ EXPORTS = [
     "rc_abi_version", "rc_status_string", "rc_create", "rc_destroy", "rc_last_error", "rc_device_info_get",
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
     "rc_errors", "rc_run", "rc_sync", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
-    "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_device_flags",
+    "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
 ]
 
 
@@ -58,6 +59,11 @@ class SceneInfo(ctypes.Structure):
 class DeviceInfo(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 256), ("sm_count", ctypes.c_int), ("cc_major", ctypes.c_int),
                 ("cc_minor", ctypes.c_int), ("mem_used_mb", ctypes.c_double), ("mem_total_mb", ctypes.c_double)]
+
+
+class RunStats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_longlong), ("rays", ctypes.c_longlong), ("launches", ctypes.c_longlong),
+                ("last_frame_kernels", ctypes.c_int), ("last_frame_fused", ctypes.c_int), ("last_frame_event", ctypes.c_int)]
 
 
 class RayRec(ctypes.Structure):
@@ -119,6 +125,8 @@ def load_library():
     L.rc_probe_rays.argtypes = [vp, i, ip, i, ctypes.POINTER(RayRec), i, ip]
     L.rc_trace_check_count.restype = i
     L.rc_trace_check_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
+    L.rc_run_stats_get.restype = i
+    L.rc_run_stats_get.argtypes = [vp, ctypes.POINTER(RunStats)]
     L.rc_device_flags.restype = i
     L.rc_device_flags.argtypes = [vp, ctypes.POINTER(ctypes.c_uint)]
     _lib = L
@@ -263,6 +271,11 @@ class Context:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
         self._chk(self.L.rc_trace_check_count(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def stats(self) -> dict:
+        st = RunStats()
+        self._chk(self.L.rc_run_stats_get(self.h, ctypes.byref(st)))
+        return {n: getattr(st, n) for n, _ in RunStats._fields_}
 
     def device_flags(self) -> int:
         v = ctypes.c_uint()

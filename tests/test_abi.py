@@ -1,0 +1,70 @@
+"""The C-ABI library builds, loads and exports every entry point of include/rc_api.h (no GPU
+needed: nothing here launches a kernel)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "rc_api.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(rc_[a-z_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from render_engine_gb300 import build
+    path = build.build()
+    return path
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "rc_create" in names and "rc_frame" in names and len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol(lib):
+    L = ctypes.CDLL(lib)
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (rc_[a-z_]+)$", out, flags=re.M))
+    assert set(declared_functions()) <= exported
+
+
+def test_python_binding_lists_every_symbol():
+    from render_engine_gb300 import native
+    assert sorted(native.EXPORTS) == declared_functions()
+
+
+def test_status_strings_and_version(lib):
+    L = ctypes.CDLL(lib)
+    L.rc_status_string.restype = ctypes.c_char_p
+    assert L.rc_abi_version() == 1
+    assert L.rc_status_string(0) == b"ok"
+    assert b"CUDA" in L.rc_status_string(4)
+
+
+def test_binaries_built(lib):
+    d = os.path.dirname(lib)
+    for n in ("poc_gpu_l3", "poc_gpu_l8"):
+        assert os.access(os.path.join(d, n), os.X_OK)
+
+
+def test_cli_rejects_unknown_mode_without_gpu(lib):
+    exe = os.path.join(os.path.dirname(lib), "poc_gpu_l3")
+    r = subprocess.run([exe, "taa", "x.bin"], capture_output=True, text=True)
+    assert r.returncode == 1 and "not provided" in r.stderr
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    from render_engine_gb300 import native
+    monkeypatch.setattr(native, "LIB_PATH", str(tmp_path / "absent.so"))
+    monkeypatch.setattr(native, "_lib", None)
+    with pytest.raises(RuntimeError):
+        native.load_library()
