@@ -102,6 +102,13 @@ typedef struct rc_run_stats {
     int last_frame_event;    /* 1 when the last frame started with an event */
 } rc_run_stats;
 
+/* Pinhole camera of the image pass. */
+typedef struct rc_camera {
+    float eye[3], at[3], up[3];
+    float fov_y_deg;     /* vertical field of view */
+    int width, height;   /* pixels, e.g. 1920 x 1080 */
+} rc_camera;
+
 /* Per-ray record of rc_probe_rays. */
 typedef struct rc_ray_rec {
     int point, ray;
@@ -160,6 +167,13 @@ rc_status rc_errors(rc_ctx* ctx, float* out, int max, int* n);
 rc_status rc_run(rc_ctx* ctx, const rc_method* m, const int* seq, int nframes, uint32_t seed,
                  int want_err, float* errs, rc_timers* tm);
 rc_status rc_sync(rc_ctx* ctx);
+
+/* Image pass (no counterpart in the reference, whose bench B has no camera): one primary ray
+ * per pixel through the geometry of `state`, shaded from the current cache with the light
+ * every cache ray gathers, A * (direct + cached indirect).  Asynchronous when `image` is NULL
+ * (the image stays in a buffer of the context); otherwise the image (width * height floats,
+ * row-major, top row first) is copied to `image`. */
+rc_status rc_render(rc_ctx* ctx, int state, const rc_camera* cam, float* image, size_t image_floats);
 
 /* Run-state access for parity harnesses: size and device pointer of an array, and a copy
  * between the array and a host buffer of exactly `nbytes` (to_device=0: device to host,

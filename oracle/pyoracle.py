@@ -69,6 +69,7 @@ def lib():
         L.osc_run_scalar.restype = ctypes.c_int
         L.osc_run_scalar.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.osc_set_threads.argtypes = [ctypes.c_int]
+        L.osc_run_set_scalar.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.osc_probe_rays.restype = ctypes.c_int
         L.osc_probe_rays.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(RayRec), ctypes.c_int]
@@ -157,6 +158,9 @@ class Run:
 
     def scalar(self, which: int) -> int:
         return lib().osc_run_scalar(self.p, which)
+
+    def set_scalar(self, which: int, value: int):
+        lib().osc_run_set_scalar(self.p, which, int(value))
 
     def probe(self, state: int, points) -> list[tuple]:
         pts = (ctypes.c_int * len(points))(*[int(x) for x in points])

@@ -542,6 +542,18 @@ void* osc_run_array(osc_run* r, int which, size_t* nb) {
     return NULL;
 }
 
+void osc_run_set_scalar(osc_run* r, int which, int v) {
+    switch (which) {
+        case 0: r->pend_left = v; break;
+        case 1: r->dormant = v; break;
+        case 2: r->proj_left = v; break;
+        case 3: r->f = v; break;
+        case 4: r->nslots = v; break;
+        case 5: r->last_event_f = v; break;
+        case 6: r->projK = v; break;
+    }
+}
+
 int osc_run_scalar(osc_run* r, int which) {
     switch (which) {
         case 0: return r->pend_left;

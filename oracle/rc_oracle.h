@@ -66,6 +66,7 @@ int osc_frame(osc_run* r, int si, int want_err, double err3[3], float* err);
 void* osc_run_array(osc_run* r, int which, size_t* nbytes);
 /* Scalars: 0 pend_left, 1 dormant, 2 proj_left, 3 frame, 4 nslots, 5 last_event_f, 6 projK */
 int osc_run_scalar(osc_run* r, int which);
+void osc_run_set_scalar(osc_run* r, int which, int value);
 void osc_set_threads(int n);
 
 /* One-frame trace probe: rays of the listed points for (state, seed, frame) with the

@@ -147,10 +147,10 @@ __device__ __forceinline__ void mt_tri(const float4* __restrict__ tri, int j, f3
 }
 
 // Plane-culling group: the axis-aligned triangles of one quad lying in one plane k = c.
-// 2 float4: (c, lo_a, hi_a, lo_b) (hi_b, first triangle bits, count bits, 0), where a, b are
-// the two other axes in increasing order and the box is the triangles' bounding box grown by
-// a margin far above the rounding error of the exact test, so the filter never drops the
-// triangle the exact scan would pick.
+// 2 float4: (c, centre_a, half_a, centre_b) (half_b, first triangle bits, count bits, 0), where
+// a, b are the two other axes in increasing order and the box is the triangles' bounding box
+// grown by a margin far above the rounding error of the exact test, so the filter never drops
+// the triangle the exact scan would pick.
 struct GroupRanges { int g0[4]; };  // groups of axis 0 in [g0[0], g0[1]), axis 1 [g0[1], g0[2]), axis 2 [g0[2], g0[3])
 
 }  // namespace rc

@@ -94,6 +94,14 @@ struct FrameParams {
     int brute, check;          // trace options
 };
 
+// Pinhole camera of the image pass: pixel (x, y) looks along
+// fwd + right * ((x + 0.5) / w * 2 - 1) * tx + up * (1 - (y + 0.5) / h * 2) * ty.
+struct CameraD {
+    float eye[3], fwd[3], right[3], up[3];
+    float tx, ty;
+    int w, h;
+};
+
 // Event program: the per-point kernels of one event of Runner::run, in launch order.
 enum EvKind { EV_SNAP_SAVE = 0, EV_ORACLE, EV_RESCALE, EV_WAKE, EV_TOUCHED, EV_SNAP_RESTORE, EV_RESTORED };
 struct EvOp {
@@ -130,6 +138,8 @@ struct Ops {
     static cudaError_t event(const EvProgram& ev, const DevCache& c, cudaStream_t st);
     static cudaError_t error(const DState& s, const DevCache& c, const FrameParams& p, cudaStream_t st);
     static cudaError_t proj_apply(const DevCache& c, const DStatic& g, const FrameParams& p, cudaStream_t st);
+    static cudaError_t camera(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                              const CameraD& cam, float* img, cudaStream_t st);
     static cudaError_t probe(int NW, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                              const int* pts, int npts, void* recs, int maxrec, int* nrec, cudaStream_t st);
 };

@@ -145,16 +145,51 @@ struct TraceSmem {
     const int* misc;
 };
 
-// Plane filter of one group: the ray's crossing of the group's plane (t = (c - o_k) / d_k)
-// is a candidate when it lies ahead of the origin and inside the group's outer box.
+// Plane filter of one group: the ray's crossing of the group's plane (t = (c - o_k) / d_k) is a
+// candidate when it lies ahead of the origin and inside the group's outer box, stored as centre
+// and half extent so each in-plane test is one subtraction and one |x| <= h comparison.  The
+// candidate bit is shifted in (mask = mask << 1 | hit), so group g ends at bit ng - 1 - g.
+template <typename MaskT>
 __device__ __forceinline__ void filter_group(const float4* __restrict__ grp, int g, float ok, float idk, float oa, float da,
-                                             float ob, float db, unsigned long long& mask) {
+                                             float ob, float db, MaskT& mask) {
     const float4 G0 = grp[2 * g];
     const float hb = grp[2 * g + 1].x;
     const float tk = (G0.x - ok) * idk;
     const float xa = oa + tk * da, xb = ob + tk * db;
-    const bool in = tk > 5e-5f && xa >= G0.y && xa <= G0.z && xb >= G0.w && xb <= hb;
-    mask |= in ? (1ull << g) : 0ull;
+    const bool in = tk > 5e-5f && fabsf(xa - G0.y) <= G0.z && fabsf(xb - G0.w) <= hb;
+    mask = (mask << 1) | (MaskT)in;
+}
+
+template <typename MaskT>
+__device__ __forceinline__ void trace_groups(const TraceSmem& sm, const DState& s, f3 o, f3 d, float& tmin, int& q, int& jb) {
+    MaskT mask = 0;
+    const float idx = 1.f / d.x, idy = 1.f / d.y, idz = 1.f / d.z;
+#pragma unroll 4
+    for (int g = s.gr.g0[0]; g < s.gr.g0[1]; ++g) filter_group(sm.grp, g, o.x, idx, o.y, d.y, o.z, d.z, mask);
+#pragma unroll 4
+    for (int g = s.gr.g0[1]; g < s.gr.g0[2]; ++g) filter_group(sm.grp, g, o.y, idy, o.x, d.x, o.z, d.z, mask);
+#pragma unroll 4
+    for (int g = s.gr.g0[2]; g < s.gr.g0[3]; ++g) filter_group(sm.grp, g, o.z, idz, o.x, d.x, o.y, d.y, mask);
+    const int top = s.ng - 1;
+    float thr = tmin * 1.0001f + 1e-5f;
+    while (mask) {
+        float best = __int_as_float(0x7f800000);
+        int bb = 0;
+        for (MaskT m = mask; m; m &= m - 1) {
+            const int b = sizeof(MaskT) == 8 ? __ffsll((long long)m) - 1 : __ffs((int)m) - 1;
+            const int g = top - b;
+            const float ok = g < s.gr.g0[1] ? o.x : (g < s.gr.g0[2] ? o.y : o.z);
+            const float idk = g < s.gr.g0[1] ? idx : (g < s.gr.g0[2] ? idy : idz);
+            const float tk = (sm.grp[2 * g].x - ok) * idk;
+            if (tk < best) { best = tk; bb = b; }
+        }
+        if (!(best <= thr)) break;
+        mask &= ~((MaskT)1 << bb);
+        const float4 G1 = sm.grp[2 * (top - bb) + 1];
+        const int j0 = __float_as_int(G1.y), cnt = __float_as_int(G1.z);
+        for (int j = j0; j < j0 + cnt; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
+        thr = tmin * 1.0001f + 1e-5f;
+    }
 }
 
 // Closest dynamic-triangle hit, equal to the reference's in-order scan (poc_gpu.cu:199-220).
@@ -171,32 +206,8 @@ __device__ __forceinline__ void trace_dyn(const TraceSmem& sm, const DState& s, 
         return;
     }
     for (int k = 0; k < s.nmisc; ++k) mt_tri(sm.tri, sm.misc[k], o, d, tmin, q, jb);
-    unsigned long long mask = 0ull;
-    const float idx = 1.f / d.x, idy = 1.f / d.y, idz = 1.f / d.z;
-#pragma unroll 4
-    for (int g = s.gr.g0[0]; g < s.gr.g0[1]; ++g) filter_group(sm.grp, g, o.x, idx, o.y, d.y, o.z, d.z, mask);
-#pragma unroll 4
-    for (int g = s.gr.g0[1]; g < s.gr.g0[2]; ++g) filter_group(sm.grp, g, o.y, idy, o.x, d.x, o.z, d.z, mask);
-#pragma unroll 4
-    for (int g = s.gr.g0[2]; g < s.gr.g0[3]; ++g) filter_group(sm.grp, g, o.z, idz, o.x, d.x, o.y, d.y, mask);
-    float thr = tmin * 1.0001f + 1e-5f;
-    while (mask) {
-        float best = __int_as_float(0x7f800000);
-        int bg = 0;
-        for (unsigned long long m = mask; m; m &= m - 1ull) {
-            const int g = __ffsll((long long)m) - 1;
-            const float ok = g < s.gr.g0[1] ? o.x : (g < s.gr.g0[2] ? o.y : o.z);
-            const float idk = g < s.gr.g0[1] ? idx : (g < s.gr.g0[2] ? idy : idz);
-            const float tk = (sm.grp[2 * g].x - ok) * idk;
-            if (tk < best) { best = tk; bg = g; }
-        }
-        if (!(best <= thr)) break;
-        mask &= ~(1ull << bg);
-        const float4 G1 = sm.grp[2 * bg + 1];
-        const int j0 = __float_as_int(G1.y), cnt = __float_as_int(G1.z);
-        for (int j = j0; j < j0 + cnt; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
-        thr = tmin * 1.0001f + 1e-5f;
-    }
+    if (s.ng <= 32) trace_groups<unsigned>(sm, s, o, d, tmin, q, jb);
+    else trace_groups<unsigned long long>(sm, s, o, d, tmin, q, jb);
 }
 
 // poc_gpu.cu:288-295
@@ -453,6 +464,15 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
         for (int w = 0; w < NW; ++w) m[w] = 0u;
         const float c0 = pend ? c.c0[i] : 0.f;
         float sd = 0.f, sq = 0.f;
+        // the point's own cache and age, read before tracing so the loads overlap the trace
+        float4 own[LCS / 4];
+        float age_i = 0.f;
+        if (FUSED) {
+            const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)i * (LCS / 4);
+#pragma unroll
+            for (int k4 = 0; k4 < LCS / 4; ++k4) own[k4] = __ldcg(lcp + k4);
+            if (p.ramp) age_i = c.age[i];
+        }
         for (int r = 0; r < k; ++r) {
             const float u1 = rnd(rs);
             const float u2 = rnd(rs);
@@ -536,14 +556,11 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
             }
         } else {
             // k_update (poc_gpu.cu:562-602) on the point's own history.
-            float4 lc[LCS / 4];
-            const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)i * (LCS / 4);
-#pragma unroll
-            for (int k4 = 0; k4 < LCS / 4; ++k4) lc[k4] = __ldcg(lcp + k4);
+            const float4 (&lc)[LCS / 4] = own;
             float nn = n_i + k;
             float nmx = p.nmax;
             if (p.ramp) {
-                float a = c.age[i];
+                const float a = age_i;
                 nmx = fminf(p.nmax, (4.f + 0.5f * a) * p.rays);
                 c.age[i] = fminf(a + 1.f, 1e4f);
             }
@@ -557,7 +574,9 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
                     const float a = comp(lc, l);
                     float al = ((p.resp_mask >> l) & 1) ? alpha_r : alpha;
                     if ((p.dormant >> l) & 1) al = 0.f;
-                    out[l] = a + al * (acc[l] * ik - a);
+                    // the reference stores m = acc * ik (one rounding) before k_update reads it;
+                    // __fmul_rn keeps that rounding (no fused multiply-add into the blend)
+                    out[l] = a + al * (__fmul_rn(acc[l], ik) - a);
                     if (!((p.dormant >> l) & 1)) est += out[l];
                 } else {
                     out[l] = 0.f;
@@ -879,6 +898,46 @@ __global__ void __launch_bounds__(BLOCK) k_error(const DState s, const DevCache 
     }
 }
 
+// ------------------------------------------------------------------ image pass
+// One primary ray per pixel from a pinhole camera: closest hit with the frame's tracer, the
+// hit's cache point, and the light leaving it toward the camera, A * sum over the lit lights
+// of (direct + cached indirect) -- the quantity every cache ray gathers (poc_gpu.cu:471-478).
+// Pixels whose ray hits nothing, a back face or an absent cell are 0.  16 x 16 pixel tiles.
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_camera(const DState s, const DStatic g, const Grid grid, const DevCache c,
+                                                  const FrameParams p, const CameraD cam, float* __restrict__ img) {
+    extern __shared__ float4 sm[];
+    constexpr int LCS = lcs_of(NL), AES = aes_of(NL);
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= cam.w || y >= cam.h) return;
+    const float sx = ((x + 0.5f) / cam.w * 2.f - 1.f) * cam.tx, sy = (1.f - (y + 0.5f) / cam.h * 2.f) * cam.ty;
+    f3 D = mk(cam.fwd[0] + cam.right[0] * sx + cam.up[0] * sy, cam.fwd[1] + cam.right[1] * sx + cam.up[1] * sy,
+              cam.fwd[2] + cam.right[2] * sx + cam.up[2] * sy);
+    D = D * rsqrtf(dot(D, D));
+    const f3 O = mk(cam.eye[0], cam.eye[1], cam.eye[2]);
+    const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, 0);
+    float val = 0.f;
+    if (h.q != -1 && !h.back) {
+        float4 ae[AES / 4], lc[LCS / 4];
+        const float4* aep = s.AE + (size_t)h.pi * (AES / 4);
+        const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)h.pi * (LCS / 4);
+#pragma unroll
+        for (int k4 = 0; k4 < AES / 4; ++k4) ae[k4] = __ldg(aep + k4);
+#pragma unroll
+        for (int k4 = 0; k4 < LCS / 4; ++k4) lc[k4] = __ldcg(lcp + k4);
+        const float A = ae[0].x;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+            const float lcv = ((p.dormant >> l) & 1) ? 0.f : comp(lc, l);
+            val += A * (comp(ae, l + 1) + lcv);
+        }
+    }
+    img[(size_t)y * cam.w + x] = val;
+}
+
 // ------------------------------------------------------------------ probe
 struct RayRecD { int point, ray, q, pi, back; float t; };
 
@@ -988,6 +1047,17 @@ cudaError_t Ops<NL>::error(const DState& s, const DevCache& c, const FrameParams
 template <int NL>
 cudaError_t Ops<NL>::proj_apply(const DevCache& c, const DStatic& g, const FrameParams& p, cudaStream_t st) {
     k_proj_apply<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(c, g, p);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::camera(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                            const CameraD& cam, float* img, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+    cudaError_t e = prep_smem(k_camera<NL>, smem);
+    if (e != cudaSuccess) return e;
+    dim3 grd((cam.w + 15) / 16, (cam.h + 15) / 16);
+    k_camera<NL><<<grd, BLOCK, smem, st>>>(s, g, grid, c, p, cam, img);
     return cudaGetLastError();
 }
 

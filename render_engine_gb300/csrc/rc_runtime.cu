@@ -94,6 +94,8 @@ struct rc_ctx {
     double cache_bytes = 0;
     long long launches = 0;
     unsigned* flags_dev = nullptr;
+    float* img = nullptr;
+    size_t img_cap = 0;
     cudaEvent_t ev[8] = {};
 };
 
@@ -246,17 +248,20 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
     out.gr.g0[2] = cnt[0] + cnt[1];
     out.gr.g0[3] = cnt[0] + cnt[1] + cnt[2];
     for (auto& g : gs) {
-        float olo[2], ohi[2];
+        // centre and half extent of the box grown by the margin, in double so the float box
+        // still contains the grown box
+        float ctr[2], half[2];
         for (int u = 0; u < 2; ++u) {
-            const float m = 2e-3f + 1e-4f * (g.hi[u] - g.lo[u]) + 1e-6f * (fabsf(g.lo[u]) + fabsf(g.hi[u]));
-            olo[u] = g.lo[u] - m;
-            ohi[u] = g.hi[u] + m;
+            const double m = 2e-3 + 1e-4 * ((double)g.hi[u] - g.lo[u]) + 1e-6 * (fabs((double)g.lo[u]) + fabs((double)g.hi[u]));
+            const double lo = (double)g.lo[u] - m, hi = (double)g.hi[u] + m;
+            ctr[u] = (float)(0.5 * (lo + hi));
+            half[u] = (float)(0.5 * (hi - lo) + 1e-6 * (fabs(lo) + fabs(hi)));
         }
         int j0 = g.j0, c = g.cnt, z = 0;
         float fj0, fc, fz;
         memcpy(&fj0, &j0, 4); memcpy(&fc, &c, 4); memcpy(&fz, &z, 4);
-        out.grp.push_back(make_float4(g.c, olo[0], ohi[0], olo[1]));
-        out.grp.push_back(make_float4(ohi[1], fj0, fc, fz));
+        out.grp.push_back(make_float4(g.c, ctr[0], half[0], ctr[1]));
+        out.grp.push_back(make_float4(half[1], fj0, fc, fz));
     }
     std::sort(misc.begin(), misc.end());
     out.misc = misc;
@@ -847,6 +852,7 @@ void rc_destroy(rc_ctx* ctx) {
     free_pool(ctx->cache_bufs);
     free_pool(ctx->scene_bufs);
     if (ctx->flags_dev) cudaFree(ctx->flags_dev);
+    if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -1004,6 +1010,52 @@ rc_status rc_run(rc_ctx* ctx, const rc_method* m, const int* seq, int nframes, u
 rc_status rc_sync(rc_ctx* ctx) {
     if (!ctx) return RC_ERR_ARG;
     CKR(cudaStreamSynchronize(ctx->stream));
+    return RC_OK;
+}
+
+rc_status rc_render(rc_ctx* ctx, int state, const rc_camera* cam, float* image, size_t image_floats) {
+    if (!ctx || !cam) return RC_ERR_ARG;
+    if (!ctx->run.active) return fail(ctx, RC_ERR_STATE, "no run begun");
+    const Scene& S = ctx->S;
+    if (state < 0 || state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", state);
+    if (cam->width <= 0 || cam->height <= 0 || cam->width > 16384 || cam->height > 16384 || !(cam->fov_y_deg > 0.f && cam->fov_y_deg < 179.f))
+        return fail(ctx, RC_ERR_ARG, "bad camera");
+    const size_t npx = (size_t)cam->width * cam->height;
+    if (image && image_floats != npx) return fail(ctx, RC_ERR_ARG, "image holds %zu floats, not %zu", image_floats, npx);
+    if (npx > ctx->img_cap) {
+        if (ctx->img) { CKR(cudaStreamSynchronize(ctx->stream)); cudaFree(ctx->img); ctx->img = nullptr; }
+        cudaError_t e = cudaMalloc(&ctx->img, npx * sizeof(float));
+        if (e != cudaSuccess) { ctx->img_cap = 0; return fail(ctx, RC_ERR_NOMEM, "image buffer: %s", cudaGetErrorString(e)); }
+        ctx->img_cap = npx;
+    }
+    // camera frame: forward to the target, right = forward x up, up re-orthogonalised
+    double f[3], r[3], u[3];
+    for (int k = 0; k < 3; ++k) f[k] = (double)cam->at[k] - cam->eye[k];
+    double fl = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    if (!(fl > 0)) return fail(ctx, RC_ERR_ARG, "camera eye equals target");
+    for (int k = 0; k < 3; ++k) f[k] /= fl;
+    r[0] = f[1] * cam->up[2] - f[2] * cam->up[1];
+    r[1] = f[2] * cam->up[0] - f[0] * cam->up[2];
+    r[2] = f[0] * cam->up[1] - f[1] * cam->up[0];
+    double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    if (!(rl > 0)) return fail(ctx, RC_ERR_ARG, "camera up is parallel to the view direction");
+    for (int k = 0; k < 3; ++k) r[k] /= rl;
+    u[0] = r[1] * f[2] - r[2] * f[1];
+    u[1] = r[2] * f[0] - r[0] * f[2];
+    u[2] = r[0] * f[1] - r[1] * f[0];
+    CameraD cd;
+    for (int k = 0; k < 3; ++k) { cd.eye[k] = cam->eye[k]; cd.fwd[k] = (float)f[k]; cd.right[k] = (float)r[k]; cd.up[k] = (float)u[k]; }
+    cd.ty = (float)tan(0.5 * cam->fov_y_deg * 3.14159265358979323846 / 180.0);
+    cd.tx = cd.ty * (float)cam->width / (float)cam->height;
+    cd.w = cam->width;
+    cd.h = cam->height;
+    FrameParams p = base_params(ctx);
+    CKR(RC_DISPATCH(S.NL, camera(S.st[state].d, S.g, S.grid, ctx->c, p, cd, ctx->img, ctx->stream)));
+    ctx->launches++;
+    if (image) {
+        CKR(cudaMemcpyAsync(image, ctx->img, npx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CKR(cudaStreamSynchronize(ctx->stream));
+    }
     return RC_OK;
 }
 

@@ -36,7 +36,7 @@ FLAG_CHECK_TRACE = 2
 EXPORTS = [
     "rc_abi_version", "rc_status_string", "rc_create", "rc_destroy", "rc_last_error", "rc_device_info_get",
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
-    "rc_errors", "rc_run", "rc_sync", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
+    "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
     "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
 ]
 
@@ -59,6 +59,21 @@ class SceneInfo(ctypes.Structure):
 class DeviceInfo(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 256), ("sm_count", ctypes.c_int), ("cc_major", ctypes.c_int),
                 ("cc_minor", ctypes.c_int), ("mem_used_mb", ctypes.c_double), ("mem_total_mb", ctypes.c_double)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_float * 3), ("at", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("fov_y_deg", ctypes.c_float), ("width", ctypes.c_int), ("height", ctypes.c_int)]
+
+
+def camera(eye, at, up=(0.0, 0.0, 1.0), fov_y_deg=70.0, width=1920, height=1080) -> Camera:
+    c = Camera()
+    c.eye[:] = [float(x) for x in eye]
+    c.at[:] = [float(x) for x in at]
+    c.up[:] = [float(x) for x in up]
+    c.fov_y_deg = float(fov_y_deg)
+    c.width, c.height = int(width), int(height)
+    return c
 
 
 class RunStats(ctypes.Structure):
@@ -111,6 +126,8 @@ def load_library():
     L.rc_run.argtypes = [vp, ctypes.POINTER(CMethod), ip, i, u32, i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(Timers)]
     L.rc_sync.restype = i
     L.rc_sync.argtypes = [vp]
+    L.rc_render.restype = i
+    L.rc_render.argtypes = [vp, i, ctypes.POINTER(Camera), ctypes.POINTER(ctypes.c_float), sz]
     L.rc_array_info.restype = i
     L.rc_array_info.argtypes = [vp, i, ctypes.POINTER(sz), ctypes.POINTER(vp)]
     L.rc_array_copy.restype = i
@@ -224,6 +241,15 @@ class Context:
 
     def sync(self):
         self._chk(self.L.rc_sync(self.h))
+
+    def render(self, state: int, cam: Camera, copy: bool = True):
+        """Image pass from the current cache; returns an (h, w) float32 image when copy."""
+        if not copy:
+            self._chk(self.L.rc_render(self.h, state, ctypes.byref(cam), None, 0))
+            return None
+        img = np.empty((cam.height, cam.width), np.float32)
+        self._chk(self.L.rc_render(self.h, state, ctypes.byref(cam), img.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), img.size))
+        return img
 
     def array(self, which: int) -> np.ndarray:
         n = ctypes.c_size_t()
