@@ -70,6 +70,10 @@ def lib():
         L.osc_run_scalar.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.osc_set_threads.argtypes = [ctypes.c_int]
         L.osc_run_set_scalar.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.osc_render.restype = ctypes.c_int
+        L.osc_render.argtypes = [ctypes.c_void_p, ctypes.c_int, fp, fp, fp, fp, ctypes.c_float, ctypes.c_float, ctypes.c_int,
+                                 ctypes.c_int, fp]
         L.osc_probe_rays.restype = ctypes.c_int
         L.osc_probe_rays.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(RayRec), ctypes.c_int]
@@ -168,6 +172,16 @@ class Run:
         out = (RayRec * cap)()
         n = lib().osc_probe_rays(self.p, state, pts, len(points), out, cap)
         return [(r.point, r.ray, r.q, r.pi, r.back, r.t) for r in out[:n]]
+
+    def render(self, state: int, basis: dict, w: int, h: int) -> np.ndarray:
+        """basis: eye, fwd, right, up (3 floats each), tx, ty -- the float camera frame."""
+        out = np.empty((h, w), np.float32)
+        f = lambda k: (ctypes.c_float * 3)(*[float(x) for x in basis[k]])
+        rc = lib().osc_render(self.p, state, f("eye"), f("fwd"), f("right"), f("up"), basis["tx"], basis["ty"], w, h,
+                              out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        if rc != 0:
+            raise ValueError("render")
+        return out
 
     def __del__(self):
         if getattr(self, "p", None):

@@ -1097,3 +1097,36 @@ int osc_probe_rays(osc_run* r, int si, const int* pts, int npts, osc_ray_rec* ou
     }
     return n;
 }
+
+/* Image pass of the product (no reference counterpart): pinhole camera, closest hit, cache
+ * point, A * sum over lights of (direct + cached indirect, dormant lights without cache). */
+int osc_render(osc_run* r, int si, const float* eye, const float* fwd, const float* right, const float* up, float tx, float ty,
+               int w, int h, float* out) {
+    const osc_scene* S = r->S;
+    if (si < 0 || si >= S->NS || w <= 0 || h <= 0) return -1;
+    const ostate* st = &S->st[si];
+    const int NL = S->NL;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            float sx = (((float)x + 0.5f) / (float)w * 2.f - 1.f) * tx, sy = (1.f - ((float)y + 0.5f) / (float)h * 2.f) * ty;
+            v3 D = V(fwd[0] + right[0] * sx + up[0] * sy, fwd[1] + right[1] * sx + up[1] * sy, fwd[2] + right[2] * sx + up[2] * sy);
+            D = vmul(D, 1.f / sqrtf(vdot(D, D)));
+            v3 O = V(eye[0], eye[1], eye[2]);
+            float t;
+            int q, pi;
+            int hit = trace_full(S, st, O, D, &t, &q);
+            v3 H = hit ? vadd(O, vmul(D, t)) : O;
+            int back = resolve_hit(S, st, hit, H, D, q, 0, &pi);
+            float val = 0.f;
+            if (hit && !back) {
+                float A = S->A[pi];
+                for (int l = 0; l < NL; ++l) {
+                    float lc = ((r->dormant >> l) & 1) ? 0.f : r->Lc[(size_t)NL * pi + l];
+                    val += A * (st->Edir[(size_t)NL * pi + l] + lc);
+                }
+            }
+            out[(size_t)y * w + x] = val;
+        }
+    return 0;
+}

@@ -74,6 +74,10 @@ void osc_set_threads(int n);
 typedef struct { int point, ray, q, pi, back; float t; } osc_ray_rec;
 int osc_probe_rays(osc_run* r, int si, const int* pts, int npts, osc_ray_rec* out, int maxrec);
 
+/* Image pass (pinhole camera, one ray per pixel), see rc_render in include/rc_api.h. */
+int osc_render(osc_run* r, int si, const float* eye, const float* fwd, const float* right, const float* up, float tx, float ty,
+               int w, int h, float* out);
+
 enum {
     OSC_A_LC = 0, OSC_A_LC2, OSC_A_M, OSC_A_N, OSC_A_C0, OSC_A_KK, OSC_A_PENDING, OSC_A_CUR, OSC_A_PREV,
     OSC_A_STALE, OSC_A_AGE, OSC_A_SNAP, OSC_A_NEQ, OSC_A_COEF, OSC_A_RSTAT, OSC_A_DSTAT, OSC_A_SUMPR,

@@ -307,3 +307,20 @@ class Context:
         v = ctypes.c_uint()
         self._chk(self.L.rc_device_flags(self.h, ctypes.byref(v)))
         return v.value
+
+
+def camera_basis(cam: Camera) -> dict:
+    """The float camera frame rc_render derives from a Camera (same double arithmetic)."""
+    import math
+    f = [float(cam.at[k]) - float(cam.eye[k]) for k in range(3)]
+    fl = math.sqrt(sum(x * x for x in f))
+    f = [x / fl for x in f]
+    u0 = [float(cam.up[k]) for k in range(3)]
+    r = [f[1] * u0[2] - f[2] * u0[1], f[2] * u0[0] - f[0] * u0[2], f[0] * u0[1] - f[1] * u0[0]]
+    rl = math.sqrt(sum(x * x for x in r))
+    r = [x / rl for x in r]
+    u = [r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]]
+    ty = np.float32(math.tan(0.5 * float(cam.fov_y_deg) * math.pi / 180.0))
+    tx = np.float32(ty * np.float32(cam.width) / np.float32(cam.height))
+    return {"eye": [float(cam.eye[k]) for k in range(3)], "fwd": [float(np.float32(x)) for x in f],
+            "right": [float(np.float32(x)) for x in r], "up": [float(np.float32(x)) for x in u], "tx": float(tx), "ty": float(ty)}

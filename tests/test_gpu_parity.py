@@ -209,3 +209,24 @@ def test_million_point_scene_runs_clean():
     lc = ctx.array(N.A_LC)
     assert np.isfinite(lc).all() and lc.max() > 0
     assert ctx.device_flags() == 0
+
+
+def test_image_pass_vs_oracle(scene_main_bytes):
+    """The 1920x1080-class image pass (no reference counterpart) against the CPU oracle's
+    restatement on the same cache: same pixel values except at geometric edges."""
+    ctx = _ctx(scene_main_bytes)
+    orc = po.Run(po.Scene(data=scene_main_bytes))
+    m = M.by_name(M.timing_methods(), "v4-A2C suivi 1/4")
+    seq = [0] * 6 + [1] * 4
+    ctx.begin(m, 0, 5)
+    orc.begin(m, 0, 5)
+    for s in seq:
+        ctx.frame(s)
+    orc.array(po.A_LC)[...] = ctx.array(N.A_LC)
+    orc.set_scalar(N.S_DORMANT, ctx.scalar(N.S_DORMANT))
+    cam = N.camera(eye=(0.5, 0.6, 1.6), at=(7.5, 3.0, 1.0), fov_y_deg=70.0, width=640, height=360)
+    img = ctx.render(1, cam)
+    ref = orc.render(1, N.camera_basis(cam), 640, 360)
+    assert np.isfinite(img).all() and img.max() > 0
+    close = np.isclose(img, ref, rtol=1e-4, atol=1e-6)
+    assert close.mean() > 0.995, close.mean()
