@@ -195,6 +195,27 @@ rc_status rc_run_stats_get(rc_ctx* ctx, rc_run_stats* out);
 /* Device-side guard flags raised since the last call (then reset); 0 = none. */
 rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags);
 
+/* Error sums without any device allocation.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory themselves -- a renderer whose per-frame path
+ * runs under a budget fixed at start-up (cudaMalloc / cudaFree synchronise the device and can
+ * fail mid-frame), or a process whose own memory manager owns all device memory and passes
+ * this library only buffers it already holds.  All pointers are device pointers owned by the
+ * caller: the cache `lc` (`lc_stride` floats per point, the first `nl` used; lights whose bit
+ * is set in `dormant` are left out, as in rc_frame's error), the reference `ref` and the
+ * valid flags `valid` of `np` points.  Writes to `out3` (3 doubles, device memory) the FP64
+ * sum of squared errors, the sum of the reference and the count of valid points -- the sums
+ * rc_frame records when asked for the error -- on `stream` (NULL = the legacy default
+ * stream), asynchronously.  Scratch space is a fixed array in the library (393,224 bytes on
+ * every GPU that loads it, held until the process exits), so np may not exceed
+ * RC_NOALLOC_MAX_POINTS (RC_ERR_ARG otherwise).  The first call on a device looks up that
+ * array's address for the device; make that first call before any stream capture.  Every
+ * call uses the same array: calls whose work overlaps on the GPU (on different streams, or
+ * from different threads) race and give wrong sums.  Allocates nothing: no cudaMalloc,
+ * no cudaFree, no allocating library routine. */
+#define RC_NOALLOC_MAX_POINTS 4194304
+rc_status rc_error_sums_noalloc(const float* lc, int lc_stride, int nl, int dormant, const float* ref,
+                                const uint8_t* valid, int np, double* out3, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,10 +62,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, deps):
             jobs.append([nv, *ARCH, *FLAGS, "-DRC_NL_ONE=%d" % nl, "-c", os.path.join(CSRC, "rc_kernels.cu"), "-o", o])
-    o = os.path.join(OUT, "rc_runtime.o")
-    objs.append(o)
-    if force or _stale(o, deps):
-        jobs.append([nv, *ARCH, *FLAGS, "-c", os.path.join(CSRC, "rc_runtime.cu"), "-o", o])
+    for name in ("rc_runtime", "rc_noalloc"):
+        o = os.path.join(OUT, name + ".o")
+        objs.append(o)
+        if force or _stale(o, deps):
+            jobs.append([nv, *ARCH, *FLAGS, "-c", os.path.join(CSRC, name + ".cu"), "-o", o])
     cli_obj = {}
     for nl in (3, 8):
         oc = os.path.join(OUT, "poc_gpu_main_l%d.o" % nl)

@@ -38,7 +38,9 @@ EXPORTS = [
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
     "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
     "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
+    "rc_error_sums_noalloc",
 ]
+NOALLOC_MAX_POINTS = 4194304
 
 
 class Config(ctypes.Structure):
@@ -146,6 +148,8 @@ def load_library():
     L.rc_run_stats_get.argtypes = [vp, ctypes.POINTER(RunStats)]
     L.rc_device_flags.restype = i
     L.rc_device_flags.argtypes = [vp, ctypes.POINTER(ctypes.c_uint)]
+    L.rc_error_sums_noalloc.restype = i
+    L.rc_error_sums_noalloc.argtypes = [vp, i, i, i, vp, vp, i, vp, vp]
     _lib = L
     return L
 
@@ -324,3 +328,13 @@ def camera_basis(cam: Camera) -> dict:
     tx = np.float32(ty * np.float32(cam.width) / np.float32(cam.height))
     return {"eye": [float(cam.eye[k]) for k in range(3)], "fwd": [float(np.float32(x)) for x in f],
             "right": [float(np.float32(x)) for x in r], "up": [float(np.float32(x)) for x in u], "tx": float(tx), "ty": float(ty)}
+
+
+def error_sums_noalloc(lc_ptr: int, lc_stride: int, nl: int, dormant: int, ref_ptr: int, valid_ptr: int, np_: int,
+                       out3_ptr: int, stream: int | None = None) -> None:
+    """rc_error_sums_noalloc on caller-owned device buffers (raw device addresses); the three
+    FP64 sums land in out3 asynchronously on `stream`.  Allocates no device memory."""
+    L = load_library()
+    st = L.rc_error_sums_noalloc(lc_ptr, lc_stride, nl, dormant, ref_ptr, valid_ptr, np_, out3_ptr, stream)
+    if st != RC_OK:
+        raise RCError(st, "rc_error_sums_noalloc (np=%d, limit %d)" % (np_, NOALLOC_MAX_POINTS))
