@@ -162,6 +162,7 @@ def run_ours(args, world, rank, local, dist):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     fused = []
+    kinds = []
     tracked = []
     l0 = ctx.stats()
     r0 = l0["rays"]
@@ -176,7 +177,9 @@ def run_ours(args, world, rank, local, dist):
         starts[k].record(stream)
         ctx.frame(seq[f])
         ends[k].record(stream)
-        fused.append(ctx.scalar(N.S_LAST_FRAME_FUSED) == 1 and ctx.scalar(N.S_LAST_FRAME_KERNELS) == 1)
+        nk = ctx.scalar(N.S_LAST_FRAME_KERNELS)
+        fused.append(ctx.scalar(N.S_LAST_FRAME_FUSED) == 1 and nk == 1)
+        kinds.append("event" if seq[f] != seq[f - 1] else ("fused" if fused[-1] else "split"))
         tracked.append(f % method.track_every == 0)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
@@ -229,6 +232,9 @@ def run_ours(args, world, rank, local, dist):
                      "peak_source": peak_kind},
         "np": np_,
         "nt": info["nt"],
+        "frame_kinds_ms": {kd: {"frames": sum(1 for x in kinds if x == kd),
+                                "mean_ms": sum(m for m, x in zip(ms, kinds) if x == kd) / max(1, sum(1 for x in kinds if x == kd))}
+                           for kd in ("fused", "split", "event")},
         "frame_1080p": {"cache_ms": total_ms / args.steps, "image_ms": camera_ms,
                         "frames_per_s": 1000.0 / (total_ms / args.steps + camera_ms),
                         "mrays_per_s": (rays / args.steps + 1920 * 1080) / ((total_ms / args.steps + camera_ms) * 1e-3) / 1e6,
@@ -359,7 +365,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
-            "rays_per_frame": res["rays_per_frame"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
+            "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
             "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu}
     print(json.dumps(line))
 

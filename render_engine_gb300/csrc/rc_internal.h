@@ -140,6 +140,9 @@ struct Ops {
     static cudaError_t proj_apply(const DevCache& c, const DStatic& g, const FrameParams& p, cudaStream_t st);
     static cudaError_t camera(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                               const CameraD& cam, float* img, cudaStream_t st);
+    // load every kernel of this light count and mask width now, so the first event or
+    // verification frame does not pay for loading its kernels
+    static cudaError_t preload(int NW);
     static cudaError_t probe(int NW, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                              const int* pts, int npts, void* recs, int maxrec, int* nrec, cudaStream_t st);
 };

@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
                 c.age[i] = fminf(a + 1.f, 1e4f);
             }
             const float alpha = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), nmx), 1.f) : 0.f;
-            const float alpha_r = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), p.nmax_resp), 1.f) : 0.f;
+            const float alpha_r = (k > 0 && p.resp_mask) ? fminf(k / fminf(fmaxf(nn, 1.f), p.nmax_resp), 1.f) : 0.f;
             float out[LCS];
             float est = 0.f;
 #pragma unroll
@@ -1075,6 +1075,30 @@ cudaError_t Ops<NL>::probe(int NW, const DState& s, const DStatic& g, const Grid
     RC_NW_LIST(X)
 #undef X
     return cudaErrorInvalidValue;
+}
+
+template <int NL>
+cudaError_t Ops<NL>::preload(int NW) {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaSuccess;
+    auto touch = [&](const void* f) { if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, f); };
+#define X(W)                                                 \
+    if (NW == W) {                                           \
+        touch((const void*)k_frame<NL, W, true, true>);      \
+        touch((const void*)k_frame<NL, W, true, false>);     \
+        touch((const void*)k_frame<NL, W, false, true>);     \
+        touch((const void*)k_frame<NL, W, false, false>);    \
+        touch((const void*)k_build<NL, W>);                  \
+        touch((const void*)k_probe<NL, W>);                  \
+    }
+    RC_NW_LIST(X)
+#undef X
+    touch((const void*)k_update<NL>);
+    touch((const void*)k_event<NL>);
+    touch((const void*)k_error<NL>);
+    touch((const void*)k_proj_apply<NL>);
+    touch((const void*)k_camera<NL>);
+    return e;
 }
 
 #ifdef RC_NL_ONE

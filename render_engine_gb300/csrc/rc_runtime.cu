@@ -327,6 +327,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated");
     for (int v : region) if (v < 0 || v >= S.NR) return fail(ctx, RC_ERR_FORMAT, "region index out of range");
     rc_status s;
+    CKR(RC_DISPATCH(NL, preload(NW)));
     const float* dL = nullptr;
     if ((s = dput(ctx, pool, &dL, L)) || (s = dput(ctx, pool, &g.A, A)) || (s = dput(ctx, pool, &g.region, region))) return s;
     S.st.resize(S.NS);

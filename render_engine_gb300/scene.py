@@ -296,3 +296,261 @@ def box_room(points: int = 1_082_802, boxes: int = 4, seed: int = 0, lights: int
                 if a != b and inten[a][l] == 0 and inten[b][l] > 0:
                     em[(a, b, l)] = [_fine_voxel(L[l])]
     return Scene(NR=nr, L=L, A=A, region=region, states=states, occ=occ, em=em, fmt=2)
+
+
+# ------------------------------------------------------------------ format 3 (mesh scenes)
+def _mix64(x: np.ndarray) -> np.ndarray:
+    """splitmix64 finaliser on uint64 arrays (the hash of the cache-point table)."""
+    x = x.astype(np.uint64)
+    with np.errstate(over="ignore"):
+        x ^= x >> np.uint64(30)
+        x *= np.uint64(0xBF58476D1CE4E5B9)
+        x ^= x >> np.uint64(27)
+        x *= np.uint64(0x94D049BB133111EB)
+        x ^= x >> np.uint64(31)
+    return x
+
+
+def _cell_key(cx, cy, cz, b) -> np.ndarray:
+    m = np.uint64(0xFFFFF)
+    k = (cx.astype(np.int64).astype(np.uint64) & m)
+    k = (k << np.uint64(20)) | (cy.astype(np.int64).astype(np.uint64) & m)
+    k = (k << np.uint64(20)) | (cz.astype(np.int64).astype(np.uint64) & m)
+    return ((k << np.uint64(3)) | b.astype(np.uint64)) + np.uint64(1)
+
+
+def _normal_bucket(n: np.ndarray) -> np.ndarray:
+    a = np.abs(n)
+    out = np.where(n[:, 2] > 0, 4, 5)
+    out = np.where((a[:, 1] >= a[:, 2]), np.where(n[:, 1] > 0, 2, 3), out)
+    out = np.where((a[:, 0] >= a[:, 1]) & (a[:, 0] >= a[:, 2]), np.where(n[:, 0] > 0, 0, 1), out)
+    return out.astype(np.int64)
+
+
+def build_bvh(V: np.ndarray, leaf: int = 4):
+    """Median-split BVH over triangles V (n, 3, 3).  Returns (nodes (K, 8) float32 in the
+    reference's layout -- bmin, left child or first triangle as int bits, bmax, triangle count
+    as int bits (0 for inner nodes, children at left and left + 1) -- and the triangle order)."""
+    n = V.shape[0]
+    tlo, thi = V.min(axis=1), V.max(axis=1)
+    cen = 0.5 * (tlo + thi)
+    order = np.arange(n)
+    nodes = [None]
+    stack = [(0, 0, n)]
+    while stack:
+        node, s, e = stack.pop()
+        idx = order[s:e]
+        lo, hi = tlo[idx].min(axis=0), thi[idx].max(axis=0)
+        cnt = e - s
+        c = cen[idx]
+        ext = c.max(axis=0) - c.min(axis=0)
+        ax = int(np.argmax(ext))
+        if cnt <= leaf or (ext[ax] < 1e-7 and cnt <= 64):
+            nodes[node] = (lo, s, hi, cnt)
+            continue
+        mid = cnt // 2
+        part = np.argpartition(c[:, ax], mid)
+        order[s:e] = idx[part]
+        left = len(nodes)
+        nodes += [None, None]
+        nodes[node] = (lo, left, hi, 0)
+        stack.append((left + 1, s + mid, e))
+        stack.append((left, s, s + mid))
+    out = np.zeros((len(nodes), 8), np.float32)
+    for k, (lo, a, hi, cnt) in enumerate(nodes):
+        out[k, 0:3] = lo
+        out[k, 3] = np.array([a], np.int32).view(np.float32)[0]
+        out[k, 4:7] = hi
+        out[k, 7] = np.array([cnt], np.int32).view(np.float32)[0]
+    return out, order
+
+
+def mesh_scene(V: np.ndarray, alb: np.ndarray, double_sided: np.ndarray, lights: np.ndarray, intensities: list,
+               box_pos: list, box_half: float, points: int, seed: int = 0, grid=(8, 4, 4)) -> Scene:
+    """Format-3 scene from a static triangle mesh (the layout the reference's `prep` writes,
+    cuda/prep_mesh.cuh:242-297): static triangles in BVH order with normals and double-sided
+    flags, a BVH, cache points sampled on the surfaces into hash cells (cell side h, dominant
+    normal bucket), the cell table with linear probing on mix64 of the cell key, 4x4x4-cell
+    verification zones, a movable cube (6 quads, 12 dynamic triangles) whose two positions
+    the states choose, and event voxel lists on the `grid` transit grid."""
+    rng = np.random.default_rng(seed)
+    V = np.asarray(V, np.float32)
+    nt = V.shape[0]
+    lo = V.reshape(-1, 3).min(axis=0)
+    hi = V.reshape(-1, 3).max(axis=0)
+    diag = float(np.linalg.norm(hi - lo))
+    pad = 0.01 * diag + 0.05
+    lo = (lo - pad).astype(np.float32)
+    hi = (hi + pad).astype(np.float32)
+    ext = (hi - lo).astype(np.float32)
+    BN, order = build_bvh(V)
+    Vo = V[order]
+    ST = np.concatenate([Vo[:, 0], Vo[:, 1] - Vo[:, 0], Vo[:, 2] - Vo[:, 0]], axis=1).astype(np.float32)
+    cr = np.cross(ST[:, 3:6].astype(np.float64), ST[:, 6:9].astype(np.float64))
+    ln = np.linalg.norm(cr, axis=1)
+    nrm = (cr / np.where(ln > 0, ln, 1.0)[:, None]).astype(np.float32)
+    flags = np.asarray(double_sided, np.int32)[order]
+    STN = np.concatenate([nrm, flags.view(np.float32)[:, None]], axis=1).astype(np.float32)
+    # cache cells: area-proportional samples, cell keyed by position and normal bucket
+    area = 0.5 * np.linalg.norm(np.cross((V[:, 1] - V[:, 0]).astype(np.float64), (V[:, 2] - V[:, 0]).astype(np.float64)), axis=1)
+    sides = np.where(np.asarray(double_sided) > 0, 2, 1)
+    h = float(np.sqrt((area * sides).sum() / points))
+    ns = np.maximum(1, np.ceil(area / (h * h) * 4.0)).astype(np.int64)
+    tri = np.repeat(np.arange(nt), ns)
+    a = rng.random(tri.size)
+    b = rng.random(tri.size)
+    flip = a + b > 1
+    a[flip], b[flip] = 1 - a[flip], 1 - b[flip]
+    P = V[tri, 0] + (V[tri, 1] - V[tri, 0]) * a[:, None] + (V[tri, 2] - V[tri, 0]) * b[:, None]
+    tn = np.cross((V[:, 1] - V[:, 0]).astype(np.float64), (V[:, 2] - V[:, 0]).astype(np.float64))
+    tn = (tn / np.maximum(np.linalg.norm(tn, axis=1), 1e-30)[:, None])
+    Ps, Ns, As = [P], [tn[tri]], [np.asarray(alb, np.float64)[tri]]
+    ds = np.asarray(double_sided)[tri] > 0
+    Ps.append(P[ds]); Ns.append(-tn[tri][ds]); As.append(np.asarray(alb, np.float64)[tri][ds])
+    P = np.concatenate(Ps).astype(np.float32)
+    Nn = np.concatenate(Ns).astype(np.float32)
+    Al = np.concatenate(As)
+    c = np.floor((P - lo) / np.float32(h)).astype(np.int64)
+    ctr = lo + (c + 0.5) * np.float32(h)
+    d2 = ((P - ctr) ** 2).sum(axis=1)
+    keys = _cell_key(c[:, 0], c[:, 1], c[:, 2], _normal_bucket(Nn))
+    srt = np.lexsort((d2, keys))
+    ks = keys[srt]
+    first = np.ones(ks.size, bool)
+    first[1:] = ks[1:] != ks[:-1]
+    rep = srt[first]
+    ukeys = keys[rep]
+    # albedo of a cell: mean over its samples
+    inv = np.searchsorted(ukeys, keys[srt]) if False else None
+    grp = np.cumsum(first) - 1
+    asum = np.bincount(grp, weights=Al[srt])
+    acnt = np.bincount(grp)
+    Ast = (asum / acnt).astype(np.float32)
+    Pst, Nst = P[rep], Nn[rep]
+    npst = ukeys.size
+    HS = 1024
+    while HS < 2 * npst:
+        HS <<= 1
+    mask = HS - 1
+    HK = np.zeros(HS, np.uint64)
+    HV = np.full(HS, -1, np.int32)
+    h0 = (_mix64(ukeys) & np.uint64(0xFFFFFFFF)).astype(np.int64) & mask
+    for i in range(npst):
+        j = int(h0[i])
+        while HK[j] != 0:
+            j = (j + 1) & mask
+        HK[j] = ukeys[i]
+        HV[j] = i
+    cx = ((ukeys - np.uint64(1)) >> np.uint64(43)).astype(np.int64) & 0xFFFFF
+    cy = ((ukeys - np.uint64(1)) >> np.uint64(23)).astype(np.int64) & 0xFFFFF
+    cz = ((ukeys - np.uint64(1)) >> np.uint64(3)).astype(np.int64) & 0xFFFFF
+    bk = ((ukeys - np.uint64(1)) & np.uint64(7)).astype(np.int64)
+    zkey = _cell_key(cx >> 2, cy >> 2, cz >> 2, bk)
+    _, zone = np.unique(zkey, return_inverse=True)
+    NR = int(zone.max()) + 1
+    # movable cube: 6 quads, bnu x bnu points per face, 4 x 4 points per zone
+    bnu = max(2, int(round(2 * box_half / h)))
+    nbox = 6 * bnu * bnu
+    tu = (bnu + 3) // 4
+    cube_region = []
+    for q in range(6):
+        for iv in range(bnu):
+            for iu in range(bnu):
+                cube_region.append(NR + q * tu * tu + (iv // 4) * tu + iu // 4)
+    NR += 6 * tu * tu
+    A = np.concatenate([Ast, np.full(nbox, 0.7, np.float32)])
+    region = np.concatenate([zone.astype(np.int32), np.array(cube_region, np.int32)])
+    Np = npst + nbox
+    L = np.asarray(lights, np.float32).reshape(-1, 3)
+    states = []
+    for si, inten in enumerate(intensities):
+        cpos = np.asarray(box_pos[si], np.float32)
+        quads = _box_quads(cpos - box_half, cpos + box_half, with_bottom=True)
+        Q = np.array([[*o, *u, *v, *n] for o, u, v, n in quads], np.float32)
+        Pc, Nc, T = [], [], []
+        for qi in range(6):
+            o, u, v, n = Q[qi, 0:3], Q[qi, 3:6], Q[qi, 6:9], Q[qi, 9:12]
+            f = ((np.arange(bnu, dtype=np.float32) + np.float32(0.5)) / np.float32(bnu)).astype(np.float32)
+            pts = o[None, None, :] + u[None, None, :] * f[None, :, None] + v[None, None, :] * f[:, None, None]
+            Pc.append(pts.reshape(-1, 3))
+            Nc.append(np.repeat(n[None, :], bnu * bnu, axis=0))
+            T.append(np.concatenate([o, u, v]))
+            T.append(np.concatenate([o + u + v, -u, -v]))
+        dims = np.full((6, 2), bnu, np.int32)
+        off = (npst + np.arange(6) * bnu * bnu).astype(np.int32)
+        states.append(State(inten=np.asarray(inten, np.float32), P=np.concatenate([Pst] + Pc).astype(np.float32),
+                            N=np.concatenate([Nst] + Nc).astype(np.float32), Q=Q, dims=dims, off=off,
+                            T=np.array(T, np.float32), TQ=np.repeat(np.arange(6, dtype=np.int32), 2)))
+    VX, VY, VZ = grid
+
+    def vox(p):
+        i = min(max(int((p[0] - lo[0]) / ext[0] * VX), 0), VX - 1)
+        j = min(max(int((p[1] - lo[1]) / ext[1] * VY), 0), VY - 1)
+        k = min(max(int((p[2] - lo[2]) / ext[2] * VZ), 0), VZ - 1)
+        return (k * VY + j) * VX + i
+
+    occ, em = {}, {}
+    NS = len(intensities)
+    for a_ in range(NS):
+        for b_ in range(NS):
+            if a_ != b_ and tuple(box_pos[a_]) != tuple(box_pos[b_]):
+                vs = set()
+                for p in (box_pos[a_], box_pos[b_]):
+                    for x in np.linspace(-box_half, box_half, 12):
+                        for y in np.linspace(-box_half, box_half, 12):
+                            for z in np.linspace(-box_half, box_half, 12):
+                                vs.add(vox(np.array(p, np.float32) + np.array([x, y, z], np.float32)))
+                occ[(a_, b_)] = sorted(vs)
+            for l in range(L.shape[0]):
+                if a_ != b_ and intensities[a_][l] == 0 and intensities[b_][l] > 0:
+                    em[(a_, b_, l)] = [vox(L[l])]
+    mesh = dict(lo=lo, ext=ext, hcell=np.float32(h), npst=npst, ST=ST, STN=STN, BN=BN, HK=HK, HV=HV)
+    return Scene(NR=NR, L=L, A=A, region=region, states=states, occ=occ, em=em, fmt=3, mesh=mesh)
+
+
+def street_mesh(buildings: int = 40, seed: int = 0, facade_cell: float = 2.0, size: float = 120.0):
+    """Seeded street: a ground plane (split into a grid of quads) and `buildings` boxes 5-30 m
+    tall along two rows, their facades subdivided into cells of about `facade_cell` metres.
+    Returns (V (n, 3, 3) float32, albedo per triangle, double-sided flags)."""
+    rng = np.random.default_rng(seed)
+    tris, albs = [], []
+
+    def quad(o, u, v, alb, nu, nv):
+        o, u, v = (np.asarray(x, np.float64) for x in (o, u, v))
+        for j in range(nv):
+            for i in range(nu):
+                a = o + u * (i / nu) + v * (j / nv)
+                du, dv = u / nu, v / nv
+                tris.append([a, a + du, a + dv])
+                tris.append([a + du + dv, a + dv, a + du])
+                albs.extend([alb, alb])
+
+    g = max(1, int(size / 8))
+    quad((-size / 2, -size / 2, 0), (size, 0, 0), (0, size, 0), 0.35, g, g)
+    for b in range(buildings):
+        side = 1 if b % 2 else -1
+        x0 = -size / 2 + 4 + (b // 2) * (size - 8) / max(1, buildings // 2)
+        w = rng.uniform(6, (size - 8) / max(1, buildings // 2) - 1)
+        d = rng.uniform(8, 16)
+        hgt = rng.uniform(5, 30)
+        y0 = side * 8 if side > 0 else -8 - d
+        alb = rng.uniform(0.2, 0.8)
+        lo = np.array([x0, y0, 0.0])
+        hi = np.array([x0 + w, y0 + d, hgt])
+        for o, u, v, n in _box_quads(lo, hi):
+            nu = max(1, int(np.linalg.norm(u) / facade_cell))
+            nv = max(1, int(np.linalg.norm(v) / facade_cell))
+            quad(o, u, v, alb, nu, nv)
+    V = np.array(tris, np.float32)
+    return V, np.array(albs, np.float32), np.zeros(len(tris), np.uint8)
+
+
+def street_scene(points: int = 20000, buildings: int = 8, seed: int = 0, facade_cell: float = 2.0, size: float = 60.0) -> Scene:
+    """Format-3 street scene: street_mesh + three lamp-post lights and the movable cube; five
+    states as the reference's prep (lights {0,1} on, 1 off, cube moved, light 2 on first time,
+    light 0 off with the cube moved)."""
+    V, alb, ds = street_mesh(buildings, seed, facade_cell, size)
+    L = np.array([[-size / 4, 0.0, 4.0], [0.0, 2.0, 4.0], [size / 4, -2.0, 4.0]], np.float32)
+    I = [[20, 20, 0], [0, 20, 0], [20, 20, 0], [20, 20, 20], [0, 20, 0]]
+    box = [(-2.0, 0.0, 1.0), (-2.0, 0.0, 1.0), (4.0, -1.0, 1.0), (-2.0, 0.0, 1.0), (4.0, -1.0, 1.0)]
+    return mesh_scene(V, alb, ds, L, I, box, 1.0, points, seed)

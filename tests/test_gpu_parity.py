@@ -230,3 +230,46 @@ def test_image_pass_vs_oracle(scene_main_bytes):
     assert np.isfinite(img).all() and img.max() > 0
     close = np.isclose(img, ref, rtol=1e-4, atol=1e-6)
     assert close.mean() > 0.995, close.mean()
+
+
+@pytest.fixture(scope="module")
+def street_bytes():
+    return S.write(S.street_scene(points=20000, buildings=8, size=60.0))
+
+
+def test_format3_state_build_bitexact_vs_reference(street_bytes):
+    if not pyref.available(3):
+        pytest.skip("reference kernels not built")
+    ctx = _ctx(street_bytes)
+    ref = pyref.RefRunner(3, street_bytes)
+    for s in range(ctx.info()["ns"]):
+        assert np.array_equal(ctx.state_array(s, N.SA_EDIR).view(np.uint32), ref.state_array(s, 0).view(np.uint32)), s
+        assert np.array_equal(ctx.state_array(s, N.SA_SV), ref.state_array(s, 1)), s
+
+
+@pytest.mark.parametrize("name", ["Classique 2.0x", "v3 complet", "v4-A2C suivi 1/4"])
+def test_format3_frames_vs_reference(street_bytes, name):
+    """BVH traversal, hash-table cache lookups and the whole frame on a format-3 scene."""
+    if not pyref.available(3):
+        pytest.skip("reference kernels not built")
+    m = M.by_name(M.timing_methods(), name)
+    seq = [0] * 10 + [1] * 6 + [2] * 6 + [3] * 6 + [4] * 6
+    _frames_vs_reference(street_bytes, 3, m, seq, 7)
+
+
+def test_format3_probe_vs_oracle(street_bytes):
+    ctx = _ctx(street_bytes)
+    run = po.Run(po.Scene(data=street_bytes))
+    m = M.by_name(M.timing_methods(), "Classique 2.0x")
+    ctx.begin(m, 0, 4)
+    run.begin(m, 0, 4)
+    pts = list(range(0, ctx.info()["np"], 5))
+    for state in (0, 2):
+        a = ctx.probe(state, pts)
+        b = sorted(run.probe(state, pts))
+        ga = np.array([r[:5] for r in a])
+        gb = np.array([r[:5] for r in b])
+        same = np.all(ga == gb, axis=1)
+        assert same.mean() > 0.999, same.mean()
+        assert (ga[:, 2] <= -2).mean() > 0.2    # most hits go through the BVH
+    assert ctx.device_flags() == 0

@@ -66,3 +66,56 @@ def test_run_is_deterministic():
         run.frame(s)
     assert np.array_equal(a, run.array(po.A_LC))
     assert np.isfinite(a).all()
+
+
+def test_street_scene_tables():
+    """Format-3 writer: BVH covers every triangle once with nested bounds; every static cache
+    point is found in the hash table under its own cell key (linear probing from mix64)."""
+    sc = S.street_scene(points=6000, buildings=4, size=40.0)
+    m = sc.mesh
+    BN = m["BN"]
+    lf = BN[:, 3].view(np.int32)
+    cnt = BN[:, 7].view(np.int32)
+    seen = np.zeros(len(m["ST"]), int)
+    stack = [0]
+    while stack:
+        k = stack.pop()
+        if cnt[k] > 0:
+            seen[lf[k]: lf[k] + cnt[k]] += 1
+        else:
+            for ch in (lf[k], lf[k] + 1):
+                assert (BN[ch, 0:3] >= BN[k, 0:3]).all() and (BN[ch, 4:7] <= BN[k, 4:7]).all()
+                stack.append(ch)
+    assert (seen == 1).all()
+    HK, HV = m["HK"], m["HV"]
+    mask = len(HK) - 1
+    npst = m["npst"]
+    lo = m["lo"]
+    h = np.float32(m["hcell"])
+    P = sc.states[0].P[:npst]
+    N = sc.states[0].N[:npst]
+    c = np.floor((P - lo) * (np.float32(1) / h)).astype(np.int64)
+    keys = S._cell_key(c[:, 0], c[:, 1], c[:, 2], S._normal_bucket(N))
+    h0 = (S._mix64(keys) & np.uint64(0xFFFFFFFF)).astype(np.int64) & mask
+    for i in range(0, npst, 7):
+        j = int(h0[i])
+        for _ in range(64):
+            if HK[j] == keys[i] or HK[j] == 0:
+                break
+            j = (j + 1) & mask
+        assert HK[j] == keys[i] and HV[j] == i
+
+
+def test_street_scene_runs_in_oracle():
+    data = S.write(S.street_scene(points=5000, buildings=4, size=40.0))
+    o = po.Scene(data=data)
+    assert o.fmt == 3 and o.nst > 0
+    run = po.Run(o)
+    m = M.by_name(M.timing_methods(), "v4-A2C suivi 1/4")
+    run.begin(m, 0, 1)
+    for s in [0] * 4 + [1] * 4 + [2] * 4 + [3] * 4:
+        run.frame(s)
+    lc = run.array(po.A_LC)
+    assert np.isfinite(lc).all() and lc.max() > 0
+    recs = run.probe(0, list(range(0, o.Np, 11)))
+    assert any(r[2] <= -2 for r in recs)   # static (BVH) hits resolved through the hash table
