@@ -127,6 +127,21 @@ def algorithmic_bytes(np_: int, tracked: bool, ramp: bool) -> float:
     return float(np_) * b
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest rank's value (the timed region ends when every replica has finished)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, max_ms: float) -> float:
+    """Units all replicas processed per second of the slowest replica's timed region."""
+    return units_per_rank * world / (max_ms * 1e-3)
+
+
 def setup_dist(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -188,9 +203,7 @@ def run_ours(args, world, rank, local, dist):
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(ms)
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, dist, "cuda")
         dist.barrier()
     # the 1920x1080 image pass of the same cache (one primary ray per pixel), timed the same way
     cam = N.camera(eye=(0.4, 0.4, 1.7), at=(7.6, 3.6, 0.8), fov_y_deg=75.0, width=1920, height=1080)
@@ -218,7 +231,7 @@ def run_ours(args, world, rank, local, dist):
     achieved = kern_bytes / (kern_ms * 1e-3) / 1e9 if fk else None
     traffic = profile_traffic()
     out = {
-        "frames_per_s": frames / (total_ms * 1e-3),
+        "frames_per_s": whole_job_rate(args.steps, world, total_ms),
         "ms_per_step": total_ms / args.steps,
         "mrays_per_s": rays * world / (total_ms * 1e-3) / 1e6,
         "cache_updates_per_s": np_ * frames / (total_ms * 1e-3),
