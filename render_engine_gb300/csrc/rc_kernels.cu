@@ -138,6 +138,64 @@ __device__ __forceinline__ bool u64_tail_reduce(unsigned long long v, U64Tail& t
     return true;
 }
 
+// ------------------------------------------------------------------ per-region sums
+// The reference adds per-point statistics into per-region slots with one float atomic per
+// point and value (poc_gpu.cu:492-497, 498-512, 517-523).  Neighbouring points mostly share a
+// region, so those atomics pile onto a few addresses; here the lanes of a warp that share a
+// region first add their values in a butterfly (non-members add 0) and one lane issues the
+// atomic.  The sums stay float sums in an unspecified order across warps, as in the
+// reference.  Must be called by the whole warp.
+__device__ __forceinline__ float warp_bfly(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NV>
+__device__ __forceinline__ void region_add(float* __restrict__ base, int stride, int rg, bool on, const float (&v)[NV]) {
+    const int lane = threadIdx.x & 31;
+    unsigned todo = __ballot_sync(0xffffffffu, on);
+    while (todo) {
+        const int lead = __ffs(todo) - 1;
+        const int r = __shfl_sync(0xffffffffu, rg, lead);
+        const bool mine = on && rg == r;
+        const unsigned grp = __ballot_sync(0xffffffffu, mine);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const float s = warp_bfly(mine ? v[q] : 0.f);
+            if (lane == lead) atomicAdd(base + (size_t)stride * r + q, s);
+        }
+        todo &= ~grp;
+    }
+}
+
+// Projection normal equations (poc_gpu.cu:498-512): k T_a T_b for a <= b, sum(acc) T_a, k.
+__device__ __forceinline__ void proj_region_add(float* __restrict__ neq, int rg, bool on, int K, const float* T, float kf,
+                                                float sv) {
+    const int lane = threadIdx.x & 31;
+    unsigned todo = __ballot_sync(0xffffffffu, on);
+    while (todo) {
+        const int lead = __ffs(todo) - 1;
+        const int r = __shfl_sync(0xffffffffu, rg, lead);
+        const bool mine = on && rg == r;
+        const unsigned grp = __ballot_sync(0xffffffffu, mine);
+        float* qn = neq + (size_t)r * NEQ;
+        int ix = 0;
+        for (int a = 0; a < K; ++a)
+            for (int b = a; b < K; ++b, ++ix) {
+                const float s = warp_bfly(mine ? kf * T[a] * T[b] : 0.f);
+                if (lane == lead) atomicAdd(qn + ix, s);
+            }
+        for (int a = 0; a < K; ++a) {
+            const float s = warp_bfly(mine ? sv * T[a] : 0.f);
+            if (lane == lead) atomicAdd(qn + 21 + a, s);
+        }
+        const float s = warp_bfly(mine ? kf : 0.f);
+        if (lane == lead) atomicAdd(qn + 27, s);
+        todo &= ~grp;
+    }
+}
+
 // ------------------------------------------------------------------ tracing
 struct TraceSmem {
     const float4* tri;
@@ -449,6 +507,13 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
     float pr_out = 0.f;
     double e_d2 = 0.0, e_rs = 0.0, e_cn = 0.0;
     int k_rays = 0;
+    // split path: per-region statistics, added by whole warps after the point's work
+    int rg = 0;
+    bool on_r = false, on_p = false, on_d = false;
+    float vr[4] = {0.f, 0.f, 0.f, 0.f}, vd[3] = {0.f, 0.f, 0.f};
+    float T[KSNAP], sv_p = 0.f;
+#pragma unroll
+    for (int a = 0; a < KSNAP; ++a) T[a] = 0.f;
     if (i < p.Np) {
         uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
         const bool pend = !FUSED && p.pend_left > 0 && c.pending[i];
@@ -510,15 +575,13 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
         }
         const float ik = k > 0 ? 1.f / k : 0.f;
         if (!FUSED) {
-            const int rg = g.region[i];
+            rg = g.region[i];
             if (pend && k > 0) {
-                atomicAdd(&c.rstat[4 * rg + 0], sd);
-                atomicAdd(&c.rstat[4 * rg + 1], sq);
-                atomicAdd(&c.rstat[4 * rg + 2], c0 * k);
-                atomicAdd(&c.rstat[4 * rg + 3], float(k));
+                on_r = true;
+                vr[0] = sd; vr[1] = sq; vr[2] = c0 * k; vr[3] = float(k);
             }
             if (p.proj_left > 0 && k > 0) {
-                float T[KSNAP];
+                on_p = true;
                 for (int a = 0; a < p.projK; ++a) {
                     const float* sp = c.snap + ((size_t)p.slot[a] * p.Np + i) * LCS;
                     float t = 0.f;
@@ -526,15 +589,8 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
                     for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) t += sp[l];
                     T[a] = t;
                 }
-                float sv = 0.f;
 #pragma unroll
-                for (int l = 0; l < NL; ++l) sv += acc[l];
-                float* qn = c.neq + (size_t)rg * NEQ;
-                int ix = 0;
-                for (int a = 0; a < p.projK; ++a)
-                    for (int b = a; b < p.projK; ++b) atomicAdd(&qn[ix++], k * T[a] * T[b]);
-                for (int a = 0; a < p.projK; ++a) atomicAdd(&qn[21 + a], sv * T[a]);
-                atomicAdd(&qn[27], float(k));
+                for (int l = 0; l < NL; ++l) sv_p += acc[l];
             }
             c.kk[i] = k;
             float mo[LCS];
@@ -550,9 +606,8 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
                 float est = 0.f;
 #pragma unroll
                 for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) est += c.Lc[(size_t)LCS * i + l];
-                atomicAdd(&c.dstat[3 * rg + 0], sa * ik);
-                atomicAdd(&c.dstat[3 * rg + 1], est);
-                atomicAdd(&c.dstat[3 * rg + 2], 1.f);
+                on_d = true;
+                vd[0] = sa * ik; vd[1] = est; vd[2] = 1.f;
             }
         } else {
             // k_update (poc_gpu.cu:562-602) on the point's own history.
@@ -612,6 +667,11 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
         // ray count of the frame: warp sum, one 64-bit atomic per warp
         const unsigned wk = __reduce_add_sync(0xffffffffu, (unsigned)k_rays);
         if ((threadIdx.x & 31) == 0 && wk) atomicAdd(c.rays, (unsigned long long)wk);
+    }
+    if (!FUSED) {
+        region_add<4>(c.rstat, 4, rg, on_r, vr);
+        if (p.proj_left > 0) proj_region_add(c.neq, rg, on_p, p.projK, T, float(k_rays), sv_p);
+        if (p.ddgi) region_add<3>(c.dstat, 3, rg, on_d, vd);
     }
     if (FUSED) {
         unsigned long long tot;

@@ -71,8 +71,12 @@ def _frames_vs_reference(data, nl, method, seq, seed):
       * Sum 1/(n+1) recomputed after an event in adaptive mode can move a ray budget by one
         on a few points.
     On those frames 99.8 % of the points must still agree: exactly for ray counts, masks and
-    flags, to 1e-5 for histories and 1e-4 for the cache.  Dependency masks may also differ on
-    a handful of points (at most 2e-5 of them) where a hit lies on a voxel boundary to within
+    flags, to 1e-5 for histories and 1e-4 for the cache.  A projection window is looser: its
+    per-region normal equations (float sums, compared to 1e-5 relative) go through a
+    Gauss-Jordan solve whose conditioning amplifies their last-bit differences, and two runs
+    of the reference itself leave up to 0.1 % of the points more than 1e-4 apart there (up to
+    5e-3); 99 % must agree to 1e-4 and all to 1e-2.  Dependency masks may also differ on a
+    handful of points (at most 2e-5 of them) where a hit lies on a voxel boundary to within
     the last bit of the hit distance; such ties are counted and printed."""
     ctx = _ctx(data)
     ref = pyref.RefRunner(nl, data)
@@ -105,8 +109,15 @@ def _frames_vs_reference(data, nl, method, seq, seed):
             ties += mask_diff
             exact_frames += 1
         else:
+            proj = proj_before > 0 or ctx.scalar(N.S_PROJ_LEFT) > 0
             close_lc = np.mean(np.isclose(a, b, rtol=1e-4, atol=1e-6).all(axis=1))
             close_n = np.mean(np.isclose(na, nb, rtol=1e-5, atol=1e-7))
+            if proj:
+                qa, qb = ctx.array(N.A_NEQ), ref.array(N.A_NEQ)
+                assert np.allclose(qa, qb, rtol=1e-5, atol=1e-3), f
+                assert np.allclose(a, b, rtol=1e-2, atol=1e-5), f
+                assert close_lc >= 0.99, (f, close_lc)
+                close_lc = 1.0
             assert min(close_lc, close_n, same_p, 1.0 - mask_diff / na.size) >= 0.998, (f, close_lc, close_n, same_p, mask_diff)
         assert abs(float(a.sum()) - float(b.sum())) <= 1e-3 * abs(float(b.sum())) + 1e-6, f
     if ties:
