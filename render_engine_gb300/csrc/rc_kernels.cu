@@ -14,7 +14,10 @@
 //    error sums in a fixed tree) and need no block-wide barrier, so runs are reproducible bit
 //    for bit and no warp waits for its block's slowest warp;
 //  * an event is one kernel applying the reference's per-point event kernels in order.
+#include <algorithm>
 #include <cstdio>
+#include <mutex>
+#include <vector>
 
 #include "rc_internal.h"
 
@@ -488,22 +491,56 @@ __global__ void __launch_bounds__(BLOCK) k_build(const DState s, const DStatic g
 // ------------------------------------------------------------------ frame kernel
 // FUSED: trace + update + reductions (frames without verification, projection or DDGI).
 // !FUSED: trace only, writing kk / m and the region statistics (poc_gpu.cu:492-529).
+//
+// Persistent: the grid is as many blocks as fit on the GPU at once, and each block walks the
+// 256-point tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The dynamic triangles are staged
+// into shared memory once per block instead of once per tile, and the frame's totals leave
+// the block once.  Error sums keep the fixed tree of one partial per tile: the tile's warp
+// sums are added in warp order into part[tile], and the last block to finish adds the tile
+// partials in the order of final_tree.
 #ifndef RC_FRAME_MINB
 #define RC_FRAME_MINB 4
 #endif
+
+// Level 2 of the fixed-order error sums over G tile partials, run by one whole warp: slot
+// t = lane + 32 j sums partials t, t+256, ... in order, each group of 32 slots goes through
+// the butterfly and the 8 group sums are added in order (the same tree as warp_tail_reduce).
+template <int NV>
+__device__ __forceinline__ void final_tree(const double* part, int G, double (&total)[NV]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double acc = 0.0;
+        for (int j = 0; j < BLOCK / 32; ++j) {
+            const int t = lane + 32 * j;
+            double x = 0.0;
+            if (t < G) x = __ldcg(part + (size_t)t * NV + k);
+            for (int b = t + BLOCK; b < G; b += BLOCK) x = x + __ldcg(part + (size_t)b * NV + k);
+            x = warp_tree(x);
+            acc = j == 0 ? x : acc + x;
+        }
+        total[k] = acc;
+    }
+}
 
 template <int NL, int NW, bool DEPS, bool FUSED>
 __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, const DStatic g, const Grid grid, const DevCache c,
                                                  const FrameParams p) {
     extern __shared__ float4 sm[];
     __shared__ U64Tail prt;
-    __shared__ WarpTail<double, 3> taild;
+    __shared__ double esh[2][3][BLOCK / 32];
     constexpr int LCS = lcs_of(NL), AES = aes_of(NL);
     stage_smem(sm, s);
-    if (threadIdx.x == 0) { prt.acc = 0ull; prt.arrived = 0u; taild.arrived = 0u; }
+    if (threadIdx.x == 0) { prt.acc = 0ull; prt.arrived = 0u; }
     __syncthreads();
     const TraceSmem tsm = smem_view(sm, s);
-    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int ntiles = (p.Np + BLOCK - 1) / BLOCK;
+    unsigned long long pr_sum = 0ull;   // this thread's Sum 1/(n+1) terms, in 2^-40 units
+    unsigned ray_sum = 0u;
+    int par = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, par ^= 1) {
+    const int i = tile * BLOCK + threadIdx.x;
     float pr_out = 0.f;
     double e_d2 = 0.0, e_rs = 0.0, e_cn = 0.0;
     int k_rays = 0;
@@ -515,174 +552,206 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
 #pragma unroll
     for (int a = 0; a < KSNAP; ++a) T[a] = 0.f;
     if (i < p.Np) {
-        uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
-        const bool pend = !FUSED && p.pend_left > 0 && c.pending[i];
-        const float n_i = c.n[i];
-        const int k = ray_count(p, c, n_i, pend, c.sumpr[p.sum_in], c.npend[0], rs);
-        k_rays = k;
-        const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
-        float acc[NL];
+            uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
+            const bool pend = !FUSED && p.pend_left > 0 && c.pending[i];
+            const float n_i = c.n[i];
+            const int k = ray_count(p, c, n_i, pend, c.sumpr[p.sum_in], c.npend[0], rs);
+            k_rays = k;
+            const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
+            float acc[NL];
 #pragma unroll
-        for (int l = 0; l < NL; ++l) acc[l] = 0.f;
-        uint32_t m[NW];
+            for (int l = 0; l < NL; ++l) acc[l] = 0.f;
+            uint32_t m[NW];
 #pragma unroll
-        for (int w = 0; w < NW; ++w) m[w] = 0u;
-        const float c0 = pend ? c.c0[i] : 0.f;
-        float sd = 0.f, sq = 0.f;
-        // the point's own cache and age, read before tracing so the loads overlap the trace
-        float4 own[LCS / 4];
-        float age_i = 0.f;
-        if (FUSED) {
-            const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)i * (LCS / 4);
+            for (int w = 0; w < NW; ++w) m[w] = 0u;
+            const float c0 = pend ? c.c0[i] : 0.f;
+            float sd = 0.f, sq = 0.f;
+            // the point's own cache and age, read before tracing so the loads overlap the trace
+            float4 own[LCS / 4];
+            float age_i = 0.f;
+            if (FUSED) {
+                const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)i * (LCS / 4);
 #pragma unroll
-            for (int k4 = 0; k4 < LCS / 4; ++k4) own[k4] = __ldcg(lcp + k4);
-            if (p.ramp) age_i = c.age[i];
-        }
-        for (int r = 0; r < k; ++r) {
-            const float u1 = rnd(rs);
-            const float u2 = rnd(rs);
-            const f3 D = cosine_dir(N, u1, u2);
-            const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
-            float val = 0.f;
-            if (!h.back) {
-                float4 ae[AES / 4], lc[LCS / 4];
-                const float4* aep = s.AE + (size_t)h.pi * (AES / 4);
-                const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)h.pi * (LCS / 4);
+                for (int k4 = 0; k4 < LCS / 4; ++k4) own[k4] = __ldcg(lcp + k4);
+                if (p.ramp) age_i = c.age[i];
+            }
+            for (int r = 0; r < k; ++r) {
+                const float u1 = rnd(rs);
+                const float u2 = rnd(rs);
+                const f3 D = cosine_dir(N, u1, u2);
+                const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+                float val = 0.f;
+                if (!h.back) {
+                    float4 ae[AES / 4], lc[LCS / 4];
+                    const float4* aep = s.AE + (size_t)h.pi * (AES / 4);
+                    const float4* lcp = reinterpret_cast<const float4*>(c.Lc) + (size_t)h.pi * (LCS / 4);
 #pragma unroll
-                for (int k4 = 0; k4 < AES / 4; ++k4) ae[k4] = __ldg(aep + k4);
+                    for (int k4 = 0; k4 < AES / 4; ++k4) ae[k4] = __ldg(aep + k4);
 #pragma unroll
-                for (int k4 = 0; k4 < LCS / 4; ++k4) lc[k4] = __ldcg(lcp + k4);
-                const float A = ae[0].x;
+                    for (int k4 = 0; k4 < LCS / 4; ++k4) lc[k4] = __ldcg(lcp + k4);
+                    const float A = ae[0].x;
 #pragma unroll
-                for (int l = 0; l < NL; ++l) {
-                    const float lcv = ((p.dormant >> l) & 1) ? 0.f : comp(lc, l);
-                    const float v = A * (comp(ae, l + 1) + lcv);
-                    acc[l] += v;
-                    val += v;
+                    for (int l = 0; l < NL; ++l) {
+                        const float lcv = ((p.dormant >> l) & 1) ? 0.f : comp(lc, l);
+                        const float v = A * (comp(ae, l + 1) + lcv);
+                        acc[l] += v;
+                        val += v;
+                    }
                 }
-            }
-            if (DEPS) {
-                const int src = h.back ? i : h.pi;
-                const uint4* sv = reinterpret_cast<const uint4*>(s.SV + (size_t)NW * src);
+                if (DEPS) {
+                    const int src = h.back ? i : h.pi;
+                    const uint4* sv = reinterpret_cast<const uint4*>(s.SV + (size_t)NW * src);
 #pragma unroll
-                for (int w = 0; w < NW / 4; ++w) {
-                    const uint4 x = __ldg(sv + w);
-                    m[4 * w] |= x.x; m[4 * w + 1] |= x.y; m[4 * w + 2] |= x.z; m[4 * w + 3] |= x.w;
+                    for (int w = 0; w < NW / 4; ++w) {
+                        const uint4 x = __ldg(sv + w);
+                        m[4 * w] |= x.x; m[4 * w + 1] |= x.y; m[4 * w + 2] |= x.z; m[4 * w + 3] |= x.w;
+                    }
+                    dda_walk<NW>(grid, O, h.H, m);
                 }
-                dda_walk<NW>(grid, O, h.H, m);
+                if (pend) { float dv = val - c0; sd += dv; sq += dv * dv; }
             }
-            if (pend) { float dv = val - c0; sd += dv; sq += dv * dv; }
-        }
-        const float ik = k > 0 ? 1.f / k : 0.f;
-        if (!FUSED) {
-            rg = g.region[i];
-            if (pend && k > 0) {
-                on_r = true;
-                vr[0] = sd; vr[1] = sq; vr[2] = c0 * k; vr[3] = float(k);
-            }
-            if (p.proj_left > 0 && k > 0) {
-                on_p = true;
-                for (int a = 0; a < p.projK; ++a) {
-                    const float* sp = c.snap + ((size_t)p.slot[a] * p.Np + i) * LCS;
-                    float t = 0.f;
-#pragma unroll
-                    for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) t += sp[l];
-                    T[a] = t;
+            const float ik = k > 0 ? 1.f / k : 0.f;
+            if (!FUSED) {
+                rg = g.region[i];
+                if (pend && k > 0) {
+                    on_r = true;
+                    vr[0] = sd; vr[1] = sq; vr[2] = c0 * k; vr[3] = float(k);
                 }
+                if (p.proj_left > 0 && k > 0) {
+                    on_p = true;
+                    for (int a = 0; a < p.projK; ++a) {
+                        const float* sp = c.snap + ((size_t)p.slot[a] * p.Np + i) * LCS;
+                        float t = 0.f;
 #pragma unroll
-                for (int l = 0; l < NL; ++l) sv_p += acc[l];
-            }
-            c.kk[i] = k;
-            float mo[LCS];
+                        for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) t += sp[l];
+                        T[a] = t;
+                    }
 #pragma unroll
-            for (int l = 0; l < LCS; ++l) mo[l] = l < NL ? acc[l] * ik : 0.f;
-            float4* mp = reinterpret_cast<float4*>(c.m) + (size_t)i * (LCS / 4);
+                    for (int l = 0; l < NL; ++l) sv_p += acc[l];
+                }
+                c.kk[i] = k;
+                float mo[LCS];
 #pragma unroll
-            for (int k4 = 0; k4 < LCS / 4; ++k4) mp[k4] = make_float4(mo[4 * k4], mo[4 * k4 + 1], mo[4 * k4 + 2], mo[4 * k4 + 3]);
-            if (p.ddgi && k > 0) {
-                float sa = 0.f;
+                for (int l = 0; l < LCS; ++l) mo[l] = l < NL ? acc[l] * ik : 0.f;
+                float4* mp = reinterpret_cast<float4*>(c.m) + (size_t)i * (LCS / 4);
 #pragma unroll
-                for (int l = 0; l < NL; ++l) sa += acc[l];
+                for (int k4 = 0; k4 < LCS / 4; ++k4) mp[k4] = make_float4(mo[4 * k4], mo[4 * k4 + 1], mo[4 * k4 + 2], mo[4 * k4 + 3]);
+                if (p.ddgi && k > 0) {
+                    float sa = 0.f;
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) sa += acc[l];
+                    float est = 0.f;
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) est += c.Lc[(size_t)LCS * i + l];
+                    on_d = true;
+                    vd[0] = sa * ik; vd[1] = est; vd[2] = 1.f;
+                }
+            } else {
+                // k_update (poc_gpu.cu:562-602) on the point's own history.
+                const float4 (&lc)[LCS / 4] = own;
+                float nn = n_i + k;
+                float nmx = p.nmax;
+                if (p.ramp) {
+                    const float a = age_i;
+                    nmx = fminf(p.nmax, (4.f + 0.5f * a) * p.rays);
+                    c.age[i] = fminf(a + 1.f, 1e4f);
+                }
+                const float alpha = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), nmx), 1.f) : 0.f;
+                const float alpha_r = (k > 0 && p.resp_mask) ? fminf(k / fminf(fmaxf(nn, 1.f), p.nmax_resp), 1.f) : 0.f;
+                float out[LCS];
                 float est = 0.f;
 #pragma unroll
-                for (int l = 0; l < NL; ++l) if (!((p.dormant >> l) & 1)) est += c.Lc[(size_t)LCS * i + l];
-                on_d = true;
-                vd[0] = sa * ik; vd[1] = est; vd[2] = 1.f;
-            }
-        } else {
-            // k_update (poc_gpu.cu:562-602) on the point's own history.
-            const float4 (&lc)[LCS / 4] = own;
-            float nn = n_i + k;
-            float nmx = p.nmax;
-            if (p.ramp) {
-                const float a = age_i;
-                nmx = fminf(p.nmax, (4.f + 0.5f * a) * p.rays);
-                c.age[i] = fminf(a + 1.f, 1e4f);
-            }
-            const float alpha = k > 0 ? fminf(k / fminf(fmaxf(nn, 1.f), nmx), 1.f) : 0.f;
-            const float alpha_r = (k > 0 && p.resp_mask) ? fminf(k / fminf(fmaxf(nn, 1.f), p.nmax_resp), 1.f) : 0.f;
-            float out[LCS];
-            float est = 0.f;
+                for (int l = 0; l < LCS; ++l) {
+                    if (l < NL) {
+                        const float a = comp(lc, l);
+                        float al = ((p.resp_mask >> l) & 1) ? alpha_r : alpha;
+                        if ((p.dormant >> l) & 1) al = 0.f;
+                        // the reference stores m = acc * ik (one rounding) before k_update reads it;
+                        // __fmul_rn keeps that rounding (no fused multiply-add into the blend)
+                        out[l] = a + al * (__fmul_rn(acc[l], ik) - a);
+                        if (!((p.dormant >> l) & 1)) est += out[l];
+                    } else {
+                        out[l] = 0.f;
+                    }
+                }
+                float4* op = reinterpret_cast<float4*>(c.Lc2) + (size_t)i * (LCS / 4);
 #pragma unroll
-            for (int l = 0; l < LCS; ++l) {
-                if (l < NL) {
-                    const float a = comp(lc, l);
-                    float al = ((p.resp_mask >> l) & 1) ? alpha_r : alpha;
-                    if ((p.dormant >> l) & 1) al = 0.f;
-                    // the reference stores m = acc * ik (one rounding) before k_update reads it;
-                    // __fmul_rn keeps that rounding (no fused multiply-add into the blend)
-                    out[l] = a + al * (__fmul_rn(acc[l], ik) - a);
-                    if (!((p.dormant >> l) & 1)) est += out[l];
-                } else {
-                    out[l] = 0.f;
+                for (int k4 = 0; k4 < LCS / 4; ++k4) op[k4] = make_float4(out[4 * k4], out[4 * k4 + 1], out[4 * k4 + 2], out[4 * k4 + 3]);
+                const float nf = fminf(nn, nmx);
+                c.n[i] = nf;
+                pr_out = 1.f / (nf + 1.f);
+                if (p.want_err && s.valid[i]) {
+                    const float e = est - s.ref[i];
+                    e_d2 = double(e) * e;
+                    e_rs = s.ref[i];
+                    e_cn = 1.0;
                 }
             }
-            float4* op = reinterpret_cast<float4*>(c.Lc2) + (size_t)i * (LCS / 4);
+            if (p.mask_op == MASK_OR) {
+                if (DEPS && k > 0) {
 #pragma unroll
-            for (int k4 = 0; k4 < LCS / 4; ++k4) op[k4] = make_float4(out[4 * k4], out[4 * k4 + 1], out[4 * k4 + 2], out[4 * k4 + 3]);
-            const float nf = fminf(nn, nmx);
-            c.n[i] = nf;
-            pr_out = 1.f / (nf + 1.f);
-            if (p.want_err && s.valid[i]) {
-                const float e = est - s.ref[i];
-                e_d2 = double(e) * e;
-                e_rs = s.ref[i];
-                e_cn = 1.0;
-            }
-        }
-        if (p.mask_op == MASK_OR) {
-            if (DEPS && k > 0) {
-#pragma unroll
-                for (int w = 0; w < NW; ++w) {
-                    const uint32_t old = c.cur[(size_t)w * p.Np + i];
-                    if ((old | m[w]) != old) c.cur[(size_t)w * p.Np + i] = old | m[w];
+                    for (int w = 0; w < NW; ++w) {
+                        const uint32_t old = c.cur[(size_t)w * p.Np + i];
+                        if ((old | m[w]) != old) c.cur[(size_t)w * p.Np + i] = old | m[w];
+                    }
                 }
-            }
-        } else if (p.mask_op == MASK_FRESH || p.mask_op == MASK_ZERO) {
+            } else if (p.mask_op == MASK_FRESH || p.mask_op == MASK_ZERO) {
 #pragma unroll
-            for (int w = 0; w < NW; ++w) c.cur[(size_t)w * p.Np + i] = (DEPS && p.mask_op == MASK_FRESH && k > 0) ? m[w] : 0u;
-        }
+                for (int w = 0; w < NW; ++w) c.cur[(size_t)w * p.Np + i] = (DEPS && p.mask_op == MASK_FRESH && k > 0) ? m[w] : 0u;
+            }
     }
-    {
-        // ray count of the frame: warp sum, one 64-bit atomic per warp
-        const unsigned wk = __reduce_add_sync(0xffffffffu, (unsigned)k_rays);
-        if ((threadIdx.x & 31) == 0 && wk) atomicAdd(c.rays, (unsigned long long)wk);
-    }
+    ray_sum += (unsigned)k_rays;
+    if (FUSED) pr_sum += pr_fixed(pr_out);
     if (!FUSED) {
         region_add<4>(c.rstat, 4, rg, on_r, vr);
         if (p.proj_left > 0) proj_region_add(c.neq, rg, on_p, p.projK, T, float(k_rays), sv_p);
         if (p.ddgi) region_add<3>(c.dstat, 3, rg, on_d, vd);
     }
+    if (FUSED && p.want_err) {
+        // this tile's error partial: warp sums, then the 8 warp sums in warp order
+        const double ev[3] = {e_d2, e_rs, e_cn};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double r = warp_tree(ev[k]);
+            if (lane == 0) esh[par][k][wid] = r;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double t = esh[par][k][0];
+#pragma unroll
+                for (int j = 1; j < BLOCK / 32; ++j) t = t + esh[par][k][j];
+                c.partd[(size_t)tile * 3 + k] = t;
+            }
+        }
+    }
+    }
+    {
+        // ray count of the frame: warp sum, one 64-bit atomic per warp
+        const unsigned wk = __reduce_add_sync(0xffffffffu, ray_sum);
+        if (lane == 0 && wk) atomicAdd(c.rays, (unsigned long long)wk);
+    }
     if (FUSED) {
         unsigned long long tot;
-        if (u64_tail_reduce(pr_fixed(pr_out), prt, c.pracc, c.ticket, tot)) c.sumpr[p.sum_out] = fixed_to_float(tot);
-        if (p.want_err) {
-            const double vd[3] = {e_d2, e_rs, e_cn};
-            double totd[3];
-            if (warp_tail_reduce<double, 3>(vd, taild, c.partd, c.ticket + 1, totd)) {
-                c.err[3 * p.err_frame] = totd[0];
-                c.err[3 * p.err_frame + 1] = totd[1];
-                c.err[3 * p.err_frame + 2] = totd[2];
+        if (u64_tail_reduce(pr_sum, prt, c.pracc, c.ticket, tot)) c.sumpr[p.sum_out] = fixed_to_float(tot);
+        if (p.want_err && wid == 0) {
+            unsigned tk = 0;
+            if (lane == 0) {
+                __threadfence();
+                tk = atomicAdd(c.ticket + 1, 1u);
+            }
+            tk = __shfl_sync(0xffffffffu, tk, 0);
+            if (tk == gridDim.x - 1) {
+                __threadfence();
+                double tot3[3];
+                final_tree<3>(c.partd, ntiles, tot3);
+                if (lane == 0) {
+                    c.err[3 * p.err_frame] = tot3[0];
+                    c.err[3 * p.err_frame + 1] = tot3[1];
+                    c.err[3 * p.err_frame + 2] = tot3[2];
+                    c.ticket[1] = 0u;
+                }
             }
         }
     }
@@ -1061,13 +1130,37 @@ cudaError_t Ops<NL>::build(int NW, const DState& s, const DStatic& g, const Grid
     return cudaErrorInvalidValue;
 }
 
+// Blocks of `kern` (BLOCK threads, `smem` dynamic shared bytes) resident on the whole current
+// device at once, looked up once per device, kernel and shared-memory size.
+static cudaError_t resident_grid(const void* kern, size_t smem, int& out) {
+    struct Entry { int dev; const void* kern; size_t smem; int blocks; };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Entry& x : cache)
+        if (x.dev == dev && x.kern == kern && x.smem == smem) { out = x.blocks; return cudaSuccess; }
+    int per_sm = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    cache.push_back({dev, kern, smem, per_sm * sms});
+    out = per_sm * sms;
+    return cudaSuccess;
+}
+
 template <int NL, int NW, bool DEPS, bool FUSED>
 static cudaError_t frame_t(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                            cudaStream_t st) {
     const size_t smem = frame_smem_bytes(s);
     cudaError_t e = prep_smem(k_frame<NL, NW, DEPS, FUSED>, smem);
     if (e != cudaSuccess) return e;
-    k_frame<NL, NW, DEPS, FUSED><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p);
+    int resident = 0;
+    if ((e = resident_grid((const void*)k_frame<NL, NW, DEPS, FUSED>, smem, resident)) != cudaSuccess) return e;
+    const int blocks = std::min(grid_of(p.Np), resident);
+    k_frame<NL, NW, DEPS, FUSED><<<blocks, BLOCK, smem, st>>>(s, g, grid, c, p);
     return cudaGetLastError();
 }
 
