@@ -60,7 +60,16 @@ __device__ __forceinline__ unsigned long long cell_key(int cx, int cy, int cz, i
 struct Grid {
     float lo[3], ext[3];
     int vx, vy, vz;
+    float scale[3];   // vx / ext[0], vy / ext[1], vz / ext[2] as float quotients (set by set_grid_scale)
 };
+
+// The float quotients every DDA walk starts from, computed once on the host (IEEE division
+// rounds the same on host and device).
+inline void set_grid_scale(Grid& g) {
+    g.scale[0] = (float)g.vx / g.ext[0];
+    g.scale[1] = (float)g.vy / g.ext[1];
+    g.scale[2] = (float)g.vz / g.ext[2];
+}
 
 // poc_gpu.cu:137-142
 __device__ __forceinline__ int vox_of(const Grid& g, f3 p) {
@@ -83,7 +92,7 @@ __device__ __forceinline__ void set_bit(uint32_t (&m)[NW], int v) {
 template <int NW>
 __device__ __forceinline__ void dda_walk(const Grid& g, f3 a, f3 b, uint32_t (&m)[NW]) {
     const int VX = g.vx, VY = g.vy, VZ = g.vz;
-    const float sx = VX / g.ext[0], sy = VY / g.ext[1], sz = VZ / g.ext[2];
+    const float sx = g.scale[0], sy = g.scale[1], sz = g.scale[2];
     float ax = (a.x - g.lo[0]) * sx, ay = (a.y - g.lo[1]) * sy, az = (a.z - g.lo[2]) * sz;
     float bx = (b.x - g.lo[0]) * sx, by = (b.y - g.lo[1]) * sy, bz = (b.z - g.lo[2]) * sz;
     int ix = min(max(int(ax), 0), VX - 1), iy = min(max(int(ay), 0), VY - 1), iz = min(max(int(az), 0), VZ - 1);
@@ -150,7 +159,11 @@ __device__ __forceinline__ void mt_tri(const float4* __restrict__ tri, int j, f3
 // 2 float4: (c, centre_a, half_a, centre_b) (half_b, first triangle bits, count bits, 0), where
 // a, b are the two other axes in increasing order and the box is the triangles' bounding box
 // grown by a margin far above the rounding error of the exact test, so the filter never drops
-// the triangle the exact scan would pick.
+// the triangle the exact scan would pick.  Each axis holds an even number of groups (a
+// padding group has c = NaN and no triangles), and after the 2 ng group records come the
+// pass-1 records of each pair (g, g + 1), g even, packed for paired FP32 arithmetic:
+// (c_g, c_g+1, -centre_a_g, -centre_a_g+1) (half_a_g, half_a_g+1, -centre_b_g, -centre_b_g+1)
+// (half_b_g, half_b_g+1, 0, 0).
 struct GroupRanges { int g0[4]; };  // groups of axis 0 in [g0[0], g0[1]), axis 1 [g0[1], g0[2]), axis 2 [g0[2], g0[3])
 
 }  // namespace rc

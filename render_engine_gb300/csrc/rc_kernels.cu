@@ -203,34 +203,49 @@ __device__ __forceinline__ void proj_region_add(float* __restrict__ neq, int rg,
 struct TraceSmem {
     const float4* tri;
     const float4* grp;
+    const float4* gpair;   // pass-1 records, 3 float4 per pair of groups
     const int* misc;
 };
 
-// Plane filter of one group: the ray's crossing of the group's plane (t = (c - o_k) / d_k) is a
-// candidate when it lies ahead of the origin and inside the group's outer box, stored as centre
-// and half extent so each in-plane test is one subtraction and one |x| <= h comparison.  The
-// candidate bit is shifted in (mask = mask << 1 | hit), so group g ends at bit ng - 1 - g.
+// Plane filter of two groups of one axis k at once, in paired FP32 arithmetic: the ray's
+// crossing of group g's plane (t = (c - o_k) / d_k) is a candidate when it lies ahead of the
+// origin and inside the group's outer box, stored as centre and half extent so each in-plane
+// test is one addition and one |x| <= h comparison.  The candidate bits are shifted in
+// (mask = mask << 2 | hit_g << 1 | hit_g+1), so group g ends at bit ng - 1 - g.  The filter
+// only has to be conservative (the box margin and the stopping slack of pass 2 are orders of
+// magnitude above its rounding), so 1 / d_k is the approximate reciprocal.
 template <typename MaskT>
-__device__ __forceinline__ void filter_group(const float4* __restrict__ grp, int g, float ok, float idk, float oa, float da,
-                                             float ob, float db, MaskT& mask) {
-    const float4 G0 = grp[2 * g];
-    const float hb = grp[2 * g + 1].x;
-    const float tk = (G0.x - ok) * idk;
-    const float xa = oa + tk * da, xb = ob + tk * db;
-    const bool in = tk > 5e-5f && fabsf(xa - G0.y) <= G0.z && fabsf(xb - G0.w) <= hb;
-    mask = (mask << 1) | (MaskT)in;
+__device__ __forceinline__ void filter_pair(const float4* __restrict__ gp, int pp, float2 nok, float2 idk, float2 oa, float2 da,
+                                            float2 ob, float2 db, MaskT& mask) {
+    const float4 P0 = gp[3 * pp], P1 = gp[3 * pp + 1];
+    const float2 P2 = *reinterpret_cast<const float2*>(gp + 3 * pp + 2);
+    const float2 tk = __fmul2_rn(__fadd2_rn(make_float2(P0.x, P0.y), nok), idk);
+    const float2 ea = __fadd2_rn(__ffma2_rn(tk, da, oa), make_float2(P0.z, P0.w));
+    const float2 eb = __fadd2_rn(__ffma2_rn(tk, db, ob), make_float2(P1.z, P1.w));
+    const bool in0 = tk.x > 5e-5f && fabsf(ea.x) <= P1.x && fabsf(eb.x) <= P2.x;
+    const bool in1 = tk.y > 5e-5f && fabsf(ea.y) <= P1.y && fabsf(eb.y) <= P2.y;
+    mask = (mask << 2) | ((MaskT)in0 << 1) | (MaskT)in1;
+}
+
+// Pass 1 over the groups [a, b) of one axis (a, b even).
+template <typename MaskT>
+__device__ __forceinline__ void filter_axis(const float4* __restrict__ gp, int a, int b, float ok, float idk, float oa, float da,
+                                            float ob, float db, MaskT& mask) {
+    const float2 nok2 = make_float2(-ok, -ok), idk2 = make_float2(idk, idk);
+    const float2 oa2 = make_float2(oa, oa), da2 = make_float2(da, da), ob2 = make_float2(ob, ob), db2 = make_float2(db, db);
+#pragma unroll 2
+    for (int pp = a >> 1; pp < (b >> 1); ++pp) filter_pair(gp, pp, nok2, idk2, oa2, da2, ob2, db2, mask);
 }
 
 template <typename MaskT>
 __device__ __forceinline__ void trace_groups(const TraceSmem& sm, const DState& s, f3 o, f3 d, float& tmin, int& q, int& jb) {
+    // pass 1: bit ng - 1 - g of mask <=> group g is a candidate
     MaskT mask = 0;
-    const float idx = 1.f / d.x, idy = 1.f / d.y, idz = 1.f / d.z;
-#pragma unroll 4
-    for (int g = s.gr.g0[0]; g < s.gr.g0[1]; ++g) filter_group(sm.grp, g, o.x, idx, o.y, d.y, o.z, d.z, mask);
-#pragma unroll 4
-    for (int g = s.gr.g0[1]; g < s.gr.g0[2]; ++g) filter_group(sm.grp, g, o.y, idy, o.x, d.x, o.z, d.z, mask);
-#pragma unroll 4
-    for (int g = s.gr.g0[2]; g < s.gr.g0[3]; ++g) filter_group(sm.grp, g, o.z, idz, o.x, d.x, o.y, d.y, mask);
+    const float idx = __fdividef(1.f, d.x), idy = __fdividef(1.f, d.y), idz = __fdividef(1.f, d.z);
+    filter_axis(sm.gpair, s.gr.g0[0], s.gr.g0[1], o.x, idx, o.y, d.y, o.z, d.z, mask);
+    filter_axis(sm.gpair, s.gr.g0[1], s.gr.g0[2], o.y, idy, o.x, d.x, o.z, d.z, mask);
+    filter_axis(sm.gpair, s.gr.g0[2], s.gr.g0[3], o.z, idz, o.x, d.x, o.y, d.y, mask);
+    // pass 2: candidates nearest first, exact test, stop past the best hit plus the slack
     const int top = s.ng - 1;
     float thr = tmin * 1.0001f + 1e-5f;
     while (mask) {
@@ -410,16 +425,18 @@ __device__ __forceinline__ Hit trace_resolve(const TraceSmem& sm, const DState& 
 __device__ __forceinline__ void stage_smem(float4* sm, const DState& s) {
     float4* st = sm;
     float4* sg = sm + 3 * s.nt;
-    int* smi = (int*)(sg + 2 * s.ng);
+    const int ngf = grp_float4s(s.ng);
+    int* smi = (int*)(sg + ngf);
     for (int j = threadIdx.x; j < 3 * s.nt; j += blockDim.x) st[j] = s.tri[j];
-    for (int j = threadIdx.x; j < 2 * s.ng; j += blockDim.x) sg[j] = s.grp[j];
+    for (int j = threadIdx.x; j < ngf; j += blockDim.x) sg[j] = s.grp[j];
     for (int j = threadIdx.x; j < s.nmisc; j += blockDim.x) smi[j] = s.misc[j];
 }
 __device__ __forceinline__ TraceSmem smem_view(float4* sm, const DState& s) {
     TraceSmem t;
     t.tri = sm;
     t.grp = sm + 3 * s.nt;
-    t.misc = (const int*)(sm + 3 * s.nt + 2 * s.ng);
+    t.gpair = t.grp + 2 * s.ng;
+    t.misc = (const int*)(t.grp + grp_float4s(s.ng));
     return t;
 }
 
@@ -439,7 +456,7 @@ __device__ __forceinline__ int ray_count(const FrameParams& p, const DevCache& c
     }
     float pr = 1.f / (n_i + 1.f);
     float rrest = float(p.Np - npend_cur);
-    float e = rrest * (0.5f / p.Np + 0.5f * pr / sumpr_cur) * p.rays;
+    float e = rrest * (p.half_inv_np + 0.5f * pr / sumpr_cur) * p.rays;
     float eb = floorf(e);
     return (pend ? 1 : 0) + int(eb) + (rnd(rs) < e - eb ? 1 : 0);
 }

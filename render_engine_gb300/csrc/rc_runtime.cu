@@ -231,18 +231,35 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
         j += g.cnt;
     }
     Groups out;
-    if ((int)gs.size() > MAX_GROUPS) {
+    // up to 3 padding groups (one per axis) must still fit in the candidate mask
+    constexpr int MAX_REAL = MAX_GROUPS - 3;
+    if ((int)gs.size() > MAX_REAL) {
         std::stable_sort(gs.begin(), gs.end(), [](const G& a, const G& b) {
             return (a.hi[0] - a.lo[0]) * (a.hi[1] - a.lo[1]) > (b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]);
         });
-        for (size_t x = MAX_GROUPS; x < gs.size(); ++x)
+        for (size_t x = MAX_REAL; x < gs.size(); ++x)
             for (int t = 0; t < gs[x].cnt; ++t) misc.push_back(gs[x].j0 + t);
-        gs.resize(MAX_GROUPS);
+        gs.resize(MAX_REAL);
     }
-    std::stable_sort(gs.begin(), gs.end(), [](const G& a, const G& b) { return a.axis < b.axis; })
-    ;
+    std::stable_sort(gs.begin(), gs.end(), [](const G& a, const G& b) { return a.axis < b.axis; });
     int cnt[3] = {0, 0, 0};
     for (auto& g : gs) cnt[g.axis]++;
+    {
+        // pad every axis to an even count: the filter tests groups two at a time
+        std::vector<G> padded;
+        size_t x = 0;
+        for (int k = 0; k < 3; ++k) {
+            for (int n = 0; n < cnt[k]; ++n) padded.push_back(gs[x++]);
+            if (cnt[k] & 1) {
+                G pad{};
+                pad.axis = k;
+                pad.c = NAN;
+                padded.push_back(pad);
+                cnt[k]++;
+            }
+        }
+        gs.swap(padded);
+    }
     out.gr.g0[0] = 0;
     out.gr.g0[1] = cnt[0];
     out.gr.g0[2] = cnt[0] + cnt[1];
@@ -262,6 +279,12 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
         memcpy(&fj0, &j0, 4); memcpy(&fc, &c, 4); memcpy(&fz, &z, 4);
         out.grp.push_back(make_float4(g.c, ctr[0], half[0], ctr[1]));
         out.grp.push_back(make_float4(half[1], fj0, fc, fz));
+    }
+    for (size_t x = 0; x + 1 < gs.size(); x += 2) {
+        const float4 a0 = out.grp[2 * x], a1 = out.grp[2 * x + 1], b0 = out.grp[2 * x + 2], b1 = out.grp[2 * x + 3];
+        out.grp.push_back(make_float4(a0.x, b0.x, -a0.y, -b0.y));
+        out.grp.push_back(make_float4(a0.z, b0.z, -a0.w, -b0.w));
+        out.grp.push_back(make_float4(a1.x, b1.x, 0.f, 0.f));
     }
     std::sort(misc.begin(), misc.end());
     out.misc = misc;
@@ -321,6 +344,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         g.nnodes = m[1];
         g.max_visits = 4 * m[1] + 64;
     }
+    set_grid_scale(S.grid);
     auto L = r.vec<float>(3 * (size_t)NL);
     auto A = r.vec<float>(Np);
     auto region = r.vec<int>(Np);
@@ -376,7 +400,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
             if ((s = dput(ctx, pool, &hs.pw, pw))) return s;
         }
         d.nt = S.Nt;
-        d.ng = (int)G.grp.size() / 2;
+        d.ng = G.gr.g0[3];
         d.nmisc = (int)G.misc.size();
         d.gr = G.gr;
         size_t smem = frame_smem_bytes(d);
@@ -694,6 +718,7 @@ FrameParams base_params(rc_ctx* ctx) {
     p.sum_out = 1 - R.sum_cur;
     p.brute = (ctx->cfg.flags & RC_FLAG_BRUTE_FORCE) ? 1 : 0;
     p.check = (ctx->cfg.flags & RC_FLAG_CHECK_TRACE) ? 1 : 0;
+    p.half_inv_np = 0.5f / (float)ctx->S.Np;
     return p;
 }
 
