@@ -46,7 +46,6 @@ struct DevBuf {
 
 struct HostState {
     std::vector<float> inten;
-    std::vector<float> ref;         // host copy of the reference
     const float* pw = nullptr;      // device warm start (padded cache layout)
     DState d{};
 };
@@ -158,7 +157,46 @@ struct Reader {
         get(v.data(), cnt);
         return v;
     }
+    // The next cnt elements of type T, left in place (no host copy; possibly unaligned, so read
+    // them on the host with memcpy only).
+    template <class T>
+    const uint8_t* raw(size_t cnt) {
+        if (bad || cnt > (n - off) / sizeof(T)) { bad = true; return nullptr; }
+        const uint8_t* q = p + off;
+        off += cnt * sizeof(T);
+        return q;
+    }
 };
+
+// Load-time kernels: the scene's large per-point arrays are copied to the device as they lie
+// in the file and re-laid out there.
+__global__ void k_load_pack4(const float* __restrict__ src, float4* __restrict__ dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f);
+}
+__global__ void k_load_pad(const float* __restrict__ src, float* __restrict__ dst, size_t n, int nl, int lcs) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        for (int l = 0; l < lcs; ++l) dst[(size_t)lcs * i + l] = l < nl ? src[(size_t)nl * i + l] : 0.f;
+}
+__global__ void k_load_check(const int* __restrict__ v, size_t n, int lo, int hi, unsigned* __restrict__ bad, unsigned bit) {
+    bool out = false;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out |= v[i] < lo || v[i] >= hi;
+    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31) == 0) atomicOr(bad, bit);
+}
+constexpr unsigned LOAD_BAD_REGION = 1u, LOAD_BAD_HASH = 2u;
+int load_grid(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 4096); }
+
+// Device copy of `bytes` bytes at `src` (host) into a new buffer of the pool.
+template <class T>
+rc_status dput_raw(rc_ctx* ctx, std::vector<DevBuf>& pool, const T** out, const uint8_t* src, size_t cnt) {
+    T* p = nullptr;
+    rc_status s = dalloc(ctx, pool, &p, cnt);
+    if (s != RC_OK) return s;
+    if (cnt) CKR(cudaMemcpyAsync(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    *out = p;
+    return RC_OK;
+}
 
 // poc_gpu.cu:720-735: fine event grid (16 x 8 x 6 over the 8 x 4 x 3 m box) -> transit grid.
 std::vector<int> to_grid(const std::vector<int>& fine, int VX, int VY, int VZ) {
@@ -312,32 +350,37 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     auto& pool = ctx->scene_bufs;
     DStatic& g = S.g;
     memset(&g, 0, sizeof g);
+    CKR(cudaMemsetAsync(ctx->flags_dev + 2, 0, sizeof(unsigned), ctx->stream));   // load checks
     if (S.fmt == 3) {
         int m[4];
         r.get(S.grid.lo, 3); r.get(S.grid.ext, 3); r.get(&S.hcell, 1); r.get(m, 4);
         if (r.bad || m[0] < 0 || m[1] <= 0 || m[2] <= 0 || (m[2] & (m[2] - 1)) || m[3] < 0)
             return fail(ctx, RC_ERR_FORMAT, "scene: bad mesh block");
         S.nst = m[0]; S.nnodes = m[1]; S.hsize = m[2]; S.npst = m[3];
-        auto ST = r.vec<float>(9 * (size_t)m[0]);
-        auto STN = r.vec<float>(4 * (size_t)m[0]);
-        auto BN = r.vec<float>(8 * (size_t)m[1]);
-        auto HK = r.vec<unsigned long long>((size_t)m[2]);
-        auto HV = r.vec<int>((size_t)m[2]);
+        const uint8_t* ST = r.raw<float>(9 * (size_t)m[0]);
+        const uint8_t* STN = r.raw<float>(4 * (size_t)m[0]);
+        const uint8_t* BN = r.raw<float>(8 * (size_t)m[1]);
+        const uint8_t* HK = r.raw<unsigned long long>((size_t)m[2]);
+        const uint8_t* HV = r.raw<int>((size_t)m[2]);
         if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated mesh block");
-        // every node link and leaf range must stay inside the arrays the traversal reads
+        // every node link and leaf range must stay inside the arrays the traversal reads (the
+        // state build traverses the tree, so this is checked before anything runs)
         for (int k = 0; k < m[1]; ++k) {
             int lf, cnt;
-            memcpy(&lf, &BN[8 * (size_t)k + 3], 4);
-            memcpy(&cnt, &BN[8 * (size_t)k + 7], 4);
+            memcpy(&lf, BN + 4 * (8 * (size_t)k + 3), 4);
+            memcpy(&cnt, BN + 4 * (8 * (size_t)k + 7), 4);
             if (cnt > 0) { if (lf < 0 || (long long)lf + cnt > m[0]) return fail(ctx, RC_ERR_FORMAT, "BVH leaf %d out of range", k); }
             else if (lf < 0 || lf + 1 >= m[1]) return fail(ctx, RC_ERR_FORMAT, "BVH node %d child out of range", k);
         }
-        for (int v : HV) if (v < -1 || v >= S.Np) return fail(ctx, RC_ERR_FORMAT, "hash value out of range");
         if (!(S.hcell > 0.f)) return fail(ctx, RC_ERR_FORMAT, "hash cell size");
         rc_status s;
-        if ((s = dput(ctx, pool, &g.ST, ST)) || (s = dput(ctx, pool, (const float**)&g.STN, STN)) ||
-            (s = dput(ctx, pool, (const float**)&g.BN, BN)) || (s = dput(ctx, pool, &g.HK, HK)) || (s = dput(ctx, pool, &g.HV, HV)))
+        if ((s = dput_raw(ctx, pool, &g.ST, ST, 9 * (size_t)m[0])) || (s = dput_raw(ctx, pool, (const float**)&g.STN, STN, 4 * (size_t)m[0])) ||
+            (s = dput_raw(ctx, pool, (const float**)&g.BN, BN, 8 * (size_t)m[1])) ||
+            (s = dput_raw(ctx, pool, &g.HK, HK, (size_t)m[2])) || (s = dput_raw(ctx, pool, &g.HV, HV, (size_t)m[2])))
             return s;
+        // hash values are cache point ids or -1; checked on the device, read back before the load returns
+        k_load_check<<<load_grid((size_t)m[2]), 256, 0, ctx->stream>>>(g.HV, (size_t)m[2], -1, S.Np, ctx->flags_dev + 2, LOAD_BAD_HASH);
+        CKR(cudaGetLastError());
         g.hmask = (unsigned)m[2] - 1u;
         g.hcell = S.hcell;
         g.has_bvh = 1;
@@ -346,36 +389,42 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     }
     set_grid_scale(S.grid);
     auto L = r.vec<float>(3 * (size_t)NL);
-    auto A = r.vec<float>(Np);
-    auto region = r.vec<int>(Np);
+    const uint8_t* A = r.raw<float>(Np);
+    const uint8_t* region = r.raw<int>(Np);
     if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated");
-    for (int v : region) if (v < 0 || v >= S.NR) return fail(ctx, RC_ERR_FORMAT, "region index out of range");
     rc_status s;
     CKR(RC_DISPATCH(NL, preload(NW)));
     const float* dL = nullptr;
-    if ((s = dput(ctx, pool, &dL, L)) || (s = dput(ctx, pool, &g.A, A)) || (s = dput(ctx, pool, &g.region, region))) return s;
+    if ((s = dput(ctx, pool, &dL, L)) || (s = dput_raw(ctx, pool, &g.A, A, Np)) || (s = dput_raw(ctx, pool, &g.region, region, Np)))
+        return s;
+    // region ids index the per-region statistics; checked on the device (no frame runs before
+    // the load has read the result back)
+    k_load_check<<<load_grid(Np), 256, 0, ctx->stream>>>(g.region, Np, 0, S.NR, ctx->flags_dev + 2, LOAD_BAD_REGION);
+    CKR(cudaGetLastError());
+    // staging for one state's per-point arrays as they lie in the file
+    float* stage = nullptr;
+    std::vector<DevBuf> stage_pool;
+    struct StageFree { std::vector<DevBuf>& p; ~StageFree() { free_pool(p); } } stage_free{stage_pool};
+    if ((s = dalloc(ctx, stage_pool, &stage, (size_t)(6 + (S.has_ref ? NL : 0)) * Np))) return s;
     S.st.resize(S.NS);
     for (int k = 0; k < S.NS; ++k) {
         HostState& hs = S.st[k];
         hs.inten = r.vec<float>(NL);
-        auto P = r.vec<float>(3 * Np), N = r.vec<float>(3 * Np), Q = r.vec<float>(12 * (size_t)S.Nq);
+        const uint8_t* P = r.raw<float>(3 * Np);
+        const uint8_t* N = r.raw<float>(3 * Np);
+        auto Q = r.vec<float>(12 * (size_t)S.Nq);
         auto dims = r.vec<int>(2 * (size_t)S.Nq), off = r.vec<int>((size_t)S.Nq);
         auto T = r.vec<float>(9 * (size_t)S.Nt);
         auto TQ = r.vec<int>((size_t)S.Nt);
-        std::vector<uint8_t> valid;
-        std::vector<float> Pw;
-        if (S.has_ref) { hs.ref = r.vec<float>(Np); valid = r.vec<uint8_t>(Np); Pw = r.vec<float>((size_t)NL * Np); }
+        const uint8_t *ref = nullptr, *valid = nullptr, *Pw = nullptr;
+        if (S.has_ref) { ref = r.raw<float>(Np); valid = r.raw<uint8_t>(Np); Pw = r.raw<float>((size_t)NL * Np); }
         if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated state %d", k);
         for (int q = 0; q < S.Nq; ++q)
             if (dims[2 * q] <= 0 || dims[2 * q + 1] <= 0 || off[q] < 0 ||
                 (long long)off[q] + (long long)dims[2 * q] * dims[2 * q + 1] > S.Np)
                 return fail(ctx, RC_ERR_FORMAT, "quad %d grid out of range", q);
         for (int t : TQ) if (t < 0 || t >= S.Nq) return fail(ctx, RC_ERR_FORMAT, "triangle quad id out of range");
-        std::vector<float4> P4(Np), N4(Np), tri(3 * (size_t)S.Nt);
-        for (size_t i = 0; i < Np; ++i) {
-            P4[i] = make_float4(P[3 * i], P[3 * i + 1], P[3 * i + 2], 0.f);
-            N4[i] = make_float4(N[3 * i], N[3 * i + 1], N[3 * i + 2], 0.f);
-        }
+        std::vector<float4> tri(3 * (size_t)S.Nt);
         for (int j = 0; j < S.Nt; ++j) {
             float qb;
             memcpy(&qb, &TQ[j], 4);
@@ -387,17 +436,30 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         Groups G = build_groups(T, TQ, S.Nt);
         DState& d = hs.d;
         memset(&d, 0, sizeof d);
-        if ((s = dput(ctx, pool, &d.P4, P4)) || (s = dput(ctx, pool, &d.N4, N4)) || (s = dput(ctx, pool, &d.Q, Q)) ||
-            (s = dput(ctx, pool, &d.dims, dims)) || (s = dput(ctx, pool, &d.off, off)) || (s = dput(ctx, pool, &d.tri, tri)) ||
-            (s = dput(ctx, pool, &d.grp, G.grp)) || (s = dput(ctx, pool, &d.misc, G.misc)))
+        if ((s = dput(ctx, pool, &d.Q, Q)) || (s = dput(ctx, pool, &d.dims, dims)) || (s = dput(ctx, pool, &d.off, off)) ||
+            (s = dput(ctx, pool, &d.tri, tri)) || (s = dput(ctx, pool, &d.grp, G.grp)) || (s = dput(ctx, pool, &d.misc, G.misc)))
             return s;
+        {
+            // positions and normals: xyz triples copied as they are, packed to float4 on the device
+            float4 *P4 = nullptr, *N4 = nullptr;
+            if ((s = dalloc(ctx, pool, &P4, Np)) || (s = dalloc(ctx, pool, &N4, Np))) return s;
+            CKR(cudaMemcpyAsync(stage, P, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
+            CKR(cudaMemcpyAsync(stage + 3 * Np, N, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
+            k_load_pack4<<<load_grid(Np), 256, 0, ctx->stream>>>(stage, P4, Np);
+            k_load_pack4<<<load_grid(Np), 256, 0, ctx->stream>>>(stage + 3 * Np, N4, Np);
+            CKR(cudaGetLastError());
+            d.P4 = P4;
+            d.N4 = N4;
+        }
         if (S.has_ref) {
-            if ((s = dput(ctx, pool, &d.ref, hs.ref)) || (s = dput(ctx, pool, &d.valid, valid))) return s;
+            if ((s = dput_raw(ctx, pool, &d.ref, ref, Np)) || (s = dput_raw(ctx, pool, &d.valid, valid, Np))) return s;
             // warm start of every run beginning in this state (poc_gpu.cu:832), padded like the cache
-            std::vector<float> pw((size_t)lcs_of(NL) * Np, 0.f);
-            for (size_t i = 0; i < Np; ++i)
-                for (int l = 0; l < NL; ++l) pw[(size_t)lcs_of(NL) * i + l] = Pw[(size_t)NL * i + l];
-            if ((s = dput(ctx, pool, &hs.pw, pw))) return s;
+            float* pw = nullptr;
+            if ((s = dalloc(ctx, pool, &pw, (size_t)lcs_of(NL) * Np))) return s;
+            CKR(cudaMemcpyAsync(stage + 6 * Np, Pw, 4 * (size_t)NL * Np, cudaMemcpyHostToDevice, ctx->stream));
+            k_load_pad<<<load_grid(Np), 256, 0, ctx->stream>>>(stage + 6 * Np, pw, Np, NL, lcs_of(NL));
+            CKR(cudaGetLastError());
+            hs.pw = pw;
         }
         d.nt = S.Nt;
         d.ng = G.gr.g0[3];
@@ -439,7 +501,11 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         if ((s = dput(ctx, pool, &p, S.ev[e]))) return s;
         S.ev_dev[e] = p;
     }
+    unsigned bad = 0;
+    CKR(cudaMemcpyAsync(&bad, ctx->flags_dev + 2, sizeof bad, cudaMemcpyDeviceToHost, ctx->stream));
     CKR(cudaStreamSynchronize(ctx->stream));
+    if (bad & LOAD_BAD_REGION) return fail(ctx, RC_ERR_FORMAT, "region index out of range");
+    if (bad & LOAD_BAD_HASH) return fail(ctx, RC_ERR_FORMAT, "hash value out of range");
     ctx->S = std::move(S);
     return RC_OK;
 }
@@ -913,7 +979,8 @@ rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
     ctx->c = DevCache{};
     ctx->err_cap = 0;
     rc_status s = load_scene(ctx, (const uint8_t*)data, nbytes);
-    if (s != RC_OK) { free_pool(ctx->scene_bufs); return s; }
+    // copies from the caller's buffer may still be in flight after a failed load
+    if (s != RC_OK) { cudaStreamSynchronize(ctx->stream); free_pool(ctx->scene_bufs); return s; }
     double b = 0;
     for (auto& x : ctx->scene_bufs) b += (double)x.n;
     ctx->S.scene_bytes = b;

@@ -255,12 +255,17 @@ class Context:
         self._chk(self.L.rc_render(self.h, state, ctypes.byref(cam), img.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), img.size))
         return img
 
-    def array(self, which: int) -> np.ndarray:
+    def array(self, which: int, out: np.ndarray | None = None) -> np.ndarray:
+        """Copy one cache array to the host; into `out` (for instance a view of pinned memory)
+        when given, which must hold exactly the array's bytes."""
         n = ctypes.c_size_t()
         self._chk(self.L.rc_array_info(self.h, which, ctypes.byref(n), None))
-        a = np.empty(n.value // np.dtype(ARRAY_DTYPE[which]).itemsize, ARRAY_DTYPE[which])
-        self._chk(self.L.rc_array_copy(self.h, which, a.ctypes.data_as(ctypes.c_void_p), a.nbytes, 0))
-        return a
+        if out is None:
+            out = np.empty(n.value // np.dtype(ARRAY_DTYPE[which]).itemsize, ARRAY_DTYPE[which])
+        elif out.nbytes != n.value or not out.flags.c_contiguous:
+            raise ValueError("out holds %d bytes, the array %d" % (out.nbytes, n.value))
+        self._chk(self.L.rc_array_copy(self.h, which, out.ctypes.data_as(ctypes.c_void_p), out.nbytes, 0))
+        return out
 
     def set_array(self, which: int, a: np.ndarray):
         a = np.ascontiguousarray(a, ARRAY_DTYPE[which])

@@ -1,0 +1,67 @@
+"""Scene loading on the GPU: the per-point arrays are copied to the device as they lie in the
+file (from pinned or pageable host memory) and re-laid out there, and the range checks of
+region ids and hash values run on the device before the load returns.  A scene that fails a
+check is rejected with a format error and leaves the context usable."""
+import numpy as np
+import pytest
+import torch
+
+from render_engine_gb300 import methods as M
+from render_engine_gb300 import native as N
+from render_engine_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_frames(ctx, n=3):
+    m = M.by_name(M.timing_methods(), "v4-A2C suivi 1/4")
+    ctx.begin(m, 0, 5)
+    for _ in range(n):
+        ctx.frame(0)
+    return ctx.array(N.A_LC)
+
+
+def test_pinned_and_pageable_sources_load_the_same_scene(scene_main_bytes):
+    a = N.Context()
+    a.load_bytes(scene_main_bytes)
+    pinned = torch.frombuffer(bytearray(scene_main_bytes), dtype=torch.uint8).pin_memory()
+    b = N.Context()
+    b.load_bytes(pinned.numpy())
+    for s in range(a.info()["ns"]):
+        for which in (N.SA_EDIR, N.SA_SV, N.SA_REF, N.SA_VALID, N.SA_PW):
+            assert np.array_equal(a.state_array(s, which), b.state_array(s, which)), (s, which)
+    assert np.array_equal(_run_frames(a).view(np.uint32), _run_frames(b).view(np.uint32))
+
+
+def test_bad_region_id_rejected_and_context_reusable(scene_main_bytes):
+    sc = S.read(scene_main_bytes)
+    sc.region = sc.region.copy()
+    sc.region[len(sc.region) // 2] = sc.NR
+    ctx = N.Context()
+    with pytest.raises(N.RCError, match="region index out of range"):
+        ctx.load_bytes(S.write(sc))
+    sc.region[len(sc.region) // 2] = -1
+    with pytest.raises(N.RCError, match="region index out of range"):
+        ctx.load_bytes(S.write(sc))
+    ctx.load_bytes(scene_main_bytes)
+    assert np.isfinite(_run_frames(ctx)).all()
+
+
+def test_bad_hash_value_rejected():
+    sc = S.street_scene(points=4000, buildings=3)
+    hv = sc.mesh["HV"].copy()
+    k = int(np.flatnonzero(hv >= 0)[0])
+    hv[k] = 10 ** 8
+    sc.mesh = dict(sc.mesh, HV=hv)
+    ctx = N.Context()
+    with pytest.raises(N.RCError, match="hash value out of range"):
+        ctx.load_bytes(S.write(sc))
+
+
+def test_truncated_scene_rejected(scene_main_bytes):
+    ctx = N.Context()
+    for cut in (16, len(scene_main_bytes) // 3, len(scene_main_bytes) - 7):
+        with pytest.raises(N.RCError):
+            ctx.load_bytes(scene_main_bytes[:cut])
+    ctx.load_bytes(scene_main_bytes)
+    assert np.isfinite(_run_frames(ctx)).all()
