@@ -156,11 +156,12 @@ __device__ __forceinline__ void mt_tri(const float4* __restrict__ tri, int j, f3
 }
 
 // Plane-culling group: the axis-aligned triangles of one quad lying in one plane k = c.
-// 2 float4: (c, centre_a, half_a, centre_b) (half_b, first triangle bits, count bits, 0), where
+// 3 float4: (c, centre_a, half_a, centre_b) (half_b, first triangle bits, count bits, 0)
+// (n_a, n_b, w, eps) -- the last is the line between the group's two triangles -- where
 // a, b are the two other axes in increasing order and the box is the triangles' bounding box
 // grown by a margin far above the rounding error of the exact test, so the filter never drops
 // the triangle the exact scan would pick.  Each axis holds an even number of groups (a
-// padding group has c = NaN and no triangles), and after the 2 ng group records come the
+// padding group has c = NaN and no triangles), and after the 3 ng group records come the
 // pass-1 records of each pair (g, g + 1), g even, packed for paired FP32 arithmetic:
 // (c_g, c_g+1, -centre_a_g, -centre_a_g+1) (half_a_g, half_a_g+1, -centre_b_g, -centre_b_g+1)
 // (half_b_g, half_b_g+1, 0, 0).

@@ -18,7 +18,7 @@ struct DState {
     const int* dims;           // nu, nv per quad
     const int* off;            // first point of each quad
     const float4* tri;         // dynamic triangles, 3 float4 each (v0 + quad id bits, e1, e2)
-    const float4* grp;         // plane-culling groups, 2 float4 each, then the pair records (grp_float4s)
+    const float4* grp;         // plane-culling groups, 3 float4 each, then the pair records (grp_float4s)
     const int* misc;           // dynamic triangles outside any group (always tested exactly)
     const float* ref;          // converged reference per point (scenes with references)
     const uint8_t* valid;
@@ -159,8 +159,8 @@ inline bool supported_nl_nw(int NL, int NW) {
 #define X(n) extern template struct Ops<n>;
 RC_NL_VALUES(X)
 #undef X
-// The group buffer: 2 float4 per group, then 3 float4 per pair of groups (pass-1 records).
-__host__ __device__ inline int grp_float4s(int ng) { return 2 * ng + 3 * (ng / 2); }
+// The group buffer: 3 float4 per group, then 3 float4 per pair of groups (pass-1 records).
+__host__ __device__ inline int grp_float4s(int ng) { return 3 * ng + 3 * (ng / 2); }
 inline size_t frame_smem_bytes(const DState& s) {
     return sizeof(float4) * (3 * (size_t)s.nt + (size_t)grp_float4s(s.ng)) + sizeof(int) * (size_t)s.nmisc + 16;
 }

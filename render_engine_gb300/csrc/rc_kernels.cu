@@ -256,14 +256,26 @@ __device__ __forceinline__ void trace_groups(const TraceSmem& sm, const DState& 
             const int g = top - b;
             const float ok = g < s.gr.g0[1] ? o.x : (g < s.gr.g0[2] ? o.y : o.z);
             const float idk = g < s.gr.g0[1] ? idx : (g < s.gr.g0[2] ? idy : idz);
-            const float tk = (sm.grp[2 * g].x - ok) * idk;
+            const float tk = (sm.grp[3 * g].x - ok) * idk;
             if (tk < best) { best = tk; bb = b; }
         }
         if (!(best <= thr)) break;
         mask &= ~((MaskT)1 << bb);
-        const float4 G1 = sm.grp[2 * (top - bb) + 1];
-        const int j0 = __float_as_int(G1.y), cnt = __float_as_int(G1.z);
-        for (int j = j0; j < j0 + cnt; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
+        const int g = top - bb;
+        const float4 G1 = sm.grp[3 * g + 1];
+        int j = __float_as_int(G1.y), jend = j + __float_as_int(G1.z);
+        if (jend - j == 2) {
+            // exact test on the triangle whose side of the diagonal holds the crossing (both
+            // within eps of the diagonal): the other one cannot hold the hit
+            const float4 GL = sm.grp[3 * g + 2];
+            const bool ax0 = g < s.gr.g0[1], ax1 = !ax0 && g < s.gr.g0[2];
+            const float oa = ax0 ? o.y : o.x, da = ax0 ? d.y : d.x;
+            const float ob = ax0 || ax1 ? o.z : o.y, db = ax0 || ax1 ? d.z : d.y;
+            const float sd = GL.x * (oa + best * da) + GL.y * (ob + best * db) + GL.z;
+            if (sd > GL.w) jend = j + 1;
+            else if (sd < -GL.w) j = j + 1;
+        }
+        for (; j < jend; ++j) mt_tri(sm.tri, j, o, d, tmin, q, jb);
         thr = tmin * 1.0001f + 1e-5f;
     }
 }
@@ -435,7 +447,7 @@ __device__ __forceinline__ TraceSmem smem_view(float4* sm, const DState& s) {
     TraceSmem t;
     t.tri = sm;
     t.grp = sm + 3 * s.nt;
-    t.gpair = t.grp + 2 * s.ng;
+    t.gpair = t.grp + 3 * s.ng;
     t.misc = (const int*)(t.grp + grp_float4s(s.ng));
     return t;
 }

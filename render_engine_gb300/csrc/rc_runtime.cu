@@ -230,7 +230,7 @@ struct Groups {
     GroupRanges gr{};
 };
 Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int nt) {
-    struct G { int axis, j0, cnt; float c, lo[2], hi[2]; };
+    struct G { int axis, j0, cnt; float c, lo[2], hi[2]; float line[4]; };
     std::vector<G> gs;
     std::vector<int> misc;
     auto axis_of = [&](int j) {
@@ -249,11 +249,57 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
             hi[u] = std::max(v0, std::max(v1, v2));
         }
     };
+    // The line separating the two triangles of a group, in the in-plane axes (a, b):
+    // n . (a, b) + w > eps holds on the first triangle's side, < -eps on the second's, with
+    // eps far above the rounding of the crossing point the trace computes.  Groups whose
+    // triangles do not share an edge with the third vertices on opposite sides get eps = inf.
+    auto split_line = [&](int j, int k, float line[4]) {
+        line[0] = line[1] = line[2] = 0.f;
+        line[3] = INFINITY;
+        const int ax[2] = {k == 0 ? 1 : 0, k == 2 ? 1 : 2};
+        double V[2][3][2];
+        double scale = 0.0;
+        for (int t = 0; t < 2; ++t) {
+            const float* tr = &T[9 * (size_t)(j + t)];
+            for (int u = 0; u < 2; ++u) {
+                V[t][0][u] = tr[ax[u]];
+                V[t][1][u] = (double)(tr[ax[u]] + tr[3 + ax[u]]);
+                V[t][2][u] = (double)(tr[ax[u]] + tr[6 + ax[u]]);
+            }
+            for (int v = 0; v < 3; ++v) scale = std::max(scale, std::max(fabs(V[t][v][0]), fabs(V[t][v][1])));
+        }
+        const double tol = 1e-6 * (1.0 + scale);
+        int sa[2], sb[2], ns = 0;
+        for (int x = 0; x < 3 && ns < 3; ++x)
+            for (int y = 0; y < 3; ++y)
+                if (fabs(V[0][x][0] - V[1][y][0]) <= tol && fabs(V[0][x][1] - V[1][y][1]) <= tol) {
+                    if (ns < 2) { sa[ns] = x; sb[ns] = y; }
+                    ++ns;
+                    break;
+                }
+        if (ns != 2) return;
+        const double* e0 = V[0][sa[0]];
+        const double* e1 = V[0][sa[1]];
+        double na = -(e1[1] - e0[1]), nb = e1[0] - e0[0];
+        const double len = sqrt(na * na + nb * nb);
+        if (!(len > tol)) return;
+        na /= len; nb /= len;
+        double w = -(na * e0[0] + nb * e0[1]);
+        const int ta = 3 - sa[0] - sa[1], tb = 3 - sb[0] - sb[1];
+        double da = na * V[0][ta][0] + nb * V[0][ta][1] + w, db = na * V[1][tb][0] + nb * V[1][tb][1] + w;
+        if (da < 0) { na = -na; nb = -nb; w = -w; da = -da; db = -db; }
+        if (!(da > tol && db < -tol)) return;
+        line[0] = (float)na;
+        line[1] = (float)nb;
+        line[2] = (float)w;
+        line[3] = (float)(2e-3 + 1e-4 * len + 1e-5 * scale);
+    };
     int j = 0;
     while (j < nt) {
         const int k = axis_of(j);
         if (k < 0) { misc.push_back(j); ++j; continue; }
         G g{};
+        g.line[3] = INFINITY;
         g.axis = k;
         g.j0 = j;
         g.c = T[9 * (size_t)j + k];
@@ -264,6 +310,7 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
             box(j + 1, k, lo2, hi2);
             for (int u = 0; u < 2; ++u) { g.lo[u] = std::min(g.lo[u], lo2[u]); g.hi[u] = std::max(g.hi[u], hi2[u]); }
             g.cnt = 2;
+            split_line(j, k, g.line);
         }
         gs.push_back(g);
         j += g.cnt;
@@ -292,6 +339,7 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
                 G pad{};
                 pad.axis = k;
                 pad.c = NAN;
+                pad.line[3] = INFINITY;
                 padded.push_back(pad);
                 cnt[k]++;
             }
@@ -317,9 +365,10 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
         memcpy(&fj0, &j0, 4); memcpy(&fc, &c, 4); memcpy(&fz, &z, 4);
         out.grp.push_back(make_float4(g.c, ctr[0], half[0], ctr[1]));
         out.grp.push_back(make_float4(half[1], fj0, fc, fz));
+        out.grp.push_back(make_float4(g.line[0], g.line[1], g.line[2], g.line[3]));
     }
     for (size_t x = 0; x + 1 < gs.size(); x += 2) {
-        const float4 a0 = out.grp[2 * x], a1 = out.grp[2 * x + 1], b0 = out.grp[2 * x + 2], b1 = out.grp[2 * x + 3];
+        const float4 a0 = out.grp[3 * x], a1 = out.grp[3 * x + 1], b0 = out.grp[3 * x + 3], b1 = out.grp[3 * x + 4];
         out.grp.push_back(make_float4(a0.x, b0.x, -a0.y, -b0.y));
         out.grp.push_back(make_float4(a0.z, b0.z, -a0.w, -b0.w));
         out.grp.push_back(make_float4(a1.x, b1.x, 0.f, 0.f));
