@@ -14,6 +14,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 SRC = os.path.join(HERE, "rc_oracle.c")
+SRCS = [SRC, os.path.join(HERE, "hg_oracle.c")]
+HDRS = [os.path.join(HERE, "rc_oracle.h"), os.path.join(HERE, "hg_oracle.h")]
 
 A_LC, A_LC2, A_M, A_N, A_C0, A_KK, A_PENDING, A_CUR, A_PREV, A_STALE, A_AGE, A_SNAP, A_NEQ, A_COEF, \
     A_RSTAT, A_DSTAT, A_SUMPR, A_NPEND = range(18)
@@ -31,10 +33,10 @@ class RayRec(ctypes.Structure):
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (-O3, OpenMP, no FP contraction so x86 and Arm agree)."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "rc_oracle.h"))):
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(f) for f in SRCS + HDRS):
         tmp = LIB + ".%d.tmp" % os.getpid()
         subprocess.check_call(["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-                               SRC, "-o", tmp, "-lm"])
+                               *SRCS, "-o", tmp, "-lm"])
         os.replace(tmp, LIB)
     return LIB
 

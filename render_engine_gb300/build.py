@@ -3,7 +3,8 @@
 Everything is compiled for sm_103a only, in-tree, into ``render_engine_gb300/_build``:
 
 * ``librc_gb300.so`` -- kernels (one translation unit per light count, compiled in parallel)
-  and the host runtime behind ``include/rc_api.h``;
+  and the host runtime behind ``include/rc_api.h``, plus the hash-grid cache with dependency
+  masks behind ``include/rc_hashgrid.h``;
 * ``poc_gpu_l3`` / ``poc_gpu_l8`` -- the command-line front end, a client of the library,
   with the names and argument conventions of the reference's binaries (cuda/build.sh).
 """
@@ -34,7 +35,7 @@ def nvcc() -> str:
 
 def _sources() -> list[str]:
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h", ".cpp"))] + \
-        [os.path.join(ROOT, "include", "rc_api.h")]
+        [os.path.join(ROOT, "include", "rc_api.h"), os.path.join(ROOT, "include", "rc_hashgrid.h")]
 
 
 def _stale(target: str, deps: list[str]) -> bool:
@@ -62,7 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, deps):
             jobs.append([nv, *ARCH, *FLAGS, "-DRC_NL_ONE=%d" % nl, "-c", os.path.join(CSRC, "rc_kernels.cu"), "-o", o])
-    for name in ("rc_runtime", "rc_noalloc"):
+    for name in ("rc_runtime", "rc_noalloc", "rc_hashgrid"):
         o = os.path.join(OUT, name + ".o")
         objs.append(o)
         if force or _stale(o, deps):

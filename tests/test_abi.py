@@ -10,10 +10,13 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
-    src = open(os.path.join(ROOT, "include", "rc_api.h")).read()
+def declared_functions(header="rc_api.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(rc_[a-z_]+)\s*\(", src)))
+
+
+HEADERS = sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h"))
 
 
 @pytest.fixture(scope="module")
@@ -28,18 +31,20 @@ def test_header_declares_entry_points():
     assert "rc_create" in names and "rc_frame" in names and len(names) >= 20
 
 
-def test_library_exports_every_declared_symbol(lib):
+@pytest.mark.parametrize("header", HEADERS)
+def test_library_exports_every_declared_symbol(lib, header):
     L = ctypes.CDLL(lib)
-    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    missing = [n for n in declared_functions(header) if not hasattr(L, n)]
     assert not missing, missing
     out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
     exported = set(re.findall(r" T (rc_[a-z_]+)$", out, flags=re.M))
-    assert set(declared_functions()) <= exported
+    assert set(declared_functions(header)) <= exported
 
 
 def test_python_binding_lists_every_symbol():
-    from render_engine_gb300 import native
-    assert sorted(native.EXPORTS) == declared_functions()
+    from render_engine_gb300 import hashgrid, native
+    assert sorted(native.EXPORTS) == declared_functions("rc_api.h")
+    assert sorted(hashgrid.EXPORTS) == declared_functions("rc_hashgrid.h")
 
 
 def test_status_strings_and_version(lib):
