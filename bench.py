@@ -48,7 +48,42 @@ def parse():
     ap.add_argument("--method", default=METHOD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=12)
+    ap.add_argument("--profile", choices=["frame", "hashgrid"], default=None,
+                    help="no timing: run --steps frames of state 0 (frame) or three resolve passes of the "
+                         "hash-grid table (hashgrid), for an ncu capture, and exit")
     return ap.parse_args()
+
+
+def profile_run(args):
+    """The small, untimed workloads the committed ncu summaries were captured on."""
+    import torch
+    from render_engine_gb300 import methods as M
+    from render_engine_gb300 import native as N
+    from render_engine_gb300 import scene as S
+    if args.profile == "frame":
+        ctx = N.Context()
+        ctx.load_bytes(S.write(S.box_room(points=args.points, seed=0)))
+        ctx.begin(M.by_name(M.timing_methods(), args.method), 0, 11)
+        for _ in range(args.steps):
+            ctx.frame(0)
+        ctx.sync()
+        ctx.close()
+        return
+    from render_engine_gb300 import hashgrid as H
+    cap, live = 1 << 24, 1 << 23
+    hg = H.HashGrid(H.make_config(capacity=cap, cell=0.02, max_depth=4, acc_frames=64, stale_frames=1000, tracing_distance=50.0))
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    pos = torch.rand(live, 3, device="cuda", generator=g) * torch.tensor([8.0, 4.0, 3.0], device="cuda")
+    nrm = torch.randn(live, 3, device="cuda", generator=g)
+    rgb = torch.rand(live, 3, device="cuda", generator=g)
+    entry = torch.empty(live, dtype=torch.int32, device="cuda")
+    hg.insert(pos, nrm, entry)
+    for _ in range(3):
+        hg.accumulate(entry, rgb)
+        hg.resolve()
+    torch.cuda.synchronize()
+    hg.close()
 
 
 def sequence(n: int, ns: int = 5) -> list[int]:
@@ -118,12 +153,12 @@ def algorithmic_bytes(np_: int, tracked: bool, ramp: bool) -> float:
     """Bytes one fused frame kernel must move for Np points (each array touched once):
     reads P 16, N 16, n 4, own cache 16, gathered albedo+direct light 16 and cache 16 at the
     hit points; writes cache 16, n 4; ramp: age read+write 8; tracked frames: shadow-voxel
-    mask gather 16 and dependency-mask write 16."""
+    mask gather 16 and dependency-mask read 16 + write 16."""
     b = 16 + 16 + 4 + 16 + 16 + 16 + 16 + 4
     if ramp:
         b += 8
     if tracked:
-        b += 32
+        b += 48
     return float(np_) * b
 
 
@@ -277,7 +312,78 @@ def run_ours(args, world, rank, local, dist):
                   "includes": "scene upload + per-state build + %d frames + final cache download" % args.steps}
     ctx2.close()
     ctx.close()
+    out["hashgrid"] = hashgrid_bench(stream, peak)
     return out, data, method
+
+
+def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20, reps=10):
+    """Secondary lines: the hash-grid cache with dependency masks (include/rc_hashgrid.h).
+
+    resolve: one pass over a 2^24-entry table with 2^23 live entries that all received samples
+    this frame (each pass preceded, untimed, by the accumulation that refills them); per
+    entry it reads key 8 B + accumulation 16 B + resolved 16 B + two mask banks 32 B, and a
+    live entry writes its accumulation and resolved words (32 B): the HBM roofline.
+    mark: dependency marking of 2^20 random paths of 1-5 bounces in the zone box."""
+    import numpy as np
+    import torch
+    from render_engine_gb300 import hashgrid as H
+
+    cfg = H.make_config(capacity=capacity, cell=0.02, max_depth=4, acc_frames=64, stale_frames=1000,
+                        tracing_distance=50.0, stream=stream.cuda_stream)
+    hg = H.HashGrid(cfg)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    pos = torch.rand(live, 3, device="cuda", generator=g) * torch.tensor([8.0, 4.0, 3.0], device="cuda")
+    nrm = torch.randn(live, 3, device="cuda", generator=g)
+    rgb = torch.rand(live, 3, device="cuda", generator=g)
+    entry = torch.empty(live, dtype=torch.int32, device="cuda")
+    hg.insert(pos, nrm, entry)
+    hg.accumulate(entry, rgb)
+    hg.resolve()
+    keys = np.frombuffer(hg.download(H.A_KEYS).tobytes(), np.uint64)
+    nlive = int(((keys != 0) & (keys != H.EVICTED)).sum())
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        hg.accumulate(entry, rgb)
+        e0.record(stream)
+        hg.resolve()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    res_ms = sum(a.elapsed_time(b) for a, b in evs) / reps
+    res_bytes = 72.0 * capacity + 32.0 * nlive
+    # path batch
+    rng = np.random.default_rng(8)
+    lens = rng.integers(1, 6, npaths)
+    start = np.zeros(npaths + 1, np.int32)
+    start[1:] = np.cumsum(lens)
+    n = int(start[-1])
+    v = np.zeros(n, H.VERTEX_DTYPE)
+    v["origin"] = rng.uniform([0, 0, 0], [8, 4, 3], (n, 3))
+    v["hit"] = rng.uniform([0, 0, 0], [8, 4, 3], (n, 3))
+    d = rng.normal(size=(n, 3))
+    v["dir"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    t = rng.normal(size=(n, 3))
+    v["to_light"] = t / np.linalg.norm(t, axis=1, keepdims=True)
+    v["light_dist"] = rng.uniform(0.5, 10.0, n)
+    v["light_index"] = rng.integers(-1, 8, n)
+    v["entry"] = entry.cpu().numpy().view(np.uint32)[rng.integers(0, live, n)]
+    v["flags"] = np.where(rng.random(n) < 0.5, H.LIGHT_VISIBLE, 0) | np.where(rng.random(n) < 0.1, H.MISS, 0)
+    dv = torch.from_numpy(v.view(np.uint8)).cuda()
+    ds = torch.from_numpy(start).cuda()
+    hg.mark_paths(dv, ds, npaths)
+    evm = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+    for e0, e1 in evm:
+        e0.record(stream)
+        hg.mark_paths(dv, ds, npaths)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    mark_ms = sum(a.elapsed_time(b) for a, b in evm) / len(evm)
+    hg.close()
+    achieved = res_bytes / (res_ms * 1e-3) / 1e9
+    return {"resolve": {"entries": capacity, "live_entries": nlive, "ms": res_ms, "entries_per_s": capacity / (res_ms * 1e-3),
+                        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                                     "algorithmic_bytes": res_bytes}},
+            "mark_paths": {"paths": npaths, "vertices": n, "ms": mark_ms, "vertices_per_s": n / (mark_ms * 1e-3)}}
 
 
 def cpu_baseline(args, data, method):
@@ -346,6 +452,9 @@ def run_reference(args, world, rank, local, dist):
 
 def main():
     args = parse()
+    if args.profile:
+        profile_run(args)
+        return
     world, rank, local, dist = setup_dist(args)
     config = {"workload": "dependency-tracked radiance cache, %s, seeded box room (%d cache points, 62 triangles, 3 point lights, "
                           "5 states x %d frames with events), one frame per step" % (args.method, args.points, FRAMES_PER_STATE),
@@ -381,7 +490,7 @@ def main():
             "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
             "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
-            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu}
+            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "hashgrid": res["hashgrid"]}
     print(json.dumps(line))
 
 
