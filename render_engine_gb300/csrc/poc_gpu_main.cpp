@@ -5,6 +5,7 @@
 //   poc_gpu_l3 scen    <scene.bin> <nseeds>
 //   poc_gpu_l3 scenf   <scene.bin> <nseeds> <scenarios.txt> [baseline budget]
 //   poc_gpu_l3 quality <scene.bin> <nseeds> <budget1,budget2,...>
+//   poc_gpu_l3 recon   <scene.bin> <nseeds>
 //
 // Same JSONL lines on stdout, same environment variables (BENCH_RAYONS, BENCH_DEBUG), so
 // cuda/run_cuda.sh and cuda/analyse_cuda.py of the reference consume the output unchanged.
@@ -13,6 +14,7 @@
 #include <sys/resource.h>
 #include <time.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -149,6 +151,37 @@ void run_scenarios(rc_ctx* ctx, const std::vector<std::pair<std::string, std::ve
     }
 }
 
+// One run with the per-point estimate of frames f0 .. f0 + nf - 1 added into sum / sq (the
+// reference's k_accum_est after each such frame, poc_gpu.cu:698-703, 1003-1004): float
+// sums, e * e fused into the square sum as the reference's compiled kernel does.
+std::vector<float> run_recorded(rc_ctx* ctx, const rc_method& m0, const std::vector<int>& seq, uint32_t seed, int f0, int nf,
+                                size_t np, int nl, std::vector<float>& sum, std::vector<float>& sq, std::vector<float>& lc) {
+    rc_method m = m0;
+    m.rays = g_rays;
+    CHK(ctx, rc_run_begin(ctx, &m, seq[0], seed), "run");
+    for (int f = 0; f < (int)seq.size(); ++f) {
+        CHK(ctx, rc_frame(ctx, seq[f], 1), "frame");
+        if (f < f0 || f >= f0 + nf) continue;
+        CHK(ctx, rc_array_copy(ctx, RC_A_LC, lc.data(), lc.size() * sizeof(float), 0), "cache");
+        int dormant = 0;
+        CHK(ctx, rc_scalar_get(ctx, RC_S_DORMANT, &dormant), "dormant");
+        float* s = sum.data() + (size_t)(f - f0) * np;
+        float* q = sq.data() + (size_t)(f - f0) * np;
+        for (size_t i = 0; i < np; ++i) {
+            float e = 0.f;   // est_of (poc_gpu.cu:427-431)
+            for (int l = 0; l < nl; ++l)
+                if (!((dormant >> l) & 1)) e += lc[(size_t)nl * i + l];
+            s[i] += e;
+            q[i] = std::fmaf(e, e, q[i]);
+        }
+    }
+    std::vector<float> errs(seq.size());
+    int n = 0;
+    CHK(ctx, rc_errors(ctx, errs.data(), (int)errs.size(), &n), "errors");
+    errs.resize((size_t)n);
+    return errs;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -156,7 +189,7 @@ int main(int argc, char** argv) {
     std::string mode = argv[1];
     if (const char* d = getenv("BENCH_DEBUG")) g_debug = atoi(d);
     if (const char* r = getenv("BENCH_RAYONS")) g_rays = std::max(0.25f, (float)atof(r));
-    if (mode == "prep" || mode == "taa" || mode == "recon") {
+    if (mode == "prep" || mode == "taa") {
         fprintf(stderr, "mode %s is not provided by this build\n", mode.c_str());
         return 1;
     }
@@ -348,6 +381,75 @@ int main(int argc, char** argv) {
             }
             fflush(stdout);
         }
+    } else if (mode == "recon") {
+        // poc_gpu.cu:1489-1547: per-seed curves, then bias^2 and variance of the estimate over
+        // frames 45..99 in three categories of points (relative change of the reference > 20 %,
+        // 5-20 %, < 5 %)
+        if (argc < 4) { fprintf(stderr, "usage : recon <scene.bin> <nseeds>\n"); return 1; }
+        int nseeds = atoi(argv[3]);
+        const int F0 = 45, NF = 55;
+        std::vector<Meth> M;
+        M.push_back({"Cache a dependances v3, suivi 1/4", mk(1, 64.f, 1.f, true, true, false, 4)});
+        { rc_method r = mk(0, 64.f, 1.52f); r.resp_mask = 1; r.nmax_resp = 8.f; r.rescale = 1; M.push_back({"SHaRC N=64 resp=8, 1.52x", r}); }
+        { rc_method r = mk(0, 32.f, 1.51f); r.rescale = 1; M.push_back({"Accumulation+parlampe N=32, 1.51x", r}); }
+        M.push_back({"Oracle", mk(1, 64.f, 1.f, false, false, true)});
+        const size_t Np = (size_t)si.np;
+        std::vector<float> hsum((size_t)NF * Np), hsq((size_t)NF * Np), lc(Np * (size_t)NL);
+        std::vector<float> rold(Np), rnew(Np);
+        std::vector<uint8_t> val(Np);
+        for (auto& m : M)
+            for (int e = 0; e < NS - 1; ++e) {
+                std::vector<int> seq(100, e);
+                for (int f = 50; f < 100; ++f) seq[f] = e + 1;
+                std::fill(hsum.begin(), hsum.end(), 0.f);
+                std::fill(hsq.begin(), hsq.end(), 0.f);
+                printf("{\"type\":\"recon_seeds\",\"name\":\"%s\",\"event\":%d,\"curves\":[", m.name.c_str(), e);
+                for (int sd = 0; sd < nseeds; ++sd) {
+                    auto er = run_recorded(ctx, m.m, seq, 1000 + sd, F0, NF, Np, NL, hsum, hsq, lc);
+                    printf("%s[", sd ? "," : "");
+                    for (size_t f = 0; f < er.size(); ++f) printf("%s%.5f", f ? "," : "", er[f]);
+                    printf("]");
+                }
+                printf("]}\n");
+                CHK(ctx, rc_state_array_copy(ctx, e, RC_SA_REF, rold.data(), Np * 4), "reference");
+                CHK(ctx, rc_state_array_copy(ctx, e + 1, RC_SA_REF, rnew.data(), Np * 4), "reference");
+                CHK(ctx, rc_state_array_copy(ctx, e + 1, RC_SA_VALID, val.data(), Np), "valid");
+                double mref = 0;
+                int nv = 0;
+                std::vector<int> cat(Np, -1);
+                for (size_t i = 0; i < Np; ++i)
+                    if (val[i]) {
+                        double rel = fabs(rnew[i] - rold[i]) / (rold[i] + 1e-2);
+                        cat[i] = rel > 0.2 ? 0 : (rel > 0.05 ? 1 : 2);
+                        mref += rnew[i];
+                        nv++;
+                    }
+                mref /= nv;
+                printf("{\"type\":\"recon_bv\",\"name\":\"%s\",\"event\":%d,\"f0\":%d,\"mref\":%.6f,\"cats\":[", m.name.c_str(), e, F0, mref);
+                for (int k = 0; k < 3; ++k) {
+                    int cnt = 0;
+                    for (size_t i = 0; i < Np; ++i) cnt += cat[i] == k;
+                    printf("%s{\"n\":%d,\"bias2\":[", k ? "," : "", cnt);
+                    std::vector<double> var(NF);
+                    for (int f = 0; f < NF; ++f) {
+                        double b2 = 0, v = 0;
+                        for (size_t i = 0; i < Np; ++i)
+                            if (cat[i] == k) {
+                                double mu = hsum[f * Np + i] / nseeds;
+                                double vv = hsq[f * Np + i] / nseeds - mu * mu;
+                                b2 += (mu - rnew[i]) * (mu - rnew[i]);
+                                v += vv > 0 ? vv : 0;
+                            }
+                        printf("%s%.6e", f ? "," : "", cnt ? b2 / cnt : 0.0);
+                        var[f] = cnt ? v / cnt : 0.0;
+                    }
+                    printf("],\"var\":[");
+                    for (int f = 0; f < NF; ++f) printf("%s%.6e", f ? "," : "", var[f]);
+                    printf("]}");
+                }
+                printf("]}\n");
+                fflush(stdout);
+            }
     } else {
         fprintf(stderr, "mode inconnu : %s\n", mode.c_str());
         rc_destroy(ctx);
