@@ -59,6 +59,7 @@ struct DevCache {
     float* coef;               // NR x KSNAP
     float* rstat;              // NR x 4
     float* dstat;              // NR x 3
+    float4* pre_hit;           // static-mesh scenes: hits traced ahead, PRE_K per point
     float* sumpr;              // 2 slots
     int* npend;                // [0] current, [1] accumulator
     double* err;               // 3 doubles per frame of the run
@@ -93,6 +94,8 @@ struct FrameParams {
     int decide;                // split update: run the verification decision first
     int brute, check;          // trace options
     float half_inv_np;         // 0.5f / Np, the float quotient the ray count uses
+    const float4* pre_hit;     // rays traced ahead by k_pretrace (pre_k per point), or null
+    int pre_k;
 };
 
 // Pinhole camera of the image pass: pixel (x, y) looks along
@@ -146,6 +149,9 @@ struct Ops {
     static cudaError_t preload(int NW);
     static cudaError_t probe(int NW, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                              const int* pts, int npts, void* recs, int maxrec, int* nrec, cudaStream_t st);
+    // the first p.pre_k rays of every point traced ahead of the frame kernel (static-mesh scenes)
+    static cudaError_t pretrace(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                                float4* out, cudaStream_t st);
 };
 // Light counts and mask widths with compiled kernels.
 #define RC_NL_VALUES(X) X(1) X(2) X(3) X(4) X(8) X(16) X(32)

@@ -607,8 +607,18 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
             for (int r = 0; r < k; ++r) {
                 const float u1 = rnd(rs);
                 const float u2 = rnd(rs);
-                const f3 D = cosine_dir(N, u1, u2);
-                const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+                Hit h;
+                if (p.pre_hit != nullptr && r < p.pre_k) {
+                    // traced ahead by k_pretrace: hit point, and the cache point (-1 = none: own)
+                    const float4 x = __ldcg(p.pre_hit + (size_t)i * p.pre_k + r);
+                    const int code = __float_as_int(x.w);
+                    h.H = mk(x.x, x.y, x.z);
+                    h.back = code < 0;
+                    h.pi = code < 0 ? i : code;
+                } else {
+                    const f3 D = cosine_dir(N, u1, u2);
+                    h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+                }
                 float val = 0.f;
                 if (!h.back) {
                     float4 ae[AES / 4], lc[LCS / 4];
@@ -783,6 +793,37 @@ __global__ void __launch_bounds__(BLOCK, RC_FRAME_MINB) k_frame(const DState s, 
                 }
             }
         }
+    }
+}
+
+// ------------------------------------------------------------------ traced ahead
+// Scenes with a static mesh spend nearly all of a frame in the tree traversal, which is
+// latency bound; it runs here as its own kernel with fewer registers per thread than the frame
+// kernel, so more warps hide the latency.  The rays are the frame kernel's (same seed, ray
+// count and directions); the first pre_k of each point are traced, and their hit points and
+// cache points written for the frame kernel to read.
+#ifndef RC_PRETRACE_MINB
+#define RC_PRETRACE_MINB 5
+#endif
+template <int NL>
+__global__ void __launch_bounds__(BLOCK, RC_PRETRACE_MINB) k_pretrace(const DState s, const DStatic g, const Grid grid,
+                                                                      const DevCache c, const FrameParams p, float4* __restrict__ out) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= p.Np) return;
+    uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
+    const bool pend = p.pend_left > 0 && c.pending[i];
+    const int k = min(ray_count(p, c, c.n[i], pend, c.sumpr[p.sum_in], c.npend[0], rs), p.pre_k);
+    const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
+    for (int r = 0; r < k; ++r) {
+        const float u1 = rnd(rs);
+        const float u2 = rnd(rs);
+        const f3 D = cosine_dir(N, u1, u2);
+        const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+        out[(size_t)i * p.pre_k + r] = make_float4(h.H.x, h.H.y, h.H.z, __int_as_float(h.back ? -1 : h.pi));
     }
 }
 
@@ -1140,6 +1181,16 @@ static cudaError_t prep_smem(K kern, size_t smem) {
     return cudaSuccess;
 }
 
+template <int NL>
+cudaError_t Ops<NL>::pretrace(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                              float4* out, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+    cudaError_t e = prep_smem(k_pretrace<NL>, smem);
+    if (e != cudaSuccess) return e;
+    k_pretrace<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, out);
+    return cudaGetLastError();
+}
+
 // Mask widths built for every light count (NW = voxels / 32 of the transit grid).
 #define RC_NW_LIST(X) X(4) X(24)
 
@@ -1277,6 +1328,7 @@ cudaError_t Ops<NL>::preload(int NW) {
 #undef X
     touch((const void*)k_update<NL>);
     touch((const void*)k_event<NL>);
+    touch((const void*)k_pretrace<NL>);
     touch((const void*)k_error<NL>);
     touch((const void*)k_proj_apply<NL>);
     touch((const void*)k_camera<NL>);

@@ -38,6 +38,7 @@ namespace {
 
 constexpr int VERIF_FRAMES = 4;   // poc_gpu.cu:115
 constexpr int PROJ_FRAMES = 4;    // poc_gpu.cu:424
+constexpr int PRE_K = 4;          // rays per point traced ahead on static-mesh scenes (more are traced inline)
 
 struct DevBuf {
     void* p = nullptr;
@@ -583,6 +584,8 @@ rc_status alloc_cache(rc_ctx* ctx) {
         (s = dalloc(ctx, pool, &c.ticket, 4)) || (s = dalloc(ctx, pool, &c.check, 2)) || (s = dalloc(ctx, pool, &c.rays, 1)) ||
         (s = dalloc(ctx, pool, &c.pracc, 1)) || (s = dalloc(ctx, pool, &c.npacc, 1)))
         return s;
+    c.pre_hit = nullptr;
+    if (S.g.has_bvh && (s = dalloc(ctx, pool, &c.pre_hit, (size_t)PRE_K * Np))) return s;
     CKR(cudaMemsetAsync(c.ticket, 0, 16, ctx->stream));
     CKR(cudaMemsetAsync(c.check, 0, 16, ctx->stream));
     CKR(cudaMemsetAsync(c.pracc, 0, 8, ctx->stream));
@@ -878,6 +881,13 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
     if (tm) CKR(cudaEventRecord(ctx->ev[1], st));
     const bool proj_apply_now = R.proj_left == 1;
     const bool fused = R.pend_left == 0 && R.proj_left == 0 && !M.ddgi;
+    if (ctx->c.pre_hit && !(ctx->cfg.flags & RC_FLAG_CHECK_TRACE)) {
+        // static-mesh scene: the traversal runs ahead in its own kernel
+        p.pre_hit = ctx->c.pre_hit;
+        p.pre_k = PRE_K;
+        CKR(RC_DISPATCH(S.NL, pretrace(d, S.g, S.grid, ctx->c, p, ctx->c.pre_hit, st)));
+        R.last_kernels += 1;
+    }
     if (fused) {
         CKR(RC_DISPATCH(S.NL, frame(ctx->NW, track, true, d, S.g, S.grid, ctx->c, p, st)));
         R.last_kernels += 1;
