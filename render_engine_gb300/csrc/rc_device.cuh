@@ -104,21 +104,42 @@ __device__ __forceinline__ void dda_walk(const Grid& g, f3 a, f3 b, uint32_t (&m
     float tmy = dy != 0 ? ((dy > 0 ? (iy + 1 - ay) : (ay - iy)) * tdy) : 1e30f;
     float tmz = dz != 0 ? ((dz > 0 ? (iz + 1 - az) : (az - iz)) * tdz) : 1e30f;
     const int steps = VX + VY + VZ;
+    // The voxel index v and the steps left before each axis leaves the grid are carried along
+    // instead of the three coordinates: the same voxels in the same order, and the same exits
+    // (at the end voxel, or when the chosen axis would step out of the grid).
+    int v = (iz * VY + iy) * VX + ix;
+    const int ve = (ez * VY + ey) * VX + ex;
+    int rx = stx > 0 ? VX - 1 - ix : ix, ry = sty > 0 ? VY - 1 - iy : iy, rz = stz > 0 ? VZ - 1 - iz : iz;
+    const int dvx = stx, dvy = sty * VX, dvz = stz * VX * VY;
+    unsigned long long lo = 0ull, hi = 0ull;   // the 128 mask bits while NW == 4
     for (int s = 0; s < steps; ++s) {
-        set_bit<NW>(m, (iz * VY + iy) * VX + ix);
-        if (ix == ex && iy == ey && iz == ez) break;
+        if (NW == 4) {
+            const unsigned long long bit = 1ull << (v & 63);
+            lo |= v < 64 ? bit : 0ull;
+            hi |= v < 64 ? 0ull : bit;
+        } else {
+            set_bit<NW>(m, v);
+        }
+        if (v == ve) break;
         // one axis steps per iteration, chosen like the reference's if / else-if chain; written
         // with selects so the lanes of a warp do not split three ways
         const bool sx = tmx < tmy && tmx < tmz;
         const bool sy = !sx && tmy < tmz;
-        const bool sz = !sx && !sy;
-        ix += sx ? stx : 0;
-        iy += sy ? sty : 0;
-        iz += sz ? stz : 0;
+        const int left = sx ? rx : (sy ? ry : rz);
+        if (left == 0) break;
+        rx -= sx ? 1 : 0;
+        ry -= sy ? 1 : 0;
+        rz -= (!sx && !sy) ? 1 : 0;
+        v += sx ? dvx : (sy ? dvy : dvz);
         tmx = sx ? tmx + tdx : tmx;
         tmy = sy ? tmy + tdy : tmy;
-        tmz = sz ? tmz + tdz : tmz;
-        if ((unsigned)ix >= (unsigned)VX || (unsigned)iy >= (unsigned)VY || (unsigned)iz >= (unsigned)VZ) break;
+        tmz = (!sx && !sy) ? tmz + tdz : tmz;
+    }
+    if (NW == 4) {
+        m[0] |= (uint32_t)lo;
+        m[1] |= (uint32_t)(lo >> 32);
+        m[2] |= (uint32_t)hi;
+        m[3 % NW] |= (uint32_t)(hi >> 32);
     }
 }
 
@@ -162,9 +183,9 @@ __device__ __forceinline__ void mt_tri(const float4* __restrict__ tri, int j, f3
 // grown by a margin far above the rounding error of the exact test, so the filter never drops
 // the triangle the exact scan would pick.  Each axis holds an even number of groups (a
 // padding group has c = NaN and no triangles), and after the 3 ng group records come the
-// pass-1 records of each pair (g, g + 1), g even, packed for paired FP32 arithmetic:
-// (c_g, c_g+1, -centre_a_g, -centre_a_g+1) (half_a_g, half_a_g+1, -centre_b_g, -centre_b_g+1)
-// (half_b_g, half_b_g+1, 0, 0).
+// pass-1 records of each pair (g, g + 1), g even, packed for paired FP32 arithmetic and
+// negated: (-c_g, -c_g+1, -centre_a_g, -centre_a_g+1) (-half_a_g, -half_a_g+1, -centre_b_g,
+// -centre_b_g+1) (-half_b_g, -half_b_g+1, 0, 0).
 struct GroupRanges { int g0[4]; };  // groups of axis 0 in [g0[0], g0[1]), axis 1 [g0[1], g0[2]), axis 2 [g0[2], g0[3])
 
 }  // namespace rc

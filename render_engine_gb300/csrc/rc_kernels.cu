@@ -209,32 +209,42 @@ struct TraceSmem {
 
 // Plane filter of two groups of one axis k at once, in paired FP32 arithmetic: the ray's
 // crossing of group g's plane (t = (c - o_k) / d_k) is a candidate when it lies ahead of the
-// origin and inside the group's outer box, stored as centre and half extent so each in-plane
-// test is one addition and one |x| <= h comparison.  The candidate bits are shifted in
+// origin and inside the group's outer box, stored as centre and half extent.  The candidate
+// bits are shifted in
 // (mask = mask << 2 | hit_g << 1 | hit_g+1), so group g ends at bit ng - 1 - g.  The filter
 // only has to be conservative (the box margin and the stopping slack of pass 2 are orders of
 // magnitude above its rounding), so 1 / d_k is the approximate reciprocal.
+//
+// The three tests are read off sign bits: 5e-5 - t, |x_a - c_a| - h_a and |x_b - c_b| - h_b are
+// all negative exactly when the crossing is a candidate, except on the grown box's boundary
+// itself (a zero difference), which lies a full margin away from the group's triangles.
+__device__ __forceinline__ float2 abs2(float2 v) { return make_float2(fabsf(v.x), fabsf(v.y)); }
+
 template <typename MaskT>
-__device__ __forceinline__ void filter_pair(const float4* __restrict__ gp, int pp, float2 nok, float2 idk, float2 oa, float2 da,
-                                            float2 ob, float2 db, MaskT& mask) {
+__device__ __forceinline__ void filter_pair(const float4* __restrict__ gp, int pp, float2 ok, float2 idk, float2 oa, float2 nda,
+                                            float2 ob, float2 ndb, MaskT& mask) {
+    // records hold -c, -centre_a, -half_a, -centre_b, -half_b; nt = (o_k - c) / d_k = -t
     const float4 P0 = gp[3 * pp], P1 = gp[3 * pp + 1];
     const float2 P2 = *reinterpret_cast<const float2*>(gp + 3 * pp + 2);
-    const float2 tk = __fmul2_rn(__fadd2_rn(make_float2(P0.x, P0.y), nok), idk);
-    const float2 ea = __fadd2_rn(__ffma2_rn(tk, da, oa), make_float2(P0.z, P0.w));
-    const float2 eb = __fadd2_rn(__ffma2_rn(tk, db, ob), make_float2(P1.z, P1.w));
-    const bool in0 = tk.x > 5e-5f && fabsf(ea.x) <= P1.x && fabsf(eb.x) <= P2.x;
-    const bool in1 = tk.y > 5e-5f && fabsf(ea.y) <= P1.y && fabsf(eb.y) <= P2.y;
-    mask = (mask << 2) | ((MaskT)in0 << 1) | (MaskT)in1;
+    const float2 nt = __fmul2_rn(__fadd2_rn(ok, make_float2(P0.x, P0.y)), idk);
+    const float2 ea = __fadd2_rn(__ffma2_rn(nt, nda, oa), make_float2(P0.z, P0.w));
+    const float2 eb = __fadd2_rn(__ffma2_rn(nt, ndb, ob), make_float2(P1.z, P1.w));
+    const float2 ga = __fadd2_rn(abs2(ea), make_float2(P1.x, P1.y));
+    const float2 gb = __fadd2_rn(abs2(eb), P2);
+    const float2 gt = __fadd2_rn(nt, make_float2(5e-5f, 5e-5f));
+    const unsigned s0 = __float_as_uint(ga.x) & __float_as_uint(gb.x) & __float_as_uint(gt.x);
+    const unsigned s1 = __float_as_uint(ga.y) & __float_as_uint(gb.y) & __float_as_uint(gt.y);
+    mask = (mask << 2) | (MaskT)((s0 >> 30) & 2u) | (MaskT)(s1 >> 31);
 }
 
 // Pass 1 over the groups [a, b) of one axis (a, b even).
 template <typename MaskT>
 __device__ __forceinline__ void filter_axis(const float4* __restrict__ gp, int a, int b, float ok, float idk, float oa, float da,
                                             float ob, float db, MaskT& mask) {
-    const float2 nok2 = make_float2(-ok, -ok), idk2 = make_float2(idk, idk);
-    const float2 oa2 = make_float2(oa, oa), da2 = make_float2(da, da), ob2 = make_float2(ob, ob), db2 = make_float2(db, db);
+    const float2 ok2 = make_float2(ok, ok), idk2 = make_float2(idk, idk);
+    const float2 oa2 = make_float2(oa, oa), nda2 = make_float2(-da, -da), ob2 = make_float2(ob, ob), ndb2 = make_float2(-db, -db);
 #pragma unroll 2
-    for (int pp = a >> 1; pp < (b >> 1); ++pp) filter_pair(gp, pp, nok2, idk2, oa2, da2, ob2, db2, mask);
+    for (int pp = a >> 1; pp < (b >> 1); ++pp) filter_pair(gp, pp, ok2, idk2, oa2, nda2, ob2, ndb2, mask);
 }
 
 template <typename MaskT>

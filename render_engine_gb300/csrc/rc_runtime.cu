@@ -370,9 +370,9 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
     }
     for (size_t x = 0; x + 1 < gs.size(); x += 2) {
         const float4 a0 = out.grp[3 * x], a1 = out.grp[3 * x + 1], b0 = out.grp[3 * x + 3], b1 = out.grp[3 * x + 4];
-        out.grp.push_back(make_float4(a0.x, b0.x, -a0.y, -b0.y));
-        out.grp.push_back(make_float4(a0.z, b0.z, -a0.w, -b0.w));
-        out.grp.push_back(make_float4(a1.x, b1.x, 0.f, 0.f));
+        out.grp.push_back(make_float4(-a0.x, -b0.x, -a0.y, -b0.y));
+        out.grp.push_back(make_float4(-a0.z, -b0.z, -a0.w, -b0.w));
+        out.grp.push_back(make_float4(-a1.x, -b1.x, 0.f, 0.f));
     }
     std::sort(misc.begin(), misc.end());
     out.misc = misc;
