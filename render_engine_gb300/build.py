@@ -35,7 +35,7 @@ def nvcc() -> str:
 
 def _sources() -> list[str]:
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h", ".cpp"))] + \
-        [os.path.join(ROOT, "include", "rc_api.h"), os.path.join(ROOT, "include", "rc_hashgrid.h")]
+        [os.path.join(ROOT, "include", h) for h in ("rc_api.h", "rc_hashgrid.h", "rc_mlp.h")]
 
 
 def _stale(target: str, deps: list[str]) -> bool:
@@ -63,7 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, deps):
             jobs.append([nv, *ARCH, *FLAGS, "-DRC_NL_ONE=%d" % nl, "-c", os.path.join(CSRC, "rc_kernels.cu"), "-o", o])
-    for name in ("rc_runtime", "rc_noalloc", "rc_hashgrid"):
+    for name in ("rc_runtime", "rc_noalloc", "rc_hashgrid", "rc_mlp"):
         o = os.path.join(OUT, name + ".o")
         objs.append(o)
         if force or _stale(o, deps):

@@ -42,9 +42,10 @@ def test_library_exports_every_declared_symbol(lib, header):
 
 
 def test_python_binding_lists_every_symbol():
-    from render_engine_gb300 import hashgrid, native
+    from render_engine_gb300 import hashgrid, mlp, native
     assert sorted(native.EXPORTS) == declared_functions("rc_api.h")
     assert sorted(hashgrid.EXPORTS) == declared_functions("rc_hashgrid.h")
+    assert sorted(mlp.EXPORTS) == declared_functions("rc_mlp.h")
 
 
 def test_status_strings_and_version(lib):
