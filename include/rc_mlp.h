@@ -25,6 +25,49 @@ extern "C" {
 rc_status rc_mlp_tile_product(const uint16_t* d_a, const uint16_t* d_b, float* d_d, int K, int N, unsigned* d_err,
                               void* stream);
 
+/* The network: 168 input features -> 64 -> 64 -> 64 -> 64 -> n_out (<= 16), ReLU between
+ * layers, no biases, bf16 weights and activations, FP32 accumulation, Adam (beta 0.9 / 0.99).
+ * Inputs per point (float4 each): position (xyz), normal (xyz), and (albedo, direct light of
+ * lights 0, 1, 2); the features are frequency and one-blob encodings of the position in the
+ * box and of the normal, plus the raw values. */
+typedef struct rc_mlp rc_mlp;
+
+typedef struct {
+    float box_lo[3], box_hi[3]; /* encoding box of the positions */
+    int n_out;                  /* outputs, 1..16 */
+    float lr;                   /* Adam learning rate */
+    uint32_t seed;              /* initial weights */
+    int max_batch;              /* largest training batch (samples) */
+    int device;
+    void* stream;               /* cudaStream_t, NULL = a stream of the network */
+} rc_mlp_config;
+
+rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out);
+void rc_mlp_destroy(rc_mlp* m);
+const char* rc_mlp_last_error(const rc_mlp* m);
+
+/* One training step on n samples (a multiple of 128, at most max_batch): sample s is point
+ * d_idx[s] (or s when d_idx is NULL) of d_pos4 / d_nrm4 / d_aux4, its target the first n_out
+ * of the tstride floats at d_target + s * tstride.  Loss: relative L2,
+ * (y - t)^2 / (y^2 + 0.01) averaged over samples and outputs; its sum is added to *d_loss
+ * (when not NULL).  Gradients are summed over the batch in a fixed order. */
+rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, const float* d_target, int tstride,
+                       const int* d_idx, int n, float* d_loss);
+
+/* The network's n_out outputs for n points into d_out (ostride floats per point). */
+rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, int n, float* d_out, int ostride);
+
+/* FP32 master weights, 24,576 floats: per layer [out][in] row-major (176, 64, 64, 64, 64
+ * inputs; 64, 64, 64, 64, 16 outputs); to_device = 1 sets them (and their bf16 copies).
+ * Synchronises the stream. */
+rc_status rc_mlp_weights(rc_mlp* m, float* host, size_t n, int to_device);
+
+/* The summed gradient of the last training step, same layout.  Synchronises the stream. */
+rc_status rc_mlp_gradients(rc_mlp* m, float* host, size_t n);
+
+/* Bit 0: a completion wait gave up.  Synchronises the stream. */
+rc_status rc_mlp_error_flags(rc_mlp* m, unsigned* flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,7 +8,11 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
+#include <string>
+#include <vector>
 
 #include "../../include/rc_mlp.h"
 #include "rc_umma.cuh"
@@ -72,6 +76,366 @@ __global__ void __launch_bounds__(128) k_tile_product(const uint16_t* __restrict
     if (warp == 0) tmem_dealloc(tmem, ncols);
 }
 
+
+// ---------------------------------------------------------------- the network
+// 168 input features (padded to 176) -> 64 -> 64 -> 64 -> 64 -> 16 outputs (the first n_out
+// used), ReLU between layers, no biases.  Weights live as FP32 masters with their Adam
+// moments, and as bf16 tiles in the K-major core-matrix layout the MMAs read: W_l (rows =
+// outputs, K = inputs) for the forward products and W_l^T (rows = inputs, K = outputs) for
+// the gradients that flow back.
+constexpr int K0 = 176, HID = 64, OUTP = 16, NLAYER = 5;
+__host__ __device__ constexpr int in_dim(int l) { return l == 0 ? K0 : HID; }
+__host__ __device__ constexpr int out_dim(int l) { return l == NLAYER - 1 ? OUTP : HID; }
+__host__ __device__ constexpr int master_off(int l) { return l == 0 ? 0 : HID * K0 + (l - 1) * HID * HID; }
+constexpr int NWEIGHT = HID * K0 + 3 * HID * HID + OUTP * HID;   // 24,576
+// bf16 tile byte offsets: forward tiles, then the transposed ones of layers 1..4
+__host__ __device__ constexpr int wf_off(int l) { return 2 * master_off(l); }
+constexpr int WF_BYTES = 2 * NWEIGHT;                                 // 49,152
+__host__ __device__ constexpr int wb_off(int l) { return WF_BYTES + 2 * (master_off(l) - master_off(1)); }
+constexpr int WB_BYTES = 2 * (3 * HID * HID + OUTP * HID);            // 26,624
+// activation tiles of one 128-sample tile kept for the backward pass (training)
+constexpr int ACT_X0T = 0;                                            // X0^T: 176 x 128
+__host__ __device__ constexpr int act_ht(int l) { return K0 * 128 * 2 + (l - 1) * HID * 128 * 2; }   // H_l^T, l = 1..4
+constexpr int ACT_DY = K0 * 128 * 2 + 4 * HID * 128 * 2;              // dY: 128 x 16 (K-major)
+constexpr int ACT_DYT = ACT_DY + 128 * OUTP * 2;                      // dY^T: 16 x 128
+constexpr int ACT_BYTES = ACT_DYT + OUTP * 128 * 2;                   // 122,880 per tile
+
+struct MlpArgs {
+    const uint8_t* wbf;        // bf16 tiles (forward, then transposed)
+    const float4* P;           // point position (xyz)
+    const float4* N;           // point normal (xyz)
+    const float4* aux;         // albedo, direct light of lights 0..2
+    const float* target;       // training targets, tstride floats per sample
+    int tstride;
+    const int* idx;            // sample -> point (null: identity)
+    int n;                     // samples (a multiple of 128 when training)
+    float* out;                // inference output, ostride floats per sample
+    int ostride;
+    int n_out;
+    float lo[3], inv_ext[3];   // encoding box
+    uint8_t* act;              // training: activation tiles, ACT_BYTES per tile
+    float* dwpart;             // training: per-tile weight gradients, NWEIGHT per tile
+    float* loss;               // training: sum of the relative L2 loss (for reporting)
+    float loss_scale;          // 1 / (samples x n_out)
+    unsigned* err;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ float bf16_at(const uint8_t* base, uint32_t off) {
+    return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(base + off));
+}
+__device__ __forceinline__ void st_bf16(uint8_t* base, uint32_t off, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
+}
+
+// The 168 input features of one point (the rest of the 176 are zero): frequency encodings of
+// the position in the box (12 octaves) and of the normal (4 octaves), one-blob encodings of
+// both (16 and 4 bins per axis), the raw position, normal, direct light of three lights,
+// albedo and a constant.
+__device__ void encode(const MlpArgs& a, int pt, float (&f)[K0]) {
+    const float4 P = a.P[pt], Nn = a.N[pt], X = a.aux[pt];
+    const float p[3] = {fminf(fmaxf((P.x - a.lo[0]) * a.inv_ext[0], 0.f), 1.f), fminf(fmaxf((P.y - a.lo[1]) * a.inv_ext[1], 0.f), 1.f),
+                        fminf(fmaxf((P.z - a.lo[2]) * a.inv_ext[2], 0.f), 1.f)};
+    const float nv[3] = {Nn.x, Nn.y, Nn.z};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        float w = 3.14159265f * p[ax];
+#pragma unroll
+        for (int o = 0; o < 12; ++o, w *= 2.f) {
+            float sn, cs;
+            sincosf(w, &sn, &cs);
+            f[ax * 24 + o * 2] = sn;
+            f[ax * 24 + o * 2 + 1] = cs;
+        }
+        float u = 3.14159265f * nv[ax];
+#pragma unroll
+        for (int o = 0; o < 4; ++o, u *= 2.f) {
+            float sn, cs;
+            sincosf(u, &sn, &cs);
+            f[72 + ax * 8 + o * 2] = sn;
+            f[72 + ax * 8 + o * 2 + 1] = cs;
+        }
+        const float bp = p[ax] * 16.f, bn = (nv[ax] * 0.5f + 0.5f) * 4.f;
+#pragma unroll
+        for (int b = 0; b < 16; ++b) f[96 + ax * 16 + b] = fmaxf(0.f, 1.f - fabsf(bp - (b + 0.5f)));
+#pragma unroll
+        for (int b = 0; b < 4; ++b) f[144 + ax * 4 + b] = fmaxf(0.f, 1.f - fabsf(bn - (b + 0.5f)));
+        f[156 + ax] = p[ax];
+        f[159 + ax] = nv[ax];
+    }
+    f[162] = X.y;
+    f[163] = X.z;
+    f[164] = X.w;
+    f[165] = X.x;
+    f[166] = 1.f;
+#pragma unroll
+    for (int k = 167; k < K0; ++k) f[k] = 0.f;
+}
+
+// Forward pass over tiles of 128 samples (persistent CTAs of 128 threads, thread = sample row).
+// TRAIN: also keeps X0^T, H_l^T and dY (with dY^T) of each tile in global memory and adds the
+// loss; otherwise writes the n_out outputs.
+template <bool TRAIN>
+__global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sw = smem;                               // forward weight tiles, WF_BYTES
+    uint8_t* sx = smem + WF_BYTES;                    // X0, 128 x 176 (K-major)
+    uint8_t* sh0 = sx + 128 * K0 * 2;                 // H ping-pong, 128 x 64 each
+    uint8_t* sh1 = sh0 + 128 * HID * 2;
+    uint8_t* st = sh1 + 128 * HID * 2;                // TRAIN: transposed staging, 176 x 128
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < WF_BYTES / 16; i += 128) reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(a.wbf)[i];
+    if (tid == 0) mbar_init(&mbar, 1);
+    if (warp == 0) tmem_alloc(&tmem_base, 64);
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    uint32_t phase = 0;
+    bool ok = true;
+    const int ntiles = (a.n + 127) / 128;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int s = tile * 128 + tid;
+        const bool live = s < a.n;
+        const int pt = live ? (a.idx ? a.idx[s] : s) : 0;
+        {
+            float f[K0];
+            encode(a, pt, f);
+#pragma unroll
+            for (int k8 = 0; k8 < K0 / 8; ++k8) {
+                uint4 v;
+                v.x = pack_bf16(f[8 * k8], f[8 * k8 + 1]);
+                v.y = pack_bf16(f[8 * k8 + 2], f[8 * k8 + 3]);
+                v.z = pack_bf16(f[8 * k8 + 4], f[8 * k8 + 5]);
+                v.w = pack_bf16(f[8 * k8 + 6], f[8 * k8 + 7]);
+                *reinterpret_cast<uint4*>(sx + kmajor_offset(tid, 8 * k8, K0)) = v;
+                if (TRAIN)
+                    for (int j = 0; j < 8; ++j) st_bf16(st, kmajor_offset(8 * k8 + j, tid, 128), f[8 * k8 + j]);
+            }
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (TRAIN) {
+            uint4* dst = reinterpret_cast<uint4*>(a.act + (size_t)tile * ACT_BYTES + ACT_X0T);
+            for (int i = tid; i < K0 * 128 * 2 / 16; i += 128) dst[i] = reinterpret_cast<const uint4*>(st)[i];
+            __syncthreads();
+        }
+        for (int l = 0; l < NLAYER && ok; ++l) {
+            const int K = in_dim(l), N = out_dim(l);
+            uint8_t* A = l == 0 ? sx : ((l & 1) ? sh0 : sh1);   // H_l is in sh0 for odd l
+            uint8_t* Hn = (l & 1) ? sh1 : sh0;                  // H_{l+1}
+            if (tid == 0) {
+                const uint32_t a0 = smem_u32(A), b0 = smem_u32(sw + wf_off(l));
+                for (int kk = 0; kk < K / 16; ++kk)
+                    mma_bf16(tmem, smem_desc(a0 + 256u * kk, 128u, 16u * K), smem_desc(b0 + 256u * kk, 128u, 16u * K),
+                             idesc_bf16_f32(128, N), kk > 0);
+                mma_commit(&mbar);
+            }
+            ok = mbar_wait(&mbar, phase, WAIT_LIMIT);
+            phase ^= 1u;
+            ok = __syncthreads_and(ok);   // the whole block leaves together
+            if (!ok) {
+                if (tid == 0) atomicOr(a.err, 1u);
+                break;
+            }
+            fence_after_sync();
+            for (int c = 0; c < N; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+                tmem_wait_ld();
+                if (l < NLAYER - 1) {
+                    uint4 lo4, hi4;
+                    lo4.x = pack_bf16(fmaxf(v[0], 0.f), fmaxf(v[1], 0.f));
+                    lo4.y = pack_bf16(fmaxf(v[2], 0.f), fmaxf(v[3], 0.f));
+                    lo4.z = pack_bf16(fmaxf(v[4], 0.f), fmaxf(v[5], 0.f));
+                    lo4.w = pack_bf16(fmaxf(v[6], 0.f), fmaxf(v[7], 0.f));
+                    hi4.x = pack_bf16(fmaxf(v[8], 0.f), fmaxf(v[9], 0.f));
+                    hi4.y = pack_bf16(fmaxf(v[10], 0.f), fmaxf(v[11], 0.f));
+                    hi4.z = pack_bf16(fmaxf(v[12], 0.f), fmaxf(v[13], 0.f));
+                    hi4.w = pack_bf16(fmaxf(v[14], 0.f), fmaxf(v[15], 0.f));
+                    *reinterpret_cast<uint4*>(Hn + kmajor_offset(tid, c, HID)) = lo4;
+                    *reinterpret_cast<uint4*>(Hn + kmajor_offset(tid, c + 8, HID)) = hi4;
+                    if (TRAIN)
+                        for (int j = 0; j < 16; ++j) st_bf16(st, kmajor_offset(c + j, tid, 128), fmaxf(v[j], 0.f));
+                } else if (!TRAIN) {
+                    if (live)
+                        for (int j = 0; j < a.n_out; ++j) a.out[(size_t)s * a.ostride + j] = v[j];
+                } else {
+                    // relative L2 loss (y - t)^2 / (sg(y)^2 + 0.01) and its gradient
+                    float lsum = 0.f;
+                    uint8_t* dy = a.act + (size_t)tile * ACT_BYTES + ACT_DY;
+                    uint8_t* dyt = a.act + (size_t)tile * ACT_BYTES + ACT_DYT;
+                    for (int j = 0; j < OUTP; ++j) {
+                        float g = 0.f;
+                        if (live && j < a.n_out) {
+                            const float t = a.target[(size_t)s * a.tstride + j];
+                            const float d = v[j] - t, den = v[j] * v[j] + 0.01f;
+                            lsum += d * d / den;
+                            g = 2.f * d / den * a.loss_scale;
+                        }
+                        st_bf16(dy, kmajor_offset(tid, j, OUTP), g);
+                        st_bf16(dyt, kmajor_offset(j, tid, 128), g);
+                    }
+                    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+                    if (lane == 0 && lsum != 0.f) atomicAdd(a.loss, lsum);
+                }
+            }
+            fence_before_sync();
+            fence_proxy_async();
+            __syncthreads();
+            if (TRAIN && l < NLAYER - 1) {
+                uint4* dst = reinterpret_cast<uint4*>(a.act + (size_t)tile * ACT_BYTES + act_ht(l + 1));
+                for (int i = tid; i < HID * 128 * 2 / 16; i += 128) dst[i] = reinterpret_cast<const uint4*>(st)[i];
+                __syncthreads();
+            }
+            fence_after_sync();
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
+// Backward pass of one tile (128 threads): for l = 4 .. 0, dW_l = dZ_l^T A_l over the tile's
+// samples (rows of dZ^T beyond the layer's outputs are zero) and, for l >= 1,
+// dZ_{l-1} = (dZ_l W_l) masked by ReLU'(H_l).  Tensor memory: dW in columns 0..175, dA in
+// 192..255.  Weight gradients go to this tile's slot of dwpart.
+__global__ void __launch_bounds__(128) k_mlp_backward(const MlpArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sat = smem;                              // A_l^T, in_l x 128
+    uint8_t* sdz = sat + K0 * 128 * 2;                // dZ, 128 x out_l (K-major)
+    uint8_t* sdzt = sdz + 128 * HID * 2;              // dZ^T, 128 x 128 (rows >= out_l zero)
+    uint8_t* swt = sdzt + 128 * 128 * 2;              // W_l^T, in_l x out_l
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tile = blockIdx.x;
+    const uint8_t* act = a.act + (size_t)tile * ACT_BYTES;
+    for (int i = tid; i < 128 * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sdzt)[i] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    for (int i = tid; i < 128 * OUTP * 2 / 16; i += 128) reinterpret_cast<uint4*>(sdz)[i] = reinterpret_cast<const uint4*>(act + ACT_DY)[i];
+    for (int i = tid; i < OUTP * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sdzt)[i] = reinterpret_cast<const uint4*>(act + ACT_DYT)[i];
+    if (tid == 0) mbar_init(&mbar, 1);
+    if (warp == 0) tmem_alloc(&tmem_base, 256);
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    uint32_t phase = 0;
+    float* dw = a.dwpart + (size_t)tile * NWEIGHT;
+    for (int l = NLAYER - 1; l >= 0; --l) {
+        const int Kin = in_dim(l), Nout = out_dim(l);
+        const uint4* src = reinterpret_cast<const uint4*>(act + (l == 0 ? ACT_X0T : act_ht(l)));
+        for (int i = tid; i < Kin * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sat)[i] = src[i];
+        if (l >= 1) {
+            const uint4* w = reinterpret_cast<const uint4*>(a.wbf + wb_off(l));
+            for (int i = tid; i < Kin * Nout * 2 / 16; i += 128) reinterpret_cast<uint4*>(swt)[i] = w[i];
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t zt = smem_u32(sdzt), at = smem_u32(sat);
+            for (int kk = 0; kk < 8; ++kk)
+                mma_bf16(tmem, smem_desc(zt + 256u * kk, 128u, 16u * 128), smem_desc(at + 256u * kk, 128u, 16u * 128),
+                         idesc_bf16_f32(128, Kin), kk > 0);
+            if (l >= 1) {
+                const uint32_t z = smem_u32(sdz), w = smem_u32(swt);
+                for (int kk = 0; kk < Nout / 16; ++kk)
+                    mma_bf16(tmem + 192u, smem_desc(z + 256u * kk, 128u, 16u * Nout), smem_desc(w + 256u * kk, 128u, 16u * Nout),
+                             idesc_bf16_f32(128, HID), kk > 0);
+            }
+            mma_commit(&mbar);
+        }
+        const bool ok = __syncthreads_and(mbar_wait(&mbar, phase, WAIT_LIMIT));
+        phase ^= 1u;
+        if (!ok) {
+            if (tid == 0) atomicOr(a.err, 1u);
+            break;
+        }
+        fence_after_sync();
+        // dW_l: rows = outputs (warps 0 and 1 hold rows 0..63)
+        if (warp < 2) {
+            const int row = warp * 32 + lane;
+            for (int c = 0; c < Kin; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+                tmem_wait_ld();
+                if (row < Nout)
+                    for (int j = 0; j < 16; ++j) dw[master_off(l) + row * Kin + c + j] = v[j];
+            }
+        }
+        if (l >= 1) {
+            // dZ_{l-1} = (dZ_l W_l) * [H_l > 0], row = sample
+            const int m = tid;
+            for (int c = 0; c < HID; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 192u + (uint32_t)c, v);
+                tmem_wait_ld();
+                for (int j = 0; j < 16; ++j) {
+                    const int k = c + j;
+                    const float h = bf16_at(sat, kmajor_offset(k, m, 128));
+                    v[j] = h > 0.f ? v[j] : 0.f;
+                }
+                for (int j = 0; j < 16; ++j) {
+                    st_bf16(sdz, kmajor_offset(m, c + j, HID), v[j]);
+                    st_bf16(sdzt, kmajor_offset(c + j, m, 128), v[j]);
+                }
+            }
+        }
+        fence_before_sync();
+        fence_proxy_async();
+        __syncthreads();
+        fence_after_sync();
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 256);
+}
+
+// Master weights (FP32, [out][in] per layer) -> bf16 tiles: W_l (rows out, K in) and, for
+// layers 1..4, W_l^T (rows in, K out).
+__global__ void k_mlp_pack(const float* __restrict__ w, uint8_t* __restrict__ wbf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NWEIGHT) return;
+    int l = 0;
+    while (l + 1 < NLAYER && i >= master_off(l + 1)) ++l;
+    const int K = in_dim(l), r = (i - master_off(l)) / K, k = (i - master_off(l)) % K;
+    const float v = w[i];
+    st_bf16(wbf + wf_off(l), kmajor_offset(r, k, K), v);
+    if (l >= 1) st_bf16(wbf + wb_off(l), kmajor_offset(k, r, out_dim(l)), v);
+}
+
+// Gradient of each weight = the tile gradients added in tile order (reproducible), then one
+// Adam step on the FP32 master weight, and its bf16 copies.
+__global__ void k_mlp_adam(const float* __restrict__ part, int ntiles, float* __restrict__ w, float* __restrict__ m1,
+                           float* __restrict__ m2, float* __restrict__ grad, uint8_t* __restrict__ wbf, float lr, float b1, float b2,
+                           float eps, float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NWEIGHT) return;
+    float g = 0.f;
+    for (int t = 0; t < ntiles; ++t) g += part[(size_t)t * NWEIGHT + i];
+    grad[i] = g;
+    const float m = b1 * m1[i] + (1.f - b1) * g;
+    const float v = b2 * m2[i] + (1.f - b2) * g * g;
+    m1[i] = m;
+    m2[i] = v;
+    const float x = w[i] - lr * (m * c1) / (sqrtf(v * c2) + eps);
+    w[i] = x;
+    int l = 0;
+    while (l + 1 < NLAYER && i >= master_off(l + 1)) ++l;
+    const int K = in_dim(l), r = (i - master_off(l)) / K, k = (i - master_off(l)) % K;
+    st_bf16(wbf + wf_off(l), kmajor_offset(r, k, K), x);
+    if (l >= 1) st_bf16(wbf + wb_off(l), kmajor_offset(k, r, out_dim(l)), x);
+}
+
+constexpr size_t FWD_SMEM_INFER = (size_t)WF_BYTES + 128 * K0 * 2 + 2 * 128 * HID * 2;
+constexpr size_t FWD_SMEM_TRAIN = FWD_SMEM_INFER + (size_t)K0 * 128 * 2;
+constexpr size_t BWD_SMEM = (size_t)K0 * 128 * 2 + 128 * HID * 2 + 128 * 128 * 2 + HID * HID * 2;
 }  // namespace
 
 extern "C" rc_status rc_mlp_tile_product(const uint16_t* d_a, const uint16_t* d_b, float* d_d, int K, int N, unsigned* d_err,
@@ -85,3 +449,179 @@ extern "C" rc_status rc_mlp_tile_product(const uint16_t* d_a, const uint16_t* d_
     k_tile_product<<<1, 128, smem, st>>>(d_a, d_b, d_d, K, N, d_err);
     return cudaGetLastError() == cudaSuccess ? RC_OK : RC_ERR_CUDA;
 }
+
+// ---------------------------------------------------------------- C ABI of the network
+struct rc_mlp {
+    rc_mlp_config cfg{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    float *w = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *part = nullptr, *loss = nullptr;
+    uint8_t *wbf = nullptr, *act = nullptr;
+    unsigned* err = nullptr;
+    int cap_tiles = 0, sms = 0;
+    long long step = 0;
+    std::string msg;
+};
+
+namespace {
+
+rc_status mfail(rc_mlp* m, rc_status s, const char* what) {
+    if (m) m->msg = what;
+    return s;
+}
+
+MlpArgs args_of(const rc_mlp* m) {
+    MlpArgs a{};
+    a.wbf = m->wbf;
+    a.n_out = m->cfg.n_out;
+    for (int k = 0; k < 3; ++k) {
+        a.lo[k] = m->cfg.box_lo[k];
+        a.inv_ext[k] = 1.f / (m->cfg.box_hi[k] - m->cfg.box_lo[k]);
+    }
+    a.err = m->err;
+    return a;
+}
+
+// A small counter-based generator for the initial weights (splitmix64).
+uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+}  // namespace
+
+extern "C" {
+
+rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out) {
+    if (!cfg || !out) return RC_ERR_ARG;
+    *out = nullptr;
+    if (cfg->n_out < 1 || cfg->n_out > OUTP || cfg->max_batch < 128 || !(cfg->lr >= 0.f)) return RC_ERR_ARG;
+    for (int k = 0; k < 3; ++k)
+        if (!(cfg->box_hi[k] > cfg->box_lo[k])) return RC_ERR_ARG;
+    rc_mlp* m = new rc_mlp();
+    m->cfg = *cfg;
+    auto bad = [&](rc_status s) { rc_mlp_destroy(m); return s; };
+    if (cudaSetDevice(cfg->device) != cudaSuccess) return bad(RC_ERR_CUDA);
+    if (cfg->stream) m->stream = (cudaStream_t)cfg->stream;
+    else {
+        if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return bad(RC_ERR_CUDA);
+        m->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, cfg->device);
+    m->cap_tiles = (cfg->max_batch + 127) / 128;
+    if (cudaMalloc(&m->w, 4 * NWEIGHT) || cudaMalloc(&m->m1, 4 * NWEIGHT) || cudaMalloc(&m->m2, 4 * NWEIGHT) ||
+        cudaMalloc(&m->grad, 4 * NWEIGHT) || cudaMalloc(&m->wbf, WF_BYTES + WB_BYTES) || cudaMalloc(&m->err, 4) ||
+        cudaMalloc(&m->loss, 4) || cudaMalloc(&m->part, (size_t)4 * NWEIGHT * m->cap_tiles) ||
+        cudaMalloc(&m->act, (size_t)ACT_BYTES * m->cap_tiles))
+        return bad(RC_ERR_NOMEM);
+    // He-uniform initial weights, seeded
+    std::vector<float> w(NWEIGHT);
+    uint64_t st = 0x5EEDull ^ (uint64_t)cfg->seed * 0x100000001B3ull;
+    for (int l = 0; l < NLAYER; ++l) {
+        const float lim = sqrtf(6.f / (float)(l == 0 ? 168 : HID));
+        for (int i = master_off(l); i < master_off(l) + out_dim(l) * in_dim(l); ++i) {
+            const double u = (double)(splitmix(st) >> 11) * (1.0 / 9007199254740992.0);
+            w[i] = (float)((2.0 * u - 1.0) * lim);
+        }
+        if (l == NLAYER - 1)   // unused outputs start (and stay, their gradient is zero) at zero
+            for (int r = cfg->n_out; r < OUTP; ++r)
+                for (int k = 0; k < HID; ++k) w[master_off(l) + r * HID + k] = 0.f;
+    }
+    rc_status s = rc_mlp_weights(m, w.data(), w.size(), 1);
+    if (s != RC_OK) return bad(s);
+    if (cudaMemsetAsync(m->m1, 0, 4 * NWEIGHT, m->stream) || cudaMemsetAsync(m->m2, 0, 4 * NWEIGHT, m->stream) ||
+        cudaMemsetAsync(m->err, 0, 4, m->stream) || cudaStreamSynchronize(m->stream))
+        return bad(RC_ERR_CUDA);
+    if (cudaFuncSetAttribute(k_mlp_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_TRAIN) ||
+        cudaFuncSetAttribute(k_mlp_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_INFER) ||
+        cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_SMEM))
+        return bad(RC_ERR_CUDA);
+    *out = m;
+    return RC_OK;
+}
+
+void rc_mlp_destroy(rc_mlp* m) {
+    if (!m) return;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    cudaFree(m->w); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad); cudaFree(m->part);
+    cudaFree(m->loss); cudaFree(m->wbf); cudaFree(m->act); cudaFree(m->err);
+    if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+}
+
+const char* rc_mlp_last_error(const rc_mlp* m) { return m ? m->msg.c_str() : "no network"; }
+
+rc_status rc_mlp_weights(rc_mlp* m, float* host, size_t n, int to_device) {
+    if (!m || !host || n != (size_t)NWEIGHT) return mfail(m, RC_ERR_ARG, "weights: 24576 floats");
+    if (to_device) {
+        if (cudaMemcpyAsync(m->w, host, 4 * NWEIGHT, cudaMemcpyHostToDevice, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "copy");
+        if (cudaMemsetAsync(m->wbf, 0, WF_BYTES + WB_BYTES, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "clear");
+        k_mlp_pack<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->w, m->wbf);
+        if (cudaGetLastError() != cudaSuccess) return mfail(m, RC_ERR_CUDA, "pack");
+    } else if (cudaMemcpyAsync(host, m->w, 4 * NWEIGHT, cudaMemcpyDeviceToHost, m->stream) != cudaSuccess) {
+        return mfail(m, RC_ERR_CUDA, "copy");
+    }
+    return cudaStreamSynchronize(m->stream) == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "sync");
+}
+
+rc_status rc_mlp_gradients(rc_mlp* m, float* host, size_t n) {
+    if (!m || !host || n != (size_t)NWEIGHT) return mfail(m, RC_ERR_ARG, "gradients: 24576 floats");
+    if (cudaMemcpyAsync(host, m->grad, 4 * NWEIGHT, cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess)
+        return mfail(m, RC_ERR_CUDA, "copy");
+    return RC_OK;
+}
+
+rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, const float* d_target, int tstride,
+                       const int* d_idx, int n, float* d_loss) {
+    if (!m || !d_pos4 || !d_nrm4 || !d_aux4 || !d_target || n < 128 || n % 128 || n > 128 * m->cap_tiles || tstride < m->cfg.n_out)
+        return mfail(m, RC_ERR_ARG, "train: n a multiple of 128 up to max_batch");
+    MlpArgs a = args_of(m);
+    a.P = reinterpret_cast<const float4*>(d_pos4);
+    a.N = reinterpret_cast<const float4*>(d_nrm4);
+    a.aux = reinterpret_cast<const float4*>(d_aux4);
+    a.target = d_target;
+    a.tstride = tstride;
+    a.idx = d_idx;
+    a.n = n;
+    a.act = m->act;
+    a.dwpart = m->part;
+    a.loss = d_loss ? d_loss : m->loss;
+    a.loss_scale = 1.f / ((float)n * (float)m->cfg.n_out);
+    const int ntiles = n / 128;
+    if (!d_loss && cudaMemsetAsync(m->loss, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "loss");
+    k_mlp_forward<true><<<std::min(ntiles, m->sms), 128, FWD_SMEM_TRAIN, m->stream>>>(a);
+    k_mlp_backward<<<ntiles, 128, BWD_SMEM, m->stream>>>(a);
+    m->step++;
+    const float b1 = 0.9f, b2 = 0.99f;
+    const float c1 = (float)(1.0 / (1.0 - pow(b1, (double)m->step))), c2 = (float)(1.0 / (1.0 - pow(b2, (double)m->step)));
+    k_mlp_adam<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->part, ntiles, m->w, m->m1, m->m2, m->grad, m->wbf, m->cfg.lr, b1,
+                                                              b2, 1e-8f, c1, c2);
+    return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
+}
+
+rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, int n, float* d_out, int ostride) {
+    if (!m || !d_pos4 || !d_nrm4 || !d_aux4 || !d_out || n < 1 || ostride < m->cfg.n_out) return mfail(m, RC_ERR_ARG, "infer");
+    MlpArgs a = args_of(m);
+    a.P = reinterpret_cast<const float4*>(d_pos4);
+    a.N = reinterpret_cast<const float4*>(d_nrm4);
+    a.aux = reinterpret_cast<const float4*>(d_aux4);
+    a.n = n;
+    a.out = d_out;
+    a.ostride = ostride;
+    const int ntiles = (n + 127) / 128;
+    k_mlp_forward<false><<<std::min(ntiles, m->sms), 128, FWD_SMEM_INFER, m->stream>>>(a);
+    return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
+}
+
+rc_status rc_mlp_error_flags(rc_mlp* m, unsigned* flags) {
+    if (!m || !flags) return RC_ERR_ARG;
+    if (cudaMemcpyAsync(flags, m->err, 4, cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess)
+        return mfail(m, RC_ERR_CUDA, "copy");
+    return RC_OK;
+}
+
+}  // extern "C"
