@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--method", default=METHOD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=12)
-    ap.add_argument("--profile", choices=["frame", "hashgrid"], default=None,
+    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp"], default=None,
                     help="no timing: run --steps frames of state 0 (frame) or three resolve passes of the "
                          "hash-grid table (hashgrid), for an ncu capture, and exit")
     return ap.parse_args()
@@ -68,6 +68,10 @@ def profile_run(args):
             ctx.frame(0)
         ctx.sync()
         ctx.close()
+        return
+    if args.profile == "mlp":
+        mlp_bench(torch.cuda.current_stream(), reps=2)
+        torch.cuda.synchronize()
         return
     from render_engine_gb300 import hashgrid as H
     cap, live = 1 << 24, 1 << 23
@@ -313,6 +317,7 @@ def run_ours(args, world, rank, local, dist):
     ctx2.close()
     ctx.close()
     out["hashgrid"] = hashgrid_bench(stream, peak)
+    out["mlp"] = mlp_bench(stream)
     return out, data, method
 
 
@@ -384,6 +389,62 @@ def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20,
                         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                                      "algorithmic_bytes": res_bytes}},
             "mark_paths": {"paths": npaths, "vertices": n, "ms": mark_ms, "vertices_per_s": n / (mark_ms * 1e-3)}}
+
+
+def mlp_bench(stream, npoints=1_082_802, batch=1 << 16, reps=10):
+    """Secondary lines: the learned radiance cache on the tensor cores (include/rc_mlp.h).
+
+    infer: the network's 3 outputs for 1,082,802 points (one per cache point of the room);
+    train: one Adam step on 2^16 samples (forward, backward, gradient sum, update).
+    Algorithmic FLOPs per query: 2 x (168 x 64 + 3 x 64 x 64 + 64 x 3) = 46,464 (forward),
+    3x that per training sample, against the measured bf16 tensor peak (burst)."""
+    import torch
+    from render_engine_gb300 import mlp as MLP
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    P = (torch.rand(npoints, 4, device="cuda", generator=g) * torch.tensor([8.0, 4.0, 3.0, 0.0], device="cuda")).contiguous()
+    N = torch.randn(npoints, 4, device="cuda", generator=g)
+    N[:, :3] /= N[:, :3].norm(dim=1, keepdim=True)
+    N = N.contiguous()
+    aux = torch.rand(npoints, 4, device="cuda", generator=g).contiguous()
+    target = torch.rand(npoints, 3, device="cuda", generator=g).contiguous()
+    out = torch.empty(npoints, 3, device="cuda")
+    net = MLP.Mlp(n_out=3, lr=1e-2, max_batch=batch, stream=stream.cuda_stream)
+    idx = torch.randint(0, npoints, (batch,), device="cuda", generator=g, dtype=torch.int32)
+    net.infer(P, N, aux, out)
+    net.train(P, N, aux, target, idx=idx)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(2 * reps)]
+    for k in range(reps):
+        ev[k][0].record(stream)
+        net.infer(P, N, aux, out)
+        ev[k][1].record(stream)
+    for k in range(reps):
+        ev[reps + k][0].record(stream)
+        net.train(P, N, aux, target, idx=idx)
+        ev[reps + k][1].record(stream)
+    torch.cuda.synchronize()
+    inf_ms = sum(a.elapsed_time(b) for a, b in ev[:reps]) / reps
+    tr_ms = sum(a.elapsed_time(b) for a, b in ev[reps:]) / reps
+    flops = 2.0 * (168 * 64 + 3 * 64 * 64 + 64 * 3)
+    flags = net.error_flags()
+    net.close()
+    peak = tensor_peak()
+    inf_tf = npoints * flops / (inf_ms * 1e-3) / 1e12
+    tr_tf = batch * 3 * flops / (tr_ms * 1e-3) / 1e12
+    return {"infer": {"queries": npoints, "ms": inf_ms, "queries_per_s": npoints / (inf_ms * 1e-3),
+                      "roofline": {"bound": "tensor", "achieved": inf_tf, "peak": peak, "unit": "TFLOP/s", "frac": inf_tf / peak}},
+            "train_step": {"samples": batch, "ms": tr_ms, "samples_per_s": batch / (tr_ms * 1e-3),
+                           "roofline": {"bound": "tensor", "achieved": tr_tf, "peak": peak, "unit": "TFLOP/s", "frac": tr_tf / peak}},
+            "error_flags": flags}
+
+
+def tensor_peak() -> float:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["bf16_tflops"])
+    return 1900.0
 
 
 def cpu_baseline(args, data, method):
@@ -490,7 +551,7 @@ def main():
             "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
             "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
-            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "hashgrid": res["hashgrid"]}
+            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "hashgrid": res["hashgrid"], "mlp": res["mlp"]}
     print(json.dumps(line))
 
 

@@ -134,45 +134,55 @@ __device__ __forceinline__ void st_bf16(uint8_t* base, uint32_t off, float v) {
 // The 168 input features of one point (the rest of the 176 are zero): frequency encodings of
 // the position in the box (12 octaves) and of the normal (4 octaves), one-blob encodings of
 // both (16 and 4 bins per axis), the raw position, normal, direct light of three lights,
-// albedo and a constant.
-__device__ void encode(const MlpArgs& a, int pt, float (&f)[K0]) {
+// albedo and a constant.  Produced eight at a time (one 16-byte group of the K-major tile);
+// emit(group, f) stores them.
+template <class Emit>
+__device__ __forceinline__ void encode(const MlpArgs& a, int pt, Emit&& emit) {
     const float4 P = a.P[pt], Nn = a.N[pt], X = a.aux[pt];
     const float p[3] = {fminf(fmaxf((P.x - a.lo[0]) * a.inv_ext[0], 0.f), 1.f), fminf(fmaxf((P.y - a.lo[1]) * a.inv_ext[1], 0.f), 1.f),
                         fminf(fmaxf((P.z - a.lo[2]) * a.inv_ext[2], 0.f), 1.f)};
     const float nv[3] = {Nn.x, Nn.y, Nn.z};
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
+    float f[8];
+    for (int ax = 0; ax < 3; ++ax) {   // features 24 ax .. 24 ax + 23: sin / cos of 2^o pi p
         float w = 3.14159265f * p[ax];
+        for (int g = 0; g < 3; ++g) {
 #pragma unroll
-        for (int o = 0; o < 12; ++o, w *= 2.f) {
-            float sn, cs;
-            sincosf(w, &sn, &cs);
-            f[ax * 24 + o * 2] = sn;
-            f[ax * 24 + o * 2 + 1] = cs;
+            for (int j = 0; j < 4; ++j, w *= 2.f) sincosf(w, &f[2 * j], &f[2 * j + 1]);
+            emit(ax * 3 + g, f);
         }
+    }
+    for (int ax = 0; ax < 3; ++ax) {   // 72 + 8 ax: sin / cos of 2^o pi n
         float u = 3.14159265f * nv[ax];
 #pragma unroll
-        for (int o = 0; o < 4; ++o, u *= 2.f) {
-            float sn, cs;
-            sincosf(u, &sn, &cs);
-            f[72 + ax * 8 + o * 2] = sn;
-            f[72 + ax * 8 + o * 2 + 1] = cs;
-        }
-        const float bp = p[ax] * 16.f, bn = (nv[ax] * 0.5f + 0.5f) * 4.f;
-#pragma unroll
-        for (int b = 0; b < 16; ++b) f[96 + ax * 16 + b] = fmaxf(0.f, 1.f - fabsf(bp - (b + 0.5f)));
-#pragma unroll
-        for (int b = 0; b < 4; ++b) f[144 + ax * 4 + b] = fmaxf(0.f, 1.f - fabsf(bn - (b + 0.5f)));
-        f[156 + ax] = p[ax];
-        f[159 + ax] = nv[ax];
+        for (int j = 0; j < 4; ++j, u *= 2.f) sincosf(u, &f[2 * j], &f[2 * j + 1]);
+        emit(9 + ax, f);
     }
-    f[162] = X.y;
-    f[163] = X.z;
-    f[164] = X.w;
-    f[165] = X.x;
-    f[166] = 1.f;
+    for (int ax = 0; ax < 3; ++ax) {   // 96 + 16 ax: one-blob of p, 16 bins
+        const float bp = p[ax] * 16.f;
+        for (int g = 0; g < 2; ++g) {
 #pragma unroll
-    for (int k = 167; k < K0; ++k) f[k] = 0.f;
+            for (int j = 0; j < 8; ++j) f[j] = fmaxf(0.f, 1.f - fabsf(bp - (8 * g + j + 0.5f)));
+            emit(12 + 2 * ax + g, f);
+        }
+    }
+    float nb[12];   // 144 + 4 ax: one-blob of n, 4 bins
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        const float bn = (nv[ax] * 0.5f + 0.5f) * 4.f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) nb[4 * ax + j] = fmaxf(0.f, 1.f - fabsf(bn - (j + 0.5f)));
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) f[j] = nb[j];
+    emit(18, f);
+    f[0] = nb[8]; f[1] = nb[9]; f[2] = nb[10]; f[3] = nb[11];
+    f[4] = p[0]; f[5] = p[1]; f[6] = p[2]; f[7] = nv[0];          // 156..159
+    emit(19, f);
+    f[0] = nv[1]; f[1] = nv[2]; f[2] = X.y; f[3] = X.z; f[4] = X.w; f[5] = X.x; f[6] = 1.f; f[7] = 0.f;   // 160..167
+    emit(20, f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) f[j] = 0.f;
+    emit(21, f);
 }
 
 // Forward pass over tiles of 128 samples (persistent CTAs of 128 threads, thread = sample row).
@@ -184,10 +194,10 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
     __shared__ uint64_t mbar;
     __shared__ uint32_t tmem_base;
     uint8_t* sw = smem;                               // forward weight tiles, WF_BYTES
-    uint8_t* sx = smem + WF_BYTES;                    // X0, 128 x 176 (K-major)
-    uint8_t* sh0 = sx + 128 * K0 * 2;                 // H ping-pong, 128 x 64 each
-    uint8_t* sh1 = sh0 + 128 * HID * 2;
-    uint8_t* st = sh1 + 128 * HID * 2;                // TRAIN: transposed staging, 176 x 128
+    // one activation tile: X0 (128 x 176) and then each H_l (128 x 64) in its place, H_{l+1}
+    // written once the product that reads H_l has completed
+    uint8_t* sx = smem + WF_BYTES;
+    uint8_t* st = sx + 128 * K0 * 2;                  // TRAIN: transposed staging, 176 x 128
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int i = tid; i < WF_BYTES / 16; i += 128) reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(a.wbf)[i];
     if (tid == 0) mbar_init(&mbar, 1);
@@ -203,21 +213,16 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
         const int s = tile * 128 + tid;
         const bool live = s < a.n;
         const int pt = live ? (a.idx ? a.idx[s] : s) : 0;
-        {
-            float f[K0];
-            encode(a, pt, f);
-#pragma unroll
-            for (int k8 = 0; k8 < K0 / 8; ++k8) {
-                uint4 v;
-                v.x = pack_bf16(f[8 * k8], f[8 * k8 + 1]);
-                v.y = pack_bf16(f[8 * k8 + 2], f[8 * k8 + 3]);
-                v.z = pack_bf16(f[8 * k8 + 4], f[8 * k8 + 5]);
-                v.w = pack_bf16(f[8 * k8 + 6], f[8 * k8 + 7]);
-                *reinterpret_cast<uint4*>(sx + kmajor_offset(tid, 8 * k8, K0)) = v;
-                if (TRAIN)
-                    for (int j = 0; j < 8; ++j) st_bf16(st, kmajor_offset(8 * k8 + j, tid, 128), f[8 * k8 + j]);
-            }
-        }
+        encode(a, pt, [&](int k8, const float (&f)[8]) {
+            uint4 v;
+            v.x = pack_bf16(f[0], f[1]);
+            v.y = pack_bf16(f[2], f[3]);
+            v.z = pack_bf16(f[4], f[5]);
+            v.w = pack_bf16(f[6], f[7]);
+            *reinterpret_cast<uint4*>(sx + kmajor_offset(tid, 8 * k8, K0)) = v;
+            if (TRAIN)
+                for (int j = 0; j < 8; ++j) st_bf16(st, kmajor_offset(8 * k8 + j, tid, 128), f[j]);
+        });
         fence_proxy_async();
         __syncthreads();
         if (TRAIN) {
@@ -227,8 +232,8 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
         }
         for (int l = 0; l < NLAYER && ok; ++l) {
             const int K = in_dim(l), N = out_dim(l);
-            uint8_t* A = l == 0 ? sx : ((l & 1) ? sh0 : sh1);   // H_l is in sh0 for odd l
-            uint8_t* Hn = (l & 1) ? sh1 : sh0;                  // H_{l+1}
+            uint8_t* A = sx;
+            uint8_t* Hn = sx;
             if (tid == 0) {
                 const uint32_t a0 = smem_u32(A), b0 = smem_u32(sw + wf_off(l));
                 for (int kk = 0; kk < K / 16; ++kk)
@@ -410,15 +415,24 @@ __global__ void k_mlp_pack(const float* __restrict__ w, uint8_t* __restrict__ wb
     if (l >= 1) st_bf16(wbf + wb_off(l), kmajor_offset(k, r, out_dim(l)), v);
 }
 
-// Gradient of each weight = the tile gradients added in tile order (reproducible), then one
-// Adam step on the FP32 master weight, and its bf16 copies.
-__global__ void k_mlp_adam(const float* __restrict__ part, int ntiles, float* __restrict__ w, float* __restrict__ m1,
-                           float* __restrict__ m2, float* __restrict__ grad, uint8_t* __restrict__ wbf, float lr, float b1, float b2,
-                           float eps, float c1, float c2) {
+// Gradient of each weight = the tile gradients added in a fixed order (reproducible): slice s
+// of GSLICES adds tiles s, s + GSLICES, ... in order, then the slices are added in order; then
+// one Adam step on the FP32 master weight, and its bf16 copies.
+constexpr int GSLICES = 16;
+__global__ void k_mlp_gsum(const float* __restrict__ part, int ntiles, float* __restrict__ slices) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (i >= NWEIGHT) return;
+    float g = 0.f;
+    for (int t = s; t < ntiles; t += GSLICES) g += part[(size_t)t * NWEIGHT + i];
+    slices[(size_t)s * NWEIGHT + i] = g;
+}
+__global__ void k_mlp_adam(const float* __restrict__ slices, float* __restrict__ w, float* __restrict__ m1, float* __restrict__ m2,
+                           float* __restrict__ grad, uint8_t* __restrict__ wbf, float lr, float b1, float b2, float eps, float c1,
+                           float c2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= NWEIGHT) return;
     float g = 0.f;
-    for (int t = 0; t < ntiles; ++t) g += part[(size_t)t * NWEIGHT + i];
+    for (int s = 0; s < GSLICES; ++s) g += slices[(size_t)s * NWEIGHT + i];
     grad[i] = g;
     const float m = b1 * m1[i] + (1.f - b1) * g;
     const float v = b2 * m2[i] + (1.f - b2) * g * g;
@@ -433,7 +447,7 @@ __global__ void k_mlp_adam(const float* __restrict__ part, int ntiles, float* __
     if (l >= 1) st_bf16(wbf + wb_off(l), kmajor_offset(k, r, out_dim(l)), x);
 }
 
-constexpr size_t FWD_SMEM_INFER = (size_t)WF_BYTES + 128 * K0 * 2 + 2 * 128 * HID * 2;
+constexpr size_t FWD_SMEM_INFER = (size_t)WF_BYTES + 128 * K0 * 2;
 constexpr size_t FWD_SMEM_TRAIN = FWD_SMEM_INFER + (size_t)K0 * 128 * 2;
 constexpr size_t BWD_SMEM = (size_t)K0 * 128 * 2 + 128 * HID * 2 + 128 * 128 * 2 + HID * HID * 2;
 }  // namespace
@@ -455,7 +469,7 @@ struct rc_mlp {
     rc_mlp_config cfg{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    float *w = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *part = nullptr, *loss = nullptr;
+    float *w = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *part = nullptr, *slices = nullptr, *loss = nullptr;
     uint8_t *wbf = nullptr, *act = nullptr;
     unsigned* err = nullptr;
     int cap_tiles = 0, sms = 0;
@@ -514,6 +528,7 @@ rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out) {
     if (cudaMalloc(&m->w, 4 * NWEIGHT) || cudaMalloc(&m->m1, 4 * NWEIGHT) || cudaMalloc(&m->m2, 4 * NWEIGHT) ||
         cudaMalloc(&m->grad, 4 * NWEIGHT) || cudaMalloc(&m->wbf, WF_BYTES + WB_BYTES) || cudaMalloc(&m->err, 4) ||
         cudaMalloc(&m->loss, 4) || cudaMalloc(&m->part, (size_t)4 * NWEIGHT * m->cap_tiles) ||
+        cudaMalloc(&m->slices, (size_t)4 * NWEIGHT * GSLICES) ||
         cudaMalloc(&m->act, (size_t)ACT_BYTES * m->cap_tiles))
         return bad(RC_ERR_NOMEM);
     // He-uniform initial weights, seeded
@@ -545,7 +560,7 @@ rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out) {
 void rc_mlp_destroy(rc_mlp* m) {
     if (!m) return;
     if (m->stream) cudaStreamSynchronize(m->stream);
-    cudaFree(m->w); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad); cudaFree(m->part);
+    cudaFree(m->w); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad); cudaFree(m->part); cudaFree(m->slices);
     cudaFree(m->loss); cudaFree(m->wbf); cudaFree(m->act); cudaFree(m->err);
     if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
     delete m;
@@ -597,8 +612,9 @@ rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     m->step++;
     const float b1 = 0.9f, b2 = 0.99f;
     const float c1 = (float)(1.0 / (1.0 - pow(b1, (double)m->step))), c2 = (float)(1.0 / (1.0 - pow(b2, (double)m->step)));
-    k_mlp_adam<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->part, ntiles, m->w, m->m1, m->m2, m->grad, m->wbf, m->cfg.lr, b1,
-                                                              b2, 1e-8f, c1, c2);
+    k_mlp_gsum<<<dim3((NWEIGHT + 255) / 256, GSLICES), 256, 0, m->stream>>>(m->part, ntiles, m->slices);
+    k_mlp_adam<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->w, m->m1, m->m2, m->grad, m->wbf, m->cfg.lr, b1, b2,
+                                                              1e-8f, c1, c2);
     return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
 }
 
@@ -612,7 +628,7 @@ rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.out = d_out;
     a.ostride = ostride;
     const int ntiles = (n + 127) / 128;
-    k_mlp_forward<false><<<std::min(ntiles, m->sms), 128, FWD_SMEM_INFER, m->stream>>>(a);
+    k_mlp_forward<false><<<std::min(ntiles, 2 * m->sms), 128, FWD_SMEM_INFER, m->stream>>>(a);   // two per SM fit
     return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
 }
 
