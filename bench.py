@@ -316,9 +316,34 @@ def run_ours(args, world, rank, local, dist):
                   "includes": "scene upload + per-state build + %d frames + final cache download" % args.steps}
     ctx2.close()
     ctx.close()
+    out["quality"] = quality(args, data, method, seq, local, stream)
     out["hashgrid"] = hashgrid_bench(stream, peak)
     out["mlp"] = mlp_bench(stream)
     return out, data, method
+
+
+def quality(args, data, method, seq, local, stream):
+    """The metric's error part: the per-frame luminance error of the cache against converged
+    references (the error formula of the reference, sqrt(sum (est - ref)^2 / n) / (sum ref / n)
+    over valid points), averaged over the 30 frames after each event and the 20 before it.
+    The scene carries no references, so they are computed first on the GPU by the stochastic
+    Jacobi of the reference's scene preparation (rc_reference_build)."""
+    from render_engine_gb300 import native as N
+    q = N.Context(device=local, stream=stream.cuda_stream)
+    q.load_bytes(data)
+    t0 = time.perf_counter()
+    noise, iters = q.build_reference()
+    tref = time.perf_counter() - t0
+    errs = [float(x) for x in q.run(method, seq, 11, want_err=True)]
+    q.close()
+    events = [f for f in range(1, len(seq)) if seq[f] != seq[f - 1]]
+    post = [statistics.mean(errs[e:e + 30]) for e in events if e + 30 <= len(errs)]
+    pre = [statistics.mean(errs[e - 20:e]) for e in events if e >= 20]
+    return {"luma_err_post_event_pct": 100 * statistics.mean(post) if post else None,
+            "luma_err_pre_event_pct": 100 * statistics.mean(pre) if pre else None,
+            "events": len(post), "reference_noise": [float(x) for x in noise], "reference_iterations": [int(x) for x in iters],
+            "reference_build_s": tref,
+            "note": "references from the GPU stochastic Jacobi of the reference's scene preparation (K=32, two chains, 3 % noise)"}
 
 
 def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20, reps=10):
@@ -551,7 +576,7 @@ def main():
             "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
             "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
-            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "hashgrid": res["hashgrid"], "mlp": res["mlp"]}
+            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "quality": res["quality"], "hashgrid": res["hashgrid"], "mlp": res["mlp"]}
     print(json.dumps(line))
 
 

@@ -195,6 +195,23 @@ rc_status rc_run_stats_get(rc_ctx* ctx, rc_run_stats* out);
 /* Device-side guard flags raised since the last call (then reset); 0 = none. */
 rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags);
 
+/* Converged references of every state of the loaded scene, computed on the GPU the way the
+ * reference's scene preparation does (prep_mesh.cuh:459-518, kernel k_ref :182-213): two
+ * chains of stochastic Jacobi iterations of K rays per point, `warmup` iterations, then blocks
+ * of `block` iterations averaged until the chains' relative difference is below noise_target
+ * or max_iter iterations are averaged.  ref = the mean over lights of the chains' mean, Pw =
+ * the per-light warm start, valid = fewer than 30 % of the rays hit within 0.02.  The scene
+ * then has references (error sums, warm starts).  noise / iters (NS entries each, may be NULL)
+ * receive the final noise and iteration count per state.  Synchronises. */
+typedef struct {
+    int K;               /* rays per point and iteration (32) */
+    int warmup;          /* iterations before averaging (16) */
+    int block;           /* iterations per block (64) */
+    int max_iter;        /* most averaged iterations (2048) */
+    double noise_target; /* relative noise between the two chains (0.03) */
+} rc_ref_params;
+rc_status rc_reference_build(rc_ctx* ctx, const rc_ref_params* prm, double* noise, int* iters);
+
 /* Error sums without any device allocation.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory themselves -- a renderer whose per-frame path
  * runs under a budget fixed at start-up (cudaMalloc / cudaFree synchronise the device and can

@@ -149,6 +149,10 @@ struct Ops {
     static cudaError_t preload(int NW);
     static cudaError_t probe(int NW, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                              const int* pts, int npts, void* recs, int maxrec, int* nrec, cudaStream_t st);
+    // one iteration of the converged-reference solve (scene preparation)
+    static cudaError_t ref_iter(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                                const float* Lin, float* Lout, float* acc, float* closec, uint32_t seed, int K, int accumulate,
+                                int count_close, cudaStream_t st);
     // the first p.pre_k rays of every point traced ahead of the frame kernel (static-mesh scenes)
     static cudaError_t pretrace(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                 float4* out, cudaStream_t st);

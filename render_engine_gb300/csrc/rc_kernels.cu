@@ -1181,6 +1181,56 @@ __global__ void __launch_bounds__(BLOCK) k_probe(const DState s, const DStatic g
     }
 }
 
+// ------------------------------------------------------------------ converged references
+// One stochastic Jacobi iteration of the reference's scene preparation (prep_mesh.cuh:182-213):
+// each point averages K rays of albedo x (direct light + the previous iterate) at its hit
+// points; the iterate of every light goes to Lout, and is added to acc from the warm-up on.
+// close counts the rays that hit within 0.02 (points mostly hemmed in are not valid for the
+// error metric).  Buffers are padded like the cache (LCS floats per point).
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_ref(const DState s, const DStatic g, const Grid grid, const DevCache c, const FrameParams p,
+                                               const float* __restrict__ Lin, float* __restrict__ Lout, float* __restrict__ acc,
+                                               float* __restrict__ closec, uint32_t seed, int K, int accumulate, int count_close) {
+    extern __shared__ float4 sm[];
+    constexpr int LCS = lcs_of(NL), AES = aes_of(NL);
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= p.Np) return;
+    uint32_t rs = hash32(seed ^ hash32(i + 1));
+    const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
+    float sum[NL];
+#pragma unroll
+    for (int l = 0; l < NL; ++l) sum[l] = 0.f;
+    int close = 0;
+    for (int r = 0; r < K; ++r) {
+        const float u1 = rnd(rs);
+        const float u2 = rnd(rs);
+        const f3 D = cosine_dir(N, u1, u2);
+        const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+        if (h.q != -1 && h.t < 0.02f) close++;
+        if (h.back) continue;
+        float4 ae[AES / 4], lc[LCS / 4];
+        const float4* aep = s.AE + (size_t)h.pi * (AES / 4);
+        const float4* lcp = reinterpret_cast<const float4*>(Lin) + (size_t)h.pi * (LCS / 4);
+#pragma unroll
+        for (int k4 = 0; k4 < AES / 4; ++k4) ae[k4] = __ldg(aep + k4);
+#pragma unroll
+        for (int k4 = 0; k4 < LCS / 4; ++k4) lc[k4] = __ldcg(lcp + k4);
+        const float A = ae[0].x;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) sum[l] += A * (comp(ae, l + 1) + comp(lc, l));
+    }
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+        const float v = sum[l] / K;
+        Lout[(size_t)LCS * i + l] = v;
+        if (accumulate) acc[(size_t)LCS * i + l] += v;
+    }
+    if (count_close) closec[i] += (float)close;
+}
+
 // ------------------------------------------------------------------ launch wrappers
 
 static int grid_of(int Np) { return (Np + BLOCK - 1) / BLOCK; }
@@ -1198,6 +1248,17 @@ cudaError_t Ops<NL>::pretrace(const DState& s, const DStatic& g, const Grid& gri
     cudaError_t e = prep_smem(k_pretrace<NL>, smem);
     if (e != cudaSuccess) return e;
     k_pretrace<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, out);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::ref_iter(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                              const float* Lin, float* Lout, float* acc, float* closec, uint32_t seed, int K, int accumulate,
+                              int count_close, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+    cudaError_t e = prep_smem(k_ref<NL>, smem);
+    if (e != cudaSuccess) return e;
+    k_ref<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, Lin, Lout, acc, closec, seed, K, accumulate, count_close);
     return cudaGetLastError();
 }
 
@@ -1339,6 +1400,7 @@ cudaError_t Ops<NL>::preload(int NW) {
     touch((const void*)k_update<NL>);
     touch((const void*)k_event<NL>);
     touch((const void*)k_pretrace<NL>);
+    touch((const void*)k_ref<NL>);
     touch((const void*)k_error<NL>);
     touch((const void*)k_proj_apply<NL>);
     touch((const void*)k_camera<NL>);

@@ -1413,6 +1413,102 @@ rc_status rc_run_stats_get(rc_ctx* ctx, rc_run_stats* out) {
     return RC_OK;
 }
 
+rc_status rc_reference_build(rc_ctx* ctx, const rc_ref_params* prm, double* noise, int* iters) {
+    if (!ctx || !prm || prm->K < 1 || prm->warmup < 0 || prm->block < 1 || prm->max_iter < prm->block) return RC_ERR_ARG;
+    if (!ctx->have_scene) return fail(ctx, RC_ERR_STATE, "no scene loaded");
+    Scene& S = ctx->S;
+    const size_t Np = (size_t)S.Np;
+    const int NL = S.NL, LCS = lcs_of(NL);
+    cudaStream_t st = ctx->stream;
+    std::vector<DevBuf> tmp;
+    struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
+    float *chain[2], *acc[2], *out = nullptr, *closec = nullptr;
+    rc_status s;
+    for (int ch = 0; ch < 2; ++ch)
+        if ((s = dalloc(ctx, tmp, &chain[ch], LCS * Np)) || (s = dalloc(ctx, tmp, &acc[ch], LCS * Np))) return s;
+    if ((s = dalloc(ctx, tmp, &out, LCS * Np)) || (s = dalloc(ctx, tmp, &closec, Np))) return s;
+    FrameParams p{};
+    p.Np = S.Np;
+    auto mix = [](unsigned long long x) {   // poc_gpu.cu:260-262
+        x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ull; x ^= x >> 27; x *= 0x94d049bb133111ebull; x ^= x >> 31;
+        return x;
+    };
+    std::vector<float> a0(LCS * Np), a1(LCS * Np), cc(Np);
+    for (int si = 0; si < S.NS; ++si) {
+        HostState& hs = S.st[si];
+        const DState& d = hs.d;
+        CKR(cudaMemsetAsync(closec, 0, Np * 4, st));
+        for (int ch = 0; ch < 2; ++ch) {
+            CKR(cudaMemsetAsync(chain[ch], 0, LCS * Np * 4, st));
+            CKR(cudaMemsetAsync(acc[ch], 0, LCS * Np * 4, st));
+        }
+        int done = 0, T = 0;
+        double nz = 1.0;
+        std::vector<float> ref(Np), pw(LCS * Np, 0.f);
+        std::vector<uint8_t> val(Np);
+        while (true) {
+            const int n_it = done == 0 ? prm->warmup + prm->block : prm->block;
+            for (int ch = 0; ch < 2; ++ch) {
+                float* a = chain[ch];
+                float* b = out;
+                for (int k = 0; k < n_it; ++k) {
+                    const int it = done + k;
+                    const uint32_t seed = (uint32_t)mix(0x51ull + 7919ull * (unsigned long long)si + 104729ull * (unsigned long long)ch +
+                                                        31ull * (unsigned long long)it);
+                    CKR(RC_DISPATCH(NL, ref_iter(d, S.g, S.grid, ctx->c, p, a, b, acc[ch], closec, seed, prm->K, it >= prm->warmup,
+                                                 ch == 0, st)));
+                    std::swap(a, b);
+                }
+                if (a != chain[ch]) {   // the last iterate is in `out`: keep it as the chain's state
+                    CKR(cudaMemcpyAsync(chain[ch], a, LCS * Np * 4, cudaMemcpyDeviceToDevice, st));
+                }
+            }
+            done += n_it;
+            T = done - prm->warmup;
+            CKR(cudaMemcpyAsync(a0.data(), acc[0], a0.size() * 4, cudaMemcpyDeviceToHost, st));
+            CKR(cudaMemcpyAsync(a1.data(), acc[1], a1.size() * 4, cudaMemcpyDeviceToHost, st));
+            CKR(cudaMemcpyAsync(cc.data(), closec, Np * 4, cudaMemcpyDeviceToHost, st));
+            CKR(cudaStreamSynchronize(st));
+            double d2 = 0, rs = 0;
+            int nv = 0;
+            for (size_t i = 0; i < Np; ++i) {
+                float e0 = 0, e1 = 0;
+                for (int l = 0; l < NL; ++l) {
+                    const float x0 = a0[LCS * i + l] / T, x1 = a1[LCS * i + l] / T;
+                    pw[LCS * i + l] = 0.5f * (x0 + x1);
+                    e0 += x0;
+                    e1 += x1;
+                }
+                ref[i] = 0.5f * (e0 + e1);
+                val[i] = cc[i] / ((double)prm->K * done) < 0.3;
+                if (val[i]) { d2 += 0.25 * (e0 - e1) * (e0 - e1); rs += ref[i]; nv++; }
+            }
+            nz = nv && rs > 0 ? sqrt(d2 / nv) / (rs / nv) : 0.0;
+            if (nz <= prm->noise_target || T >= prm->max_iter) break;
+        }
+        if (noise) noise[si] = nz;
+        if (iters) iters[si] = T;
+        DState& dm = hs.d;
+        if (!dm.ref) {
+            float* r = nullptr;
+            uint8_t* v = nullptr;
+            float* w = nullptr;
+            if ((s = dalloc(ctx, ctx->scene_bufs, &r, Np)) || (s = dalloc(ctx, ctx->scene_bufs, &v, Np)) ||
+                (s = dalloc(ctx, ctx->scene_bufs, &w, LCS * Np)))
+                return s;
+            dm.ref = r;
+            dm.valid = v;
+            hs.pw = w;
+        }
+        CKR(cudaMemcpyAsync((void*)dm.ref, ref.data(), Np * 4, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemcpyAsync((void*)dm.valid, val.data(), Np, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemcpyAsync((void*)hs.pw, pw.data(), LCS * Np * 4, cudaMemcpyHostToDevice, st));
+        CKR(cudaStreamSynchronize(st));
+    }
+    S.has_ref = 1;
+    return RC_OK;
+}
+
 rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags) {
     if (!ctx || !flags) return RC_ERR_ARG;
     CKR(cudaMemcpyAsync(flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -38,7 +38,7 @@ EXPORTS = [
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
     "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
     "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
-    "rc_error_sums_noalloc",
+    "rc_error_sums_noalloc", "rc_reference_build",
 ]
 NOALLOC_MAX_POINTS = 4194304
 
@@ -148,10 +148,17 @@ def load_library():
     L.rc_run_stats_get.argtypes = [vp, ctypes.POINTER(RunStats)]
     L.rc_device_flags.restype = i
     L.rc_device_flags.argtypes = [vp, ctypes.POINTER(ctypes.c_uint)]
+    L.rc_reference_build.restype = i
+    L.rc_reference_build.argtypes = [vp, ctypes.POINTER(RefParams), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.rc_error_sums_noalloc.restype = i
     L.rc_error_sums_noalloc.argtypes = [vp, i, i, i, vp, vp, i, vp, vp]
     _lib = L
     return L
+
+
+class RefParams(ctypes.Structure):
+    _fields_ = [("K", ctypes.c_int), ("warmup", ctypes.c_int), ("block", ctypes.c_int), ("max_iter", ctypes.c_int),
+                ("noise_target", ctypes.c_double)]
 
 
 class RCError(RuntimeError):
@@ -311,6 +318,16 @@ class Context:
         st = RunStats()
         self._chk(self.L.rc_run_stats_get(self.h, ctypes.byref(st)))
         return {n: getattr(st, n) for n, _ in RunStats._fields_}
+
+    def build_reference(self, K: int = 32, warmup: int = 16, block: int = 64, max_iter: int = 2048, noise_target: float = 0.03):
+        """Converged references of every state (rc_reference_build); returns (noise, iterations) per state."""
+        ns = self._info["ns"]
+        noise = (ctypes.c_double * ns)()
+        iters = (ctypes.c_int * ns)()
+        prm = RefParams(K, warmup, block, max_iter, noise_target)
+        self._chk(self.L.rc_reference_build(self.h, ctypes.byref(prm), noise, iters))
+        self._info = self.info()
+        return list(noise), list(iters)
 
     def device_flags(self) -> int:
         v = ctypes.c_uint()

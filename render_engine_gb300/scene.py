@@ -554,3 +554,16 @@ def street_scene(points: int = 20000, buildings: int = 8, seed: int = 0, facade_
     I = [[20, 20, 0], [0, 20, 0], [20, 20, 0], [20, 20, 20], [0, 20, 0]]
     box = [(-2.0, 0.0, 1.0), (-2.0, 0.0, 1.0), (4.0, -1.0, 1.0), (-2.0, 0.0, 1.0), (4.0, -1.0, 1.0)]
     return mesh_scene(V, alb, ds, L, I, box, 1.0, points, seed)
+
+
+def with_references(scene: Scene, ctx) -> Scene:
+    """The scene with the converged references a context computed for it
+    (``native.Context.build_reference`` on this scene): ref, valid and the per-light warm
+    start of every state, so that the written file carries them (has_ref = 1)."""
+    from . import native as N
+    nl = scene.NL
+    for k, st in enumerate(scene.states):
+        st.ref = ctx.state_array(k, N.SA_REF).astype(np.float32)
+        st.valid = ctx.state_array(k, N.SA_VALID).astype(np.uint8)
+        st.Pw = ctx.state_array(k, N.SA_PW).reshape(-1, nl).astype(np.float32)
+    return scene
