@@ -319,6 +319,7 @@ def run_ours(args, world, rank, local, dist):
     out["quality"] = quality(args, data, method, seq, local, stream)
     out["hashgrid"] = hashgrid_bench(stream, peak)
     out["mlp"] = mlp_bench(stream)
+    out["adjoint"] = adjoint_bench(peak)
     return out, data, method
 
 
@@ -414,6 +415,38 @@ def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20,
                         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                                      "algorithmic_bytes": res_bytes}},
             "mark_paths": {"paths": npaths, "vertices": n, "ms": mark_ms, "vertices_per_s": n / (mark_ms * 1e-3)}}
+
+
+def adjoint_bench(peak, points=1_082_802, lights=16, K=16):
+    """Secondary line: dJ/dE for all 16 lights of a 1.08 M-point room (rc_adjoint): K frozen rays
+    per point, the transposed ray lists, 64 forward + 64 adjoint Jacobi sweeps, the FP64
+    gradient.  A sweep pair's time is (t(64) - t(16)) / 48 from two calls; its algorithmic HBM
+    bytes: the hit list and the transposed source list (4 B per ray each), offsets, weights and
+    the two iterates (about 24 B per point); the gathers of the iterates stay in L2 (4 MB)."""
+    import numpy as np
+    from render_engine_gb300 import native as N
+    from render_engine_gb300 import scene as S
+    ctx = N.Context()
+    info = ctx.load_bytes(S.write(S.box_room(points=points, seed=0, lights=lights)))
+    rng = np.random.default_rng(1)
+    w = np.zeros(info["np"], np.float32)
+    w[rng.choice(info["np"], 4096, replace=False)] = 1.0 / 4096
+    ctx.adjoint(0, w, K=K, seed=5, iterations=16)   # warm-up (kernel loading, allocation)
+    t = {}
+    for it in (16, 64):
+        t0 = time.perf_counter()
+        g, res = ctx.adjoint(0, w, K=K, seed=5, iterations=it)
+        t[it] = (time.perf_counter() - t0) * 1e3
+    ctx.close()
+    pair_ms = (t[64] - t[16]) / 48
+    counted = res["rays"] - res["back"]
+    pair_bytes = 4.0 * res["rays"] + 4.0 * counted + 24.0 * info["np"]
+    gbs = pair_bytes / (pair_ms * 1e-3) / 1e9 if pair_ms > 0 else None
+    return {"points": info["np"], "lights": lights, "rays_per_point": K, "iterations": 64, "ms": t[64],
+            "sweep_pair_ms": pair_ms, "J_rel_linearity_gap": abs(res["J_grad"] - res["J"]) / abs(res["J"]),
+            "fwd_change": res["fwd_change"], "adj_change": res["adj_change"],
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak if gbs else None,
+                         "bytes_per_sweep_pair": pair_bytes}}
 
 
 def mlp_bench(stream, npoints=1_082_802, batch=1 << 16, reps=10):
@@ -576,7 +609,8 @@ def main():
             "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
             "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
-            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "quality": res["quality"], "hashgrid": res["hashgrid"], "mlp": res["mlp"]}
+            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "quality": res["quality"], "hashgrid": res["hashgrid"], "mlp": res["mlp"],
+            "adjoint": res["adjoint"]}
     print(json.dumps(line))
 
 

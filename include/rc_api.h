@@ -212,6 +212,38 @@ typedef struct {
 } rc_ref_params;
 rc_status rc_reference_build(rc_ctx* ctx, const rc_ref_params* prm, double* noise, int* iters);
 
+/* Adjoint of the cache transport with respect to the lights' emission.  No counterpart in the
+ * reference.  For state `state`, K rays per point are traced once and kept -- the rays of one
+ * reference iteration with `seed` (prep_mesh.cuh:182-200) -- which fixes the linear transport
+ * every frame and every reference iteration samples:
+ *     L_l = T (E_l G_l + L_l),  T[i, j] = A_j / K x (rays of point i reaching point j),
+ * G_l = the direct light of light l at unit emission (k_build, poc_gpu.cu:369-391).  For the
+ * objective J = sum_i w_i sum_l L_l[i] (e.g. w = 1 / n on n sampled points), one adjoint solve
+ * u = w + T^T u gives every light's derivative:  dJ/dE_l = sum_j (u_j - w_j) G_l[j].
+ * Both solves run `iterations` Jacobi sweeps from zero (from w for u); sums over points are
+ * FP64 in a fixed order, so results are reproducible.  `weights` (Np floats) and `dJ_dE`
+ * (NL floats) are host buffers.  Synchronises. */
+typedef struct {
+    int state;          /* scene state whose transport is differentiated */
+    int K;              /* frozen rays per point (1..1024, Np * K < 2^31) */
+    uint32_t seed;      /* seed of the frozen rays */
+    int iterations;     /* Jacobi sweeps of each solve (0 = 64) */
+} rc_adjoint_params;
+typedef struct {
+    double J;           /* w . L from the forward solve (L summed over lights) */
+    double J_grad;      /* sum_l E_l dJ/dE_l: equal to J up to rounding, L being linear in E */
+    double fwd_change;  /* last forward sweep: max |L_t - L_{t-1}| / max |L_t| */
+    double adj_change;  /* last adjoint sweep: max |u_t - u_{t-1}| / max |u_t| */
+    long long rays;     /* frozen rays, K * Np */
+    long long back;     /* frozen rays that do not count (no hit, back face, cell absent) */
+    int max_incoming;   /* most rays reaching one point */
+} rc_adjoint_result;
+rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* weights, float* dJ_dE, rc_adjoint_result* res);
+/* Arrays of the last rc_adjoint call (host buffers, any may be NULL): the forward solution L
+ * (Np floats, summed over lights), the adjoint importance u (Np floats) and the frozen rays'
+ * hit points (Np * K ints, ray r of point i at i * K + r, -1 = not counted).  Synchronises. */
+rc_status rc_adjoint_arrays(rc_ctx* ctx, float* L, float* u, int* hits);
+
 /* Error sums without any device allocation.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory themselves -- a renderer whose per-frame path
  * runs under a budget fixed at start-up (cudaMalloc / cudaFree synchronise the device and can

@@ -79,6 +79,11 @@ def lib():
         L.osc_probe_rays.restype = ctypes.c_int
         L.osc_probe_rays.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(RayRec), ctypes.c_int]
+        L.osc_frozen_hits.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p]
+        L.osc_direct_unit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.osc_path_trace.restype = ctypes.c_int
+        L.osc_path_trace.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -116,6 +121,29 @@ class Scene:
         if not ptr or nb.value == 0:
             return np.zeros(0, dt)
         return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)), (nb.value,)).view(dt).copy()
+
+    def frozen_hits(self, state: int, seed: int, K: int) -> np.ndarray:
+        """(Np, K) cache point reached by each of the K rays of one reference iteration, -1 = not counted."""
+        out = np.empty((self.Np, K), np.int32)
+        lib().osc_frozen_hits(self.p, state, seed & 0xFFFFFFFF, K, out.ctypes.data)
+        return out
+
+    def direct_unit(self, state: int) -> np.ndarray:
+        """(Np, NL) direct light of each light at unit emission (FP32)."""
+        out = np.empty((self.Np, self.NL), np.float32)
+        lib().osc_direct_unit(self.p, state, out.ctypes.data)
+        return out
+
+    def path_trace(self, state: int, points, paths: int = 4096, min_bounces: int = 3, seed: int = 1):
+        """FP64 path-traced cache transport (summed over lights) at the points: (mean, standard error)."""
+        pts = np.ascontiguousarray(points, np.int32)
+        mean = np.empty(len(pts), np.float64)
+        sem = np.empty(len(pts), np.float64)
+        rc = lib().osc_path_trace(self.p, state, pts.ctypes.data, len(pts), paths, min_bounces, seed, mean.ctypes.data,
+                                  sem.ctypes.data)
+        if rc != 0:
+            raise ValueError("oracle: path_trace arguments")
+        return mean, sem
 
     def event_list(self, pair: int, kind: int) -> np.ndarray:
         n = ctypes.c_int()

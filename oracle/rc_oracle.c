@@ -1130,3 +1130,241 @@ int osc_render(osc_run* r, int si, const float* eye, const float* fwd, const flo
         }
     return 0;
 }
+
+/* ------------------------------------------------------------------ adjoint support */
+
+/* The K rays of one reference iteration with `seed` (prep_mesh.cuh:182-200: per-point seed
+ * hash32(seed ^ hash32(i + 1)), cosine directions, trace and hit resolution of the frame),
+ * kept: hits[i * K + r] = the cache point reached, -1 when the ray does not count. */
+void osc_frozen_hits(const osc_scene* S, int si, uint32_t seed, int K, int* hits) {
+    const ostate* st = &S->st[si];
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < S->Np; ++i) {
+        uint32_t rs = hash32(seed ^ hash32((uint32_t)i + 1u));
+        v3 P = vld(st->P, i), N = vld(st->N, i), O = vadd(P, vmul(N, 1e-3f));
+        for (int r = 0; r < K; ++r) {
+            float u1 = rnd(&rs);
+            float u2 = rnd(&rs);
+            v3 D = cosine_dir(N, u1, u2);
+            float t;
+            int q, pi;
+            int hit = trace_full(S, st, O, D, &t, &q);
+            v3 H = hit ? vadd(O, vmul(D, t)) : O;
+            int back = resolve_hit(S, st, hit, H, D, q, i, &pi);
+            hits[(size_t)i * K + r] = back ? -1 : pi;
+        }
+    }
+}
+
+/* Direct light of every light at unit emission (k_build's formula, poc_gpu.cu:369-391, with
+ * inten = 1): out[i * NL + l]. */
+void osc_direct_unit(const osc_scene* S, int si, float* out) {
+    const ostate* st = &S->st[si];
+    const int NL = S->NL;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < S->Np; ++i) {
+        v3 P = vld(st->P, i), N = vld(st->N, i), O = vadd(P, vmul(N, 1e-3f));
+        for (int l = 0; l < NL; ++l) {
+            v3 d = vsub(vld(S->L, l), P);
+            float r = sqrtf(vdot(d, d));
+            v3 D = vmul(d, 1.f / r);
+            float c = vdot(N, D), t;
+            int q;
+            trace_full(S, st, O, D, &t, &q);
+            int vis = t >= r - 1e-3f;
+            float rr = fmaxf(r, 0.05f);
+            out[(size_t)NL * i + l] = 1.f * fmaxf(c, 0.f) / (rr * rr) * (vis ? 1.f : 0.f);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ FP64 path tracer
+ * An independent estimate of the converged cache (the fixed point the reference's scene
+ * preparation iterates to, prep_mesh.cuh:182-213 and :459-518): random walks over the cache
+ * points, everything in double -- directions, ray-triangle and ray-box tests, hit resolution,
+ * direct light with its shadow ray (the formula of k_build, poc_gpu.cu:369-391) and the path
+ * throughput.  A walk from point i takes a cosine ray from P_i + 1e-3 N_i, resolves the hit to
+ * its cache point j as every frame does (poc_gpu.cu:339-358), adds throughput x A_j x direct_j
+ * and continues from point j; it ends on a ray that does not count, or by Russian roulette
+ * (survival probability A_j) after `min_bounces`.  Random numbers: splitmix64 streams. */
+typedef struct { double x, y, z; } d3;
+static inline d3 D3(double x, double y, double z) { d3 r = {x, y, z}; return r; }
+static inline d3 dadd(d3 a, d3 b) { return D3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline d3 dsub(d3 a, d3 b) { return D3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline d3 dmul(d3 a, double s) { return D3(a.x * s, a.y * s, a.z * s); }
+static inline double ddot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline d3 dcross(d3 a, d3 b) { return D3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static inline d3 dld(const float* p, long i) { return D3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+
+static inline double urand(uint64_t* s) {
+    *s += 0x9E3779B97F4A7C15ull;
+    return (double)(mix64(*s) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* Moller-Trumbore in double; single triangle (v0, e1, e2), closest t > 1e-4 */
+static inline int tri_d(d3 o, d3 d, const float* T, double eps, int clamp_u, double* t_out) {
+    d3 v0 = D3(T[0], T[1], T[2]), e1 = D3(T[3], T[4], T[5]), e2 = D3(T[6], T[7], T[8]);
+    d3 p = dcross(d, e2);
+    double det = ddot(e1, p);
+    if (fabs(det) <= eps) return 0;
+    double inv = 1.0 / det;
+    d3 tv = dsub(o, v0);
+    double u = ddot(tv, p) * inv;
+    if (u < 0.0 || (clamp_u && u > 1.0)) return 0;
+    d3 qv = dcross(tv, e1);
+    double v = ddot(d, qv) * inv;
+    if (v < 0.0 || u + v > 1.0) return 0;
+    *t_out = ddot(e2, qv) * inv;
+    return 1;
+}
+
+static inline double box_d(const float* a, const float* b, d3 o, d3 inv, double tmax) {
+    double tx1 = (a[0] - o.x) * inv.x, tx2 = (b[0] - o.x) * inv.x;
+    double ty1 = (a[1] - o.y) * inv.y, ty2 = (b[1] - o.y) * inv.y;
+    double tz1 = (a[2] - o.z) * inv.z, tz2 = (b[2] - o.z) * inv.z;
+    double tn = fmax(fmax(fmin(tx1, tx2), fmin(ty1, ty2)), fmax(fmin(tz1, tz2), 0.0));
+    double tf = fmin(fmin(fmax(tx1, tx2), fmax(ty1, ty2)), fmin(fmax(tz1, tz2), tmax));
+    return tn <= tf ? tn : 1e300;
+}
+
+/* closest hit: dynamic triangles (q = quad id) then the static BVH (q = -2 - triangle) */
+static int trace_d(const osc_scene* s, const ostate* st, d3 o, d3 d, double* tmin, int* q) {
+    *tmin = INFINITY;
+    *q = -1;
+    double t;
+    for (int j = 0; j < s->Nt; ++j)
+        if (tri_d(o, d, st->T + 9 * (size_t)j, 1e-15, 0, &t) && t > 1e-4 && t < *tmin) { *tmin = t; *q = st->TQ[j]; }
+    if (!s->BN) return *q != -1;
+    d3 inv = D3(d.x != 0.0 ? 1.0 / d.x : copysign(1e300, d.x), d.y != 0.0 ? 1.0 / d.y : copysign(1e300, d.y),
+                d.z != 0.0 ? 1.0 / d.z : copysign(1e300, d.z));
+    int stack[128], sp = 0, node = 0;
+    for (;;) {
+        const float* a = s->BN + 8 * (size_t)node;
+        const float* b = a + 4;
+        int lf = f2i(a[3]), cnt = f2i(b[3]);
+        if (cnt > 0) {
+            for (int j = lf; j < lf + cnt; ++j)
+                if (tri_d(o, d, s->ST + 9 * (size_t)j, 1e-18, 1, &t) && t > 1e-4 && t < *tmin) { *tmin = t; *q = -2 - j; }
+        } else {
+            const float* la = s->BN + 8 * (size_t)lf;
+            double tl = box_d(la, la + 4, o, inv, *tmin), tr = box_d(la + 8, la + 12, o, inv, *tmin);
+            int first = lf, second = lf + 1;
+            if (tr < tl) { double x = tl; tl = tr; tr = x; first = lf + 1; second = lf; }
+            if (tl < 1e300) {
+                if (tr < 1e300 && sp < 128) stack[sp++] = second;
+                node = first;
+                continue;
+            }
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    return *q != -1;
+}
+
+/* cache point of a hit in double (poc_gpu.cu:239-287, 346-358); -1 when it does not count */
+static int resolve_d(const osc_scene* s, const ostate* st, d3 H, d3 D, int q) {
+    if (q >= 0) {
+        const float* Q = st->Q + 12 * (size_t)q;
+        if (ddot(D3(Q[9], Q[10], Q[11]), D) > 0.0) return -1;
+        d3 o = D3(Q[0], Q[1], Q[2]), u = D3(Q[3], Q[4], Q[5]), v = D3(Q[6], Q[7], Q[8]);
+        d3 dd = dsub(H, o);
+        double a = ddot(dd, u) / ddot(u, u), b = ddot(dd, v) / ddot(v, v);
+        int nu = st->dims[2 * q], nv = st->dims[2 * q + 1];
+        int iu = imin(imax((int)(a * nu), 0), nu - 1), iv = imin(imax((int)(b * nv), 0), nv - 1);
+        return st->off[q] + iv * nu + iu;
+    }
+    const float* n4 = s->STN + 4 * (size_t)(-2 - q);
+    d3 n = D3(n4[0], n4[1], n4[2]);
+    if (ddot(n, D) > 0.0) {
+        if (!(f2i(n4[3]) & 1)) return -1;
+        n = dmul(n, -1.0);
+    }
+    int bk = normal_bucket((float)n.x, (float)n.y, (float)n.z);
+    double ih = 1.0 / s->hcell;
+    int cx = (int)floor((H.x - s->lo[0]) * ih), cy = (int)floor((H.y - s->lo[1]) * ih), cz = (int)floor((H.z - s->lo[2]) * ih);
+    int p = hash_find(s, cell_key(cx, cy, cz, bk));   /* own cell, then the 26 neighbours */
+    if (p >= 0) return p;
+    for (int k = 0; k < 27; ++k) {
+        int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+        if (dx == 0 && dy == 0 && dz == 0) continue;
+        p = hash_find(s, cell_key(cx + dx, cy + dy, cz + dz, bk));
+        if (p >= 0) return p;
+    }
+    return -1;
+}
+
+static d3 cosine_d(d3 N, double u1, double u2) {
+    double r = sqrt(u1), phi = 6.283185307179586 * u2;
+    d3 a = fabs(N.x) > 0.9 ? D3(0, 1, 0) : D3(1, 0, 0);
+    d3 T = dcross(N, a);
+    T = dmul(T, 1.0 / sqrt(ddot(T, T)));
+    d3 B = dcross(N, T);
+    return dadd(dadd(dmul(T, r * cos(phi)), dmul(B, r * sin(phi))), dmul(N, sqrt(fmax(0.0, 1.0 - u1))));
+}
+
+/* direct light summed over the lights, per point, in double (k_build's formula) */
+static void direct_d(const osc_scene* S, const ostate* st, double* out) {
+    const int NL = S->NL;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < S->Np; ++i) {
+        d3 P = dld(st->P, i), N = dld(st->N, i), O = dadd(P, dmul(N, 1e-3));
+        double e = 0.0;
+        for (int l = 0; l < NL; ++l) {
+            d3 d = dsub(dld(S->L, l), P);
+            double r = sqrt(ddot(d, d));
+            d3 D = dmul(d, 1.0 / r);
+            double c = ddot(N, D), t;
+            int q;
+            trace_d(S, st, O, D, &t, &q);
+            if (!(t >= r - 1e-3)) continue;
+            double rr = fmax(r, 0.05);
+            e += (double)st->inten[l] * fmax(c, 0.0) / (rr * rr);
+        }
+        out[i] = e;
+    }
+}
+
+int osc_path_trace(const osc_scene* S, int si, const int* pts, int npts, int paths, int min_bounces, uint64_t seed, double* mean,
+                   double* sem) {
+    if (si < 0 || si >= S->NS || paths < 2) return -1;
+    const ostate* st = &S->st[si];
+    double* dir = (double*)malloc(sizeof(double) * (size_t)S->Np);
+    if (!dir) return -1;
+    direct_d(S, st, dir);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < npts; ++k) {
+        const int i0 = pts[k];
+        double s1 = 0.0, s2 = 0.0;
+        for (int p = 0; p < paths; ++p) {
+            uint64_t rs = mix64(seed ^ mix64(((uint64_t)(uint32_t)i0 << 32) | (uint32_t)p));
+            int cur = i0;
+            double beta = 1.0, val = 0.0;
+            for (int b = 1; b <= 4096; ++b) {
+                d3 P = dld(st->P, cur), N = dld(st->N, cur), O = dadd(P, dmul(N, 1e-3));
+                double u1 = urand(&rs), u2 = urand(&rs);
+                d3 D = cosine_d(N, u1, u2);
+                double t;
+                int q;
+                if (!trace_d(S, st, O, D, &t, &q)) break;
+                int j = resolve_d(S, st, dadd(O, dmul(D, t)), D, q);
+                if (j < 0) break;
+                const double A = S->A[j];
+                beta *= A;
+                val += beta * dir[j];
+                if (b >= min_bounces) {
+                    if (urand(&rs) >= A) break;
+                    beta /= A;
+                }
+                cur = j;
+            }
+            s1 += val;
+            s2 += val * val;
+        }
+        const double m = s1 / paths;
+        mean[k] = m;
+        sem[k] = sqrt(fmax(0.0, s2 / paths - m * m) / (paths - 1));
+    }
+    free(dir);
+    return 0;
+}

@@ -78,6 +78,16 @@ int osc_probe_rays(osc_run* r, int si, const int* pts, int npts, osc_ray_rec* ou
 int osc_render(osc_run* r, int si, const float* eye, const float* fwd, const float* right, const float* up, float tx, float ty,
                int w, int h, float* out);
 
+/* Adjoint support: the K rays of one reference iteration with `seed` (prep_mesh.cuh:182-200)
+ * kept per point, hits[i * K + r] = cache point reached or -1 (the FP32 trace of the frames). */
+void osc_frozen_hits(const osc_scene* s, int si, uint32_t seed, int K, int* hits);
+/* Direct light of every light at unit emission, out[i * NL + l] (FP32, k_build's formula). */
+void osc_direct_unit(const osc_scene* s, int si, float* out);
+/* FP64 path tracer: per listed point, the mean over `paths` random walks of the cache transport
+ * (summed over lights) and its standard error; 0 = ok. */
+int osc_path_trace(const osc_scene* s, int si, const int* pts, int npts, int paths, int min_bounces, uint64_t seed, double* mean,
+                   double* sem);
+
 enum {
     OSC_A_LC = 0, OSC_A_LC2, OSC_A_M, OSC_A_N, OSC_A_C0, OSC_A_KK, OSC_A_PENDING, OSC_A_CUR, OSC_A_PREV,
     OSC_A_STALE, OSC_A_AGE, OSC_A_SNAP, OSC_A_NEQ, OSC_A_COEF, OSC_A_RSTAT, OSC_A_DSTAT, OSC_A_SUMPR,

@@ -153,6 +153,9 @@ struct Ops {
     static cudaError_t ref_iter(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                 const float* Lin, float* Lout, float* acc, float* closec, uint32_t seed, int K, int accumulate,
                                 int count_close, cudaStream_t st);
+    // K frozen rays per point (the rays of one reference iteration with `seed`): hit cache point or -1
+    static cudaError_t frozen_hits(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                                   uint32_t seed, int K, int* hits, cudaStream_t st);
     // the first p.pre_k rays of every point traced ahead of the frame kernel (static-mesh scenes)
     static cudaError_t pretrace(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                 float4* out, cudaStream_t st);

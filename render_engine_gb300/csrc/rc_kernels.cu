@@ -1231,6 +1231,30 @@ __global__ void __launch_bounds__(BLOCK) k_ref(const DState s, const DStatic g, 
     if (count_close) closec[i] += (float)close;
 }
 
+// The rays of one k_ref iteration with this seed (prep_mesh.cuh:182-200: same seed, directions
+// and hit resolution), kept: hits[i * K + r] = the cache point ray r of point i reaches, or -1
+// when the ray does not count (no hit, back face, cell absent).  The frozen ray set defines a
+// fixed linear transport for the adjoint.
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_frozen(const DState s, const DStatic g, const Grid grid, const DevCache c, const FrameParams p,
+                                                  uint32_t seed, int K, int* __restrict__ hits) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= p.Np) return;
+    uint32_t rs = hash32(seed ^ hash32(i + 1));
+    const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
+    for (int r = 0; r < K; ++r) {
+        const float u1 = rnd(rs);
+        const float u2 = rnd(rs);
+        const f3 D = cosine_dir(N, u1, u2);
+        const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+        hits[(size_t)i * K + r] = h.back ? -1 : h.pi;
+    }
+}
+
 // ------------------------------------------------------------------ launch wrappers
 
 static int grid_of(int Np) { return (Np + BLOCK - 1) / BLOCK; }
@@ -1248,6 +1272,16 @@ cudaError_t Ops<NL>::pretrace(const DState& s, const DStatic& g, const Grid& gri
     cudaError_t e = prep_smem(k_pretrace<NL>, smem);
     if (e != cudaSuccess) return e;
     k_pretrace<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, out);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::frozen_hits(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                                 uint32_t seed, int K, int* hits, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+    cudaError_t e = prep_smem(k_frozen<NL>, smem);
+    if (e != cudaSuccess) return e;
+    k_frozen<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, seed, K, hits);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/rc_api.h"
+#include "rc_adjoint.h"
 #include "rc_internal.h"
 
 using namespace rc;
@@ -58,6 +59,7 @@ struct Scene {
     Grid grid{};
     std::vector<HostState> st;
     DStatic g{};
+    const float* L = nullptr;       // device light positions, 3 floats per light
     // events: [pair * (1 + NL) + 0] = occluder voxels, [.. + 1 + l] = voxels of light l
     std::vector<std::vector<int>> ev;
     std::vector<const int*> ev_dev;
@@ -85,7 +87,9 @@ struct rc_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::string err;
-    std::vector<DevBuf> scene_bufs, cache_bufs;
+    std::vector<DevBuf> scene_bufs, cache_bufs, adj_bufs;
+    int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
+    rc::adj::Bufs adj{};
     Scene S;
     bool have_scene = false;
     DevCache c{};
@@ -447,6 +451,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     const float* dL = nullptr;
     if ((s = dput(ctx, pool, &dL, L)) || (s = dput_raw(ctx, pool, &g.A, A, Np)) || (s = dput_raw(ctx, pool, &g.region, region, Np)))
         return s;
+    S.L = dL;
     // region ids index the per-region statistics; checked on the device (no frame runs before
     // the load has read the result back)
     k_load_check<<<load_grid(Np), 256, 0, ctx->stream>>>(g.region, Np, 0, S.NR, ctx->flags_dev + 2, LOAD_BAD_REGION);
@@ -1002,6 +1007,7 @@ void rc_destroy(rc_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_pool(ctx->cache_bufs);
     free_pool(ctx->scene_bufs);
+    free_pool(ctx->adj_bufs);
     if (ctx->flags_dev) cudaFree(ctx->flags_dev);
     if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
@@ -1033,6 +1039,8 @@ rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
     CKR(cudaStreamSynchronize(ctx->stream));
     free_pool(ctx->cache_bufs);
     free_pool(ctx->scene_bufs);
+    free_pool(ctx->adj_bufs);
+    ctx->adj_np = ctx->adj_k = 0;
     ctx->have_scene = false;
     ctx->run.active = false;
     ctx->c = DevCache{};
@@ -1506,6 +1514,86 @@ rc_status rc_reference_build(rc_ctx* ctx, const rc_ref_params* prm, double* nois
         CKR(cudaStreamSynchronize(st));
     }
     S.has_ref = 1;
+    return RC_OK;
+}
+
+rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* weights, float* dJ_dE, rc_adjoint_result* res) {
+    if (!ctx || !prm || !weights || !dJ_dE || prm->K < 1 || prm->K > 1024 || prm->iterations < 0) return RC_ERR_ARG;
+    if (!ctx->have_scene) return fail(ctx, RC_ERR_STATE, "no scene loaded");
+    Scene& S = ctx->S;
+    if (prm->state < 0 || prm->state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", prm->state);
+    if ((long long)S.Np * prm->K >= (1ll << 31)) return fail(ctx, RC_ERR_ARG, "Np * K must stay below 2^31");
+    if (S.NL + 1 > adj::MAX_COLS) return fail(ctx, RC_ERR_UNSUPPORTED, "%d lights", S.NL);
+    CKR(cudaSetDevice(ctx->cfg.device));
+    cudaStream_t st = ctx->stream;
+    CKR(cudaStreamSynchronize(st));
+    free_pool(ctx->adj_bufs);
+    ctx->adj_np = ctx->adj_k = 0;
+    const size_t Np = (size_t)S.Np, K = (size_t)prm->K;
+    const int NL = S.NL, AES = aes_of(NL), iters = prm->iterations ? prm->iterations : 64;
+    auto& pool = ctx->adj_bufs;
+    adj::Bufs b{};
+    rc_status s;
+    if ((s = dalloc(ctx, pool, &b.hits, Np * K)) || (s = dalloc(ctx, pool, &b.cnt, Np + 1)) || (s = dalloc(ctx, pool, &b.off, Np + 1)) ||
+        (s = dalloc(ctx, pool, &b.fill, Np)) || (s = dalloc(ctx, pool, &b.src, Np * K)) ||
+        (s = dalloc(ctx, pool, &b.scratch, adj::scan_scratch_ints((long long)Np + 1))) || (s = dalloc(ctx, pool, &b.da, Np)) ||
+        (s = dalloc(ctx, pool, &b.L[0], Np)) || (s = dalloc(ctx, pool, &b.L[1], Np)) || (s = dalloc(ctx, pool, &b.u[0], Np)) ||
+        (s = dalloc(ctx, pool, &b.u[1], Np)) || (s = dalloc(ctx, pool, &b.w, Np)) ||
+        (s = dalloc(ctx, pool, &b.part, (size_t)adj::GRAD_BLOCKS * (NL + 1))) || (s = dalloc(ctx, pool, &b.stats, 1)))
+        return s;
+    // scratch of this call only: the unordered ray lists and the unit-emission direct light
+    std::vector<DevBuf> tmp;
+    struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
+    float4* AEu = nullptr;
+    uint32_t* SVu = nullptr;
+    const float* ones = nullptr;
+    if ((s = dalloc(ctx, tmp, &b.unordered, Np * K)) || (s = dalloc(ctx, tmp, &AEu, (size_t)AES / 4 * Np)) ||
+        (s = dalloc(ctx, tmp, &SVu, (size_t)ctx->NW * Np)) || (s = dput(ctx, tmp, &ones, std::vector<float>((size_t)NL, 1.f))))
+        return s;
+    const DState& d = S.st[prm->state].d;
+    FrameParams p{};
+    p.Np = S.Np;
+    CKR(cudaMemcpyAsync(b.w, weights, Np * 4, cudaMemcpyHostToDevice, st));
+    CKR(RC_DISPATCH(NL, frozen_hits(d, S.g, S.grid, ctx->c, p, prm->seed, prm->K, b.hits, st)));
+    CKR(RC_DISPATCH(NL, build(ctx->NW, d, S.g, S.grid, S.L, ones, AEu, SVu, S.Np, ctx->flags_dev, st)));
+    CKR(adj::build_transpose(b, S.Np, prm->K, st));
+    CKR(adj::solve(&b, S.Np, prm->K, NL, AES, reinterpret_cast<const float*>(d.AE), reinterpret_cast<const float*>(AEu), iters, st));
+    adj::Stats hs{};
+    CKR(cudaMemcpyAsync(&hs, b.stats, sizeof hs, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    ctx->launches += 10 + 2 * iters;
+    const std::vector<float>& E = S.st[prm->state].inten;
+    double jg = 0.0;
+    for (int l = 0; l < NL; ++l) {
+        dJ_dE[l] = (float)hs.out[l];
+        jg += (double)E[l] * hs.out[l];
+    }
+    if (res) {
+        auto f = [](unsigned x) { float v; memcpy(&v, &x, 4); return (double)v; };
+        res->J = hs.out[NL];
+        res->J_grad = jg;
+        res->fwd_change = f(hs.chg[1]) > 0 ? f(hs.chg[0]) / f(hs.chg[1]) : 0.0;
+        res->adj_change = f(hs.chg[3]) > 0 ? f(hs.chg[2]) / f(hs.chg[3]) : 0.0;
+        res->rays = (long long)(Np * K);
+        res->back = (long long)hs.back;
+        res->max_incoming = hs.max_incoming;
+    }
+    b.unordered = nullptr;
+    ctx->adj = b;
+    ctx->adj_np = S.Np;
+    ctx->adj_k = prm->K;
+    return RC_OK;
+}
+
+rc_status rc_adjoint_arrays(rc_ctx* ctx, float* L, float* u, int* hits) {
+    if (!ctx) return RC_ERR_ARG;
+    if (!ctx->adj_np) return fail(ctx, RC_ERR_STATE, "no adjoint computed");
+    const size_t Np = (size_t)ctx->adj_np, K = (size_t)ctx->adj_k;
+    cudaStream_t st = ctx->stream;
+    if (L) CKR(cudaMemcpyAsync(L, ctx->adj.L_final, Np * 4, cudaMemcpyDeviceToHost, st));
+    if (u) CKR(cudaMemcpyAsync(u, ctx->adj.u_final, Np * 4, cudaMemcpyDeviceToHost, st));
+    if (hits) CKR(cudaMemcpyAsync(hits, ctx->adj.hits, Np * K * 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
     return RC_OK;
 }
 

@@ -38,7 +38,7 @@ EXPORTS = [
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
     "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
     "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
-    "rc_error_sums_noalloc", "rc_reference_build",
+    "rc_error_sums_noalloc", "rc_reference_build", "rc_adjoint", "rc_adjoint_arrays",
 ]
 NOALLOC_MAX_POINTS = 4194304
 
@@ -152,6 +152,11 @@ def load_library():
     L.rc_reference_build.argtypes = [vp, ctypes.POINTER(RefParams), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.rc_error_sums_noalloc.restype = i
     L.rc_error_sums_noalloc.argtypes = [vp, i, i, i, vp, vp, i, vp, vp]
+    L.rc_adjoint.restype = i
+    L.rc_adjoint.argtypes = [vp, ctypes.POINTER(AdjointParams), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                             ctypes.POINTER(AdjointResult)]
+    L.rc_adjoint_arrays.restype = i
+    L.rc_adjoint_arrays.argtypes = [vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -159,6 +164,16 @@ def load_library():
 class RefParams(ctypes.Structure):
     _fields_ = [("K", ctypes.c_int), ("warmup", ctypes.c_int), ("block", ctypes.c_int), ("max_iter", ctypes.c_int),
                 ("noise_target", ctypes.c_double)]
+
+
+class AdjointParams(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("K", ctypes.c_int), ("seed", ctypes.c_uint32), ("iterations", ctypes.c_int)]
+
+
+class AdjointResult(ctypes.Structure):
+    _fields_ = [("J", ctypes.c_double), ("J_grad", ctypes.c_double), ("fwd_change", ctypes.c_double),
+                ("adj_change", ctypes.c_double), ("rays", ctypes.c_longlong), ("back", ctypes.c_longlong),
+                ("max_incoming", ctypes.c_int)]
 
 
 class RCError(RuntimeError):
@@ -328,6 +343,29 @@ class Context:
         self._chk(self.L.rc_reference_build(self.h, ctypes.byref(prm), noise, iters))
         self._info = self.info()
         return list(noise), list(iters)
+
+    def adjoint(self, state: int, weights, K: int = 32, seed: int = 0, iterations: int = 64):
+        """dJ/dE per light for J = sum_i w_i sum_l L_l[i] over K frozen rays per point (rc_adjoint);
+        returns (gradient, result dict)."""
+        nl, np_ = self._info["nl"], self._info["np"]
+        w = np.ascontiguousarray(weights, np.float32)
+        if w.shape != (np_,):
+            raise ValueError("weights must have one entry per cache point")
+        g = (ctypes.c_float * nl)()
+        res = AdjointResult()
+        prm = AdjointParams(state, K, seed & 0xFFFFFFFF, iterations)
+        self._chk(self.L.rc_adjoint(self.h, ctypes.byref(prm), w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), g, ctypes.byref(res)))
+        self._adj_k = K
+        return np.array(g[:], np.float32), {n: getattr(res, n) for n, _ in AdjointResult._fields_}
+
+    def adjoint_arrays(self) -> tuple:
+        """(L, u, hits) of the last adjoint call: forward solution, importance, frozen hit points (Np x K)."""
+        np_ = self._info["np"]
+        L = np.empty(np_, np.float32)
+        u = np.empty(np_, np.float32)
+        h = np.empty((np_, self._adj_k), np.int32)
+        self._chk(self.L.rc_adjoint_arrays(self.h, L.ctypes.data, u.ctypes.data, h.ctypes.data))
+        return L, u, h
 
     def device_flags(self) -> int:
         v = ctypes.c_uint()

@@ -545,13 +545,23 @@ def street_mesh(buildings: int = 40, seed: int = 0, facade_cell: float = 2.0, si
     return V, np.array(albs, np.float32), np.zeros(len(tris), np.uint8)
 
 
-def street_scene(points: int = 20000, buildings: int = 8, seed: int = 0, facade_cell: float = 2.0, size: float = 60.0) -> Scene:
+def street_scene(points: int = 20000, buildings: int = 8, seed: int = 0, facade_cell: float = 2.0, size: float = 60.0,
+                 lights: int = 3) -> Scene:
     """Format-3 street scene: street_mesh + three lamp-post lights and the movable cube; five
     states as the reference's prep (lights {0,1} on, 1 off, cube moved, light 2 on first time,
-    light 0 off with the cube moved)."""
+    light 0 off with the cube moved).  With lights > 3 the extra lamps stand along the street
+    (4-6 m high, seeded), emission U[1, 50], on in every state."""
     V, alb, ds = street_mesh(buildings, seed, facade_cell, size)
-    L = np.array([[-size / 4, 0.0, 4.0], [0.0, 2.0, 4.0], [size / 4, -2.0, 4.0]], np.float32)
+    L = [[-size / 4, 0.0, 4.0], [0.0, 2.0, 4.0], [size / 4, -2.0, 4.0]][:lights]
     I = [[20, 20, 0], [0, 20, 0], [20, 20, 0], [20, 20, 20], [0, 20, 0]]
+    I = [row[:lights] for row in I]
+    if lights > 3:
+        rng = np.random.default_rng(seed + 1000)
+        for _ in range(lights - 3):
+            L.append([rng.uniform(-size / 2 + 2, size / 2 - 2), rng.uniform(-5.0, 5.0), rng.uniform(4.0, 6.0)])
+        extra = rng.uniform(1.0, 50.0, lights - 3).round(3).tolist()
+        I = [row + extra for row in I]
+    L = np.array(L, np.float32)
     box = [(-2.0, 0.0, 1.0), (-2.0, 0.0, 1.0), (4.0, -1.0, 1.0), (-2.0, 0.0, 1.0), (4.0, -1.0, 1.0)]
     return mesh_scene(V, alb, ds, L, I, box, 1.0, points, seed)
 
