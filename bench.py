@@ -48,9 +48,11 @@ def parse():
     ap.add_argument("--method", default=METHOD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=12)
-    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp"], default=None,
-                    help="no timing: run --steps frames of state 0 (frame) or three resolve passes of the "
-                         "hash-grid table (hashgrid), for an ncu capture, and exit")
+    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp", "adjoint"], default=None,
+                    help="no timing: run --steps frames of state 0 (frame), three resolve passes of the "
+                         "hash-grid table (hashgrid), two inference and training passes of the MLP (mlp) or "
+                         "one 16-sweep adjoint of a 16-light room of --points points (adjoint), for an ncu "
+                         "capture, and exit")
     return ap.parse_args()
 
 
@@ -72,6 +74,14 @@ def profile_run(args):
     if args.profile == "mlp":
         mlp_bench(torch.cuda.current_stream(), reps=2)
         torch.cuda.synchronize()
+        return
+    if args.profile == "adjoint":
+        import numpy as np
+        ctx = N.Context()
+        info = ctx.load_bytes(S.write(S.box_room(points=args.points, seed=0, lights=16)))
+        w = np.full(info["np"], 1.0 / info["np"], np.float32)
+        ctx.adjoint(0, w, K=16, seed=5, iterations=16)
+        ctx.close()
         return
     from render_engine_gb300 import hashgrid as H
     cap, live = 1 << 24, 1 << 23
@@ -459,6 +469,8 @@ def mlp_bench(stream, npoints=1_082_802, batch=1 << 16, reps=10):
     import torch
     from render_engine_gb300 import mlp as MLP
 
+    if stream.cuda_stream == 0:   # a null handle would make the library use a stream of its own
+        stream = torch.cuda.Stream()
     g = torch.Generator(device="cuda")
     g.manual_seed(11)
     P = (torch.rand(npoints, 4, device="cuda", generator=g) * torch.tensor([8.0, 4.0, 3.0, 0.0], device="cuda")).contiguous()

@@ -244,6 +244,30 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
  * hit points (Np * K ints, ray r of point i at i * K + r, -1 = not counted).  Synchronises. */
 rc_status rc_adjoint_arrays(rc_ctx* ctx, float* L, float* u, int* hits);
 
+/* Screen-space temporal accumulator of the reference's `taa` mode (poc_gpu.cu:1047-1282): every
+ * cache point is a pixel that gets one unbiased sample per frame (one cosine ray; radiance at
+ * the hit = A x (direct + converged reference)), blended into a history with a 3x3
+ * neighbourhood clamp; a reactive mask (history rejected for 4 frames, replaced by the
+ * neighbourhood mean) comes from none, a blind per-zone test, the dependency masks, the
+ * dependency masks verified over two frames, or the references (oracle).  Format-2 scenes with
+ * references only, as in the reference.  The state is separate from rc_run_begin's. */
+typedef struct {
+    float alpha;        /* history blend (0.05 .. 0.2) */
+    float gamma;        /* neighbourhood clamp in standard deviations (0 = none) */
+    int mask;           /* 0 none, 1 blind zones, 2 dependencies, 3 dependencies verified, 4 oracle */
+} rc_taa_method;
+/* Start: history = the converged reference of first_state, masks and counters cleared;
+ * `seed` is the per-run seed of the samples (the reference uses 5000 + seed index). */
+rc_status rc_taa_begin(rc_ctx* ctx, const rc_taa_method* m, int first_state, uint32_t seed);
+/* One frame in `state` (event handling when the state changed).  With err != NULL the frame's
+ * error sqrt(sum (H - ref)^2 / n) / (sum ref / n) over valid points is returned (synchronises). */
+rc_status rc_taa_frame(rc_ctx* ctx, int state, float* err);
+/* TAA arrays (host copies, `nbytes` exactly the array's size; to_device = 1 writes the array):
+ * per point x (float), H (float), mu, sg (float), react (int32), pend (uint8), and the
+ * word-major dependency masks cur, prev (NW uint32 words per point, word w of point i at w*Np+i). */
+enum { RC_T_X = 0, RC_T_H, RC_T_MU, RC_T_SG, RC_T_REACT, RC_T_PEND, RC_T_CUR, RC_T_PREV, RC_T_COUNT };
+rc_status rc_taa_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, int to_device);
+
 /* Error sums without any device allocation.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory themselves -- a renderer whose per-frame path
  * runs under a budget fixed at start-up (cudaMalloc / cudaFree synchronise the device and can

@@ -79,6 +79,14 @@ def lib():
         L.osc_probe_rays.restype = ctypes.c_int
         L.osc_probe_rays.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(RayRec), ctypes.c_int]
+        L.osc_taa_new.restype = ctypes.c_void_p
+        L.osc_taa_new.argtypes = [ctypes.c_void_p]
+        L.osc_taa_free.argtypes = [ctypes.c_void_p]
+        L.osc_taa_begin.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_uint32]
+        L.osc_taa_frame.restype = ctypes.c_int
+        L.osc_taa_frame.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float)]
+        L.osc_taa_array.restype = ctypes.c_void_p
+        L.osc_taa_array.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
         L.osc_frozen_hits.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p]
         L.osc_direct_unit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.osc_path_trace.restype = ctypes.c_int
@@ -216,4 +224,45 @@ class Run:
     def __del__(self):
         if getattr(self, "p", None):
             lib().osc_run_free(self.p)
+            self.p = None
+
+
+class Taa:
+    """The taa mode of the reference (run_taa_mode, poc_gpu.cu:1175-1282) on the CPU."""
+
+    DT = {0: np.float32, 1: np.float32, 2: np.float32, 3: np.float32, 4: np.int32, 5: np.uint8, 6: np.uint32, 7: np.uint32}
+
+    def __init__(self, scene: Scene):
+        if not scene.built:
+            scene.build()
+        self.scene = scene
+        self.p = lib().osc_taa_new(scene.p)
+        if not self.p:
+            raise ValueError("oracle: taa needs a format-2 scene with references")
+
+    def begin(self, alpha: float, gamma: float, mask: int, s0: int, seed: int):
+        lib().osc_taa_begin(self.p, alpha, gamma, mask, s0, seed & 0xFFFFFFFF)
+
+    def frame(self, state: int):
+        e3 = (ctypes.c_double * 3)()
+        e = ctypes.c_float()
+        if lib().osc_taa_frame(self.p, state, e3, ctypes.byref(e)) != 0:
+            raise ValueError("oracle: taa frame")
+        return float(e.value), np.array(e3[:])
+
+    def array(self, which: int) -> np.ndarray:
+        nb = ctypes.c_size_t()
+        ptr = lib().osc_taa_array(self.p, which, ctypes.byref(nb))
+        return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)), (nb.value,)).view(self.DT[which]).copy()
+
+    def set_array(self, which: int, value: np.ndarray):
+        nb = ctypes.c_size_t()
+        ptr = lib().osc_taa_array(self.p, which, ctypes.byref(nb))
+        v = np.ascontiguousarray(value, self.DT[which]).reshape(-1)
+        assert v.nbytes == nb.value
+        ctypes.memmove(ptr, v.ctypes.data, v.nbytes)
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            lib().osc_taa_free(self.p)
             self.p = None

@@ -48,6 +48,12 @@ def lib():
         L.ref_scalar.argtypes = [vp, i, i, i]
         L.ref_state_array.restype = i
         L.ref_state_array.argtypes = [vp, i, i, vp, sz]
+        L.ref_taa_begin.restype = i
+        L.ref_taa_begin.argtypes = [vp, ctypes.c_float, ctypes.c_float, i, i, ctypes.c_uint32]
+        L.ref_taa_frame.restype = i
+        L.ref_taa_frame.argtypes = [vp, i, ctypes.POINTER(ctypes.c_float)]
+        L.ref_taa_array.restype = i
+        L.ref_taa_array.argtypes = [vp, i, vp, sz, i]
         _lib = L
     return _lib
 
@@ -121,6 +127,27 @@ class RefRunner:
         a = np.empty(n, np.float32 if which == 0 else np.uint32)
         if self.L.ref_state_array(self.p, state, which, a.ctypes.data_as(ctypes.c_void_p), a.nbytes) != 0:
             raise RuntimeError("state array")
+        return a
+
+    # taa mode (run_taa_mode, poc_gpu.cu:1175-1282)
+    _TAA_DT = {0: np.float32, 1: np.float32, 2: np.float32, 3: np.float32, 4: np.int32, 5: np.uint8, 6: np.uint32, 7: np.uint32}
+
+    def taa_begin(self, alpha: float, gamma: float, mask: int, s0: int, seed: int):
+        if self.L.ref_taa_begin(self.p, alpha, gamma, mask, s0, seed & 0xFFFFFFFF) != 0:
+            raise RuntimeError(self.L.ref_last_error(self.p).decode())
+
+    def taa_frame(self, state: int) -> float:
+        e = ctypes.c_float()
+        if self.L.ref_taa_frame(self.p, state, ctypes.byref(e)) != 0:
+            raise RuntimeError(self.L.ref_last_error(self.p).decode())
+        return float(e.value)
+
+    def taa_array(self, which: int, value: np.ndarray | None = None) -> np.ndarray:
+        n = self.Np * (self.NW if which in (6, 7) else 1)
+        dt = self._TAA_DT[which]
+        a = np.empty(n, dt) if value is None else np.ascontiguousarray(value, dt).reshape(-1)
+        if self.L.ref_taa_array(self.p, which, a.ctypes.data_as(ctypes.c_void_p), a.nbytes, 0 if value is None else 1) != 0:
+            raise RuntimeError(self.L.ref_last_error(self.p).decode())
         return a
 
     def close(self):

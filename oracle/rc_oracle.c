@@ -1368,3 +1368,251 @@ int osc_path_trace(const osc_scene* S, int si, const int* pts, int npts, int pat
     free(dir);
     return 0;
 }
+
+/* ------------------------------------------------------------------ taa mode
+ * run_taa_mode (poc_gpu.cu:1175-1282) and its kernels k_taa_* (:1062-1166), sequentially:
+ * region sums in point order, FP64 error sums in point order. */
+struct osc_taa {
+    osc_scene* S;
+    float *x, *H, *H2, *mu, *sg, *rs, *cnt;
+    int *nb, *react;
+    uint8_t* pend;
+    uint32_t *cur, *prev;
+    int** V; int* nV;       /* event voxels per state pair */
+    float alpha, gamma;
+    int mask, f, prev_state, verify_left;
+    uint32_t seed;
+};
+
+osc_taa* osc_taa_new(osc_scene* S) {
+    if (S->fmt != 2 || !S->has_ref) return NULL;   /* the scene must have been built (osc_build) */
+    osc_taa* t = (osc_taa*)calloc(1, sizeof(osc_taa));
+    const size_t Np = (size_t)S->Np, NW = (size_t)S->NW;
+    t->S = S;
+    t->x = (float*)calloc(Np, 4); t->H = (float*)calloc(Np, 4); t->H2 = (float*)calloc(Np, 4);
+    t->mu = (float*)calloc(Np, 4); t->sg = (float*)calloc(Np, 4);
+    t->rs = (float*)calloc(3 * (size_t)S->NR, 4); t->cnt = (float*)calloc((size_t)S->NR, 4);
+    t->nb = (int*)malloc(9 * Np * 4); t->react = (int*)calloc(Np, 4); t->pend = (uint8_t*)calloc(Np, 1);
+    t->cur = (uint32_t*)calloc(NW * Np, 4); t->prev = (uint32_t*)calloc(NW * Np, 4);
+    /* 3x3 neighbourhood on each quad's grid (poc_gpu.cu:1192-1203), state 0's grids */
+    for (size_t k = 0; k < 9 * Np; ++k) t->nb[k] = -1;
+    const ostate* s0 = &S->st[0];
+    for (int q = 0; q < S->Nq; ++q) {
+        int nu = s0->dims[2 * q], nv = s0->dims[2 * q + 1], o = s0->off[q];
+        for (int iv = 0; iv < nv; ++iv)
+            for (int iu = 0; iu < nu; ++iu) {
+                size_t i = (size_t)o + (size_t)iv * nu + iu;
+                int k = 0;
+                for (int dv = -1; dv <= 1; ++dv)
+                    for (int du = -1; du <= 1; ++du) {
+                        int a = iu + du, b = iv + dv;
+                        t->nb[9 * i + k++] = (a >= 0 && a < nu && b >= 0 && b < nv) ? o + b * nu + a : -1;
+                    }
+            }
+    }
+    /* event voxels: light voxels of changed intensities + occluders (poc_gpu.cu:1210-1219) */
+    const int NS = S->NS, NL = S->NL;
+    t->V = (int**)calloc((size_t)NS * NS, sizeof(int*));
+    t->nV = (int*)calloc((size_t)NS * NS, sizeof(int));
+    for (int a = 0; a < NS; ++a)
+        for (int b = 0; b < NS; ++b) {
+            if (a == b) continue;
+            int fine[64], nf = 0;
+            for (int l = 0; l < NL && nf < 64; ++l)
+                if (S->st[a].inten[l] != S->st[b].inten[l]) {
+                    const float* p = S->L + 3 * (size_t)l;
+                    int i = imin(imax((int)(p[0] / 8.f * 16), 0), 15), j = imin(imax((int)(p[1] / 4.f * 8), 0), 7),
+                        k = imin(imax((int)(p[2] / 3.f * 6), 0), 5);
+                    fine[nf++] = (k * 8 + j) * 16 + i;
+                }
+            int ng = 0;
+            int* g = to_grid(S, fine, nf, &ng);
+            const int pe = a * NS + b, no = S->nev[pe * (1 + NL)];
+            const int* occ = S->ev[pe * (1 + NL)];
+            char* mark = (char*)calloc((size_t)S->NV, 1);
+            for (int k = 0; k < ng; ++k) mark[g[k]] = 1;
+            for (int k = 0; k < no; ++k) mark[occ[k]] = 1;
+            free(g);
+            int n = 0;
+            for (int v = 0; v < S->NV; ++v) n += mark[v];
+            t->V[pe] = (int*)malloc(sizeof(int) * (size_t)(n ? n : 1));
+            n = 0;
+            for (int v = 0; v < S->NV; ++v) if (mark[v]) t->V[pe][n++] = v;
+            t->nV[pe] = n;
+            free(mark);
+        }
+    return t;
+}
+
+void osc_taa_free(osc_taa* t) {
+    if (!t) return;
+    for (int e = 0; e < t->S->NS * t->S->NS; ++e) free(t->V[e]);
+    free(t->V); free(t->nV);
+    free(t->x); free(t->H); free(t->H2); free(t->mu); free(t->sg); free(t->rs); free(t->cnt);
+    free(t->nb); free(t->react); free(t->pend); free(t->cur); free(t->prev);
+    free(t);
+}
+
+void osc_taa_begin(osc_taa* t, float alpha, float gamma, int mask, int s0, uint32_t seed) {
+    const size_t Np = (size_t)t->S->Np, NW = (size_t)t->S->NW;
+    memcpy(t->H, t->S->st[s0].ref, Np * 4);
+    memset(t->react, 0, Np * 4);
+    memset(t->pend, 0, Np);
+    memset(t->cur, 0, NW * Np * 4);
+    memset(t->prev, 0, NW * Np * 4);
+    t->alpha = alpha; t->gamma = gamma; t->mask = mask; t->seed = seed;
+    t->f = 0; t->prev_state = s0; t->verify_left = 0;
+}
+
+/* k_taa_zone_acc + k_count_zone (poc_gpu.cu:1111-1118, 1129-1134) */
+static void taa_zone_acc(osc_taa* t, int only_pending) {
+    const osc_scene* S = t->S;
+    for (int i = 0; i < S->Np; ++i) {
+        if (only_pending && !t->pend[i]) continue;
+        float d = t->x[i] - t->H[i];
+        int r = S->region[i];
+        t->rs[3 * r] += d; t->rs[3 * r + 1] += d * d; t->rs[3 * r + 2] += t->H[i];
+        t->cnt[r] += 1.f;
+    }
+}
+/* k_taa_zone_decide (poc_gpu.cu:1119-1128) */
+static void taa_zone_decide(osc_taa* t, int only_pending, int rf, int clear_pending) {
+    const osc_scene* S = t->S;
+    for (int i = 0; i < S->Np; ++i) {
+        if (only_pending && !t->pend[i]) continue;
+        int r = S->region[i];
+        float n = t->cnt[r];
+        if (n >= 8.f) {
+            float m = t->rs[3 * r] / n, se = sqrtf(fmaxf(t->rs[3 * r + 1] / n - m * m, 0.f) / n), base = t->rs[3 * r + 2] / n;
+            if (fabsf(m) > 2.f * se && fabsf(m) > 0.05f * fmaxf(base, 1e-3f)) t->react[i] = rf;
+        }
+        if (clear_pending) t->pend[i] = 0;
+    }
+}
+
+/* One frame of the loop of run_taa_mode (poc_gpu.cu:1246-1274). */
+int osc_taa_frame(osc_taa* t, int si, double err3[3], float* err) {
+    osc_scene* S = t->S;
+    if (si < 0 || si >= S->NS) return -1;
+    const int Np = S->Np, NW = S->NW, NL = S->NL, f = t->f, mask = t->mask, RF = 4;
+    const float ALPHA_R = 0.5f;
+    const ostate* st = &S->st[si];
+    const int deps = mask == 2 || mask == 3;
+    if (deps && f % 32 == 0) {
+        uint32_t* x = t->cur; t->cur = t->prev; t->prev = x;
+        memset(t->cur, 0, (size_t)NW * Np * 4);
+    }
+    /* k_taa_pt (poc_gpu.cu:1062-1098) */
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < Np; ++i) {
+        uint32_t rs = hash32(t->seed * 0x9E3779B9u ^ hash32((uint32_t)f * 0x85EBCA6Bu ^ hash32((uint32_t)i + 7u)));
+        v3 P = vld(st->P, i), N = vld(st->N, i), O = vadd(P, vmul(N, 1e-3f));
+        float u1 = rnd(&rs);
+        float u2 = rnd(&rs);
+        v3 D = cosine_dir(N, u1, u2);
+        float tt;
+        int q, pi;
+        int hit = trace_full(S, st, O, D, &tt, &q);
+        v3 H = hit ? vadd(O, vmul(D, tt)) : O;
+        int back = resolve_hit(S, st, hit, H, D, q, i, &pi);
+        float v = 0.f;
+        if (!back) {
+            float ed = 0.f;
+            for (int l = 0; l < NL; ++l) ed += st->Edir[(size_t)NL * pi + l];
+            v = S->A[pi] * (ed + st->ref[pi]);
+        }
+        t->x[i] = v;
+        if (deps) {
+            uint32_t m[64];
+            const uint32_t* sv = st->SV + (size_t)NW * (back ? i : pi);
+            for (int w = 0; w < NW; ++w) m[w] = sv[w];
+            dda(S, O, H, m);
+            for (int w = 0; w < NW; ++w) t->cur[(size_t)w * Np + i] |= m[w];
+        }
+    }
+    if (f > 0 && t->prev_state != si) {
+        const int pe = t->prev_state * S->NS + si;
+        if (mask == 2 || mask == 3) {   /* k_taa_touch (poc_gpu.cu:1136-1145) */
+            for (int i = 0; i < Np; ++i) {
+                int hitv = 0;
+                for (int j = 0; j < t->nV[pe] && !hitv; ++j) {
+                    int v = t->V[pe][j];
+                    size_t o = (size_t)(v >> 5) * Np + i;
+                    hitv = ((t->cur[o] | t->prev[o]) >> (v & 31)) & 1u;
+                }
+                if (!hitv) continue;
+                if (mask == 3) t->pend[i] = 1;
+                else t->react[i] = RF;
+            }
+            if (mask == 3) {
+                t->verify_left = 2;
+                memset(t->rs, 0, 12 * (size_t)S->NR);
+                memset(t->cnt, 0, 4 * (size_t)S->NR);
+            }
+        }
+        if (mask == 4) {   /* k_taa_oracle (poc_gpu.cu:1146-1150) */
+            const float* ro = S->st[t->prev_state].ref;
+            for (int i = 0; i < Np; ++i)
+                if (fabsf(st->ref[i] - ro[i]) / (ro[i] + 1e-2f) > 0.10f) t->react[i] = RF;
+        }
+    }
+    if (mask == 1) {
+        memset(t->rs, 0, 12 * (size_t)S->NR);
+        memset(t->cnt, 0, 4 * (size_t)S->NR);
+        taa_zone_acc(t, 0);
+        taa_zone_decide(t, 0, RF, 0);
+    }
+    if (mask == 3 && t->verify_left > 0) {
+        taa_zone_acc(t, 1);
+        if (--t->verify_left == 0) taa_zone_decide(t, 1, RF, 1);
+    }
+    /* k_taa_stats + k_taa_update (poc_gpu.cu:1100-1108, 1152-1159) */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < Np; ++i) {
+        float s1 = 0.f, s2 = 0.f;
+        int n = 0;
+        for (int k = 0; k < 9; ++k) {
+            int j = t->nb[9 * (size_t)i + k];
+            if (j < 0) continue;
+            float v = t->x[j];
+            s1 += v;
+            s2 += v * v;
+            n++;
+        }
+        float mu = s1 / (float)n;
+        float sg = sqrtf(fmaxf(s2 / (float)n - mu * mu, 0.f));
+        t->mu[i] = mu; t->sg[i] = sg;
+        float h = t->H[i];
+        if (t->gamma > 0.f) { float lo = mu - t->gamma * sg, hi = mu + t->gamma * sg; h = fminf(fmaxf(h, lo), hi); }
+        float a = t->alpha, target = t->x[i];
+        if (t->react[i] > 0) { a = ALPHA_R; t->react[i]--; target = mu; }
+        t->H2[i] = h + a * (target - h);
+    }
+    { float* x = t->H; t->H = t->H2; t->H2 = x; }
+    /* k_taa_err (poc_gpu.cu:1160-1166) */
+    double d2 = 0, rsum = 0, c = 0;
+    for (int i = 0; i < Np; ++i)
+        if (st->valid[i]) { double e = t->H[i] - st->ref[i]; d2 += e * e; rsum += st->ref[i]; c += 1; }
+    if (err3) { err3[0] = d2; err3[1] = rsum; err3[2] = c; }
+    if (err) *err = (float)(sqrt(d2 / c) / (rsum / c));
+    t->prev_state = si;
+    t->f = f + 1;
+    return 0;
+}
+
+/* 0 x, 1 H, 2 mu, 3 sg, 4 react, 5 pend, 6 cur, 7 prev */
+void* osc_taa_array(osc_taa* t, int which, size_t* nbytes) {
+    const size_t Np = (size_t)t->S->Np, NW = (size_t)t->S->NW;
+    switch (which) {
+        case 0: *nbytes = 4 * Np; return t->x;
+        case 1: *nbytes = 4 * Np; return t->H;
+        case 2: *nbytes = 4 * Np; return t->mu;
+        case 3: *nbytes = 4 * Np; return t->sg;
+        case 4: *nbytes = 4 * Np; return t->react;
+        case 5: *nbytes = Np; return t->pend;
+        case 6: *nbytes = 4 * NW * Np; return t->cur;
+        case 7: *nbytes = 4 * NW * Np; return t->prev;
+    }
+    *nbytes = 0;
+    return NULL;
+}

@@ -88,6 +88,15 @@ void osc_direct_unit(const osc_scene* s, int si, float* out);
 int osc_path_trace(const osc_scene* s, int si, const int* pts, int npts, int paths, int min_bounces, uint64_t seed, double* mean,
                    double* sem);
 
+/* taa mode (run_taa_mode, poc_gpu.cu:1175-1282): format-2 scenes with references. */
+typedef struct osc_taa osc_taa;
+osc_taa* osc_taa_new(osc_scene* s);
+void osc_taa_free(osc_taa* t);
+void osc_taa_begin(osc_taa* t, float alpha, float gamma, int mask, int s0, uint32_t seed);
+int osc_taa_frame(osc_taa* t, int si, double err3[3], float* err);
+/* 0 x, 1 H, 2 mu, 3 sg, 4 react, 5 pend, 6 cur, 7 prev (host memory of the oracle) */
+void* osc_taa_array(osc_taa* t, int which, size_t* nbytes);
+
 enum {
     OSC_A_LC = 0, OSC_A_LC2, OSC_A_M, OSC_A_N, OSC_A_C0, OSC_A_KK, OSC_A_PENDING, OSC_A_CUR, OSC_A_PREV,
     OSC_A_STALE, OSC_A_AGE, OSC_A_SNAP, OSC_A_NEQ, OSC_A_COEF, OSC_A_RSTAT, OSC_A_DSTAT, OSC_A_SUMPR,

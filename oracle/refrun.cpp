@@ -4,8 +4,9 @@
 // reference checkout) into a device-only cubin under oracle/_ref/.  This file loads that
 // cubin with the CUDA driver API and runs its kernels (k_build, k_trace2<DEPS>, k_decide,
 // k_update, k_sumpr, k_touched, k_wake, k_rescale, k_restored, k_proj_apply, k_oracle,
-// k_error) with the host logic of the reference's load() and Runner::run
-// (poc_gpu.cu:751-801, 826-1016) restated here, including its per-frame event timing.
+// k_error, and the taa mode's k_taa_*) with the host logic of the reference's load(),
+// Runner::run and run_taa_mode (poc_gpu.cu:751-801, 826-1016, 1175-1282) restated here,
+// including its per-frame event timing.
 // The kernel argument structs below mirror the reference's DevState / Cache / Params
 // (poc_gpu.cu:222-237, 394-422) field for field, since the kernels read them by value.
 //
@@ -71,6 +72,16 @@ struct HostState {
 
 struct Timers { double trace = 0, decide = 0, update = 0, swap = 0, event = 0; int frames = 0, events = 0; };
 
+struct Taa {   // poc_gpu.cu:1051-1060
+    float *x, *H, *H2, *mu, *sg;
+    int* nb;
+    int* react;
+    uint8_t* pend;
+    uint32_t *cur, *prev;
+    float* rs;
+    double* err;
+};
+
 }  // namespace
 
 struct ref_ctx {
@@ -99,6 +110,17 @@ struct ref_ctx {
     float nmax = 0.f;
     CUevent ev[6] = {};
     bool loaded = false;
+    // taa mode (run_taa_mode, poc_gpu.cu:1175-1282)
+    CUfunction f_taa_pt[2], f_taa_stats, f_taa_zacc, f_taa_zdec, f_taa_count, f_taa_touch, f_taa_oracle, f_taa_update, f_taa_err;
+    std::vector<float> hL;
+    std::vector<int> hdims, hoff;
+    Taa taa{};
+    float* taa_cnt = nullptr;
+    std::vector<std::vector<int>> taaV;
+    std::vector<CUdeviceptr> dTaaV;
+    float taa_alpha = 0.1f, taa_gamma = 1.f;
+    int taa_mask = 0, taa_f = 0, taa_prev = 0, taa_verify = 0;
+    uint32_t taa_seed = 0;
 };
 
 namespace {
@@ -213,6 +235,16 @@ ref_ctx* ref_create(const char* cubin, int nl, char* err, int errlen) {
         {&r->f_proj, "_Z12k_proj_apply5Cache6ParamsPKi"},
         {&r->f_oracle, "_Z8k_oracle5CacheiPKfS1_"},
         {&r->f_error, "_Z7k_error5CacheiPKfPKhi"},
+        {&r->f_taa_pt[0], "_Z8k_taa_ptILb0EEv8DevState3TaaijjPKf"},
+        {&r->f_taa_pt[1], "_Z8k_taa_ptILb1EEv8DevState3TaaijjPKf"},
+        {&r->f_taa_stats, "_Z11k_taa_stats3Taai"},
+        {&r->f_taa_zacc, "_Z14k_taa_zone_acc3TaaiPKii"},
+        {&r->f_taa_zdec, "_Z17k_taa_zone_decide3TaaiPKiPKfiii"},
+        {&r->f_taa_count, "_Z12k_count_zoneiPKiPKhiPf"},
+        {&r->f_taa_touch, "_Z11k_taa_touch3TaaiPKiiii"},
+        {&r->f_taa_oracle, "_Z12k_taa_oracle3TaaiPKfS1_i"},
+        {&r->f_taa_update, "_Z12k_taa_update3Taaifff"},
+        {&r->f_taa_err, "_Z9k_taa_err3TaaiPKfPKh"},
     };
     for (auto& x : fns)
         if (cuModuleGetFunction(x.f, r->mod, x.n) != CUDA_SUCCESS) { seterr(x.n); delete r; return nullptr; }
@@ -257,6 +289,7 @@ int ref_load(ref_ctx* r, const void* data, size_t n) {
     CKD(cuMemcpyHtoD(r->c_lo, lo, 12), "c_lo");
     CKD(cuMemcpyHtoD(r->c_ext, ext, 12), "c_ext");
     auto L = rd.vec<float>(3 * (size_t)NL);
+    r->hL = L;
     auto A = rd.vec<float>(Np);
     auto region = rd.vec<int>(Np);
     r->st.assign(r->NS, HostState());
@@ -264,7 +297,9 @@ int ref_load(ref_ctx* r, const void* data, size_t n) {
         HostState& d = r->st[s];
         d.inten = rd.vec<float>(NL);
         d.P = put(r, rd.vec<float>(3 * Np)); d.N = put(r, rd.vec<float>(3 * Np)); d.Q = put(r, rd.vec<float>(12 * (size_t)r->Nq));
-        d.dims = put(r, rd.vec<int>(2 * (size_t)r->Nq)); d.off = put(r, rd.vec<int>((size_t)r->Nq));
+        auto dims = rd.vec<int>(2 * (size_t)r->Nq), off = rd.vec<int>((size_t)r->Nq);
+        if (s == 0) { r->hdims = dims; r->hoff = off; }   // poc_gpu.cu:783
+        d.dims = put(r, dims); d.off = put(r, off);
         d.T = put(r, rd.vec<float>(9 * (size_t)r->Nt)); d.TQ = put(r, rd.vec<int>((size_t)r->Nt));
         if (r->has_ref) { d.ref = put(r, rd.vec<float>(Np)); d.valid = put(r, rd.vec<uint8_t>(Np)); d.Pw = put(r, rd.vec<float>((size_t)NL * Np)); }
         d.Edir = alloc(r, 4 * (size_t)NL * Np); d.SV = alloc(r, 4 * (size_t)r->NW * Np);
@@ -551,6 +586,145 @@ int ref_frame(ref_ctx* r, int si, int want_err, float* errv, double* ms) {
     }
     r->f = f + 1;
     return have;
+}
+
+// ---------------------------------------------------------------- taa mode
+// Set-up of run_taa_mode (poc_gpu.cu:1189-1222) and the per-seed reset (:1241-1245).
+int ref_taa_begin(ref_ctx* r, float alpha, float gamma, int mask, int s0, uint32_t seed) {
+    if (!r->loaded || !r->has_ref || r->fmt != 2) { r->err = "taa: format-2 scene with references needed"; return -1; }
+    cuCtxSetCurrent(r->cu);
+    const size_t Np = r->Np;
+    Taa& t = r->taa;
+    if (!t.x) {
+        std::vector<int> nb(9 * Np, -1);
+        for (int q = 0; q < r->Nq; ++q) {
+            int nu = r->hdims[2 * q], nv = r->hdims[2 * q + 1], o = r->hoff[q];
+            for (int iv = 0; iv < nv; ++iv) for (int iu = 0; iu < nu; ++iu) {
+                size_t i = (size_t)o + (size_t)iv * nu + iu;
+                int k = 0;
+                for (int dv = -1; dv <= 1; ++dv) for (int du = -1; du <= 1; ++du) {
+                    int a = iu + du, b = iv + dv;
+                    nb[9 * i + k++] = (a >= 0 && a < nu && b >= 0 && b < nv) ? o + b * nu + a : -1;
+                }
+            }
+        }
+        t.x = (float*)alloc(r, 4 * Np); t.H = (float*)alloc(r, 4 * Np); t.H2 = (float*)alloc(r, 4 * Np);
+        t.mu = (float*)alloc(r, 4 * Np); t.sg = (float*)alloc(r, 4 * Np); t.nb = (int*)put(r, nb);
+        t.react = (int*)alloc(r, 4 * Np); t.pend = (uint8_t*)alloc(r, Np);
+        t.cur = (uint32_t*)alloc(r, 4 * r->NW * Np); t.prev = (uint32_t*)alloc(r, 4 * r->NW * Np);
+        t.rs = (float*)alloc(r, 12 * (size_t)r->NR); t.err = (double*)alloc(r, 24);
+        r->taa_cnt = (float*)alloc(r, 4 * (size_t)r->NR);
+        r->taaV.assign((size_t)r->NS * r->NS, {});
+        r->dTaaV.assign((size_t)r->NS * r->NS, 0);
+        for (int a = 0; a < r->NS; ++a) for (int b = 0; b < r->NS; ++b) {
+            if (a == b) continue;
+            std::vector<int> fine;
+            for (int l = 0; l < r->NL; ++l)
+                if (r->st[a].inten[l] != r->st[b].inten[l]) {   // host_vox_fine (poc_gpu.cu:1170-1173)
+                    const float* pl = &r->hL[3 * (size_t)l];
+                    int i = std::min(std::max(int(pl[0] / 8.f * 16), 0), 15), j = std::min(std::max(int(pl[1] / 4.f * 8), 0), 7),
+                        k = std::min(std::max(int(pl[2] / 3.f * 6), 0), 5);
+                    fine.push_back((k * 8 + j) * 16 + i);
+                }
+            std::vector<int> v = to_grid(r, fine);
+            for (int x : r->occ[a * r->NS + b]) v.push_back(x);
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+            r->taaV[a * r->NS + b] = v;
+            r->dTaaV[a * r->NS + b] = put(r, v.empty() ? std::vector<int>{0} : v);
+        }
+    }
+    CKD(cuMemcpyDtoD((CUdeviceptr)t.H, r->st[s0].ref, Np * 4), "taa history");
+    if (dzero(r, t.react, Np * 4) || dzero(r, t.pend, Np) || dzero(r, t.cur, r->NW * Np * 4) || dzero(r, t.prev, r->NW * Np * 4)) return -1;
+    r->taa_alpha = alpha; r->taa_gamma = gamma; r->taa_mask = mask; r->taa_seed = seed;
+    r->taa_f = 0; r->taa_prev = s0; r->taa_verify = 0;
+    return 0;
+}
+
+// One frame of run_taa_mode's loop (poc_gpu.cu:1246-1274); err (may be NULL) receives the frame's error.
+int ref_taa_frame(ref_ctx* r, int si, float* err) {
+    cuCtxSetCurrent(r->cu);
+    Taa& t = r->taa;
+    if (!t.x) { r->err = "no taa run"; return -1; }
+    const int G = grid_of(r), f = r->taa_f, mask = r->taa_mask, RF = 4;
+    const float ALPHA_R = 0.5f;
+    const size_t Np = r->Np;
+    int Npi = r->Np;
+    HostState& st = r->st[si];
+    const bool deps = mask == 2 || mask == 3;
+    if (deps && f % 32 == 0) { std::swap(t.cur, t.prev); if (dzero(r, t.cur, r->NW * Np * 4)) return -1; }
+    auto b = dev_state_bytes(r, st);
+    uint32_t seed = r->taa_seed, fr = (uint32_t)f;
+    CUdeviceptr dA = r->dA, reg = r->dRegion;
+    unsigned shm = r->Nt * 10 * 4;
+    if (launch(r, r->f_taa_pt[deps ? 1 : 0], G, shm, {b.data(), &t, &Npi, &seed, &fr, &dA}, "k_taa_pt")) return -1;
+    if (f > 0 && r->taa_prev != si) {
+        int pe = r->taa_prev * r->NS + si, nv = (int)r->taaV[pe].size(), rf = RF;
+        CUdeviceptr V = r->dTaaV[pe];
+        if (mask == 2) { int tp = 0; if (launch(r, r->f_taa_touch, G, 0, {&t, &Npi, &V, &nv, &rf, &tp}, "k_taa_touch")) return -1; }
+        if (mask == 3) {
+            int tp = 1;
+            if (launch(r, r->f_taa_touch, G, 0, {&t, &Npi, &V, &nv, &rf, &tp}, "k_taa_touch")) return -1;
+            r->taa_verify = 2;
+            if (dzero(r, t.rs, 12 * (size_t)r->NR) || dzero(r, r->taa_cnt, 4 * (size_t)r->NR)) return -1;
+        }
+        if (mask == 4) {
+            CUdeviceptr ro = r->st[r->taa_prev].ref, rn = st.ref;
+            if (launch(r, r->f_taa_oracle, G, 0, {&t, &Npi, &ro, &rn, &rf}, "k_taa_oracle")) return -1;
+        }
+    }
+    CUdeviceptr cnt = (CUdeviceptr)r->taa_cnt, pend = (CUdeviceptr)t.pend;
+    if (mask == 1) {
+        int zero = 0, rf = RF;
+        if (dzero(r, t.rs, 12 * (size_t)r->NR) || dzero(r, r->taa_cnt, 4 * (size_t)r->NR)) return -1;
+        if (launch(r, r->f_taa_zacc, G, 0, {&t, &Npi, &reg, &zero}, "k_taa_zone_acc")) return -1;
+        if (launch(r, r->f_taa_count, G, 0, {&Npi, &reg, &pend, &zero, &cnt}, "k_count_zone")) return -1;
+        if (launch(r, r->f_taa_zdec, G, 0, {&t, &Npi, &reg, &cnt, &zero, &rf, &zero}, "k_taa_zone_decide")) return -1;
+    }
+    if (mask == 3 && r->taa_verify > 0) {
+        int one = 1, rf = RF;
+        if (launch(r, r->f_taa_zacc, G, 0, {&t, &Npi, &reg, &one}, "k_taa_zone_acc")) return -1;
+        if (launch(r, r->f_taa_count, G, 0, {&Npi, &reg, &pend, &one, &cnt}, "k_count_zone")) return -1;
+        if (--r->taa_verify == 0)
+            if (launch(r, r->f_taa_zdec, G, 0, {&t, &Npi, &reg, &cnt, &one, &rf, &one}, "k_taa_zone_decide")) return -1;
+    }
+    if (launch(r, r->f_taa_stats, G, 0, {&t, &Npi}, "k_taa_stats")) return -1;
+    float al = r->taa_alpha, ar = ALPHA_R, ga = r->taa_gamma;
+    if (launch(r, r->f_taa_update, G, 0, {&t, &Npi, &al, &ar, &ga}, "k_taa_update")) return -1;
+    std::swap(t.H, t.H2);
+    if (dzero(r, t.err, 24)) return -1;
+    CUdeviceptr ref = st.ref, valid = st.valid;
+    if (launch(r, r->f_taa_err, G, 0, {&t, &Npi, &ref, &valid}, "k_taa_err")) return -1;
+    double h[3];
+    CKD(cuMemcpyDtoH(h, (CUdeviceptr)t.err, 24), "taa err");
+    if (err) *err = (float)(sqrt(h[0] / h[2]) / (h[1] / h[2]));
+    r->taa_prev = si;
+    r->taa_f = f + 1;
+    return 0;
+}
+
+// taa arrays: 0 x, 1 H, 2 mu, 3 sg, 4 react, 5 pend, 6 cur, 7 prev (layouts of rc_taa_array_copy)
+int ref_taa_array(ref_ctx* r, int which, void* host, size_t nbytes, int to_device) {
+    cuCtxSetCurrent(r->cu);
+    Taa& t = r->taa;
+    const size_t Np = r->Np, NW = r->NW;
+    void* p = nullptr;
+    size_t n = 0;
+    switch (which) {
+        case 0: p = t.x; n = 4 * Np; break;
+        case 1: p = t.H; n = 4 * Np; break;
+        case 2: p = t.mu; n = 4 * Np; break;
+        case 3: p = t.sg; n = 4 * Np; break;
+        case 4: p = t.react; n = 4 * Np; break;
+        case 5: p = t.pend; n = Np; break;
+        case 6: p = t.cur; n = 4 * NW * Np; break;
+        case 7: p = t.prev; n = 4 * NW * Np; break;
+        default: r->err = "taa array"; return -1;
+    }
+    if (!p || nbytes != n) { r->err = "taa array size"; return -1; }
+    if (to_device) CKD(cuMemcpyHtoD((CUdeviceptr)p, host, n), "taa array");
+    else CKD(cuMemcpyDtoH(host, (CUdeviceptr)p, n), "taa array");
+    return 0;
 }
 
 int ref_sync(ref_ctx* r) { cuCtxSetCurrent(r->cu); CKD(cuCtxSynchronize(), "sync"); return 0; }

@@ -63,7 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, deps):
             jobs.append([nv, *ARCH, *FLAGS, "-DRC_NL_ONE=%d" % nl, "-c", os.path.join(CSRC, "rc_kernels.cu"), "-o", o])
-    for name in ("rc_runtime", "rc_adjoint", "rc_noalloc", "rc_hashgrid", "rc_mlp"):
+    for name in ("rc_runtime", "rc_adjoint", "rc_taa", "rc_noalloc", "rc_hashgrid", "rc_mlp"):
         o = os.path.join(OUT, name + ".o")
         objs.append(o)
         if force or _stale(o, deps):

@@ -6,6 +6,7 @@
 //   poc_gpu_l3 scenf   <scene.bin> <nseeds> <scenarios.txt> [baseline budget]
 //   poc_gpu_l3 quality <scene.bin> <nseeds> <budget1,budget2,...>
 //   poc_gpu_l3 recon   <scene.bin> <nseeds>
+//   poc_gpu_l3 taa     <scene.bin> <nseeds> <scenarios.txt>
 //
 // Same JSONL lines on stdout, same environment variables (BENCH_RAYONS, BENCH_DEBUG), so
 // cuda/run_cuda.sh and cuda/analyse_cuda.py of the reference consume the output unchanged.
@@ -182,6 +183,88 @@ std::vector<float> run_recorded(rc_ctx* ctx, const rc_method& m0, const std::vec
     return errs;
 }
 
+// Scenario file `name;state:frames,state:frames,...` (poc_gpu.cu:1376-1392, 1178-1187).
+using Scenarios = std::vector<std::pair<std::string, std::vector<std::pair<int, int>>>>;
+bool read_scenarios(const char* path, int NS, Scenarios& SC) {
+    FILE* sf = fopen(path, "r");
+    if (!sf) { fprintf(stderr, "fichier de scenarios %s\n", path); return false; }
+    char line[512];
+    while (fgets(line, sizeof line, sf)) {
+        std::string L(line);
+        while (!L.empty() && (L.back() == '\n' || L.back() == '\r')) L.pop_back();
+        if (L.empty() || L[0] == '#') continue;
+        size_t sc = L.find(';');
+        if (sc == std::string::npos) continue;
+        std::pair<std::string, std::vector<std::pair<int, int>>> x;
+        x.first = L.substr(0, sc);
+        std::string rest = L.substr(sc + 1);
+        size_t pos = 0;
+        while (pos < rest.size()) {
+            size_t comma = rest.find(',', pos);
+            if (comma == std::string::npos) comma = rest.size();
+            std::string tok = rest.substr(pos, comma - pos);
+            size_t colon = tok.find(':');
+            int st = atoi(tok.substr(0, colon).c_str());
+            int nf = colon == std::string::npos ? 0 : atoi(tok.substr(colon + 1).c_str());
+            if (st < 0 || st >= NS) {
+                fprintf(stderr, "scenario %s : etat %d hors limites\n", x.first.c_str(), st);
+                fclose(sf);
+                return false;
+            }
+            x.second.push_back({st, nf});
+            pos = comma + 1;
+        }
+        SC.push_back(x);
+    }
+    fclose(sf);
+    return true;
+}
+
+// taa mode (run_taa_mode, poc_gpu.cu:1175-1282): 8 accumulator variants per scenario, one
+// JSONL line each with the 20-frame pre-event and 30-frame post-event errors and the curve.
+int taa_mode(rc_ctx* ctx, int NS, const char* scen_file, int nseeds) {
+    Scenarios SC;
+    if (!read_scenarios(scen_file, NS, SC)) return 1;
+    struct TM { std::string name; rc_taa_method m; };
+    std::vector<TM> M;
+    char nm[96];
+    for (float a : {0.05f, 0.1f, 0.2f}) {
+        snprintf(nm, sizeof nm, "TAA borne alpha=%.2f", a);
+        M.push_back({nm, {a, 1.f, 0}});
+    }
+    M.push_back({"TAA simple alpha=0.10 (sans bornage)", {0.1f, 0.f, 0}});
+    M.push_back({"TAA + detection aveugle", {0.1f, 1.f, 1}});
+    M.push_back({"TAA + masque dependances", {0.1f, 1.f, 2}});
+    M.push_back({"TAA + masque dependances verifie", {0.1f, 1.f, 3}});
+    M.push_back({"TAA + masque oracle", {0.1f, 1.f, 4}});
+    for (auto& sc : SC) {
+        std::vector<int> seq;
+        for (auto& pr : sc.second) for (int k = 0; k < pr.second; ++k) seq.push_back(pr.first);
+        if (seq.empty()) continue;
+        const int last = (int)seq.size() - sc.second.back().second;
+        for (auto& m : M) {
+            double pre = 0, post = 0;
+            std::vector<double> curve(seq.size(), 0.0);
+            for (int sd = 0; sd < nseeds; ++sd) {
+                CHK(ctx, rc_taa_begin(ctx, &m.m, seq[0], 5000u + (uint32_t)sd), "taa");
+                for (size_t f = 0; f < seq.size(); ++f) {
+                    float e = 0.f;
+                    CHK(ctx, rc_taa_frame(ctx, seq[f], &e), "taa frame");
+                    curve[f] += (double)e / nseeds;
+                    if ((int)f >= last - 20 && (int)f < last) pre += e / 20.0 / nseeds;
+                    if ((int)f >= last && (int)f < last + 30) post += e / 30.0 / nseeds;
+                }
+            }
+            printf("{\"type\":\"taa\",\"scen\":\"%s\",\"name\":\"%s\",\"pre\":%.5f,\"post\":%.5f,\"last\":%d,\"curve\":[", sc.first.c_str(),
+                   m.name.c_str(), pre, post, last);
+            for (size_t f = 0; f < curve.size(); ++f) printf("%s%.5f", f ? "," : "", curve[f]);
+            printf("]}\n");
+            fflush(stdout);
+        }
+    }
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -189,7 +272,7 @@ int main(int argc, char** argv) {
     std::string mode = argv[1];
     if (const char* d = getenv("BENCH_DEBUG")) g_debug = atoi(d);
     if (const char* r = getenv("BENCH_RAYONS")) g_rays = std::max(0.25f, (float)atof(r));
-    if (mode == "prep" || mode == "taa") {
+    if (mode == "prep") {
         fprintf(stderr, "mode %s is not provided by this build\n", mode.c_str());
         return 1;
     }
@@ -261,38 +344,17 @@ int main(int argc, char** argv) {
                    t.events ? t.event / t.events : 0.0);
             fflush(stdout);
         }
+    } else if (mode == "taa") {
+        // poc_gpu.cu:1368-1370
+        if (argc < 5) { fprintf(stderr, "usage : taa <scene.bin> <nseeds> <scenarios.txt>\n"); return 1; }
+        if (si.fmt == 3) { fprintf(stderr, "mode taa non supporte sur les scenes maillees\n"); return 1; }
+        return taa_mode(ctx, NS, argv[4], atoi(argv[3]));
     } else if (mode == "scenf") {
         // poc_gpu.cu:1371-1437
         if (argc < 5) { fprintf(stderr, "usage : scenf <scene.bin> <nseeds> <scenarios.txt> [budget]\n"); return 1; }
         int nseeds = atoi(argv[3]);
-        FILE* sf = fopen(argv[4], "r");
-        if (!sf) { fprintf(stderr, "fichier de scenarios %s\n", argv[4]); return 1; }
-        std::vector<std::pair<std::string, std::vector<std::pair<int, int>>>> SC;
-        char line[512];
-        while (fgets(line, sizeof line, sf)) {
-            std::string L(line);
-            while (!L.empty() && (L.back() == '\n' || L.back() == '\r')) L.pop_back();
-            if (L.empty() || L[0] == '#') continue;
-            size_t sc = L.find(';');
-            if (sc == std::string::npos) continue;
-            std::pair<std::string, std::vector<std::pair<int, int>>> x;
-            x.first = L.substr(0, sc);
-            std::string rest = L.substr(sc + 1);
-            size_t pos = 0;
-            while (pos < rest.size()) {
-                size_t comma = rest.find(',', pos);
-                if (comma == std::string::npos) comma = rest.size();
-                std::string tok = rest.substr(pos, comma - pos);
-                size_t colon = tok.find(':');
-                int st = atoi(tok.substr(0, colon).c_str());
-                int nf = colon == std::string::npos ? 0 : atoi(tok.substr(colon + 1).c_str());
-                if (st < 0 || st >= NS) { fprintf(stderr, "scenario %s : etat %d hors limites\n", x.first.c_str(), st); return 1; }
-                x.second.push_back({st, nf});
-                pos = comma + 1;
-            }
-            SC.push_back(x);
-        }
-        fclose(sf);
+        Scenarios SC;
+        if (!read_scenarios(argv[4], NS, SC)) return 1;
         // lights whose intensity differs from state 0 are "responsive" for SHaRC (poc_gpu.cu:1396-1397)
         std::vector<float> in0(NL), ink(NL);
         int dyn = 0;

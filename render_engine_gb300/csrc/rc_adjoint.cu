@@ -116,33 +116,51 @@ __global__ void k_rank(const int* __restrict__ off, int Np, const int* __restric
     }
 }
 
-// per point: direct light summed over the lights (l ascending) and albedo
-__global__ void k_prep(const float* __restrict__ AE, int aes, int NL, int Np, float2* __restrict__ da) {
+// per point: direct light summed over the lights (l ascending) and albedo; the first gathered
+// values A_j (d_j + L_j) with L = 0
+__global__ void k_prep(const float* __restrict__ AE, int aes, int NL, int Np, float2* __restrict__ da, float* __restrict__ g0) {
     const int j = blockIdx.x * B + threadIdx.x;
     if (j >= Np) return;
     const float* ae = AE + (size_t)aes * j;
     float d = 0.f;
     for (int l = 0; l < NL; ++l) d += ae[1 + l];
     da[j] = make_float2(d, ae[0]);
+    g0[j] = ae[0] * (d + 0.f);
 }
 
-// forward sweep: Lout[i] = (1/K) sum over i's counted rays of A_j (d_j + Lin_j), rays in order
+// forward sweep: L_i = (1/K) sum over i's counted rays, in ray order, of g_j = A_j (d_j + L_j)
+// from the previous sweep; writes L and the next sweep's g.  Hit lists are read four rays at a
+// time when K is a multiple of 4 (rows of 16 K bytes stay 16-byte aligned).
 __global__ void __launch_bounds__(B) k_fwd(const int* __restrict__ hits, int K, int Np, const float2* __restrict__ da,
-                                           const float* __restrict__ Lin, float* __restrict__ Lout, unsigned* chg) {
+                                           const float* __restrict__ gin, const float* __restrict__ Lprev, float* __restrict__ Lout,
+                                           float* __restrict__ gout, unsigned* chg) {
     const int i = blockIdx.x * B + threadIdx.x;
     float v = 0.f, dv = 0.f;
     if (i < Np) {
         float sum = 0.f;
         const int* h = hits + (size_t)i * K;
-        for (int r = 0; r < K; ++r) {
-            const int j = __ldg(h + r);
-            if (j < 0) continue;
-            const float2 x = __ldg(da + j);
-            sum += x.y * (x.x + __ldcg(Lin + j));
+        if ((K & 3) == 0) {
+            const int4* h4 = reinterpret_cast<const int4*>(h);
+            for (int r = 0; r < K / 4; ++r) {
+                const int4 q = __ldg(h4 + r);
+                const float a = q.x >= 0 ? __ldcg(gin + q.x) : 0.f, b = q.y >= 0 ? __ldcg(gin + q.y) : 0.f;
+                const float c = q.z >= 0 ? __ldcg(gin + q.z) : 0.f, d = q.w >= 0 ? __ldcg(gin + q.w) : 0.f;
+                if (q.x >= 0) sum += a;
+                if (q.y >= 0) sum += b;
+                if (q.z >= 0) sum += c;
+                if (q.w >= 0) sum += d;
+            }
+        } else {
+            for (int r = 0; r < K; ++r) {
+                const int j = __ldg(h + r);
+                if (j >= 0) sum += __ldcg(gin + j);
+            }
         }
         v = sum / (float)K;
         Lout[i] = v;
-        dv = fabsf(v - Lin[i]);
+        const float2 x = da[i];
+        gout[i] = x.y * (x.x + v);
+        dv = fabsf(v - Lprev[i]);
     }
     if (chg) {   // change of the sweep, and the largest value (non-negative floats order as their bits)
         const unsigned a = warp_max(__float_as_uint(dv)), b = warp_max(__float_as_uint(fabsf(v)));
@@ -153,7 +171,8 @@ __global__ void __launch_bounds__(B) k_fwd(const int* __restrict__ hits, int K, 
     }
 }
 
-// adjoint sweep: uout[j] = w_j + (A_j / K) sum over the rays reaching j of uin[source]
+// adjoint sweep: uout[j] = w_j + (A_j / K) sum over the rays reaching j, in ray order, of
+// uin[source] (four sources fetched at a time)
 __global__ void __launch_bounds__(B) k_bwd(const int* __restrict__ off, const int* __restrict__ src, int K, int Np,
                                            const float2* __restrict__ da, const float* __restrict__ w,
                                            const float* __restrict__ uin, float* __restrict__ uout, unsigned* chg) {
@@ -162,7 +181,16 @@ __global__ void __launch_bounds__(B) k_bwd(const int* __restrict__ off, const in
     if (j < Np) {
         float sum = 0.f;
         const int a = off[j], b = off[j + 1];
-        for (int q = a; q < b; ++q) sum += __ldcg(uin + __ldg(src + q));
+        int q = a;
+        for (; q + 4 <= b; q += 4) {
+            const int s0 = __ldg(src + q), s1 = __ldg(src + q + 1), s2 = __ldg(src + q + 2), s3 = __ldg(src + q + 3);
+            const float x0 = __ldcg(uin + s0), x1 = __ldcg(uin + s1), x2 = __ldcg(uin + s2), x3 = __ldcg(uin + s3);
+            sum += x0;
+            sum += x1;
+            sum += x2;
+            sum += x3;
+        }
+        for (; q < b; ++q) sum += __ldcg(uin + __ldg(src + q));
         v = w[j] + da[j].y * sum / (float)K;
         uout[j] = v;
         dv = fabsf(v - uin[j]);
@@ -251,12 +279,13 @@ cudaError_t build_transpose(const Bufs& b, int Np, int K, cudaStream_t st) {
 cudaError_t solve(Bufs* bp, int Np, int K, int NL, int aes, const float* AE, const float* AEu, int iters, cudaStream_t st) {
     const Bufs& b = *bp;
     cudaError_t e;
-    k_prep<<<blocks_for(Np), B, 0, st>>>(AE, aes, NL, Np, b.da);
+    k_prep<<<blocks_for(Np), B, 0, st>>>(AE, aes, NL, Np, b.da, b.g[0]);
     if ((e = cudaMemsetAsync(b.L[0], 0, sizeof(float) * (size_t)Np, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(b.u[0], b.w, sizeof(float) * (size_t)Np, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
     for (int t = 0; t < iters; ++t) {
         const bool last = t == iters - 1;
-        k_fwd<<<blocks_for(Np), B, 0, st>>>(b.hits, K, Np, b.da, b.L[t & 1], b.L[(t + 1) & 1], last ? b.stats->chg : nullptr);
+        k_fwd<<<blocks_for(Np), B, 0, st>>>(b.hits, K, Np, b.da, b.g[t & 1], b.L[t & 1], b.L[(t + 1) & 1], b.g[(t + 1) & 1],
+                                            last ? b.stats->chg : nullptr);
         k_bwd<<<blocks_for(Np), B, 0, st>>>(b.off, b.src, K, Np, b.da, b.w, b.u[t & 1], b.u[(t + 1) & 1], last ? b.stats->chg : nullptr);
     }
     bp->L_final = b.L[iters & 1];

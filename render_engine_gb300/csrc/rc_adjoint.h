@@ -28,6 +28,7 @@ struct Bufs {
     int* scratch;     // scan_scratch_ints(Np + 1)
     float2* da;       // Np: (direct light summed over lights, albedo)
     float* L[2];      // forward iterates (total radiance per point)
+    float* g[2];      // gathered values A_j (d_j + L_j) of the forward iterates
     float* u[2];      // adjoint iterates (importance per point)
     const float* L_final;   // the iterate holding the forward solution (set by solve)
     const float* u_final;   // the iterate holding the adjoint solution (set by solve)

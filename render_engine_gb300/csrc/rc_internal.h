@@ -153,6 +153,9 @@ struct Ops {
     static cudaError_t ref_iter(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                 const float* Lin, float* Lout, float* acc, float* closec, uint32_t seed, int K, int accumulate,
                                 int count_close, cudaStream_t st);
+    // one taa-mode sample per point (x), with deps the rays' dependency masks or-ed into cur
+    static cudaError_t taa_sample(int NW, bool deps, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c,
+                                  const FrameParams& p, float* x, uint32_t* cur, uint32_t seed, uint32_t frame, cudaStream_t st);
     // K frozen rays per point (the rays of one reference iteration with `seed`): hit cache point or -1
     static cudaError_t frozen_hits(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                    uint32_t seed, int K, int* hits, cudaStream_t st);

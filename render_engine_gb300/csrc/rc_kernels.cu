@@ -1231,6 +1231,57 @@ __global__ void __launch_bounds__(BLOCK) k_ref(const DState s, const DStatic g, 
     if (count_close) closec[i] += (float)close;
 }
 
+// One sample per point of the reference's taa mode (k_taa_pt, poc_gpu.cu:1062-1098): one cosine
+// ray; the radiance at its hit point = A x (direct light summed over lights + the converged
+// reference), 0 when the ray does not count; with DEPS the ray's dependency mask (the hit's
+// shadow voxels and the ray's own transit voxels) is or-ed into cur.
+template <int NL, int NW, bool DEPS>
+__global__ void __launch_bounds__(BLOCK) k_taa_pt(const DState s, const DStatic g, const Grid grid, const DevCache c, const FrameParams p,
+                                                  float* __restrict__ x, uint32_t* __restrict__ cur, uint32_t seed, uint32_t frame) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= p.Np) return;
+    constexpr int AES = aes_of(NL);
+    uint32_t rs = hash32(seed * 0x9E3779B9u ^ hash32(frame * 0x85EBCA6Bu ^ hash32(i + 7)));
+    const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]), O = P + N * 1e-3f;
+    const float u1 = rnd(rs);
+    const float u2 = rnd(rs);
+    const f3 D = cosine_dir(N, u1, u2);
+    const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
+    float v = 0.f;
+    if (!h.back) {
+        float4 ae[AES / 4];
+        const float4* aep = s.AE + (size_t)h.pi * (AES / 4);
+#pragma unroll
+        for (int k4 = 0; k4 < AES / 4; ++k4) ae[k4] = __ldg(aep + k4);
+        float ed = 0.f;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) ed += comp(ae, l + 1);
+        v = ae[0].x * (ed + s.ref[h.pi]);
+    }
+    x[i] = v;
+    if (DEPS) {
+        uint32_t m[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) m[w] = 0u;
+        const uint4* sv = reinterpret_cast<const uint4*>(s.SV + (size_t)NW * (h.back ? i : h.pi));
+#pragma unroll
+        for (int w = 0; w < NW / 4; ++w) {
+            const uint4 a = __ldg(sv + w);
+            m[4 * w] |= a.x; m[4 * w + 1] |= a.y; m[4 * w + 2] |= a.z; m[4 * w + 3] |= a.w;
+        }
+        dda_walk<NW>(grid, O, h.H, m);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            const uint32_t o = cur[(size_t)w * p.Np + i];
+            if ((o | m[w]) != o) cur[(size_t)w * p.Np + i] = o | m[w];
+        }
+    }
+}
+
 // The rays of one k_ref iteration with this seed (prep_mesh.cuh:182-200: same seed, directions
 // and hit resolution), kept: hits[i * K + r] = the cache point ray r of point i reaches, or -1
 // when the ray does not count (no hit, back face, cell absent).  The frozen ray set defines a
@@ -1298,6 +1349,24 @@ cudaError_t Ops<NL>::ref_iter(const DState& s, const DStatic& g, const Grid& gri
 
 // Mask widths built for every light count (NW = voxels / 32 of the transit grid).
 #define RC_NW_LIST(X) X(4) X(24)
+
+template <int NL>
+cudaError_t Ops<NL>::taa_sample(int NW, bool deps, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c,
+                                const FrameParams& p, float* x, uint32_t* cur, uint32_t seed, uint32_t frame, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+#define X(W)                                                                                                   \
+    if (NW == W) {                                                                                             \
+        auto kern = deps ? k_taa_pt<NL, W, true> : k_taa_pt<NL, W, false>;                                     \
+        cudaError_t e = prep_smem(kern, smem);                                                                 \
+        if (e != cudaSuccess) return e;                                                                        \
+        kern<<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, x, cur, seed, frame);                       \
+        return cudaGetLastError();                                                                             \
+    }
+    RC_NW_LIST(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
 
 template <int NL>
 cudaError_t Ops<NL>::build(int NW, const DState& s, const DStatic& g, const Grid& grid, const float* L, const float* inten,

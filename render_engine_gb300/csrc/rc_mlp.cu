@@ -135,10 +135,11 @@ __device__ __forceinline__ void st_bf16(uint8_t* base, uint32_t off, float v) {
 // the position in the box (12 octaves) and of the normal (4 octaves), one-blob encodings of
 // both (16 and 4 bins per axis), the raw position, normal, direct light of three lights,
 // albedo and a constant.  Produced eight at a time (one 16-byte group of the K-major tile);
-// emit(group, f) stores them.
+// emit(group, f) stores them.  Two threads share a point: half 0 produces groups 0..8 (the
+// position octaves), half 1 groups 9..21 (about the same work).
 template <class Emit>
-__device__ __forceinline__ void encode(const MlpArgs& a, int pt, Emit&& emit) {
-    const float4 P = a.P[pt], Nn = a.N[pt], X = a.aux[pt];
+__device__ __forceinline__ void encode(const MlpArgs& a, int pt, int half, Emit&& emit) {
+    const float4 P = a.P[pt], Nn = a.N[pt];
     const float p[3] = {fminf(fmaxf((P.x - a.lo[0]) * a.inv_ext[0], 0.f), 1.f), fminf(fmaxf((P.y - a.lo[1]) * a.inv_ext[1], 0.f), 1.f),
                         fminf(fmaxf((P.z - a.lo[2]) * a.inv_ext[2], 0.f), 1.f)};
     const float nv[3] = {Nn.x, Nn.y, Nn.z};
@@ -156,17 +157,25 @@ __device__ __forceinline__ void encode(const MlpArgs& a, int pt, Emit&& emit) {
             f[2 * j + 1] = (c - s) * (c + s);
         }
     };
-    for (int ax = 0; ax < 3; ++ax) {   // features 24 ax .. 24 ax + 23: sin / cos of 2^o pi p
-        float w = 3.14159265f * p[ax];
-        for (int g = 0; g < 3; ++g, w *= 16.f) {
-            octaves(w);
-            emit(ax * 3 + g, f);
+    if (half == 0) {
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {   // features 24 ax .. 24 ax + 23: sin / cos of 2^o pi p
+            float w = 3.14159265f * p[ax];
+#pragma unroll
+            for (int g = 0; g < 3; ++g, w *= 16.f) {
+                octaves(w);
+                emit(ax * 3 + g, f);
+            }
         }
+        return;
     }
+    const float4 X = a.aux[pt];
+#pragma unroll
     for (int ax = 0; ax < 3; ++ax) {   // 72 + 8 ax: sin / cos of 2^o pi n
         octaves(3.14159265f * nv[ax]);
         emit(9 + ax, f);
     }
+#pragma unroll
     for (int ax = 0; ax < 3; ++ax) {   // 96 + 16 ax: one-blob of p, 16 bins
         const float bp = p[ax] * 16.f;
         for (int g = 0; g < 2; ++g) {
@@ -195,11 +204,14 @@ __device__ __forceinline__ void encode(const MlpArgs& a, int pt, Emit&& emit) {
     emit(21, f);
 }
 
-// Forward pass over tiles of 128 samples (persistent CTAs of 128 threads, thread = sample row).
+// Forward pass over tiles of 128 samples (persistent CTAs of two warpgroups: thread t works on
+// sample row t % 128, the two threads of a row split the input features and the columns of
+// each accumulator -- warp w reads the tensor-memory lanes of its quarter w % 4).
 // TRAIN: also keeps X0^T, H_l^T and dY (with dY^T) of each tile in global memory and adds the
 // loss; otherwise writes the n_out outputs.
+constexpr int FWD_THREADS = 256;
 template <bool TRAIN>
-__global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
+__global__ void __launch_bounds__(FWD_THREADS) k_mlp_forward(const MlpArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar;
     __shared__ uint32_t tmem_base;
@@ -209,7 +221,8 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
     uint8_t* sx = smem + WF_BYTES;
     uint8_t* st = sx + 128 * K0 * 2;                  // TRAIN: transposed staging, 176 x 128
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int i = tid; i < WF_BYTES / 16; i += 128) reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(a.wbf)[i];
+    const int row = tid & 127, half = tid >> 7, quarter = warp & 3;
+    for (int i = tid; i < WF_BYTES / 16; i += FWD_THREADS) reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(a.wbf)[i];
     if (tid == 0) mbar_init(&mbar, 1);
     if (warp == 0) tmem_alloc(&tmem_base, 64);
     fence_before_sync();
@@ -220,24 +233,24 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
     bool ok = true;
     const int ntiles = (a.n + 127) / 128;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int s = tile * 128 + tid;
+        const int s = tile * 128 + row;
         const bool live = s < a.n;
         const int pt = live ? (a.idx ? a.idx[s] : s) : 0;
-        encode(a, pt, [&](int k8, const float (&f)[8]) {
+        encode(a, pt, half, [&](int k8, const float (&f)[8]) {
             uint4 v;
             v.x = pack_bf16(f[0], f[1]);
             v.y = pack_bf16(f[2], f[3]);
             v.z = pack_bf16(f[4], f[5]);
             v.w = pack_bf16(f[6], f[7]);
-            *reinterpret_cast<uint4*>(sx + kmajor_offset(tid, 8 * k8, K0)) = v;
+            *reinterpret_cast<uint4*>(sx + kmajor_offset(row, 8 * k8, K0)) = v;
             if (TRAIN)
-                for (int j = 0; j < 8; ++j) st_bf16(st, kmajor_offset(8 * k8 + j, tid, 128), f[j]);
+                for (int j = 0; j < 8; ++j) st_bf16(st, kmajor_offset(8 * k8 + j, row, 128), f[j]);
         });
         fence_proxy_async();
         __syncthreads();
         if (TRAIN) {
             uint4* dst = reinterpret_cast<uint4*>(a.act + (size_t)tile * ACT_BYTES + ACT_X0T);
-            for (int i = tid; i < K0 * 128 * 2 / 16; i += 128) dst[i] = reinterpret_cast<const uint4*>(st)[i];
+            for (int i = tid; i < K0 * 128 * 2 / 16; i += FWD_THREADS) dst[i] = reinterpret_cast<const uint4*>(st)[i];
             __syncthreads();
         }
         for (int l = 0; l < NLAYER && ok; ++l) {
@@ -251,7 +264,12 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
                              idesc_bf16_f32(128, N), kk > 0);
                 mma_commit(&mbar);
             }
-            ok = mbar_wait(&mbar, phase, WAIT_LIMIT);
+            // one warp watches the barrier; the others wait at the block barrier without issuing
+            // (the fence orders the products before the block barrier for every thread)
+            if (warp == 0) {
+                ok = mbar_wait(&mbar, phase, WAIT_LIMIT);
+                fence_before_sync();
+            }
             phase ^= 1u;
             ok = __syncthreads_and(ok);   // the whole block leaves together
             if (!ok) {
@@ -259,9 +277,12 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
                 break;
             }
             fence_after_sync();
-            for (int c = 0; c < N; c += 16) {
+            // columns of this thread: one half of a hidden layer; all 16 outputs for half 0
+            const int c0 = l < NLAYER - 1 ? half * (N / 2) : 0;
+            const int c1 = l < NLAYER - 1 ? c0 + N / 2 : (half == 0 ? N : 0);
+            for (int c = c0; c < c1; c += 16) {
                 float v[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+                tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
                 tmem_wait_ld();
                 if (l < NLAYER - 1) {
                     uint4 lo4, hi4;
@@ -273,10 +294,10 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
                     hi4.y = pack_bf16(fmaxf(v[10], 0.f), fmaxf(v[11], 0.f));
                     hi4.z = pack_bf16(fmaxf(v[12], 0.f), fmaxf(v[13], 0.f));
                     hi4.w = pack_bf16(fmaxf(v[14], 0.f), fmaxf(v[15], 0.f));
-                    *reinterpret_cast<uint4*>(Hn + kmajor_offset(tid, c, HID)) = lo4;
-                    *reinterpret_cast<uint4*>(Hn + kmajor_offset(tid, c + 8, HID)) = hi4;
+                    *reinterpret_cast<uint4*>(Hn + kmajor_offset(row, c, HID)) = lo4;
+                    *reinterpret_cast<uint4*>(Hn + kmajor_offset(row, c + 8, HID)) = hi4;
                     if (TRAIN)
-                        for (int j = 0; j < 16; ++j) st_bf16(st, kmajor_offset(c + j, tid, 128), fmaxf(v[j], 0.f));
+                        for (int j = 0; j < 16; ++j) st_bf16(st, kmajor_offset(c + j, row, 128), fmaxf(v[j], 0.f));
                 } else if (!TRAIN) {
                     if (live)
                         for (int j = 0; j < a.n_out; ++j) a.out[(size_t)s * a.ostride + j] = v[j];
@@ -293,8 +314,8 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
                             lsum += d * d / den;
                             g = 2.f * d / den * a.loss_scale;
                         }
-                        st_bf16(dy, kmajor_offset(tid, j, OUTP), g);
-                        st_bf16(dyt, kmajor_offset(j, tid, 128), g);
+                        st_bf16(dy, kmajor_offset(row, j, OUTP), g);
+                        st_bf16(dyt, kmajor_offset(j, row, 128), g);
                     }
                     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
                     if (lane == 0 && lsum != 0.f) atomicAdd(a.loss, lsum);
@@ -305,7 +326,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpArgs a) {
             __syncthreads();
             if (TRAIN && l < NLAYER - 1) {
                 uint4* dst = reinterpret_cast<uint4*>(a.act + (size_t)tile * ACT_BYTES + act_ht(l + 1));
-                for (int i = tid; i < HID * 128 * 2 / 16; i += 128) dst[i] = reinterpret_cast<const uint4*>(st)[i];
+                for (int i = tid; i < HID * 128 * 2 / 16; i += FWD_THREADS) dst[i] = reinterpret_cast<const uint4*>(st)[i];
                 __syncthreads();
             }
             fence_after_sync();
@@ -366,7 +387,12 @@ __global__ void __launch_bounds__(128) k_mlp_backward(const MlpArgs a) {
             }
             mma_commit(&mbar);
         }
-        const bool ok = __syncthreads_and(mbar_wait(&mbar, phase, WAIT_LIMIT));
+        bool seen = true;
+        if (warp == 0) {   // one warp watches the barrier (see k_mlp_forward)
+            seen = mbar_wait(&mbar, phase, WAIT_LIMIT);
+            fence_before_sync();
+        }
+        const bool ok = __syncthreads_and(seen);
         phase ^= 1u;
         if (!ok) {
             if (tid == 0) atomicOr(a.err, 1u);
@@ -617,7 +643,7 @@ rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.loss_scale = 1.f / ((float)n * (float)m->cfg.n_out);
     const int ntiles = n / 128;
     if (!d_loss && cudaMemsetAsync(m->loss, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "loss");
-    k_mlp_forward<true><<<std::min(ntiles, m->sms), 128, FWD_SMEM_TRAIN, m->stream>>>(a);
+    k_mlp_forward<true><<<std::min(ntiles, m->sms), FWD_THREADS, FWD_SMEM_TRAIN, m->stream>>>(a);
     k_mlp_backward<<<ntiles, 128, BWD_SMEM, m->stream>>>(a);
     m->step++;
     const float b1 = 0.9f, b2 = 0.99f;
@@ -638,7 +664,7 @@ rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.out = d_out;
     a.ostride = ostride;
     const int ntiles = (n + 127) / 128;
-    k_mlp_forward<false><<<std::min(ntiles, 2 * m->sms), 128, FWD_SMEM_INFER, m->stream>>>(a);   // two per SM fit
+    k_mlp_forward<false><<<std::min(ntiles, 2 * m->sms), FWD_THREADS, FWD_SMEM_INFER, m->stream>>>(a);   // two per SM fit
     return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
 }
 

@@ -17,6 +17,7 @@
 #include "../../include/rc_api.h"
 #include "rc_adjoint.h"
 #include "rc_internal.h"
+#include "rc_taa.h"
 
 using namespace rc;
 
@@ -60,10 +61,27 @@ struct Scene {
     std::vector<HostState> st;
     DStatic g{};
     const float* L = nullptr;       // device light positions, 3 floats per light
+    std::vector<float> hL;          // host copies: light positions, state 0's quad grids
+    std::vector<int> hdims, hoff;
     // events: [pair * (1 + NL) + 0] = occluder voxels, [.. + 1 + l] = voxels of light l
     std::vector<std::vector<int>> ev;
     std::vector<const int*> ev_dev;
     double scene_bytes = 0;
+};
+
+// State of the taa mode (run_taa_mode, poc_gpu.cu:1175-1282).
+struct TaaRun {
+    bool active = false;
+    rc_taa_method M{};
+    uint32_t seed = 0;
+    int f = 0, prev_state = 0, verify_left = 0;
+    float *x = nullptr, *H = nullptr, *H2 = nullptr, *mu = nullptr, *sg = nullptr, *rs = nullptr, *cnt = nullptr;
+    int *nb = nullptr, *react = nullptr;
+    uint8_t* pend = nullptr;
+    uint32_t *cur = nullptr, *prev = nullptr;
+    double *part = nullptr, *out = nullptr;
+    std::vector<const int*> dV;     // event voxels per state pair (device), and their counts
+    std::vector<int> nV;
 };
 
 struct Run {
@@ -87,7 +105,8 @@ struct rc_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::string err;
-    std::vector<DevBuf> scene_bufs, cache_bufs, adj_bufs;
+    std::vector<DevBuf> scene_bufs, cache_bufs, adj_bufs, taa_bufs;
+    TaaRun taa;
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
     rc::adj::Bufs adj{};
     Scene S;
@@ -443,6 +462,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     }
     set_grid_scale(S.grid);
     auto L = r.vec<float>(3 * (size_t)NL);
+    S.hL = L;
     const uint8_t* A = r.raw<float>(Np);
     const uint8_t* region = r.raw<int>(Np);
     if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated");
@@ -469,6 +489,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         const uint8_t* N = r.raw<float>(3 * Np);
         auto Q = r.vec<float>(12 * (size_t)S.Nq);
         auto dims = r.vec<int>(2 * (size_t)S.Nq), off = r.vec<int>((size_t)S.Nq);
+        if (k == 0) { S.hdims = dims; S.hoff = off; }
         auto T = r.vec<float>(9 * (size_t)S.Nt);
         auto TQ = r.vec<int>((size_t)S.Nt);
         const uint8_t *ref = nullptr, *valid = nullptr, *Pw = nullptr;
@@ -950,6 +971,73 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
 }  // namespace
 
 // ============================================================================ C ABI
+namespace {
+
+constexpr float TAA_ALPHA_R = 0.5f;   // poc_gpu.cu:1231
+constexpr int TAA_RF = 4;
+
+// fine event voxel of a light (host_vox_fine, poc_gpu.cu:1170-1173)
+int taa_vox_fine(const float* p) {
+    const int i = std::min(std::max(int(p[0] / 8.f * 16), 0), 15), j = std::min(std::max(int(p[1] / 4.f * 8), 0), 7),
+              k = std::min(std::max(int(p[2] / 3.f * 6), 0), 5);
+    return (k * 8 + j) * 16 + i;
+}
+
+// buffers, neighbourhoods and event voxel lists (run_taa_mode's set-up, poc_gpu.cu:1189-1222)
+rc_status taa_alloc(rc_ctx* ctx) {
+    free_pool(ctx->taa_bufs);
+    TaaRun& t = ctx->taa;
+    t = TaaRun{};
+    const Scene& S = ctx->S;
+    const size_t Np = (size_t)S.Np, NW = (size_t)ctx->NW;
+    auto& pool = ctx->taa_bufs;
+    std::vector<int> nb(9 * Np, -1);
+    for (int q = 0; q < S.Nq; ++q) {
+        const int nu = S.hdims[2 * q], nv = S.hdims[2 * q + 1], o = S.hoff[q];
+        for (int iv = 0; iv < nv; ++iv)
+            for (int iu = 0; iu < nu; ++iu) {
+                const size_t i = (size_t)o + (size_t)iv * nu + iu;
+                int k = 0;
+                for (int dv = -1; dv <= 1; ++dv)
+                    for (int du = -1; du <= 1; ++du) {
+                        const int a = iu + du, b = iv + dv;
+                        nb[9 * i + k++] = (a >= 0 && a < nu && b >= 0 && b < nv) ? o + b * nu + a : -1;
+                    }
+            }
+    }
+    const int* dnb = nullptr;
+    rc_status s;
+    if ((s = dalloc(ctx, pool, &t.x, Np)) || (s = dalloc(ctx, pool, &t.H, Np)) || (s = dalloc(ctx, pool, &t.H2, Np)) ||
+        (s = dalloc(ctx, pool, &t.mu, Np)) || (s = dalloc(ctx, pool, &t.sg, Np)) || (s = dalloc(ctx, pool, &t.react, Np)) ||
+        (s = dalloc(ctx, pool, &t.pend, Np)) || (s = dalloc(ctx, pool, &t.cur, NW * Np)) || (s = dalloc(ctx, pool, &t.prev, NW * Np)) ||
+        (s = dalloc(ctx, pool, &t.rs, 3 * (size_t)S.NR)) || (s = dalloc(ctx, pool, &t.cnt, (size_t)S.NR)) ||
+        (s = dalloc(ctx, pool, &t.part, 3 * (size_t)taa::post_blocks(S.Np))) || (s = dalloc(ctx, pool, &t.out, 3)) ||
+        (s = dput(ctx, pool, &dnb, nb)))
+        return s;
+    t.nb = const_cast<int*>(dnb);
+    const int NS = S.NS, NL = S.NL;
+    t.dV.assign((size_t)NS * NS, nullptr);
+    t.nV.assign((size_t)NS * NS, 0);
+    for (int a = 0; a < NS; ++a)
+        for (int b = 0; b < NS; ++b) {
+            if (a == b) continue;
+            std::vector<int> fine;
+            for (int l = 0; l < NL; ++l)
+                if (S.st[a].inten[l] != S.st[b].inten[l]) fine.push_back(taa_vox_fine(&S.hL[3 * (size_t)l]));
+            std::vector<int> v = to_grid(fine, S.grid.vx, S.grid.vy, S.grid.vz);
+            for (int x : S.ev[((size_t)a * NS + b) * (1 + NL)]) v.push_back(x);
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+            t.nV[(size_t)a * NS + b] = (int)v.size();
+            const int* dv = nullptr;
+            if ((s = dput(ctx, pool, &dv, v.empty() ? std::vector<int>{0} : v))) return s;
+            t.dV[(size_t)a * NS + b] = dv;
+        }
+    return RC_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int rc_abi_version(void) { return RC_ABI_VERSION; }
@@ -1008,6 +1096,7 @@ void rc_destroy(rc_ctx* ctx) {
     free_pool(ctx->cache_bufs);
     free_pool(ctx->scene_bufs);
     free_pool(ctx->adj_bufs);
+    free_pool(ctx->taa_bufs);
     if (ctx->flags_dev) cudaFree(ctx->flags_dev);
     if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
@@ -1040,6 +1129,8 @@ rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
     free_pool(ctx->cache_bufs);
     free_pool(ctx->scene_bufs);
     free_pool(ctx->adj_bufs);
+    free_pool(ctx->taa_bufs);
+    ctx->taa = TaaRun{};
     ctx->adj_np = ctx->adj_k = 0;
     ctx->have_scene = false;
     ctx->run.active = false;
@@ -1537,7 +1628,8 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
     if ((s = dalloc(ctx, pool, &b.hits, Np * K)) || (s = dalloc(ctx, pool, &b.cnt, Np + 1)) || (s = dalloc(ctx, pool, &b.off, Np + 1)) ||
         (s = dalloc(ctx, pool, &b.fill, Np)) || (s = dalloc(ctx, pool, &b.src, Np * K)) ||
         (s = dalloc(ctx, pool, &b.scratch, adj::scan_scratch_ints((long long)Np + 1))) || (s = dalloc(ctx, pool, &b.da, Np)) ||
-        (s = dalloc(ctx, pool, &b.L[0], Np)) || (s = dalloc(ctx, pool, &b.L[1], Np)) || (s = dalloc(ctx, pool, &b.u[0], Np)) ||
+        (s = dalloc(ctx, pool, &b.L[0], Np)) || (s = dalloc(ctx, pool, &b.L[1], Np)) || (s = dalloc(ctx, pool, &b.g[0], Np)) ||
+        (s = dalloc(ctx, pool, &b.g[1], Np)) || (s = dalloc(ctx, pool, &b.u[0], Np)) ||
         (s = dalloc(ctx, pool, &b.u[1], Np)) || (s = dalloc(ctx, pool, &b.w, Np)) ||
         (s = dalloc(ctx, pool, &b.part, (size_t)adj::GRAD_BLOCKS * (NL + 1))) || (s = dalloc(ctx, pool, &b.stats, 1)))
         return s;
@@ -1594,6 +1686,125 @@ rc_status rc_adjoint_arrays(rc_ctx* ctx, float* L, float* u, int* hits) {
     if (u) CKR(cudaMemcpyAsync(u, ctx->adj.u_final, Np * 4, cudaMemcpyDeviceToHost, st));
     if (hits) CKR(cudaMemcpyAsync(hits, ctx->adj.hits, Np * K * 4, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
+    return RC_OK;
+}
+
+
+rc_status rc_taa_begin(rc_ctx* ctx, const rc_taa_method* m, int first_state, uint32_t seed) {
+    if (!ctx || !m || m->mask < 0 || m->mask > 4) return RC_ERR_ARG;
+    if (!ctx->have_scene) return fail(ctx, RC_ERR_STATE, "no scene loaded");
+    const Scene& S = ctx->S;
+    if (S.fmt != 2) return fail(ctx, RC_ERR_UNSUPPORTED, "taa mode: format-2 scenes only (as the reference)");
+    if (!S.has_ref) return fail(ctx, RC_ERR_STATE, "taa mode needs a scene with references");
+    if (first_state < 0 || first_state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", first_state);
+    CKR(cudaSetDevice(ctx->cfg.device));
+    rc_status s;
+    if (!ctx->taa.x && (s = taa_alloc(ctx))) return s;
+    TaaRun& t = ctx->taa;
+    const size_t Np = (size_t)S.Np, NW = (size_t)ctx->NW;
+    cudaStream_t st = ctx->stream;
+    // poc_gpu.cu:1241-1245: converged history, masks and counters cleared
+    CKR(cudaMemcpyAsync(t.H, S.st[first_state].d.ref, Np * 4, cudaMemcpyDeviceToDevice, st));
+    CKR(cudaMemsetAsync(t.react, 0, Np * 4, st));
+    CKR(cudaMemsetAsync(t.pend, 0, Np, st));
+    CKR(cudaMemsetAsync(t.cur, 0, NW * Np * 4, st));
+    CKR(cudaMemsetAsync(t.prev, 0, NW * Np * 4, st));
+    t.M = *m;
+    t.seed = seed;
+    t.f = 0;
+    t.prev_state = first_state;
+    t.verify_left = 0;
+    t.active = true;
+    return RC_OK;
+}
+
+// One frame of run_taa_mode's loop (poc_gpu.cu:1246-1274).
+rc_status rc_taa_frame(rc_ctx* ctx, int state, float* err) {
+    if (!ctx) return RC_ERR_ARG;
+    TaaRun& t = ctx->taa;
+    if (!t.active) return fail(ctx, RC_ERR_STATE, "no taa run begun");
+    const Scene& S = ctx->S;
+    if (state < 0 || state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", state);
+    const int Np = S.Np, NW = ctx->NW, f = t.f;
+    const size_t nbytes_mask = (size_t)NW * Np * 4;
+    cudaStream_t st = ctx->stream;
+    const rc_taa_method& M = t.M;
+    const bool deps = M.mask == 2 || M.mask == 3;
+    if (deps && f % 32 == 0) {
+        std::swap(t.cur, t.prev);
+        CKR(cudaMemsetAsync(t.cur, 0, nbytes_mask, st));
+    }
+    const DState& d = S.st[state].d;
+    FrameParams p{};
+    p.Np = Np;
+    p.NR = S.NR;
+    CKR(RC_DISPATCH(S.NL, taa_sample(NW, deps, d, S.g, S.grid, ctx->c, p, t.x, t.cur, t.seed, (uint32_t)f, st)));
+    int kernels = 1;
+    if (f > 0 && t.prev_state != state) {
+        const size_t pe = (size_t)t.prev_state * S.NS + state;
+        if (M.mask == 2) { CKR(taa::touch(t.cur, t.prev, Np, t.dV[pe], t.nV[pe], t.react, t.pend, TAA_RF, 0, st)); ++kernels; }
+        if (M.mask == 3) {
+            CKR(taa::touch(t.cur, t.prev, Np, t.dV[pe], t.nV[pe], t.react, t.pend, TAA_RF, 1, st));
+            t.verify_left = 2;
+            CKR(cudaMemsetAsync(t.rs, 0, 3 * (size_t)S.NR * 4, st));
+            CKR(cudaMemsetAsync(t.cnt, 0, (size_t)S.NR * 4, st));
+            ++kernels;
+        }
+        if (M.mask == 4) { CKR(taa::oracle(S.st[t.prev_state].d.ref, d.ref, Np, t.react, TAA_RF, st)); ++kernels; }
+    }
+    if (M.mask == 1) {   // blind detection every frame
+        CKR(cudaMemsetAsync(t.rs, 0, 3 * (size_t)S.NR * 4, st));
+        CKR(cudaMemsetAsync(t.cnt, 0, (size_t)S.NR * 4, st));
+        CKR(taa::zone_acc(t.x, t.H, t.pend, S.g.region, Np, t.rs, t.cnt, 0, st));
+        CKR(taa::zone_decide(t.rs, t.cnt, t.pend, S.g.region, Np, t.react, 0, TAA_RF, 0, st));
+        kernels += 2;
+    }
+    if (M.mask == 3 && t.verify_left > 0) {   // verification over the flagged points, two frames
+        CKR(taa::zone_acc(t.x, t.H, t.pend, S.g.region, Np, t.rs, t.cnt, 1, st));
+        ++kernels;
+        if (--t.verify_left == 0) {
+            CKR(taa::zone_decide(t.rs, t.cnt, t.pend, S.g.region, Np, t.react, 1, TAA_RF, 1, st));
+            ++kernels;
+        }
+    }
+    CKR(taa::post(t.x, t.nb, t.H, t.H2, t.mu, t.sg, t.react, Np, M.alpha, TAA_ALPHA_R, M.gamma, d.ref, d.valid, err ? t.part : nullptr,
+                  t.out, st));
+    kernels += err ? 2 : 1;
+    std::swap(t.H, t.H2);
+    ctx->launches += kernels;
+    t.prev_state = state;
+    t.f = f + 1;
+    if (err) {
+        double h[3];
+        CKR(cudaMemcpyAsync(h, t.out, sizeof h, cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));
+        *err = (float)(h[2] > 0 && h[1] > 0 ? std::sqrt(h[0] / h[2]) / (h[1] / h[2]) : 0.0);
+    }
+    return RC_OK;
+}
+
+rc_status rc_taa_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, int to_device) {
+    if (!ctx || !host) return RC_ERR_ARG;
+    TaaRun& t = ctx->taa;
+    if (!t.x) return fail(ctx, RC_ERR_STATE, "no taa run begun");
+    const size_t Np = (size_t)ctx->S.Np, NW = (size_t)ctx->NW;
+    void* p = nullptr;
+    size_t n = 0;
+    switch (which) {
+        case RC_T_X: p = t.x; n = 4 * Np; break;
+        case RC_T_H: p = t.H; n = 4 * Np; break;
+        case RC_T_MU: p = t.mu; n = 4 * Np; break;
+        case RC_T_SG: p = t.sg; n = 4 * Np; break;
+        case RC_T_REACT: p = t.react; n = 4 * Np; break;
+        case RC_T_PEND: p = t.pend; n = Np; break;
+        case RC_T_CUR: p = t.cur; n = 4 * NW * Np; break;
+        case RC_T_PREV: p = t.prev; n = 4 * NW * Np; break;
+        default: return fail(ctx, RC_ERR_ARG, "taa array %d", which);
+    }
+    if (nbytes != n) return fail(ctx, RC_ERR_ARG, "taa array %d holds %zu bytes", which, n);
+    CKR(cudaMemcpyAsync(to_device ? p : host, to_device ? host : p, n, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                        ctx->stream));
+    CKR(cudaStreamSynchronize(ctx->stream));
     return RC_OK;
 }
 

@@ -38,7 +38,8 @@ EXPORTS = [
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
     "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
     "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
-    "rc_error_sums_noalloc", "rc_reference_build", "rc_adjoint", "rc_adjoint_arrays",
+    "rc_error_sums_noalloc", "rc_reference_build", "rc_adjoint", "rc_adjoint_arrays", "rc_taa_begin", "rc_taa_frame",
+    "rc_taa_array_copy",
 ]
 NOALLOC_MAX_POINTS = 4194304
 
@@ -157,6 +158,12 @@ def load_library():
                              ctypes.POINTER(AdjointResult)]
     L.rc_adjoint_arrays.restype = i
     L.rc_adjoint_arrays.argtypes = [vp, vp, vp, vp]
+    L.rc_taa_begin.restype = i
+    L.rc_taa_begin.argtypes = [vp, ctypes.POINTER(TaaMethod), i, u32]
+    L.rc_taa_frame.restype = i
+    L.rc_taa_frame.argtypes = [vp, i, ctypes.POINTER(ctypes.c_float)]
+    L.rc_taa_array_copy.restype = i
+    L.rc_taa_array_copy.argtypes = [vp, i, vp, sz, i]
     _lib = L
     return L
 
@@ -164,6 +171,15 @@ def load_library():
 class RefParams(ctypes.Structure):
     _fields_ = [("K", ctypes.c_int), ("warmup", ctypes.c_int), ("block", ctypes.c_int), ("max_iter", ctypes.c_int),
                 ("noise_target", ctypes.c_double)]
+
+
+class TaaMethod(ctypes.Structure):
+    _fields_ = [("alpha", ctypes.c_float), ("gamma", ctypes.c_float), ("mask", ctypes.c_int)]
+
+
+(T_X, T_H, T_MU, T_SG, T_REACT, T_PEND, T_CUR, T_PREV) = range(8)
+TAA_DTYPE = {T_X: np.float32, T_H: np.float32, T_MU: np.float32, T_SG: np.float32, T_REACT: np.int32, T_PEND: np.uint8,
+             T_CUR: np.uint32, T_PREV: np.uint32}
 
 
 class AdjointParams(ctypes.Structure):
@@ -366,6 +382,29 @@ class Context:
         h = np.empty((np_, self._adj_k), np.int32)
         self._chk(self.L.rc_adjoint_arrays(self.h, L.ctypes.data, u.ctypes.data, h.ctypes.data))
         return L, u, h
+
+    def taa_begin(self, alpha: float, gamma: float, mask: int, s0: int, seed: int):
+        """Start a run of the taa mode (rc_taa_begin)."""
+        m = TaaMethod(alpha, gamma, mask)
+        self._chk(self.L.rc_taa_begin(self.h, ctypes.byref(m), s0, seed & 0xFFFFFFFF))
+
+    def taa_frame(self, state: int, want_err: bool = False):
+        e = ctypes.c_float()
+        self._chk(self.L.rc_taa_frame(self.h, state, ctypes.byref(e) if want_err else None))
+        return float(e.value) if want_err else None
+
+    def taa_array(self, which: int, value: np.ndarray | None = None) -> np.ndarray:
+        """Copy a taa array out (value None) or in."""
+        np_, nw = self._info["np"], self._info["nw"]
+        n = np_ * nw if which in (T_CUR, T_PREV) else np_
+        dt = TAA_DTYPE[which]
+        if value is None:
+            out = np.empty(n, dt)
+            self._chk(self.L.rc_taa_array_copy(self.h, which, out.ctypes.data, out.nbytes, 0))
+            return out
+        v = np.ascontiguousarray(value, dt).reshape(-1)
+        self._chk(self.L.rc_taa_array_copy(self.h, which, v.ctypes.data, v.nbytes, 1))
+        return v
 
     def device_flags(self) -> int:
         v = ctypes.c_uint()

@@ -62,9 +62,9 @@ def test_binaries_built(lib):
         assert os.access(os.path.join(d, n), os.X_OK)
 
 
-def test_cli_rejects_unknown_mode_without_gpu(lib):
+def test_cli_rejects_a_mode_it_does_not_provide_without_gpu(lib):
     exe = os.path.join(os.path.dirname(lib), "poc_gpu_l3")
-    r = subprocess.run([exe, "taa", "x.bin"], capture_output=True, text=True)
+    r = subprocess.run([exe, "prep", "x.mesh", "x.bin"], capture_output=True, text=True)
     assert r.returncode == 1 and "not provided" in r.stderr
 
 
