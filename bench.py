@@ -48,11 +48,11 @@ def parse():
     ap.add_argument("--method", default=METHOD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=12)
-    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp", "adjoint"], default=None,
+    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp", "adjoint", "taa"], default=None,
                     help="no timing: run --steps frames of state 0 (frame), three resolve passes of the "
                          "hash-grid table (hashgrid), two inference and training passes of the MLP (mlp) or "
-                         "one 16-sweep adjoint of a 16-light room of --points points (adjoint), for an ncu "
-                         "capture, and exit")
+                         "one 16-sweep adjoint of a 16-light room of --points points (adjoint) or --steps "
+                         "frames of the taa mode (taa), for an ncu capture, and exit")
     return ap.parse_args()
 
 
@@ -74,6 +74,14 @@ def profile_run(args):
     if args.profile == "mlp":
         mlp_bench(torch.cuda.current_stream(), reps=2)
         torch.cuda.synchronize()
+        return
+    if args.profile == "taa":
+        ctx = N.Context()
+        ctx.load_bytes(taa_scene(args.points))
+        ctx.taa_begin(0.1, 1.0, 2, 0, 5000)
+        for f in range(args.steps):
+            ctx.taa_frame(taa_state(f), want_err=True)
+        ctx.close()
         return
     if args.profile == "adjoint":
         import numpy as np
@@ -330,6 +338,7 @@ def run_ours(args, world, rank, local, dist):
     out["hashgrid"] = hashgrid_bench(stream, peak)
     out["mlp"] = mlp_bench(stream)
     out["adjoint"] = adjoint_bench(peak)
+    out["taa"] = taa_bench()
     return out, data, method
 
 
@@ -425,6 +434,43 @@ def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20,
                         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                                      "algorithmic_bytes": res_bytes}},
             "mark_paths": {"paths": npaths, "vertices": n, "ms": mark_ms, "vertices_per_s": n / (mark_ms * 1e-3)}}
+
+
+def taa_scene(points: int) -> bytes:
+    """The room with stand-in references (1.0 everywhere, all points valid) so that the taa mode
+    runs: its cost does not depend on the reference values."""
+    import numpy as np
+    from render_engine_gb300 import scene as S
+    sc = S.box_room(points=points, seed=0)
+    n = len(sc.A)
+    for st in sc.states:
+        st.ref = np.ones(n, np.float32)
+        st.valid = np.ones(n, np.uint8)
+        st.Pw = np.zeros((n, len(sc.L)), np.float32)
+    return S.write(sc)
+
+
+def taa_state(f: int) -> int:
+    return (f // 50) % 5
+
+
+def taa_bench(frames=200, warm=10, points=1_082_802):
+    """Secondary line: the taa mode (rc_taa_frame, dependency mask, alpha 0.1, clamp 1) on the
+    1.08 M-point room, each frame with its error read back as the reference's run_taa_mode does;
+    wall-clock frames/s over 200 frames with 4 events."""
+    from render_engine_gb300 import native as N
+    ctx = N.Context()
+    ctx.load_bytes(taa_scene(points))
+    ctx.taa_begin(0.1, 1.0, 2, 0, 5000)
+    for f in range(warm):
+        ctx.taa_frame(0, want_err=True)
+    t0 = time.perf_counter()
+    for f in range(frames):
+        ctx.taa_frame(taa_state(f), want_err=True)
+    dt = time.perf_counter() - t0
+    ctx.close()
+    return {"points": points, "frames": frames, "frames_per_s": frames / dt, "ms_per_frame": dt * 1e3 / frames,
+            "method": "TAA + masque dependances"}
 
 
 def adjoint_bench(peak, points=1_082_802, lights=16, K=16):
@@ -576,9 +622,21 @@ def run_reference(args, world, rank, local, dist):
         ref.frame(seq[f], timers=tm)
     nf = min(args.steps, 5 * FRAMES_PER_STATE)
     ref.close()
+    # the taa mode with the reference's own kernels, as taa_bench times the product's
+    rt = pyref.RefRunner(3, taa_scene(args.points))
+    rt.taa_begin(0.1, 1.0, 2, 0, 5000)
+    for f in range(10):
+        rt.taa_frame(0)
+    t0 = time.perf_counter()
+    for f in range(200):
+        rt.taa_frame(taa_state(f))
+    dt = time.perf_counter() - t0
+    rt.close()
     return {"frames_per_s": args.steps / (total_ms * 1e-3), "ms_per_step": total_ms / args.steps, "clocks": clk,
             "timing_mode": {"trace": tm[1] / nf, "decide": tm[2] / nf, "update": tm[3] / nf, "swap": tm[0] / nf,
-                            "event_total": tm[4]}}, None
+                            "event_total": tm[4]},
+            "taa": {"points": args.points, "frames": 200, "frames_per_s": 200 / dt, "ms_per_frame": dt * 1e3 / 200,
+                    "method": "TAA + masque dependances"}}, None
 
 
 def main():
@@ -603,7 +661,7 @@ def main():
         line = {"metric": METRIC, "value": res["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
-                "impl": "reference", "clocks": res["clocks"], "reference_timing_mode_ms": res["timing_mode"],
+                "impl": "reference", "clocks": res["clocks"], "reference_timing_mode_ms": res["timing_mode"], "taa": res["taa"],
                 "cpu_baseline": {"value": res["frames_per_s"], "unit": "frames/s", "cores": 1, "kind": "reference",
                                  "sample": "the reference's own kernels (cuda/poc_gpu.cu for sm_103a) on the GB300, driven by one host thread; "
                                            "the reference has no CPU implementation of this path"},
@@ -622,7 +680,7 @@ def main():
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
             "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
             "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "quality": res["quality"], "hashgrid": res["hashgrid"], "mlp": res["mlp"],
-            "adjoint": res["adjoint"]}
+            "adjoint": res["adjoint"], "taa": res["taa"]}
     print(json.dumps(line))
 
 

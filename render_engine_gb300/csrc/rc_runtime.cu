@@ -76,7 +76,8 @@ struct TaaRun {
     uint32_t seed = 0;
     int f = 0, prev_state = 0, verify_left = 0;
     float *x = nullptr, *H = nullptr, *H2 = nullptr, *mu = nullptr, *sg = nullptr, *rs = nullptr, *cnt = nullptr;
-    int *nb = nullptr, *react = nullptr;
+    int *qid = nullptr, *react = nullptr;   // quad of each point (-1: none)
+    const int4* quad = nullptr;              // per quad: first point, nu, nv
     uint8_t* pend = nullptr;
     uint32_t *cur = nullptr, *prev = nullptr;
     double *part = nullptr, *out = nullptr;
@@ -991,30 +992,27 @@ rc_status taa_alloc(rc_ctx* ctx) {
     const Scene& S = ctx->S;
     const size_t Np = (size_t)S.Np, NW = (size_t)ctx->NW;
     auto& pool = ctx->taa_bufs;
-    std::vector<int> nb(9 * Np, -1);
+    // the quad grid of each point (state 0's grids, as the reference's neighbourhood table);
+    // a point listed by two quads keeps the later one, as the table's rows would
+    std::vector<int> qid(Np, -1);
+    std::vector<int4> quad((size_t)std::max(S.Nq, 1));
     for (int q = 0; q < S.Nq; ++q) {
         const int nu = S.hdims[2 * q], nv = S.hdims[2 * q + 1], o = S.hoff[q];
-        for (int iv = 0; iv < nv; ++iv)
-            for (int iu = 0; iu < nu; ++iu) {
-                const size_t i = (size_t)o + (size_t)iv * nu + iu;
-                int k = 0;
-                for (int dv = -1; dv <= 1; ++dv)
-                    for (int du = -1; du <= 1; ++du) {
-                        const int a = iu + du, b = iv + dv;
-                        nb[9 * i + k++] = (a >= 0 && a < nu && b >= 0 && b < nv) ? o + b * nu + a : -1;
-                    }
-            }
+        quad[q] = make_int4(o, nu, nv, 0);
+        for (size_t i = (size_t)o; i < (size_t)o + (size_t)nu * nv; ++i) qid[i] = q;
     }
-    const int* dnb = nullptr;
+    const int* dq = nullptr;
+    const int4* dquad = nullptr;
     rc_status s;
     if ((s = dalloc(ctx, pool, &t.x, Np)) || (s = dalloc(ctx, pool, &t.H, Np)) || (s = dalloc(ctx, pool, &t.H2, Np)) ||
         (s = dalloc(ctx, pool, &t.mu, Np)) || (s = dalloc(ctx, pool, &t.sg, Np)) || (s = dalloc(ctx, pool, &t.react, Np)) ||
         (s = dalloc(ctx, pool, &t.pend, Np)) || (s = dalloc(ctx, pool, &t.cur, NW * Np)) || (s = dalloc(ctx, pool, &t.prev, NW * Np)) ||
         (s = dalloc(ctx, pool, &t.rs, 3 * (size_t)S.NR)) || (s = dalloc(ctx, pool, &t.cnt, (size_t)S.NR)) ||
         (s = dalloc(ctx, pool, &t.part, 3 * (size_t)taa::post_blocks(S.Np))) || (s = dalloc(ctx, pool, &t.out, 3)) ||
-        (s = dput(ctx, pool, &dnb, nb)))
+        (s = dput(ctx, pool, &dq, qid)) || (s = dput(ctx, pool, &dquad, quad)))
         return s;
-    t.nb = const_cast<int*>(dnb);
+    t.qid = const_cast<int*>(dq);
+    t.quad = dquad;
     const int NS = S.NS, NL = S.NL;
     t.dV.assign((size_t)NS * NS, nullptr);
     t.nV.assign((size_t)NS * NS, 0);
@@ -1767,7 +1765,7 @@ rc_status rc_taa_frame(rc_ctx* ctx, int state, float* err) {
             ++kernels;
         }
     }
-    CKR(taa::post(t.x, t.nb, t.H, t.H2, t.mu, t.sg, t.react, Np, M.alpha, TAA_ALPHA_R, M.gamma, d.ref, d.valid, err ? t.part : nullptr,
+    CKR(taa::post(t.x, t.qid, t.quad, t.H, t.H2, t.mu, t.sg, t.react, Np, M.alpha, TAA_ALPHA_R, M.gamma, d.ref, d.valid, err ? t.part : nullptr,
                   t.out, st));
     kernels += err ? 2 : 1;
     std::swap(t.H, t.H2);

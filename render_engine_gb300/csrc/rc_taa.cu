@@ -101,8 +101,12 @@ __global__ void k_zone_decide(const float* __restrict__ rs, const float* __restr
 
 // k_taa_stats + k_taa_update + k_taa_err (poc_gpu.cu:1100-1108, 1152-1166) for one point:
 // 3x3 mean and deviation of the samples, the clamped and blended history, and this block's
-// FP64 partial error sums over the new history (summed in a fixed order).
-__global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const int* __restrict__ nb, const float* __restrict__ H,
+// FP64 partial error sums over the new history (summed in a fixed order).  The 3x3
+// neighbourhood on the point's quad grid (run_taa_mode's table, poc_gpu.cu:1192-1203) is
+// derived from the point's quad: quad[q] = (first point, nu, nv), neighbours in the table's
+// order (dv outer, du inner), -1 outside the grid; a point of no quad has no neighbours.
+__global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const int* __restrict__ qid, const int4* __restrict__ quad,
+                                            const float* __restrict__ H,
                                             float* __restrict__ H2, float* __restrict__ mu_out, float* __restrict__ sg_out,
                                             int* __restrict__ react, int Np, float alpha, float alpha_r, float gamma,
                                             const float* __restrict__ ref, const uint8_t* __restrict__ valid, double* __restrict__ part) {
@@ -112,13 +116,19 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
     if (i < Np) {
         float s1 = 0.f, s2 = 0.f;
         int n = 0;
-        for (int k = 0; k < 9; ++k) {
-            const int j = nb[9 * (size_t)i + k];
-            if (j < 0) continue;
-            const float v = x[j];
-            s1 += v;
-            s2 += v * v;
-            n++;
+        const int q = qid[i];
+        if (q >= 0) {
+            const int4 g = quad[q];   // first point, nu, nv
+            const int r = i - g.x, iu = r % g.y, iv = r / g.y;
+            for (int dv = -1; dv <= 1; ++dv)
+                for (int du = -1; du <= 1; ++du) {
+                    const int a = iu + du, b = iv + dv;
+                    if (a < 0 || a >= g.y || b < 0 || b >= g.z) continue;
+                    const float v = x[g.x + b * g.y + a];
+                    s1 += v;
+                    s2 += v * v;
+                    n++;
+                }
         }
         const float mu = s1 / n;
         const float sg = sqrtf(fmaxf(s2 / n - mu * mu, 0.f));
@@ -214,9 +224,9 @@ cudaError_t zone_decide(const float* rs, const float* cnt, uint8_t* pend, const 
     return cudaGetLastError();
 }
 
-cudaError_t post(const float* x, const int* nb, const float* H, float* H2, float* mu, float* sg, int* react, int Np, float alpha,
-                 float alpha_r, float gamma, const float* ref, const uint8_t* valid, double* part, double* out, cudaStream_t st) {
-    k_post<<<blocks(Np), B, 0, st>>>(x, nb, H, H2, mu, sg, react, Np, alpha, alpha_r, gamma, ref, valid, part);
+cudaError_t post(const float* x, const int* qid, const int4* quad, const float* H, float* H2, float* mu, float* sg, int* react, int Np,
+                 float alpha, float alpha_r, float gamma, const float* ref, const uint8_t* valid, double* part, double* out, cudaStream_t st) {
+    k_post<<<blocks(Np), B, 0, st>>>(x, qid, quad, H, H2, mu, sg, react, Np, alpha, alpha_r, gamma, ref, valid, part);
     if (part) k_err_final<<<1, B, 0, st>>>(part, blocks(Np), out);
     return cudaGetLastError();
 }

@@ -15,9 +15,10 @@ cudaError_t zone_acc(const float* x, const float* H, const uint8_t* pend, const 
                      cudaStream_t st);
 cudaError_t zone_decide(const float* rs, const float* cnt, uint8_t* pend, const int* region, int Np, int* react, int only_pending, int rf,
                         int clear_pending, cudaStream_t st);
-// statistics, update into H2 and (part != NULL) the error sums of H2 into out[3]
-cudaError_t post(const float* x, const int* nb, const float* H, float* H2, float* mu, float* sg, int* react, int Np, float alpha,
-                 float alpha_r, float gamma, const float* ref, const uint8_t* valid, double* part, double* out, cudaStream_t st);
+// statistics, update into H2 and (part != NULL) the error sums of H2 into out[3]; qid = the
+// quad of each point (-1: none), quad[q] = (first point, nu, nv, 0)
+cudaError_t post(const float* x, const int* qid, const int4* quad, const float* H, float* H2, float* mu, float* sg, int* react, int Np,
+                 float alpha, float alpha_r, float gamma, const float* ref, const uint8_t* valid, double* part, double* out, cudaStream_t st);
 
 }  // namespace taa
 }  // namespace rc
