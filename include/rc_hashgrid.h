@@ -115,7 +115,8 @@ rc_status rc_hg_clear(rc_hg* hg);
 
 /* Entries of n surface points (d_pos, d_nrm: 3 floats each), inserted when missing (linear
  * probing over at most 64 slots; a missing key takes the first evicted slot it passed, else
- * the empty slot that ended the probe); d_entry[i] = RC_HG_INVALID when there was none. */
+ * the empty slot that ended the probe); d_entry[i] = RC_HG_INVALID when there was none, and
+ * for a point whose normal is (0, 0, 0) (no surface: nothing is inserted). */
 rc_status rc_hg_insert(rc_hg* hg, const float* d_pos, const float* d_nrm, int n, uint32_t* d_entry);
 
 /* Add n radiance samples (d_rgb: 3 floats each) to their entries. */
@@ -128,6 +129,57 @@ rc_status rc_hg_begin_frame(rc_hg* hg, uint32_t dep_frame, uint32_t period);
 /* Dependency marking of npaths paths; path p is d_vertices[d_path_start[p] ..
  * d_path_start[p + 1]) (npaths + 1 offsets). */
 rc_status rc_hg_mark_paths(rc_hg* hg, const rc_hg_vertex* d_vertices, const int* d_path_start, int npaths);
+
+/* The same for paths in fixed slots: path p is d_vertices[p * stride .. p * stride + d_len[p]). */
+rc_status rc_hg_mark_paths_strided(rc_hg* hg, const rc_hg_vertex* d_vertices, const int* d_len, int stride, int npaths);
+
+/* Per-voxel light masks (new, no reference): a res^3 grid (res <= 256) over the zone box,
+ * 64 bits per voxel; bit l of a voxel is set when a shadow ray toward light l crossed it.  Where
+ * the 96 zones of the entry masks say which region a path crossed, these say which lights'
+ * visibility a change in a region can alter, at up to 256^3 resolution: an occluder event's
+ * light bits are the OR of the voxel masks under the object (rc_hg_voxels_box_lights).
+ * init (re)allocates and clears; clear empties the masks (e.g. every bank period). */
+rc_status rc_hg_voxels_init(rc_hg* hg, int res);
+rc_status rc_hg_voxels_clear(rc_hg* hg);
+/* For every vertex whose sampled light l < 64 was visible: bit l in the voxels of 20 evenly
+ * spaced samples of its shadow segment (the hit to the light, at most tracing_distance), as
+ * k_build rasterises its shadow rays (poc_gpu.cu:192-197).  Voxel of a point:
+ * min(max(int((x - zone_lo) / (zone_hi - zone_lo) * res), 0), res - 1) per axis. */
+rc_status rc_hg_voxels_mark(rc_hg* hg, const rc_hg_vertex* d_vertices, const int* d_len, int stride, int npaths);
+/* OR of the masks of the voxels a box [lo, hi] overlaps (host arrays; synchronises). */
+rc_status rc_hg_voxels_box_lights(rc_hg* hg, const float lo[3], const float hi[3], uint64_t* lights);
+/* All res^3 masks to host memory, voxel (x, y, z) at (z * res + y) * res + x (synchronises). */
+rc_status rc_hg_voxels_copy(rc_hg* hg, uint64_t* host, size_t count);
+
+/* Camera paths over a loaded scene feeding the cache (new, no reference: bench B has no
+ * camera, bench A's path tracer is HLSL).  One path per pixel of `cam` through the geometry
+ * of `state` of the context's scene: a primary ray and `bounces` cosine-sampled bounces; a
+ * back face, a surface without cache point or an escaping ray ends the path.  At every vertex
+ * one light is sampled among the scene's point lights (intensity of the state x light_rgb),
+ * the rectangle light and the sun, with probability proportional to its unshadowed
+ * contribution, and its shadow ray traced; the vertex's radiance sample is
+ * L_k = A_k (E_k + L_{k+1}) in RGB (A: the albedo of the hit's cache point, E: the sampled
+ * direct light over its probability, L after the last vertex: sky_rgb for an escaping ray,
+ * 0 otherwise), the convention of the reference's gather A (Edir + Lc), poc_gpu.cu:472-478.
+ * Every vertex is inserted and its sample accumulated; the paths' dependency masks are marked
+ * (rc_hg_mark_paths_strided: light index NL = the rectangle, NL + 1 = the sun) and, after
+ * rc_hg_voxels_init, the per-voxel light masks.  d_image (may be NULL): width x height RGB
+ * floats, the primary vertices' L_0.  Runs on the cache's stream after the context's work. */
+typedef struct {
+    rc_camera cam;
+    int bounces;               /* 0 .. RC_HG_MAX_DEPTH - 1 */
+    uint32_t seed, frame;
+    float light_rgb[32][3];    /* colour of each point light (all zero = white) */
+    float area_corner[3], area_u[3], area_v[3], area_rgb[3];   /* one-sided rectangle light facing u x v; rgb 0 = none */
+    float sun_dir[3], sun_rgb[3];  /* direction towards the sun, irradiance; rgb 0 = none */
+    float sky_rgb[3];          /* radiance of escaping rays */
+} rc_hg_path_params;
+rc_status rc_hg_camera_paths(rc_hg* hg, rc_ctx* ctx, int state, const rc_hg_path_params* prm, float* d_image);
+/* Device arrays of the last camera pass, per slot (pixel p, vertex k at p * (bounces + 1) + k):
+ * vertices (rc_hg_vertex), radiance samples (3 floats), entries (uint32) and per pixel the
+ * path length (int); for harnesses.  Pointers stay valid until the next pass. */
+rc_status rc_hg_camera_arrays(rc_ctx* ctx, const rc_hg_vertex** d_vertices, const float** d_rgb, const uint32_t** d_entry,
+                              const int** d_len, int* stride, int* npaths);
 
 /* Resolve every entry: invalidation by inv[4] (zones x, y, z, lights; all zero = none),
  * accumulation into the resolved radiance, eviction of entries stale for more than

@@ -308,9 +308,11 @@ uint64_t hgo_key(const hgo_config* c, const float p[3], const float n[3]) {
 void hgo_insert(const hgo_config* c, hgo_state* s, const float* pos, const float* nrm, int n, uint32_t* entry) {
     const uint32_t mask = c->capacity - 1u;
     for (int i = 0; i < n; ++i) {
-        const uint64_t key = hgo_key(c, pos + 3 * (size_t)i, nrm + 3 * (size_t)i);
-        uint32_t h = (uint32_t)mix64(key) & mask, tomb = INVALID;
         entry[i] = INVALID;
+        const float* nn = nrm + 3 * (size_t)i;
+        if (nn[0] == 0.f && nn[1] == 0.f && nn[2] == 0.f) continue;   /* no surface point: no entry */
+        const uint64_t key = hgo_key(c, pos + 3 * (size_t)i, nn);
+        uint32_t h = (uint32_t)mix64(key) & mask, tomb = INVALID;
         for (int probe = 0; probe < 64; ++probe) {
             const uint64_t k = s->keys[h];
             if (k == key) { entry[i] = h; break; }
@@ -373,4 +375,30 @@ void hgo_restore(hgo_state* s, const hgo_snap_rec* recs, uint32_t count) {
         r[2] = recs[i].sample_data & 0xFFFFu;
         r[3] = 0;
     }
+}
+
+/* Per-voxel light masks (rc_hg_voxels_mark): voxel of a point per axis
+ * min(max(int((x - lo) / (hi - lo) * res), 0), res - 1); for each vertex whose sampled light
+ * l < 64 was visible, bit l in the voxels of 20 samples h + (to_light * min(dist, td)) * k / 19. */
+static int hgo_vox_axis(float x, float lo, float hi, int res) {
+    int i = (int)((x - lo) / (hi - lo) * (float)res);
+    return i < 0 ? 0 : (i > res - 1 ? res - 1 : i);
+}
+void hgo_voxels_mark(const hgo_config* c, int res, uint64_t* vox, const hgo_vertex* v, const int* len, int stride, int npaths) {
+    for (int p = 0; p < npaths; ++p)
+        for (int j = 0; j < len[p]; ++j) {
+            const hgo_vertex* x = &v[(size_t)p * stride + j];
+            if ((x->flags & 1u) || x->light_index < 0 || x->light_index >= 64 || !(x->flags & 2u)) continue;
+            const uint64_t bit = 1ull << x->light_index;
+            const float r = x->light_dist < c->tracing_distance ? x->light_dist : c->tracing_distance;
+            float d[3];
+            for (int k = 0; k < 3; ++k) d[k] = x->to_light[k] * r;
+            for (int k = 0; k < 20; ++k) {
+                const float t = (float)k / 19.f;
+                const int ix = hgo_vox_axis(x->hit[0] + d[0] * t, c->zone_lo[0], c->zone_hi[0], res);
+                const int iy = hgo_vox_axis(x->hit[1] + d[1] * t, c->zone_lo[1], c->zone_hi[1], res);
+                const int iz = hgo_vox_axis(x->hit[2] + d[2] * t, c->zone_lo[2], c->zone_hi[2], res);
+                vox[((size_t)iz * res + iy) * res + ix] |= bit;
+            }
+        }
 }

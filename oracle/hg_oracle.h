@@ -70,6 +70,7 @@ void hgo_insert(const hgo_config* c, hgo_state* s, const float* pos, const float
 void hgo_accumulate(hgo_state* s, const uint32_t* entry, const float* rgb, int n);
 uint32_t hgo_snapshot(const hgo_config* c, const hgo_state* s, hgo_snap_rec* recs, uint32_t cap);
 void hgo_restore(hgo_state* s, const hgo_snap_rec* recs, uint32_t count);
+void hgo_voxels_mark(const hgo_config* c, int res, uint64_t* vox, const hgo_vertex* v, const int* len, int stride, int npaths);
 uint16_t hgo_f2h(float f);
 float hgo_h2f(uint16_t h);
 

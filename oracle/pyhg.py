@@ -61,6 +61,7 @@ def _lib():
         L.hgo_f2h.restype = ctypes.c_uint16
         L.hgo_h2f.argtypes = [ctypes.c_uint16]
         L.hgo_h2f.restype = ctypes.c_float
+        L.hgo_voxels_mark.argtypes = [C, i, vp, vp, vp, i, i]
         _bound = True
     return L
 
@@ -162,3 +163,12 @@ def f2h(x: float) -> int:
 
 def h2f(h: int) -> float:
     return float(_lib().hgo_h2f(h))
+
+
+def voxels_mark(cfg: Config, res: int, vertices: np.ndarray, lengths: np.ndarray, stride: int) -> np.ndarray:
+    """Per-voxel light masks of a batch of paths in fixed slots (rc_hg_voxels_mark), from zero."""
+    vox = np.zeros(res ** 3, np.uint64)
+    v = np.ascontiguousarray(vertices)
+    ln = np.ascontiguousarray(lengths, np.int32)
+    _lib().hgo_voxels_mark(ctypes.byref(cfg), res, _p(vox), _p(v), _p(ln), stride, len(ln))
+    return vox

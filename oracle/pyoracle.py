@@ -87,6 +87,8 @@ def lib():
         L.osc_taa_frame.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float)]
         L.osc_taa_array.restype = ctypes.c_void_p
         L.osc_taa_array.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+        L.osc_camera_paths.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.osc_frozen_hits.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p]
         L.osc_direct_unit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.osc_path_trace.restype = ctypes.c_int
@@ -98,6 +100,20 @@ def lib():
 
 def set_threads(n: int) -> None:
     lib().osc_set_threads(int(n))
+
+
+VERTEX_DTYPE = np.dtype([("origin", "<f4", 3), ("dir", "<f4", 3), ("hit", "<f4", 3), ("to_light", "<f4", 3),
+                         ("light_dist", "<f4"), ("light_index", "<i4"), ("entry", "<u4"), ("flags", "<u4")])
+
+
+class _PathParams(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_float * 3), ("fwd", ctypes.c_float * 3), ("right", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("tx", ctypes.c_float), ("ty", ctypes.c_float), ("w", ctypes.c_int), ("h", ctypes.c_int), ("bounces", ctypes.c_int),
+                ("seed", ctypes.c_uint32), ("frame", ctypes.c_uint32), ("td", ctypes.c_float),
+                ("lpos", (ctypes.c_float * 3) * 32), ("lrgb", (ctypes.c_float * 3) * 32), ("lint", ctypes.c_float * 32),
+                ("area_corner", ctypes.c_float * 3), ("area_u", ctypes.c_float * 3), ("area_v", ctypes.c_float * 3),
+                ("area_rgb", ctypes.c_float * 3), ("sun_dir", ctypes.c_float * 3), ("sun_rgb", ctypes.c_float * 3),
+                ("sky_rgb", ctypes.c_float * 3)]
 
 
 class Scene:
@@ -129,6 +145,40 @@ class Scene:
         if not ptr or nb.value == 0:
             return np.zeros(0, dt)
         return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)), (nb.value,)).view(dt).copy()
+
+    def camera_paths(self, state: int, basis: dict, width: int, height: int, bounces: int, seed: int, frame: int, td: float,
+                     lpos, inten, light_rgb=None, area=None, sun=None, sky=(0.0, 0.0, 0.0)) -> dict:
+        """The camera-path pass (rc_hg_camera_paths) on the CPU; basis as native.camera_basis gives it,
+        lpos / inten: the scene's light positions and the state's intensities."""
+        if not self.built:
+            self.build()
+        P = _PathParams()
+        for k in range(3):
+            P.eye[k], P.fwd[k], P.right[k], P.up[k] = basis["eye"][k], basis["fwd"][k], basis["right"][k], basis["up"][k]
+        P.tx, P.ty = basis["tx"], basis["ty"]
+        P.w, P.h, P.bounces, P.seed, P.frame, P.td = width, height, bounces, seed & 0xFFFFFFFF, frame & 0xFFFFFFFF, td
+        L = np.asarray(lpos, np.float32).reshape(-1, 3)
+        white = light_rgb is None or not np.any(np.asarray(light_rgb))
+        for l in range(self.NL):
+            P.lpos[l][:] = [float(x) for x in L[l]]
+            P.lrgb[l][:] = [1.0, 1.0, 1.0] if white else [float(x) for x in light_rgb[l]]
+            P.lint[l] = float(inten[l])
+        if area is not None:
+            P.area_corner[:], P.area_u[:], P.area_v[:], P.area_rgb[:] = (list(map(float, v)) for v in area)
+        if sun is not None:
+            P.sun_dir[:], P.sun_rgb[:] = (list(map(float, v)) for v in sun)
+        P.sky_rgb[:] = [float(x) for x in sky]
+        S = bounces + 1
+        n = width * height * S
+        vtx = np.zeros(n, VERTEX_DTYPE)
+        pos = np.zeros((n, 3), np.float32)
+        nrm = np.zeros((n, 3), np.float32)
+        rgb = np.zeros((n, 3), np.float32)
+        ln = np.zeros(width * height, np.int32)
+        img = np.zeros((width * height, 3), np.float32)
+        lib().osc_camera_paths(self.p, state, ctypes.byref(P), vtx.ctypes.data, pos.ctypes.data, nrm.ctypes.data, rgb.ctypes.data,
+                               ln.ctypes.data, img.ctypes.data)
+        return {"vertices": vtx, "pos": pos, "nrm": nrm, "rgb": rgb, "len": ln, "image": img, "stride": S}
 
     def frozen_hits(self, state: int, seed: int, K: int) -> np.ndarray:
         """(Np, K) cache point reached by each of the K rays of one reference iteration, -1 = not counted."""

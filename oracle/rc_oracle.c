@@ -1616,3 +1616,183 @@ void* osc_taa_array(osc_taa* t, int which, size_t* nbytes) {
     *nbytes = 0;
     return NULL;
 }
+
+/* ------------------------------------------------------------------ camera paths
+ * The camera-path pass feeding the hash-grid cache (rc_hg_camera_paths; new, no reference),
+ * in FP32 with this file's trace and hit resolution.  Per pixel: the primary ray through the
+ * pixel centre, then `bounces` cosine bounces; one light sampled per vertex among the point
+ * lights, the rectangle and the sun in proportion to its unshadowed contribution (the
+ * rectangle's estimated at its centre with both cosines at least 0.1), its shadow ray traced;
+ * radiance L_k = A_k (E_k + L_{k+1}) from the last surface vertex back.  Random numbers: the
+ * frames' generator seeded per pixel. */
+static inline float lumf(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
+static float shadow_tf(const osc_scene* S, const ostate* st, v3 O, v3 D) {
+    float t;
+    int q;
+    trace_full(S, st, O, D, &t, &q);
+    return q == -1 ? INFINITY : t;
+}
+
+void osc_camera_paths(const osc_scene* S, int si, const osc_path_params* P, osc_path_vertex* vtx, float* pos, float* nrm, float* rgb,
+                      int* len, float* img) {
+    const ostate* st = &S->st[si];
+    const int W = P->w, Hh = P->h, SL = P->bounces + 1, NL = S->NL;
+    float an[3] = {0, 0, 0}, aarea = 0.f;
+    const int area_on = P->area_rgb[0] > 0.f || P->area_rgb[1] > 0.f || P->area_rgb[2] > 0.f;
+    const int sun_on = P->sun_rgb[0] > 0.f || P->sun_rgb[1] > 0.f || P->sun_rgb[2] > 0.f;
+    if (area_on) {
+        double n[3] = {(double)P->area_u[1] * P->area_v[2] - (double)P->area_u[2] * P->area_v[1],
+                       (double)P->area_u[2] * P->area_v[0] - (double)P->area_u[0] * P->area_v[2],
+                       (double)P->area_u[0] * P->area_v[1] - (double)P->area_u[1] * P->area_v[0]};
+        double a = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int k = 0; k < 3; ++k) an[k] = (float)(n[k] / a);
+        aarea = (float)a;
+    }
+    float sdir[3] = {0, 0, 0};
+    if (sun_on) {
+        double d[3] = {P->sun_dir[0], P->sun_dir[1], P->sun_dir[2]};
+        double l = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int k = 0; k < 3; ++k) sdir[k] = (float)(d[k] / l);
+    }
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int y = 0; y < Hh; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t pix = (size_t)y * W + x, base = pix * SL;
+            uint32_t rs = hash32(P->seed * 0x9E3779B9u ^ hash32(P->frame * 0x85EBCA6Bu ^ hash32((uint32_t)pix + 1u)));
+            float sx = (((float)x + 0.5f) / (float)W * 2.f - 1.f) * P->tx, sy = (1.f - ((float)y + 0.5f) / (float)Hh * 2.f) * P->ty;
+            v3 D = V(P->fwd[0] + P->right[0] * sx + P->up[0] * sy, P->fwd[1] + P->right[1] * sx + P->up[1] * sy,
+                     P->fwd[2] + P->right[2] * sx + P->up[2] * sy);
+            D = vmul(D, 1.f / sqrtf(vdot(D, D)));
+            v3 O = V(P->eye[0], P->eye[1], P->eye[2]);
+            float A[8], E[8][3];
+            int n = 0, escaped = 0;
+            for (int k = 0; k < SL; ++k) {
+                float t;
+                int q, pi;
+                int hit = trace_full(S, st, O, D, &t, &q);
+                v3 Hp = hit ? vadd(O, vmul(D, t)) : O;
+                osc_path_vertex vx;
+                memset(&vx, 0, sizeof vx);
+                vx.origin[0] = O.x; vx.origin[1] = O.y; vx.origin[2] = O.z;
+                vx.dir[0] = D.x; vx.dir[1] = D.y; vx.dir[2] = D.z;
+                vx.light_index = -1;
+                vx.entry = 0xFFFFFFFFu;
+                if (!hit) {
+                    vx.hit[0] = O.x; vx.hit[1] = O.y; vx.hit[2] = O.z;
+                    vx.flags = 1u;
+                    vtx[base + k] = vx;
+                    escaped = 1;
+                    n = k + 1;
+                    break;
+                }
+                if (resolve_hit(S, st, hit, Hp, D, q, 0, &pi)) break;
+                v3 nn;
+                if (q >= 0) {
+                    const float* Q = st->Q + 12 * (size_t)q;
+                    nn = V(Q[9], Q[10], Q[11]);
+                } else {
+                    const float* n4 = S->STN + 4 * (size_t)(-2 - q);
+                    nn = V(n4[0], n4[1], n4[2]);
+                    if (vdot(nn, D) > 0.f) nn = vmul(nn, -1.f);
+                }
+                const float alb = S->A[pi];
+                const v3 Os = vadd(Hp, vmul(nn, 1e-3f));
+                float Wp = 0.f, wa = 0.f, ws = 0.f;
+                for (int l = 0; l < NL; ++l) {
+                    v3 d = vsub(V(P->lpos[l][0], P->lpos[l][1], P->lpos[l][2]), Hp);
+                    float r = sqrtf(vdot(d, d)), rr = fmaxf(r, 0.05f);
+                    Wp += P->lint[l] * lumf(P->lrgb[l][0], P->lrgb[l][1], P->lrgb[l][2]) * fmaxf(vdot(nn, d) / r, 0.f) / (rr * rr);
+                }
+                if (area_on) {
+                    v3 C = V(P->area_corner[0] + 0.5f * (P->area_u[0] + P->area_v[0]), P->area_corner[1] + 0.5f * (P->area_u[1] + P->area_v[1]),
+                             P->area_corner[2] + 0.5f * (P->area_u[2] + P->area_v[2]));
+                    v3 d = vsub(C, Hp);
+                    float r = sqrtf(vdot(d, d)), rr = fmaxf(r, 0.05f);
+                    v3 w = vmul(d, 1.f / r);
+                    wa = lumf(P->area_rgb[0], P->area_rgb[1], P->area_rgb[2]) * aarea * fmaxf(vdot(nn, w), 0.1f) *
+                         fmaxf(-(an[0] * w.x + an[1] * w.y + an[2] * w.z), 0.1f) / (rr * rr);
+                }
+                if (sun_on) ws = lumf(P->sun_rgb[0], P->sun_rgb[1], P->sun_rgb[2]) * fmaxf(nn.x * sdir[0] + nn.y * sdir[1] + nn.z * sdir[2], 0.f);
+                const float Wt = Wp + wa + ws;
+                float e3[3] = {0.f, 0.f, 0.f};
+                if (Wt > 0.f) {
+                    const float u = rnd(&rs) * Wt;
+                    if (u < Wp) {
+                        int l;
+                        float acc = 0.f, wl = 0.f, r = 0.f;
+                        v3 d = V(0, 0, 0);
+                        for (l = 0; l < NL; ++l) {
+                            d = vsub(V(P->lpos[l][0], P->lpos[l][1], P->lpos[l][2]), Hp);
+                            r = sqrtf(vdot(d, d));
+                            float rr = fmaxf(r, 0.05f), cs = fmaxf(vdot(nn, d) / r, 0.f);
+                            wl = P->lint[l] * lumf(P->lrgb[l][0], P->lrgb[l][1], P->lrgb[l][2]) * cs / (rr * rr);
+                            acc += wl;
+                            if (u < acc && wl > 0.f) break;
+                        }
+                        if (l > NL - 1) l = NL - 1;
+                        v3 w = vmul(d, 1.f / r);
+                        int vis = shadow_tf(S, st, Os, w) >= r - 1e-3f;
+                        vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
+                        vx.light_dist = r;
+                        vx.light_index = l;
+                        if (vis && wl > 0.f) {
+                            vx.flags |= 2u;
+                            float ln = lumf(P->lrgb[l][0], P->lrgb[l][1], P->lrgb[l][2]);
+                            for (int ch = 0; ch < 3; ++ch) e3[ch] = Wt * P->lrgb[l][ch] / ln;
+                        }
+                    } else if (u < Wp + wa) {
+                        float u1 = rnd(&rs);
+                        float u2 = rnd(&rs);
+                        v3 Y = V(P->area_corner[0] + u1 * P->area_u[0] + u2 * P->area_v[0], P->area_corner[1] + u1 * P->area_u[1] + u2 * P->area_v[1],
+                                 P->area_corner[2] + u1 * P->area_u[2] + u2 * P->area_v[2]);
+                        v3 d = vsub(Y, Hp);
+                        float r = sqrtf(vdot(d, d)), rr = fmaxf(r, 0.05f);
+                        v3 w = vmul(d, 1.f / r);
+                        float cs = fmaxf(vdot(nn, w), 0.f), ca = fmaxf(-(an[0] * w.x + an[1] * w.y + an[2] * w.z), 0.f);
+                        int vis = cs > 0.f && ca > 0.f && shadow_tf(S, st, Os, w) >= r - 1e-3f;
+                        vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
+                        vx.light_dist = r;
+                        vx.light_index = NL;
+                        if (vis) {
+                            vx.flags |= 2u;
+                            float geo = aarea * cs * ca / (rr * rr) * (Wt / wa);
+                            for (int ch = 0; ch < 3; ++ch) e3[ch] = P->area_rgb[ch] * geo;
+                        }
+                    } else {
+                        v3 w = V(sdir[0], sdir[1], sdir[2]);
+                        int vis = shadow_tf(S, st, Os, w) == INFINITY;
+                        vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
+                        vx.light_dist = P->td;
+                        vx.light_index = NL + 1;
+                        if (vis) {
+                            vx.flags |= 2u;
+                            float ln = lumf(P->sun_rgb[0], P->sun_rgb[1], P->sun_rgb[2]);
+                            for (int ch = 0; ch < 3; ++ch) e3[ch] = Wt * P->sun_rgb[ch] / ln;
+                        }
+                    }
+                }
+                vx.hit[0] = Hp.x; vx.hit[1] = Hp.y; vx.hit[2] = Hp.z;
+                vtx[base + k] = vx;
+                pos[3 * (base + k)] = Hp.x; pos[3 * (base + k) + 1] = Hp.y; pos[3 * (base + k) + 2] = Hp.z;
+                nrm[3 * (base + k)] = nn.x; nrm[3 * (base + k) + 1] = nn.y; nrm[3 * (base + k) + 2] = nn.z;
+                A[k] = alb;
+                E[k][0] = e3[0]; E[k][1] = e3[1]; E[k][2] = e3[2];
+                n = k + 1;
+                float u1 = rnd(&rs);
+                float u2 = rnd(&rs);
+                O = Os;
+                D = cosine_dir(nn, u1, u2);
+            }
+            const int nsurf = n - (escaped ? 1 : 0);
+            for (int k = nsurf; k < SL; ++k)
+                for (int ch = 0; ch < 3; ++ch) { rgb[3 * (base + k) + ch] = 0.f; nrm[3 * (base + k) + ch] = 0.f; pos[3 * (base + k) + ch] = 0.f; }
+            float L[3] = {0.f, 0.f, 0.f};
+            if (escaped) { L[0] = P->sky_rgb[0]; L[1] = P->sky_rgb[1]; L[2] = P->sky_rgb[2]; }
+            for (int k = nsurf - 1; k >= 0; --k)
+                for (int ch = 0; ch < 3; ++ch) { L[ch] = A[k] * (E[k][ch] + L[ch]); rgb[3 * (base + k) + ch] = L[ch]; }
+            len[pix] = n;
+            if (img)
+                for (int ch = 0; ch < 3; ++ch) img[3 * pix + ch] = nsurf > 0 || escaped ? L[ch] : 0.f;
+        }
+}

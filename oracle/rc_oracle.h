@@ -88,6 +88,25 @@ void osc_direct_unit(const osc_scene* s, int si, float* out);
 int osc_path_trace(const osc_scene* s, int si, const int* pts, int npts, int paths, int min_bounces, uint64_t seed, double* mean,
                    double* sem);
 
+/* Camera paths feeding the hash-grid cache (rc_hg_camera_paths in include/rc_hashgrid.h). */
+typedef struct {
+    float eye[3], fwd[3], right[3], up[3], tx, ty;   /* camera frame as rc_render derives it */
+    int w, h, bounces;
+    uint32_t seed, frame;
+    float td;                                        /* tracing distance (sun shadow segments) */
+    float lpos[32][3], lrgb[32][3], lint[32];        /* point lights: position, colour, intensity */
+    float area_corner[3], area_u[3], area_v[3], area_rgb[3];
+    float sun_dir[3], sun_rgb[3], sky_rgb[3];
+} osc_path_params;
+typedef struct {   /* the layout of rc_hg_vertex */
+    float origin[3], dir[3], hit[3], to_light[3];
+    float light_dist;
+    int32_t light_index;
+    uint32_t entry, flags;
+} osc_path_vertex;
+void osc_camera_paths(const osc_scene* s, int si, const osc_path_params* p, osc_path_vertex* vtx, float* pos, float* nrm, float* rgb,
+                      int* len, float* img);
+
 /* taa mode (run_taa_mode, poc_gpu.cu:1175-1282): format-2 scenes with references. */
 typedef struct osc_taa osc_taa;
 osc_taa* osc_taa_new(osc_scene* s);

@@ -34,6 +34,9 @@ struct rc_hg {
     int bank_sel = 0;
     uint32_t* scratch = nullptr;   // counters (4) + per-block snapshot counts
     size_t scratch_words = 0;
+    unsigned long long* vox = nullptr;   // per-voxel light masks, vres^3 (rc_hg_voxels_init)
+    unsigned long long* vox_out = nullptr;
+    int vres = 0;
     std::string err;
 };
 
@@ -157,16 +160,19 @@ __device__ __forceinline__ void dep_or(uint4* bank, uint32_t e, uint4 m) {
 // thread reads them, to the earlier vertices (the reference reads them the same way, racing
 // with other paths' updates of that entry).
 // bw is one of b0 / b1 (no __restrict__ on them: they alias).
+// Paths are either contiguous (ps = npaths + 1 offsets) or in fixed slots (ps = NULL, path p is
+// v[p * stride .. p * stride + plen[p])).
 __global__ void __launch_bounds__(HG_BLOCK) k_hg_mark(const HgDev c, const rc_hg_vertex* __restrict__ v,
-                                                      const int* __restrict__ ps, int npaths, uint4* bw, const uint4* b0,
-                                                      const uint4* b1) {
+                                                      const int* __restrict__ ps, const int* __restrict__ plen, int stride, int npaths,
+                                                      uint4* bw, const uint4* b0, const uint4* b1) {
     const int p = blockIdx.x * HG_BLOCK + threadIdx.x;
     if (p >= npaths) return;
     uint32_t idx[RC_HG_MAX_DEPTH];
     int len = 0;
     const int D = c.depth;
-    const int j1 = ps[p + 1];
-    for (int j = ps[p]; j < j1; ++j) {
+    const long long j0 = ps ? ps[p] : (long long)p * stride;
+    const long long j1 = ps ? ps[p + 1] : j0 + plen[p];
+    for (long long j = j0; j < j1; ++j) {
         const rc_hg_vertex x = v[j];
         const float o[3] = {x.origin[0], x.origin[1], x.origin[2]};
         if (x.flags & RC_HG_MISS) {
@@ -207,6 +213,57 @@ __global__ void __launch_bounds__(HG_BLOCK) k_hg_mark(const HgDev c, const rc_hg
     }
 }
 
+// ------------------------------------------------------------------ per-voxel light masks
+// A res^3 grid over the zone box; voxel of a point as the reference's vox_of (poc_gpu.cu:137-142)
+// with explicitly rounded operations.
+__device__ __forceinline__ int vox_axis(float x, float lo, float hi, int res) {
+    const int i = (int)__fmul_rn(__fdiv_rn(__fsub_rn(x, lo), __fsub_rn(hi, lo)), (float)res);
+    return min(max(i, 0), res - 1);
+}
+
+// Bit l of every voxel on the shadow segment of a vertex whose sampled light l (< 64) was
+// visible: 20 evenly spaced samples from the hit to the light (at most tracing_distance), as
+// k_build rasterises its shadow rays (poc_gpu.cu:192-197).  A bit already set is not written.
+__global__ void __launch_bounds__(HG_BLOCK) k_vox_mark(const HgDev c, const rc_hg_vertex* __restrict__ v, const int* __restrict__ plen,
+                                                       int stride, int npaths, unsigned long long* __restrict__ vox, int res) {
+    const int p = blockIdx.x * HG_BLOCK + threadIdx.x;
+    if (p >= npaths) return;
+    const long long j0 = (long long)p * stride;
+    for (long long j = j0; j < j0 + plen[p]; ++j) {
+        const rc_hg_vertex x = v[j];
+        if ((x.flags & RC_HG_MISS) || x.light_index < 0 || x.light_index >= 64 || !(x.flags & RC_HG_LIGHT_VISIBLE)) continue;
+        const unsigned long long bit = 1ull << x.light_index;
+        const float r = mn(x.light_dist, c.td);
+        float a[3], d[3];
+        for (int k = 0; k < 3; ++k) {
+            a[k] = x.hit[k];
+            d[k] = __fmul_rn(x.to_light[k], r);
+        }
+        for (int k = 0; k < 20; ++k) {
+            const float t = __fdiv_rn((float)k, 19.f);
+            const int ix = vox_axis(__fadd_rn(a[0], __fmul_rn(d[0], t)), c.zlo[0], c.zhi[0], res);
+            const int iy = vox_axis(__fadd_rn(a[1], __fmul_rn(d[1], t)), c.zlo[1], c.zhi[1], res);
+            const int iz = vox_axis(__fadd_rn(a[2], __fmul_rn(d[2], t)), c.zlo[2], c.zhi[2], res);
+            unsigned long long* w = vox + ((size_t)iz * res + iy) * res + ix;
+            if (!(__ldcg(w) & bit)) atomicOr(w, bit);
+        }
+    }
+}
+
+// OR of the masks of the voxels [i0, i1] (inclusive, per axis)
+__global__ void __launch_bounds__(HG_BLOCK) k_vox_box(const unsigned long long* __restrict__ vox, int res, int3 i0, int3 i1,
+                                                      unsigned long long* out) {
+    const int nx = i1.x - i0.x + 1, ny = i1.y - i0.y + 1, nz = i1.z - i0.z + 1;
+    const long long n = (long long)nx * ny * nz;
+    unsigned long long m = 0ull;
+    for (long long t = blockIdx.x * (long long)HG_BLOCK + threadIdx.x; t < n; t += (long long)gridDim.x * HG_BLOCK) {
+        const int x = i0.x + (int)(t % nx), y = i0.y + (int)((t / nx) % ny), z = i0.z + (int)(t / ((long long)nx * ny));
+        m |= vox[((size_t)z * res + y) * res + x];
+    }
+    for (int o = 16; o > 0; o >>= 1) m |= __shfl_xor_sync(0xffffffffu, m, o);
+    if ((threadIdx.x & 31) == 0 && m) atomicOr(out, m);
+}
+
 // ------------------------------------------------------------------ hash grid
 // The reference's cache-point hash (poc_gpu.cu:251-262)
 __device__ __forceinline__ unsigned long long hg_mix64(unsigned long long x) {
@@ -237,8 +294,12 @@ __global__ void __launch_bounds__(HG_BLOCK) k_hg_insert(const HgDev c, const flo
                                                         int n, unsigned long long* __restrict__ keys, uint32_t* __restrict__ entry) {
     const int i = blockIdx.x * HG_BLOCK + threadIdx.x;
     if (i >= n) return;
-    const unsigned long long key = hg_key(c, pos[3 * (size_t)i], pos[3 * (size_t)i + 1], pos[3 * (size_t)i + 2],
-                                          nrm[3 * (size_t)i], nrm[3 * (size_t)i + 1], nrm[3 * (size_t)i + 2]);
+    const float nx = nrm[3 * (size_t)i], ny = nrm[3 * (size_t)i + 1], nz = nrm[3 * (size_t)i + 2];
+    if (nx == 0.f && ny == 0.f && nz == 0.f) {   // no surface point: no entry
+        entry[i] = RC_HG_INVALID;
+        return;
+    }
+    const unsigned long long key = hg_key(c, pos[3 * (size_t)i], pos[3 * (size_t)i + 1], pos[3 * (size_t)i + 2], nx, ny, nz);
     uint32_t h = (uint32_t)hg_mix64(key) & c.mask;
     uint32_t out = RC_HG_INVALID, tomb = RC_HG_INVALID;
     for (int probe = 0; probe < 64 && out == RC_HG_INVALID; ++probe) {
@@ -529,6 +590,8 @@ void rc_hg_destroy(rc_hg* hg) {
     cudaFree(hg->bank[0]);
     cudaFree(hg->bank[1]);
     cudaFree(hg->scratch);
+    cudaFree(hg->vox);
+    cudaFree(hg->vox_out);
     if (hg->own_stream && hg->stream) cudaStreamDestroy(hg->stream);
     delete hg;
 }
@@ -606,9 +669,85 @@ rc_status rc_hg_begin_frame(rc_hg* hg, uint32_t dep_frame, uint32_t period) {
 rc_status rc_hg_mark_paths(rc_hg* hg, const rc_hg_vertex* d_vertices, const int* d_path_start, int npaths) {
     if (!hg || npaths < 0 || (npaths > 0 && (!d_vertices || !d_path_start))) return RC_ERR_ARG;
     if (npaths == 0) return RC_OK;
-    k_hg_mark<<<grid_for(npaths, HG_BLOCK), HG_BLOCK, 0, hg->stream>>>(dev_of(hg), d_vertices, d_path_start, npaths,
+    k_hg_mark<<<grid_for(npaths, HG_BLOCK), HG_BLOCK, 0, hg->stream>>>(dev_of(hg), d_vertices, d_path_start, nullptr, 0, npaths,
                                                                         hg->bank[hg->bank_sel], hg->bank[0], hg->bank[1]);
     HGCK(cudaGetLastError());
+    return RC_OK;
+}
+
+rc_status rc_hg_mark_paths_strided(rc_hg* hg, const rc_hg_vertex* d_vertices, const int* d_len, int stride, int npaths) {
+    if (!hg || npaths < 0 || stride < 1 || (npaths > 0 && (!d_vertices || !d_len))) return RC_ERR_ARG;
+    if (npaths == 0) return RC_OK;
+    k_hg_mark<<<grid_for(npaths, HG_BLOCK), HG_BLOCK, 0, hg->stream>>>(dev_of(hg), d_vertices, nullptr, d_len, stride, npaths,
+                                                                        hg->bank[hg->bank_sel], hg->bank[0], hg->bank[1]);
+    HGCK(cudaGetLastError());
+    return RC_OK;
+}
+
+rc_status rc_hg_voxels_init(rc_hg* hg, int res) {
+    if (!hg || res < 1 || res > 256) return RC_ERR_ARG;
+    HGCK(cudaStreamSynchronize(hg->stream));
+    cudaFree(hg->vox);
+    cudaFree(hg->vox_out);
+    hg->vox = nullptr;
+    hg->vox_out = nullptr;
+    hg->vres = 0;
+    const size_t n = (size_t)res * res * res;
+    if (cudaMalloc(&hg->vox, 8 * n) != cudaSuccess || cudaMalloc(&hg->vox_out, 8) != cudaSuccess)
+        return fail(hg, RC_ERR_NOMEM, "voxel masks of %d^3", res);
+    hg->vres = res;
+    return rc_hg_voxels_clear(hg);
+}
+
+rc_status rc_hg_voxels_clear(rc_hg* hg) {
+    if (!hg) return RC_ERR_ARG;
+    if (!hg->vres) return fail(hg, RC_ERR_STATE, "no voxel masks (rc_hg_voxels_init)");
+    HGCK(cudaMemsetAsync(hg->vox, 0, 8 * (size_t)hg->vres * hg->vres * hg->vres, hg->stream));
+    return RC_OK;
+}
+
+rc_status rc_hg_voxels_mark(rc_hg* hg, const rc_hg_vertex* d_vertices, const int* d_len, int stride, int npaths) {
+    if (!hg || npaths < 0 || stride < 1 || (npaths > 0 && (!d_vertices || !d_len))) return RC_ERR_ARG;
+    if (!hg->vres) return fail(hg, RC_ERR_STATE, "no voxel masks (rc_hg_voxels_init)");
+    if (npaths == 0) return RC_OK;
+    k_vox_mark<<<grid_for(npaths, HG_BLOCK), HG_BLOCK, 0, hg->stream>>>(dev_of(hg), d_vertices, d_len, stride, npaths, hg->vox, hg->vres);
+    HGCK(cudaGetLastError());
+    return RC_OK;
+}
+
+rc_status rc_hg_voxels_box_lights(rc_hg* hg, const float lo[3], const float hi[3], uint64_t* lights) {
+    if (!hg || !lo || !hi || !lights) return RC_ERR_ARG;
+    if (!hg->vres) return fail(hg, RC_ERR_STATE, "no voxel masks (rc_hg_voxels_init)");
+    const int res = hg->vres;
+    int a[3], b[3];
+    for (int k = 0; k < 3; ++k) {   // the host restatement of vox_axis
+        const float zl = hg->cfg.zone_lo[k], zh = hg->cfg.zone_hi[k];
+        volatile float e = zh - zl;
+        volatile float u0 = (lo[k] - zl) / e, u1 = (hi[k] - zl) / e;
+        volatile float f0 = u0 * (float)res, f1 = u1 * (float)res;
+        a[k] = std::min(std::max((int)f0, 0), res - 1);
+        b[k] = std::min(std::max((int)f1, 0), res - 1);
+        if (b[k] < a[k]) std::swap(a[k], b[k]);
+    }
+    HGCK(cudaMemsetAsync(hg->vox_out, 0, 8, hg->stream));
+    const long long n = (long long)(b[0] - a[0] + 1) * (b[1] - a[1] + 1) * (b[2] - a[2] + 1);
+    const int blocks = (int)std::min<long long>((n + HG_BLOCK - 1) / HG_BLOCK, 4096);
+    k_vox_box<<<blocks, HG_BLOCK, 0, hg->stream>>>(hg->vox, res, make_int3(a[0], a[1], a[2]), make_int3(b[0], b[1], b[2]), hg->vox_out);
+    HGCK(cudaGetLastError());
+    unsigned long long m = 0ull;
+    HGCK(cudaMemcpyAsync(&m, hg->vox_out, 8, cudaMemcpyDeviceToHost, hg->stream));
+    HGCK(cudaStreamSynchronize(hg->stream));
+    *lights = m;
+    return RC_OK;
+}
+
+rc_status rc_hg_voxels_copy(rc_hg* hg, uint64_t* host, size_t count) {
+    if (!hg || !host) return RC_ERR_ARG;
+    if (!hg->vres) return fail(hg, RC_ERR_STATE, "no voxel masks (rc_hg_voxels_init)");
+    const size_t n = (size_t)hg->vres * hg->vres * hg->vres;
+    if (count != n) return fail(hg, RC_ERR_ARG, "the voxel masks hold %zu words", n);
+    HGCK(cudaMemcpyAsync(host, hg->vox, 8 * n, cudaMemcpyDeviceToHost, hg->stream));
+    HGCK(cudaStreamSynchronize(hg->stream));
     return RC_OK;
 }
 
@@ -668,3 +807,21 @@ rc_status rc_hg_restore(rc_hg* hg, const rc_hg_snap_rec* d_recs, uint32_t count)
 }
 
 }  // extern "C"
+
+namespace {
+__global__ void k_set_entries(rc_hg_vertex* __restrict__ v, const uint32_t* __restrict__ entry, long long n) {
+    const long long i = blockIdx.x * (long long)HG_BLOCK + threadIdx.x;
+    if (i < n) v[i].entry = entry[i];
+}
+}  // namespace
+
+namespace rc {
+cudaStream_t hg_stream(rc_hg* hg) { return hg->stream; }
+const rc_hg_config& hg_config(const rc_hg* hg) { return hg->cfg; }
+bool hg_has_voxels(const rc_hg* hg) { return hg->vres > 0; }
+cudaError_t hg_set_entries(rc_hg* hg, rc_hg_vertex* v, const uint32_t* entry, long long n) {
+    if (n <= 0) return cudaSuccess;
+    k_set_entries<<<(unsigned)((n + HG_BLOCK - 1) / HG_BLOCK), HG_BLOCK, 0, hg->stream>>>(v, entry, n);
+    return cudaGetLastError();
+}
+}  // namespace rc

@@ -106,6 +106,20 @@ struct CameraD {
     int w, h;
 };
 
+// Camera-path pass feeding the hash-grid cache (rc_hg_camera_paths): lights and path shape.
+struct PathD {
+    int bounces, slots;          // slots = bounces + 1 vertices per path
+    uint32_t seed, frame;
+    float td;                    // length of the sun's shadow rays
+    int nl;
+    float lpos[32][3], lrgb[32][3], lint[32];   // point lights: position, colour, intensity of the state
+    int area_on;
+    float ac[3], au[3], av[3], an[3], aarea, argb[3];   // rectangle: corner, edges, unit normal, area, radiance
+    int sun_on;
+    float sdir[3], srgb[3];
+    float sky[3];
+};
+
 // Event program: the per-point kernels of one event of Runner::run, in launch order.
 enum EvKind { EV_SNAP_SAVE = 0, EV_ORACLE, EV_RESCALE, EV_WAKE, EV_TOUCHED, EV_SNAP_RESTORE, EV_RESTORED };
 struct EvOp {
@@ -156,6 +170,10 @@ struct Ops {
     // one taa-mode sample per point (x), with deps the rays' dependency masks or-ed into cur
     static cudaError_t taa_sample(int NW, bool deps, const DState& s, const DStatic& g, const Grid& grid, const DevCache& c,
                                   const FrameParams& p, float* x, uint32_t* cur, uint32_t seed, uint32_t frame, cudaStream_t st);
+    // one camera path per pixel (vertex records in `vtx`, which is an rc_hg_vertex array)
+    static cudaError_t paths(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
+                             const CameraD& cam, const PathD& pd, float* pos, float* nrm, float* rgb, void* vtx, int* len, float* img,
+                             cudaStream_t st);
     // K frozen rays per point (the rays of one reference iteration with `seed`): hit cache point or -1
     static cudaError_t frozen_hits(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                    uint32_t seed, int K, int* hits, cudaStream_t st);

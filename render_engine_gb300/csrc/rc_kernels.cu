@@ -19,6 +19,7 @@
 #include <mutex>
 #include <vector>
 
+#include "../../include/rc_hashgrid.h"
 #include "rc_internal.h"
 
 namespace rc {
@@ -1147,6 +1148,184 @@ __global__ void __launch_bounds__(BLOCK) k_camera(const DState s, const DStatic 
     img[(size_t)y * cam.w + x] = val;
 }
 
+// ------------------------------------------------------------------ camera paths
+// One path per pixel feeding the hash-grid cache (rc_hg_camera_paths, new: the reference has
+// no camera).  Same trace, hit resolution and cosine sampling as the frames; RGB light.
+__device__ __forceinline__ float lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
+// closest hit distance along a shadow ray (no cache-point resolution)
+__device__ __forceinline__ float shadow_t(const TraceSmem& sm, const DState& s, const DStatic& g, f3 O, f3 D, unsigned* flags) {
+    float t;
+    int q, jb;
+    trace_dyn(sm, s, false, O, D, t, q, jb);
+    if (g.has_bvh) trace_bvh(g, O, D, t, q, flags);
+    return q == -1 ? INFINITY : t;
+}
+
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_paths(const DState s, const DStatic g, const Grid grid, const DevCache c, const FrameParams p,
+                                                 const CameraD cam, const PathD pd, float* __restrict__ pos, float* __restrict__ nrm,
+                                                 float* __restrict__ rgb, rc_hg_vertex* __restrict__ vtx, int* __restrict__ plen,
+                                                 float* __restrict__ img) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= cam.w || y >= cam.h) return;
+    const size_t pix = (size_t)y * cam.w + x, base = pix * pd.slots;
+    uint32_t rs = hash32(pd.seed * 0x9E3779B9u ^ hash32(pd.frame * 0x85EBCA6Bu ^ hash32((uint32_t)pix + 1u)));
+    const float sx = ((x + 0.5f) / cam.w * 2.f - 1.f) * cam.tx, sy = (1.f - (y + 0.5f) / cam.h * 2.f) * cam.ty;
+    f3 D = mk(cam.fwd[0] + cam.right[0] * sx + cam.up[0] * sy, cam.fwd[1] + cam.right[1] * sx + cam.up[1] * sy,
+              cam.fwd[2] + cam.right[2] * sx + cam.up[2] * sy);
+    D = D * rsqrtf(dot(D, D));
+    f3 O = mk(cam.eye[0], cam.eye[1], cam.eye[2]);
+    float A[RC_HG_MAX_DEPTH], E[RC_HG_MAX_DEPTH][3];
+    int n = 0;
+    bool escaped = false;
+    for (int k = 0; k < pd.slots; ++k) {
+        const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, 0);
+        rc_hg_vertex vx;
+        vx.origin[0] = O.x; vx.origin[1] = O.y; vx.origin[2] = O.z;
+        vx.dir[0] = D.x; vx.dir[1] = D.y; vx.dir[2] = D.z;
+        vx.to_light[0] = vx.to_light[1] = vx.to_light[2] = 0.f;
+        vx.light_dist = 0.f;
+        vx.light_index = -1;
+        vx.entry = RC_HG_INVALID;
+        vx.flags = 0u;
+        if (h.q == -1) {   // escaped: the sky
+            vx.hit[0] = O.x; vx.hit[1] = O.y; vx.hit[2] = O.z;
+            vx.flags = RC_HG_MISS;
+            vtx[base + k] = vx;
+            escaped = true;
+            n = k + 1;
+            break;
+        }
+        if (h.back) break;   // back face or no cache point: the path ends
+        const f3 H = h.H;
+        f3 nn;
+        if (h.q >= 0) {
+            const float* Q = s.Q + 12 * h.q;
+            nn = mk(__ldg(Q + 9), __ldg(Q + 10), __ldg(Q + 11));
+        } else {
+            const float4 n4 = __ldg(g.STN + (-2 - h.q));
+            nn = mk(n4.x, n4.y, n4.z);
+            if (dot(nn, D) > 0.f) nn = nn * -1.f;
+        }
+        const float alb = __ldg(g.A + h.pi);
+        const f3 Os = H + nn * 1e-3f;
+        // light choice proportional to the unshadowed contribution (never zero for the rectangle)
+        float W = 0.f;
+        for (int l = 0; l < pd.nl; ++l) {
+            const f3 d = mk(pd.lpos[l][0], pd.lpos[l][1], pd.lpos[l][2]) - H;
+            const float r = sqrtf(dot(d, d)), rr = fmaxf(r, 0.05f);
+            W += pd.lint[l] * lum(pd.lrgb[l][0], pd.lrgb[l][1], pd.lrgb[l][2]) * fmaxf(dot(nn, d) / r, 0.f) / (rr * rr);
+        }
+        float wa = 0.f, ws = 0.f;
+        if (pd.area_on) {
+            const f3 C = mk(pd.ac[0] + 0.5f * (pd.au[0] + pd.av[0]), pd.ac[1] + 0.5f * (pd.au[1] + pd.av[1]),
+                            pd.ac[2] + 0.5f * (pd.au[2] + pd.av[2]));
+            const f3 d = C - H;
+            const float r = sqrtf(dot(d, d)), rr = fmaxf(r, 0.05f);
+            const f3 w = d * (1.f / r);
+            wa = lum(pd.argb[0], pd.argb[1], pd.argb[2]) * pd.aarea * fmaxf(dot(nn, w), 0.1f) *
+                 fmaxf(-(pd.an[0] * w.x + pd.an[1] * w.y + pd.an[2] * w.z), 0.1f) / (rr * rr);
+        }
+        if (pd.sun_on) ws = lum(pd.srgb[0], pd.srgb[1], pd.srgb[2]) * fmaxf(nn.x * pd.sdir[0] + nn.y * pd.sdir[1] + nn.z * pd.sdir[2], 0.f);
+        const float Wt = W + wa + ws;
+        float e3[3] = {0.f, 0.f, 0.f};
+        if (Wt > 0.f) {
+            const float u = rnd(rs) * Wt;
+            if (u < W) {   // a point light
+                int l = 0;
+                float acc = 0.f, wl = 0.f;
+                f3 d;
+                float r = 0.f, cs = 0.f;
+                for (l = 0; l < pd.nl; ++l) {
+                    d = mk(pd.lpos[l][0], pd.lpos[l][1], pd.lpos[l][2]) - H;
+                    r = sqrtf(dot(d, d));
+                    const float rr = fmaxf(r, 0.05f);
+                    cs = fmaxf(dot(nn, d) / r, 0.f);
+                    wl = pd.lint[l] * lum(pd.lrgb[l][0], pd.lrgb[l][1], pd.lrgb[l][2]) * cs / (rr * rr);
+                    acc += wl;
+                    if (u < acc && wl > 0.f) break;
+                }
+                l = min(l, pd.nl - 1);
+                const f3 w = d * (1.f / r);
+                const bool vis = shadow_t(tsm, s, g, Os, w, c.flags) >= r - 1e-3f;
+                vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
+                vx.light_dist = r;
+                vx.light_index = l;
+                if (vis && wl > 0.f) {
+                    vx.flags |= RC_HG_LIGHT_VISIBLE;
+                    const float ln = lum(pd.lrgb[l][0], pd.lrgb[l][1], pd.lrgb[l][2]);
+                    for (int ch = 0; ch < 3; ++ch) e3[ch] = Wt * pd.lrgb[l][ch] / ln;
+                }
+            } else if (u < W + wa) {   // a point of the rectangle
+                const float u1 = rnd(rs);
+                const float u2 = rnd(rs);
+                const f3 Y = mk(pd.ac[0] + u1 * pd.au[0] + u2 * pd.av[0], pd.ac[1] + u1 * pd.au[1] + u2 * pd.av[1],
+                                pd.ac[2] + u1 * pd.au[2] + u2 * pd.av[2]);
+                const f3 d = Y - H;
+                const float r = sqrtf(dot(d, d)), rr = fmaxf(r, 0.05f);
+                const f3 w = d * (1.f / r);
+                const float cs = fmaxf(dot(nn, w), 0.f), ca = fmaxf(-(pd.an[0] * w.x + pd.an[1] * w.y + pd.an[2] * w.z), 0.f);
+                const bool vis = cs > 0.f && ca > 0.f && shadow_t(tsm, s, g, Os, w, c.flags) >= r - 1e-3f;
+                vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
+                vx.light_dist = r;
+                vx.light_index = pd.nl;
+                if (vis) {
+                    vx.flags |= RC_HG_LIGHT_VISIBLE;
+                    const float geo = pd.aarea * cs * ca / (rr * rr) * (Wt / wa);
+                    for (int ch = 0; ch < 3; ++ch) e3[ch] = pd.argb[ch] * geo;
+                }
+            } else {   // the sun
+                const f3 w = mk(pd.sdir[0], pd.sdir[1], pd.sdir[2]);
+                const bool vis = shadow_t(tsm, s, g, Os, w, c.flags) == INFINITY;
+                vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
+                vx.light_dist = pd.td;
+                vx.light_index = pd.nl + 1;
+                if (vis) {
+                    vx.flags |= RC_HG_LIGHT_VISIBLE;
+                    const float ln = lum(pd.srgb[0], pd.srgb[1], pd.srgb[2]);
+                    for (int ch = 0; ch < 3; ++ch) e3[ch] = Wt * pd.srgb[ch] / ln;
+                }
+            }
+        }
+        vx.hit[0] = H.x; vx.hit[1] = H.y; vx.hit[2] = H.z;
+        vtx[base + k] = vx;
+        pos[3 * (base + k)] = H.x; pos[3 * (base + k) + 1] = H.y; pos[3 * (base + k) + 2] = H.z;
+        nrm[3 * (base + k)] = nn.x; nrm[3 * (base + k) + 1] = nn.y; nrm[3 * (base + k) + 2] = nn.z;
+        A[k] = alb;
+        E[k][0] = e3[0]; E[k][1] = e3[1]; E[k][2] = e3[2];
+        n = k + 1;
+        const float u1 = rnd(rs);
+        const float u2 = rnd(rs);
+        O = Os;
+        D = cosine_dir(nn, u1, u2);
+    }
+    // radiance leaving each vertex toward the previous one, from the last surface vertex back;
+    // slots without a surface vertex (the escaping ray, unused slots) get a zero normal: no entry
+    const int nsurf = n - (escaped ? 1 : 0);
+    for (int k = nsurf; k < pd.slots; ++k) {
+        for (int ch = 0; ch < 3; ++ch) {
+            rgb[3 * (base + k) + ch] = 0.f;
+            nrm[3 * (base + k) + ch] = 0.f;
+            pos[3 * (base + k) + ch] = 0.f;
+        }
+    }
+    float L[3] = {0.f, 0.f, 0.f};
+    if (escaped) { L[0] = pd.sky[0]; L[1] = pd.sky[1]; L[2] = pd.sky[2]; }
+    for (int k = nsurf - 1; k >= 0; --k)
+        for (int ch = 0; ch < 3; ++ch) {
+            L[ch] = A[k] * (E[k][ch] + L[ch]);
+            rgb[3 * (base + k) + ch] = L[ch];
+        }
+    plen[pix] = n;
+    if (img)   // the pixel: the primary vertex's radiance (L after the loop), the sky, or black
+        for (int ch = 0; ch < 3; ++ch) img[3 * pix + ch] = nsurf > 0 || escaped ? L[ch] : 0.f;
+}
+
 // ------------------------------------------------------------------ probe
 struct RayRecD { int point, ray, q, pi, back; float t; };
 
@@ -1465,6 +1644,17 @@ cudaError_t Ops<NL>::camera(const DState& s, const DStatic& g, const Grid& grid,
     if (e != cudaSuccess) return e;
     dim3 grd((cam.w + 15) / 16, (cam.h + 15) / 16);
     k_camera<NL><<<grd, BLOCK, smem, st>>>(s, g, grid, c, p, cam, img);
+    return cudaGetLastError();
+}
+
+template <int NL>
+cudaError_t Ops<NL>::paths(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p, const CameraD& cam,
+                           const PathD& pd, float* pos, float* nrm, float* rgb, void* vtx, int* len, float* img, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+    cudaError_t e = prep_smem(k_paths<NL>, smem);
+    if (e != cudaSuccess) return e;
+    dim3 grd((cam.w + 15) / 16, (cam.h + 15) / 16);
+    k_paths<NL><<<grd, BLOCK, smem, st>>>(s, g, grid, c, p, cam, pd, pos, nrm, rgb, (rc_hg_vertex*)vtx, len, img);
     return cudaGetLastError();
 }
 

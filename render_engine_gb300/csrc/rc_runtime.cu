@@ -15,7 +15,9 @@
 #include <vector>
 
 #include "../../include/rc_api.h"
+#include "../../include/rc_hashgrid.h"
 #include "rc_adjoint.h"
+#include "rc_hg_internal.h"
 #include "rc_internal.h"
 #include "rc_taa.h"
 
@@ -106,8 +108,18 @@ struct rc_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::string err;
-    std::vector<DevBuf> scene_bufs, cache_bufs, adj_bufs, taa_bufs;
+    std::vector<DevBuf> scene_bufs, cache_bufs, adj_bufs, taa_bufs, cam_bufs;
     TaaRun taa;
+    // camera-path pass (rc_hg_camera_paths): per slot and per pixel buffers of the last pass
+    struct CamPass {
+        size_t slots_cap = 0, pix_cap = 0;
+        float *pos = nullptr, *nrm = nullptr, *rgb = nullptr;
+        rc_hg_vertex* vtx = nullptr;
+        uint32_t* entry = nullptr;
+        int* len = nullptr;
+        int stride = 0, npaths = 0;
+        cudaEvent_t ready = nullptr;
+    } cam;
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
     rc::adj::Bufs adj{};
     Scene S;
@@ -1095,6 +1107,8 @@ void rc_destroy(rc_ctx* ctx) {
     free_pool(ctx->scene_bufs);
     free_pool(ctx->adj_bufs);
     free_pool(ctx->taa_bufs);
+    free_pool(ctx->cam_bufs);
+    if (ctx->cam.ready) cudaEventDestroy(ctx->cam.ready);
     if (ctx->flags_dev) cudaFree(ctx->flags_dev);
     if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
@@ -1262,21 +1276,7 @@ rc_status rc_sync(rc_ctx* ctx) {
     return RC_OK;
 }
 
-rc_status rc_render(rc_ctx* ctx, int state, const rc_camera* cam, float* image, size_t image_floats) {
-    if (!ctx || !cam) return RC_ERR_ARG;
-    if (!ctx->run.active) return fail(ctx, RC_ERR_STATE, "no run begun");
-    const Scene& S = ctx->S;
-    if (state < 0 || state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", state);
-    if (cam->width <= 0 || cam->height <= 0 || cam->width > 16384 || cam->height > 16384 || !(cam->fov_y_deg > 0.f && cam->fov_y_deg < 179.f))
-        return fail(ctx, RC_ERR_ARG, "bad camera");
-    const size_t npx = (size_t)cam->width * cam->height;
-    if (image && image_floats != npx) return fail(ctx, RC_ERR_ARG, "image holds %zu floats, not %zu", image_floats, npx);
-    if (npx > ctx->img_cap) {
-        if (ctx->img) { CKR(cudaStreamSynchronize(ctx->stream)); cudaFree(ctx->img); ctx->img = nullptr; }
-        cudaError_t e = cudaMalloc(&ctx->img, npx * sizeof(float));
-        if (e != cudaSuccess) { ctx->img_cap = 0; return fail(ctx, RC_ERR_NOMEM, "image buffer: %s", cudaGetErrorString(e)); }
-        ctx->img_cap = npx;
-    }
+static rc_status camera_basis(rc_ctx* ctx, const rc_camera* cam, CameraD* out) {
     // camera frame: forward to the target, right = forward x up, up re-orthogonalised
     double f[3], r[3], u[3];
     for (int k = 0; k < 3; ++k) f[k] = (double)cam->at[k] - cam->eye[k];
@@ -1292,12 +1292,33 @@ rc_status rc_render(rc_ctx* ctx, int state, const rc_camera* cam, float* image, 
     u[0] = r[1] * f[2] - r[2] * f[1];
     u[1] = r[2] * f[0] - r[0] * f[2];
     u[2] = r[0] * f[1] - r[1] * f[0];
-    CameraD cd;
+    CameraD& cd = *out;
     for (int k = 0; k < 3; ++k) { cd.eye[k] = cam->eye[k]; cd.fwd[k] = (float)f[k]; cd.right[k] = (float)r[k]; cd.up[k] = (float)u[k]; }
     cd.ty = (float)tan(0.5 * cam->fov_y_deg * 3.14159265358979323846 / 180.0);
     cd.tx = cd.ty * (float)cam->width / (float)cam->height;
     cd.w = cam->width;
     cd.h = cam->height;
+    return RC_OK;
+}
+
+rc_status rc_render(rc_ctx* ctx, int state, const rc_camera* cam, float* image, size_t image_floats) {
+    if (!ctx || !cam) return RC_ERR_ARG;
+    if (!ctx->run.active) return fail(ctx, RC_ERR_STATE, "no run begun");
+    const Scene& S = ctx->S;
+    if (state < 0 || state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", state);
+    if (cam->width <= 0 || cam->height <= 0 || cam->width > 16384 || cam->height > 16384 || !(cam->fov_y_deg > 0.f && cam->fov_y_deg < 179.f))
+        return fail(ctx, RC_ERR_ARG, "bad camera");
+    const size_t npx = (size_t)cam->width * cam->height;
+    if (image && image_floats != npx) return fail(ctx, RC_ERR_ARG, "image holds %zu floats, not %zu", image_floats, npx);
+    if (npx > ctx->img_cap) {
+        if (ctx->img) { CKR(cudaStreamSynchronize(ctx->stream)); cudaFree(ctx->img); ctx->img = nullptr; }
+        cudaError_t e = cudaMalloc(&ctx->img, npx * sizeof(float));
+        if (e != cudaSuccess) { ctx->img_cap = 0; return fail(ctx, RC_ERR_NOMEM, "image buffer: %s", cudaGetErrorString(e)); }
+        ctx->img_cap = npx;
+    }
+    CameraD cd;
+    rc_status cs = camera_basis(ctx, cam, &cd);
+    if (cs != RC_OK) return cs;
     FrameParams p = base_params(ctx);
     CKR(RC_DISPATCH(S.NL, camera(S.st[state].d, S.g, S.grid, ctx->c, p, cd, ctx->img, ctx->stream)));
     ctx->launches++;
@@ -1307,6 +1328,7 @@ rc_status rc_render(rc_ctx* ctx, int state, const rc_camera* cam, float* image, 
     }
     return RC_OK;
 }
+
 
 static bool array_geom(rc_ctx* ctx, int which, size_t* elem, size_t* count, size_t* src_stride, size_t* dst_stride, void** dev) {
     const Scene& S = ctx->S;
@@ -1803,6 +1825,122 @@ rc_status rc_taa_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, i
     CKR(cudaMemcpyAsync(to_device ? p : host, to_device ? host : p, n, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
                         ctx->stream));
     CKR(cudaStreamSynchronize(ctx->stream));
+    return RC_OK;
+}
+
+rc_status rc_hg_camera_paths(rc_hg* hg, rc_ctx* ctx, int state, const rc_hg_path_params* prm, float* d_image) {
+    if (!hg || !ctx || !prm) return RC_ERR_ARG;
+    if (!ctx->have_scene) return fail(ctx, RC_ERR_STATE, "no scene loaded");
+    const Scene& S = ctx->S;
+    if (state < 0 || state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", state);
+    if (prm->bounces < 0 || prm->bounces >= RC_HG_MAX_DEPTH) return fail(ctx, RC_ERR_ARG, "bounces %d", prm->bounces);
+    const rc_camera* cam = &prm->cam;
+    if (cam->width <= 0 || cam->height <= 0 || cam->width > 16384 || cam->height > 16384 || !(cam->fov_y_deg > 0.f && cam->fov_y_deg < 179.f))
+        return fail(ctx, RC_ERR_ARG, "bad camera");
+    if (S.NL > 32) return fail(ctx, RC_ERR_UNSUPPORTED, "%d lights", S.NL);
+    CameraD cd;
+    rc_status st = camera_basis(ctx, cam, &cd);
+    if (st != RC_OK) return st;
+    const size_t npix = (size_t)cam->width * cam->height, S1 = (size_t)prm->bounces + 1, nslots = npix * S1;
+    auto& C = ctx->cam;
+    CKR(cudaSetDevice(ctx->cfg.device));
+    cudaStream_t hs = rc::hg_stream(hg);
+    if (nslots > C.slots_cap || npix > C.pix_cap) {
+        CKR(cudaStreamSynchronize(hs));
+        CKR(cudaStreamSynchronize(ctx->stream));
+        free_pool(ctx->cam_bufs);
+        C.slots_cap = C.pix_cap = 0;
+        auto& pool = ctx->cam_bufs;
+        if ((st = dalloc(ctx, pool, &C.pos, 3 * nslots)) || (st = dalloc(ctx, pool, &C.nrm, 3 * nslots)) ||
+            (st = dalloc(ctx, pool, &C.rgb, 3 * nslots)) || (st = dalloc(ctx, pool, &C.vtx, nslots)) ||
+            (st = dalloc(ctx, pool, &C.entry, nslots)) || (st = dalloc(ctx, pool, &C.len, npix)))
+            return st;
+        C.slots_cap = nslots;
+        C.pix_cap = npix;
+    }
+    if (!C.ready) CKR(cudaEventCreateWithFlags(&C.ready, cudaEventDisableTiming));
+    // lights and path shape
+    PathD pd{};
+    pd.bounces = prm->bounces;
+    pd.slots = (int)S1;
+    pd.seed = prm->seed;
+    pd.frame = prm->frame;
+    pd.td = rc::hg_config(hg).tracing_distance;
+    pd.nl = S.NL;
+    bool white = true;
+    for (int l = 0; l < S.NL; ++l)
+        for (int k = 0; k < 3; ++k) white = white && prm->light_rgb[l][k] == 0.f;
+    for (int l = 0; l < S.NL; ++l) {
+        for (int k = 0; k < 3; ++k) {
+            pd.lpos[l][k] = S.hL[3 * (size_t)l + k];
+            pd.lrgb[l][k] = white ? 1.f : prm->light_rgb[l][k];
+        }
+        pd.lint[l] = S.st[state].inten[l];
+    }
+    const float* ar = prm->area_rgb;
+    pd.area_on = ar[0] > 0.f || ar[1] > 0.f || ar[2] > 0.f;
+    if (pd.area_on) {
+        const float* u = prm->area_u;
+        const float* v = prm->area_v;
+        const double n[3] = {(double)u[1] * v[2] - (double)u[2] * v[1], (double)u[2] * v[0] - (double)u[0] * v[2],
+                             (double)u[0] * v[1] - (double)u[1] * v[0]};
+        const double a = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (!(a > 0)) return fail(ctx, RC_ERR_ARG, "degenerate rectangle light");
+        for (int k = 0; k < 3; ++k) {
+            pd.ac[k] = prm->area_corner[k];
+            pd.au[k] = u[k];
+            pd.av[k] = v[k];
+            pd.an[k] = (float)(n[k] / a);
+            pd.argb[k] = ar[k];
+        }
+        pd.aarea = (float)a;
+    }
+    const float* sr = prm->sun_rgb;
+    pd.sun_on = sr[0] > 0.f || sr[1] > 0.f || sr[2] > 0.f;
+    if (pd.sun_on) {
+        const double d[3] = {prm->sun_dir[0], prm->sun_dir[1], prm->sun_dir[2]};
+        const double l = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        if (!(l > 0)) return fail(ctx, RC_ERR_ARG, "sun direction is zero");
+        for (int k = 0; k < 3; ++k) {
+            pd.sdir[k] = (float)(d[k] / l);
+            pd.srgb[k] = sr[k];
+        }
+    }
+    for (int k = 0; k < 3; ++k) pd.sky[k] = prm->sky_rgb[k];
+    // after the context's own work, on the cache's stream
+    CKR(cudaEventRecord(C.ready, ctx->stream));
+    CKR(cudaStreamWaitEvent(hs, C.ready, 0));
+    FrameParams p{};
+    p.Np = S.Np;
+    p.NR = S.NR;
+    CKR(RC_DISPATCH(S.NL, paths(S.st[state].d, S.g, S.grid, ctx->c, p, cd, pd, C.pos, C.nrm, C.rgb, C.vtx, C.len, d_image, hs)));
+    const int n = (int)nslots, np = (int)npix;
+    if ((st = rc_hg_insert(hg, C.pos, C.nrm, n, C.entry))) return fail(ctx, st, "insert: %s", rc_hg_last_error(hg));
+    CKR(rc::hg_set_entries(hg, C.vtx, C.entry, (long long)nslots));
+    if ((st = rc_hg_accumulate(hg, C.entry, C.rgb, n))) return fail(ctx, st, "accumulate: %s", rc_hg_last_error(hg));
+    if ((st = rc_hg_mark_paths_strided(hg, C.vtx, C.len, (int)S1, np))) return fail(ctx, st, "mark: %s", rc_hg_last_error(hg));
+    if (rc::hg_has_voxels(hg) && (st = rc_hg_voxels_mark(hg, C.vtx, C.len, (int)S1, np)))
+        return fail(ctx, st, "voxels: %s", rc_hg_last_error(hg));
+    // the context's later work waits for this pass
+    CKR(cudaEventRecord(C.ready, hs));
+    CKR(cudaStreamWaitEvent(ctx->stream, C.ready, 0));
+    C.stride = (int)S1;
+    C.npaths = np;
+    ctx->launches += 6;
+    return RC_OK;
+}
+
+rc_status rc_hg_camera_arrays(rc_ctx* ctx, const rc_hg_vertex** d_vertices, const float** d_rgb, const uint32_t** d_entry,
+                              const int** d_len, int* stride, int* npaths) {
+    if (!ctx) return RC_ERR_ARG;
+    const auto& C = ctx->cam;
+    if (!C.npaths) return fail(ctx, RC_ERR_STATE, "no camera pass");
+    if (d_vertices) *d_vertices = C.vtx;
+    if (d_rgb) *d_rgb = C.rgb;
+    if (d_entry) *d_entry = C.entry;
+    if (d_len) *d_len = C.len;
+    if (stride) *stride = C.stride;
+    if (npaths) *npaths = C.npaths;
     return RC_OK;
 }
 

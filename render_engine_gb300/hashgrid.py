@@ -14,7 +14,8 @@ from . import native
 
 EXPORTS = ["rc_hg_create", "rc_hg_destroy", "rc_hg_last_error", "rc_hg_array", "rc_hg_array_copy", "rc_hg_clear", "rc_hg_insert",
            "rc_hg_accumulate", "rc_hg_begin_frame", "rc_hg_mark_paths", "rc_hg_resolve", "rc_hg_event_mask",
-           "rc_hg_snapshot", "rc_hg_restore"]
+           "rc_hg_snapshot", "rc_hg_restore", "rc_hg_mark_paths_strided", "rc_hg_voxels_init", "rc_hg_voxels_clear",
+           "rc_hg_voxels_mark", "rc_hg_voxels_box_lights", "rc_hg_voxels_copy", "rc_hg_camera_paths", "rc_hg_camera_arrays"]
 
 INVALID = 0xFFFFFFFF
 EVICTED = 0xFFFFFFFFFFFFFFFF
@@ -62,6 +63,7 @@ def _lib():
     L = native.load_library()
     if not _bound:
         vp, i, u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32
+        fp = ctypes.POINTER(ctypes.c_float)
         L.rc_hg_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
         L.rc_hg_destroy.argtypes = [vp]
         L.rc_hg_destroy.restype = None
@@ -80,8 +82,43 @@ def _lib():
         L.rc_hg_event_mask.restype = None
         L.rc_hg_snapshot.argtypes = [vp, vp, u32, ctypes.POINTER(u32)]
         L.rc_hg_restore.argtypes = [vp, vp, u32]
+        L.rc_hg_mark_paths_strided.argtypes = [vp, vp, vp, i, i]
+        L.rc_hg_voxels_init.argtypes = [vp, i]
+        L.rc_hg_voxels_clear.argtypes = [vp]
+        L.rc_hg_voxels_mark.argtypes = [vp, vp, vp, i, i]
+        L.rc_hg_voxels_box_lights.argtypes = [vp, fp, fp, ctypes.POINTER(ctypes.c_uint64)]
+        L.rc_hg_voxels_copy.argtypes = [vp, vp, ctypes.c_size_t]
+        L.rc_hg_camera_paths.argtypes = [vp, vp, i, ctypes.POINTER(PathParams), vp]
+        L.rc_hg_camera_arrays.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                          ctypes.POINTER(i), ctypes.POINTER(i)]
         _bound = True
     return L
+
+
+class PathParams(ctypes.Structure):
+    """rc_hg_path_params: camera, bounces, seed/frame, light colours, rectangle light, sun, sky."""
+    _fields_ = [("cam", native.Camera), ("bounces", ctypes.c_int), ("seed", ctypes.c_uint32), ("frame", ctypes.c_uint32),
+                ("light_rgb", (ctypes.c_float * 3) * 32), ("area_corner", ctypes.c_float * 3), ("area_u", ctypes.c_float * 3),
+                ("area_v", ctypes.c_float * 3), ("area_rgb", ctypes.c_float * 3), ("sun_dir", ctypes.c_float * 3),
+                ("sun_rgb", ctypes.c_float * 3), ("sky_rgb", ctypes.c_float * 3)]
+
+
+def path_params(cam, bounces=2, seed=1, frame=0, light_rgb=None, area=None, sun=None, sky=(0.0, 0.0, 0.0)) -> PathParams:
+    """area = (corner, u, v, rgb), sun = (direction, rgb); None = absent."""
+    p = PathParams()
+    p.cam = cam
+    p.bounces = bounces
+    p.seed = seed & 0xFFFFFFFF
+    p.frame = frame & 0xFFFFFFFF
+    if light_rgb is not None:
+        for l, c in enumerate(light_rgb):
+            p.light_rgb[l][:] = [float(x) for x in c]
+    if area is not None:
+        p.area_corner[:], p.area_u[:], p.area_v[:], p.area_rgb[:] = (list(map(float, v)) for v in area)
+    if sun is not None:
+        p.sun_dir[:], p.sun_rgb[:] = (list(map(float, v)) for v in sun)
+    p.sky_rgb[:] = [float(x) for x in sky]
+    return p
 
 
 def _ptr(x) -> int:
@@ -180,3 +217,62 @@ class HashGrid:
 
     def restore(self, recs, count: int):
         self._chk(self.L.rc_hg_restore(self.h, _ptr(recs), count))
+
+    def mark_paths_strided(self, vertices, lengths, stride: int, npaths: int):
+        self._chk(self.L.rc_hg_mark_paths_strided(self.h, _ptr(vertices), _ptr(lengths), stride, npaths))
+
+    # per-voxel light masks
+    def voxels_init(self, res: int):
+        self._chk(self.L.rc_hg_voxels_init(self.h, res))
+        self.vres = res
+
+    def voxels_clear(self):
+        self._chk(self.L.rc_hg_voxels_clear(self.h))
+
+    def voxels_mark(self, vertices, lengths, stride: int, npaths: int):
+        self._chk(self.L.rc_hg_voxels_mark(self.h, _ptr(vertices), _ptr(lengths), stride, npaths))
+
+    def voxels_box_lights(self, lo, hi) -> int:
+        fp = ctypes.POINTER(ctypes.c_float)
+        a = np.ascontiguousarray(lo, np.float32)
+        b = np.ascontiguousarray(hi, np.float32)
+        m = ctypes.c_uint64()
+        self._chk(self.L.rc_hg_voxels_box_lights(self.h, a.ctypes.data_as(fp), b.ctypes.data_as(fp), ctypes.byref(m)))
+        return m.value
+
+    def voxels(self) -> np.ndarray:
+        n = self.vres ** 3
+        out = np.empty(n, np.uint64)
+        self._chk(self.L.rc_hg_voxels_copy(self.h, out.ctypes.data_as(ctypes.c_void_p), n))
+        return out
+
+    # camera paths over a context's scene
+    def camera_paths(self, ctx, state: int, params: PathParams, image=None):
+        self._chk(self.L.rc_hg_camera_paths(self.h, ctx.h, state, ctypes.byref(params), _ptr(image)))
+
+
+def camera_arrays(ctx) -> dict:
+    """Host copies of the last camera pass: vertices (VERTEX_DTYPE), rgb, entry (per slot), lengths (per path)."""
+    import torch
+    L = _lib()
+    vp = ctypes.c_void_p
+    v, r, e, ln = vp(), vp(), vp(), vp()
+    stride, npaths = ctypes.c_int(), ctypes.c_int()
+    st = L.rc_hg_camera_arrays(ctx.h, ctypes.byref(v), ctypes.byref(r), ctypes.byref(e), ctypes.byref(ln), ctypes.byref(stride),
+                               ctypes.byref(npaths))
+    if st != native.RC_OK:
+        raise native.RCError(st, ctx.L.rc_last_error(ctx.h).decode())
+    ns = stride.value * npaths.value
+
+    class _Dev:   # a device buffer torch can view (CUDA array interface)
+        def __init__(self, ptr, nbytes):
+            self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (ptr, False), "strides": None,
+                                             "version": 3}
+
+    def grab(ptr, nbytes):
+        torch.cuda.synchronize()
+        return torch.as_tensor(_Dev(ptr, nbytes), device="cuda").cpu().numpy()
+
+    return {"vertices": grab(v.value, 64 * ns).view(VERTEX_DTYPE), "rgb": grab(r.value, 12 * ns).view(np.float32).reshape(-1, 3),
+            "entry": grab(e.value, 4 * ns).view(np.uint32), "len": grab(ln.value, 4 * npaths.value).view(np.int32),
+            "stride": stride.value, "npaths": npaths.value}
