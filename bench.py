@@ -339,6 +339,7 @@ def run_ours(args, world, rank, local, dist):
     out["mlp"] = mlp_bench(stream)
     out["adjoint"] = adjoint_bench(peak)
     out["taa"] = taa_bench()
+    out["camera_paths"] = paths_bench()
     return out, data, method
 
 
@@ -434,6 +435,49 @@ def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20,
                         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                                      "algorithmic_bytes": res_bytes}},
             "mark_paths": {"paths": npaths, "vertices": n, "ms": mark_ms, "vertices_per_s": n / (mark_ms * 1e-3)}}
+
+
+def paths_bench(reps=10, points=1_082_802):
+    """Secondary line: the 1080p camera-path pass feeding the hash-grid cache (rc_hg_camera_paths):
+    1920 x 1080 paths with 2 bounces through the 1.08 M-point room, the room's 3 point lights
+    plus a 1 x 1 m rectangle light and a sun, one light sample and shadow ray per vertex; 2^22
+    entries, dependency marking and 128^3 per-voxel light masks.  CUDA events on the cache's
+    stream around each pass (trace, insert, accumulate, mark, voxels)."""
+    import torch
+    from render_engine_gb300 import hashgrid as H
+    from render_engine_gb300 import native as N
+    from render_engine_gb300 import scene as S
+    st = torch.cuda.Stream()
+    ctx = N.Context(stream=st.cuda_stream)
+    ctx.load_bytes(S.write(S.box_room(points=points, seed=0)))
+    cfg = H.make_config(zone_lo=(0, 0, 0), zone_hi=(8, 4, 3), cell=0.05, capacity=1 << 22, max_depth=4, tracing_distance=50.0,
+                        stream=st.cuda_stream)
+    hg = H.HashGrid(cfg)
+    hg.voxels_init(128)
+    cam = N.camera((0.5, 0.5, 1.6), (6.0, 3.0, 1.0), width=1920, height=1080, fov_y_deg=75.0)
+    area = ((3.5, 1.5, 2.95), (1.0, 0.0, 0.0), (0.0, -1.0, 0.0), (4.0, 3.5, 3.0))
+    sun = ((0.3, 0.2, 1.0), (0.5, 0.5, 0.45))
+    img = torch.zeros(1920 * 1080 * 3, device="cuda")
+    for f in range(3):
+        hg.begin_frame(f, 16)
+        hg.camera_paths(ctx, 0, H.path_params(cam, bounces=2, seed=1, frame=f, area=area, sun=sun), img)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for k in range(reps):
+        hg.begin_frame(3 + k, 16)
+        ev[k][0].record(st)
+        hg.camera_paths(ctx, 0, H.path_params(cam, bounces=2, seed=1, frame=3 + k, area=area, sun=sun), img)
+        ev[k][1].record(st)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / reps
+    a = H.camera_arrays(ctx)
+    verts = a["vertices"]
+    used = int(a["len"].sum())
+    hg.close()
+    ctx.close()
+    rays = used + int(((verts["light_index"] >= 0)).sum())   # path rays + shadow rays of the last pass
+    return {"width": 1920, "height": 1080, "bounces": 2, "ms": ms, "paths_per_s": 1920 * 1080 / (ms * 1e-3),
+            "rays_per_pass": rays, "mrays_per_s": rays / (ms * 1e-3) / 1e6, "voxel_res": 128, "capacity": 1 << 22}
 
 
 def taa_scene(points: int) -> bytes:
@@ -680,7 +724,7 @@ def main():
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
             "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
             "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "quality": res["quality"], "hashgrid": res["hashgrid"], "mlp": res["mlp"],
-            "adjoint": res["adjoint"], "taa": res["taa"]}
+            "adjoint": res["adjoint"], "taa": res["taa"], "camera_paths": res["camera_paths"]}
     print(json.dumps(line))
 
 
