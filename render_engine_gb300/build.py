@@ -63,11 +63,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, deps):
             jobs.append([nv, *ARCH, *FLAGS, "-DRC_NL_ONE=%d" % nl, "-c", os.path.join(CSRC, "rc_kernels.cu"), "-o", o])
-    for name in ("rc_runtime", "rc_adjoint", "rc_taa", "rc_noalloc", "rc_hashgrid", "rc_mlp"):
+    for name in ("rc_runtime", "rc_adjoint", "rc_taa", "rc_prep", "rc_noalloc", "rc_hashgrid", "rc_mlp"):
         o = os.path.join(OUT, name + ".o")
         objs.append(o)
+        # the scene preparation's host arithmetic rounds every operation (no contraction), the
+        # same on every host architecture
+        extra = ["-Xcompiler", "-ffp-contract=off"] if name == "rc_prep" else []
         if force or _stale(o, deps):
-            jobs.append([nv, *ARCH, *FLAGS, "-c", os.path.join(CSRC, name + ".cu"), "-o", o])
+            jobs.append([nv, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, name + ".cu"), "-o", o])
     cli_obj = {}
     for nl in (3, 8):
         oc = os.path.join(OUT, "poc_gpu_main_l%d.o" % nl)

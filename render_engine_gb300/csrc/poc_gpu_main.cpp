@@ -7,6 +7,7 @@
 //   poc_gpu_l3 quality <scene.bin> <nseeds> <budget1,budget2,...>
 //   poc_gpu_l3 recon   <scene.bin> <nseeds>
 //   poc_gpu_l3 taa     <scene.bin> <nseeds> <scenarios.txt>
+//   poc_gpu_l3 prep    <mesh.msh> <scene.bin> [points]
 //
 // Same JSONL lines on stdout, same environment variables (BENCH_RAYONS, BENCH_DEBUG), so
 // cuda/run_cuda.sh and cuda/analyse_cuda.py of the reference consume the output unchanged.
@@ -272,9 +273,33 @@ int main(int argc, char** argv) {
     std::string mode = argv[1];
     if (const char* d = getenv("BENCH_DEBUG")) g_debug = atoi(d);
     if (const char* r = getenv("BENCH_RAYONS")) g_rays = std::max(0.25f, (float)atof(r));
-    if (mode == "prep") {
-        fprintf(stderr, "mode %s is not provided by this build\n", mode.c_str());
-        return 1;
+    if (mode == "prep") {   // poc_gpu.cu:1304-1306, prep_mesh.cuh:303-531
+        if (RC_CLI_NLIGHTS != 3) { fprintf(stderr, "prep : utiliser poc_gpu_l3 (scenes maillees a 3 lampes)\n"); return 1; }
+        if (argc < 4) { fprintf(stderr, "usage : prep <maillage.mesh> <scene.bin> [points]\n"); return 1; }
+        rc_config pc;
+        memset(&pc, 0, sizeof pc);
+        pc.expect_lights = 3;
+        rc_ctx* pctx = nullptr;
+        rc_status ps = rc_create(&pc, &pctx);
+        if (ps != RC_OK) { fprintf(stderr, "CUDA: %s\n", rc_status_string(ps)); return 2; }
+        rc_prep_report r;
+        ps = rc_prep_mesh(pctx, argv[2], argv[3], argc > 4 ? atoi(argv[4]) : 300000, &r);
+        if (ps != RC_OK) {
+            fprintf(stderr, "prep: %s\n", rc_last_error(pctx));
+            rc_destroy(pctx);
+            return ps == RC_ERR_CUDA ? 2 : 1;
+        }
+        printf("{\"type\":\"prep\",\"triangles\":%d,\"np\":%d,\"cellule_m\":%.4f,\"zones\":%d,\"diag_m\":%.2f,\"cube_m\":%.2f,"
+               "\"bvh_noeuds\":%d,\"points_valides\":%.4f,\"bruit_ref\":[",
+               r.triangles, r.np, r.cell_m, r.zones, r.diag_m, r.cube_m, r.bvh_nodes, r.valid_fraction);
+        for (int k = 0; k < r.ns; ++k) printf("%s%.5f", k ? "," : "", r.noise[k]);
+        printf("],\"iterations_ref\":[");
+        for (int k = 0; k < r.ns; ++k) printf("%s%d", k ? "," : "", r.iterations[k]);
+        printf("],\"lampes\":[");
+        for (int l = 0; l < 3; ++l) printf("%s[%.3f,%.3f,%.3f]", l ? "," : "", r.lights[l][0], r.lights[l][1], r.lights[l][2]);
+        printf("],\"secondes\":%.1f}\n", r.seconds);
+        rc_destroy(pctx);
+        return 0;
     }
     rc_config cfg;
     memset(&cfg, 0, sizeof cfg);

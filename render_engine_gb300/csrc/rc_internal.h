@@ -181,6 +181,11 @@ struct Ops {
     static cudaError_t pretrace(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                 float4* out, cudaStream_t st);
 };
+// Free-space probe of the scene preparation (64 directions per candidate point through the
+// static mesh of g): out[3 i] = closest hit, out[3 i + 1] = fraction of hits closer than diag,
+// out[3 i + 2] = fraction of single-sided back faces.
+cudaError_t probe_free_space(const DStatic& g, const float* C, int nc, float diag, float* out, unsigned* flags, cudaStream_t st);
+
 // Light counts and mask widths with compiled kernels.
 #define RC_NL_VALUES(X) X(1) X(2) X(3) X(4) X(8) X(16) X(32)
 inline bool supported_nl_nw(int NL, int NW) {

@@ -1944,6 +1944,55 @@ rc_status rc_hg_camera_arrays(rc_ctx* ctx, const rc_hg_vertex** d_vertices, cons
     return RC_OK;
 }
 
+}  // extern "C"
+
+namespace rc {
+
+rc_status ctx_fail(rc_ctx* ctx, rc_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list a;
+    va_start(a, fmt);
+    vsnprintf(buf, sizeof buf, fmt, a);
+    va_end(a);
+    if (ctx) ctx->err = buf;
+    return s;
+}
+
+// the free-space probe of the scene preparation over a BVH not yet in any scene
+rc_status ctx_probe_free_space(rc_ctx* ctx, const std::vector<float>& ST, const std::vector<float>& STN, const float* BN, int nnodes,
+                               const std::vector<float>& C, float diag, std::vector<float>& out) {
+    CKR(cudaSetDevice(ctx->cfg.device));
+    std::vector<DevBuf> tmp;
+    struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
+    const float *dST = nullptr, *dSTN = nullptr, *dBN = nullptr, *dC = nullptr;
+    float* dO = nullptr;
+    rc_status s;
+    if ((s = dput(ctx, tmp, &dST, ST)) || (s = dput(ctx, tmp, &dSTN, STN)) ||
+        (s = dput(ctx, tmp, &dBN, std::vector<float>(BN, BN + 8 * (size_t)nnodes))) || (s = dput(ctx, tmp, &dC, C)) ||
+        (s = dalloc(ctx, tmp, &dO, C.size())))
+        return s;
+    DStatic g{};
+    g.ST = dST;
+    g.STN = reinterpret_cast<const float4*>(dSTN);
+    g.BN = reinterpret_cast<const float4*>(dBN);
+    g.has_bvh = 1;
+    g.nnodes = nnodes;
+    g.max_visits = 4 * nnodes + 64;
+    CKR(cudaMemsetAsync(ctx->flags_dev, 0, 4, ctx->stream));
+    CKR(probe_free_space(g, dC, (int)(C.size() / 3), diag, dO, ctx->flags_dev, ctx->stream));
+    out.resize(C.size());
+    unsigned flags = 0;
+    CKR(cudaMemcpyAsync(out.data(), dO, out.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CKR(cudaMemcpyAsync(&flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CKR(cudaStreamSynchronize(ctx->stream));
+    if (flags) return fail(ctx, RC_ERR_DEVICE, "prep: BVH traversal guard tripped (flags %u)", flags);
+    return RC_OK;
+}
+
+}  // namespace rc
+
+extern "C" {
+
 rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags) {
     if (!ctx || !flags) return RC_ERR_ARG;
     CKR(cudaMemcpyAsync(flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -577,3 +577,13 @@ def with_references(scene: Scene, ctx) -> Scene:
         st.valid = ctx.state_array(k, N.SA_VALID).astype(np.uint8)
         st.Pw = ctx.state_array(k, N.SA_PW).reshape(-1, nl).astype(np.float32)
     return scene
+
+
+def write_msh1(V: np.ndarray, albedo: np.ndarray, double_sided: np.ndarray) -> bytes:
+    """A mesh in the MSH1 layout the `prep` mode reads (prep_mesh.cuh:22-29): "MSH1", the
+    triangle count, 9 floats per triangle (metres, z up), one albedo per triangle, one
+    double-sided byte per triangle."""
+    V = np.ascontiguousarray(V, np.float32).reshape(-1, 9)
+    n = len(V)
+    return (b"MSH1" + np.int32(n).tobytes() + V.tobytes() + np.ascontiguousarray(albedo, np.float32).reshape(n).tobytes()
+            + np.ascontiguousarray(double_sided, np.uint8).reshape(n).tobytes())

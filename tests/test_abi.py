@@ -62,10 +62,12 @@ def test_binaries_built(lib):
         assert os.access(os.path.join(d, n), os.X_OK)
 
 
-def test_cli_rejects_a_mode_it_does_not_provide_without_gpu(lib):
-    exe = os.path.join(os.path.dirname(lib), "poc_gpu_l3")
-    r = subprocess.run([exe, "prep", "x.mesh", "x.bin"], capture_output=True, text=True)
-    assert r.returncode == 1 and "not provided" in r.stderr
+def test_cli_prep_needs_the_three_light_binary_and_a_gpu(lib):
+    d = os.path.dirname(lib)
+    r = subprocess.run([os.path.join(d, "poc_gpu_l8"), "prep", "x.mesh", "x.bin"], capture_output=True, text=True)
+    assert r.returncode == 1 and "poc_gpu_l3" in r.stderr     # as the reference: meshes get 3 lamps
+    r = subprocess.run([os.path.join(d, "poc_gpu_l3"), "prep", "x.mesh", "x.bin"], capture_output=True, text=True)
+    assert r.returncode == 2                                    # no GPU here: rc_create fails, nothing falls back
 
 
 def test_missing_library_fails_loudly(tmp_path, monkeypatch):
