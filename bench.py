@@ -48,11 +48,12 @@ def parse():
     ap.add_argument("--method", default=METHOD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=12)
-    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp", "adjoint", "taa"], default=None,
+    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp", "adjoint", "taa", "paths"], default=None,
                     help="no timing: run --steps frames of state 0 (frame), three resolve passes of the "
                          "hash-grid table (hashgrid), two inference and training passes of the MLP (mlp) or "
-                         "one 16-sweep adjoint of a 16-light room of --points points (adjoint) or --steps "
-                         "frames of the taa mode (taa), for an ncu capture, and exit")
+                         "one 16-sweep adjoint of a 16-light room of --points points (adjoint), --steps "
+                         "frames of the taa mode (taa) or --steps 1080p camera-path passes (paths), for an ncu "
+                         "capture, and exit")
     return ap.parse_args()
 
 
@@ -73,6 +74,10 @@ def profile_run(args):
         return
     if args.profile == "mlp":
         mlp_bench(torch.cuda.current_stream(), reps=2)
+        torch.cuda.synchronize()
+        return
+    if args.profile == "paths":
+        paths_bench(reps=args.steps, warm=0)
         torch.cuda.synchronize()
         return
     if args.profile == "taa":
@@ -437,7 +442,7 @@ def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20,
             "mark_paths": {"paths": npaths, "vertices": n, "ms": mark_ms, "vertices_per_s": n / (mark_ms * 1e-3)}}
 
 
-def paths_bench(reps=10, points=1_082_802):
+def paths_bench(reps=10, points=1_082_802, warm=3):
     """Secondary line: the 1080p camera-path pass feeding the hash-grid cache (rc_hg_camera_paths):
     1920 x 1080 paths with 2 bounces through the 1.08 M-point room, the room's 3 point lights
     plus a 1 x 1 m rectangle light and a sun, one light sample and shadow ray per vertex; 2^22
@@ -458,7 +463,7 @@ def paths_bench(reps=10, points=1_082_802):
     area = ((3.5, 1.5, 2.95), (1.0, 0.0, 0.0), (0.0, -1.0, 0.0), (4.0, 3.5, 3.0))
     sun = ((0.3, 0.2, 1.0), (0.5, 0.5, 0.45))
     img = torch.zeros(1920 * 1080 * 3, device="cuda")
-    for f in range(3):
+    for f in range(warm):
         hg.begin_frame(f, 16)
         hg.camera_paths(ctx, 0, H.path_params(cam, bounces=2, seed=1, frame=f, area=area, sun=sun), img)
     torch.cuda.synchronize()

@@ -143,8 +143,8 @@ rc_status rc_hg_voxels_init(rc_hg* hg, int res);
 rc_status rc_hg_voxels_clear(rc_hg* hg);
 /* For every vertex whose sampled light l < 64 was visible: bit l in the voxels of 20 evenly
  * spaced samples of its shadow segment (the hit to the light, at most tracing_distance), as
- * k_build rasterises its shadow rays (poc_gpu.cu:192-197).  Voxel of a point:
- * min(max(int((x - zone_lo) / (zone_hi - zone_lo) * res), 0), res - 1) per axis. */
+ * k_build rasterises its shadow rays (poc_gpu.cu:192-197).  Voxel of a point per axis:
+ * min(max(int((x - zone_lo) * scale), 0), res - 1), scale = res / (zone_hi - zone_lo) in float. */
 rc_status rc_hg_voxels_mark(rc_hg* hg, const rc_hg_vertex* d_vertices, const int* d_len, int stride, int npaths);
 /* OR of the masks of the voxels a box [lo, hi] overlaps (host arrays; synchronises). */
 rc_status rc_hg_voxels_box_lights(rc_hg* hg, const float lo[3], const float hi[3], uint64_t* lights);

@@ -378,10 +378,11 @@ void hgo_restore(hgo_state* s, const hgo_snap_rec* recs, uint32_t count) {
 }
 
 /* Per-voxel light masks (rc_hg_voxels_mark): voxel of a point per axis
- * min(max(int((x - lo) / (hi - lo) * res), 0), res - 1); for each vertex whose sampled light
- * l < 64 was visible, bit l in the voxels of 20 samples h + (to_light * min(dist, td)) * k / 19. */
-static int hgo_vox_axis(float x, float lo, float hi, int res) {
-    int i = (int)((x - lo) / (hi - lo) * (float)res);
+ * min(max(int((x - lo) * scale), 0), res - 1) with scale = res / (hi - lo) in float; for each
+ * vertex whose sampled light l < 64 was visible, bit l in the voxels of 20 samples
+ * h + (to_light * min(dist, td)) * k / 19. */
+static int hgo_vox_axis(float x, float lo, float scale, int res) {
+    int i = (int)((x - lo) * scale);
     return i < 0 ? 0 : (i > res - 1 ? res - 1 : i);
 }
 void hgo_voxels_mark(const hgo_config* c, int res, uint64_t* vox, const hgo_vertex* v, const int* len, int stride, int npaths) {
@@ -393,11 +394,13 @@ void hgo_voxels_mark(const hgo_config* c, int res, uint64_t* vox, const hgo_vert
             const float r = x->light_dist < c->tracing_distance ? x->light_dist : c->tracing_distance;
             float d[3];
             for (int k = 0; k < 3; ++k) d[k] = x->to_light[k] * r;
+            float sc[3];
+            for (int k = 0; k < 3; ++k) sc[k] = (float)res / (c->zone_hi[k] - c->zone_lo[k]);
             for (int k = 0; k < 20; ++k) {
                 const float t = (float)k / 19.f;
-                const int ix = hgo_vox_axis(x->hit[0] + d[0] * t, c->zone_lo[0], c->zone_hi[0], res);
-                const int iy = hgo_vox_axis(x->hit[1] + d[1] * t, c->zone_lo[1], c->zone_hi[1], res);
-                const int iz = hgo_vox_axis(x->hit[2] + d[2] * t, c->zone_lo[2], c->zone_hi[2], res);
+                const int ix = hgo_vox_axis(x->hit[0] + d[0] * t, c->zone_lo[0], sc[0], res);
+                const int iy = hgo_vox_axis(x->hit[1] + d[1] * t, c->zone_lo[1], sc[1], res);
+                const int iz = hgo_vox_axis(x->hit[2] + d[2] * t, c->zone_lo[2], sc[2], res);
                 vox[((size_t)iz * res + iy) * res + ix] |= bit;
             }
         }

@@ -214,18 +214,38 @@ __global__ void __launch_bounds__(HG_BLOCK) k_hg_mark(const HgDev c, const rc_hg
 }
 
 // ------------------------------------------------------------------ per-voxel light masks
-// A res^3 grid over the zone box; voxel of a point as the reference's vox_of (poc_gpu.cu:137-142)
-// with explicitly rounded operations.
-__device__ __forceinline__ int vox_axis(float x, float lo, float hi, int res) {
-    const int i = (int)__fmul_rn(__fdiv_rn(__fsub_rn(x, lo), __fsub_rn(hi, lo)), (float)res);
+// A res^3 grid over the zone box: voxel of a point per axis int((x - lo) * scale), clamped, with
+// scale = res / (hi - lo) rounded once on the host; explicitly rounded operations.
+struct VoxDev {
+    float lo[3], scale[3];
+    int res;
+};
+VoxDev vox_dev(const rc_hg* hg) {
+    VoxDev v;
+    for (int k = 0; k < 3; ++k) {
+        v.lo[k] = hg->cfg.zone_lo[k];
+        volatile float ext = hg->cfg.zone_hi[k] - hg->cfg.zone_lo[k];
+        v.scale[k] = (float)hg->vres / ext;
+    }
+    v.res = hg->vres;
+    return v;
+}
+__device__ __forceinline__ int vox_axis(float x, float lo, float scale, int res) {
+    const int i = (int)__fmul_rn(__fsub_rn(x, lo), scale);
     return min(max(i, 0), res - 1);
 }
+// sample positions k / 19 of a shadow segment (20 samples, k_build's rasterisation)
+__constant__ float c_seg19[20] = {0.f / 19.f,  1.f / 19.f,  2.f / 19.f,  3.f / 19.f,  4.f / 19.f,  5.f / 19.f,  6.f / 19.f,
+                                  7.f / 19.f,  8.f / 19.f,  9.f / 19.f,  10.f / 19.f, 11.f / 19.f, 12.f / 19.f, 13.f / 19.f,
+                                  14.f / 19.f, 15.f / 19.f, 16.f / 19.f, 17.f / 19.f, 18.f / 19.f, 19.f / 19.f};
 
 // Bit l of every voxel on the shadow segment of a vertex whose sampled light l (< 64) was
 // visible: 20 evenly spaced samples from the hit to the light (at most tracing_distance), as
 // k_build rasterises its shadow rays (poc_gpu.cu:192-197).  A bit already set is not written.
-__global__ void __launch_bounds__(HG_BLOCK) k_vox_mark(const HgDev c, const rc_hg_vertex* __restrict__ v, const int* __restrict__ plen,
-                                                       int stride, int npaths, unsigned long long* __restrict__ vox, int res) {
+__global__ void __launch_bounds__(HG_BLOCK) k_vox_mark(const HgDev c, const VoxDev g, const rc_hg_vertex* __restrict__ v,
+                                                       const int* __restrict__ plen, int stride, int npaths,
+                                                       unsigned long long* __restrict__ vox) {
+    const int res = g.res;
     const int p = blockIdx.x * HG_BLOCK + threadIdx.x;
     if (p >= npaths) return;
     const long long j0 = (long long)p * stride;
@@ -239,11 +259,12 @@ __global__ void __launch_bounds__(HG_BLOCK) k_vox_mark(const HgDev c, const rc_h
             a[k] = x.hit[k];
             d[k] = __fmul_rn(x.to_light[k], r);
         }
+#pragma unroll 4
         for (int k = 0; k < 20; ++k) {
-            const float t = __fdiv_rn((float)k, 19.f);
-            const int ix = vox_axis(__fadd_rn(a[0], __fmul_rn(d[0], t)), c.zlo[0], c.zhi[0], res);
-            const int iy = vox_axis(__fadd_rn(a[1], __fmul_rn(d[1], t)), c.zlo[1], c.zhi[1], res);
-            const int iz = vox_axis(__fadd_rn(a[2], __fmul_rn(d[2], t)), c.zlo[2], c.zhi[2], res);
+            const float t = c_seg19[k];
+            const int ix = vox_axis(__fadd_rn(a[0], __fmul_rn(d[0], t)), g.lo[0], g.scale[0], res);
+            const int iy = vox_axis(__fadd_rn(a[1], __fmul_rn(d[1], t)), g.lo[1], g.scale[1], res);
+            const int iz = vox_axis(__fadd_rn(a[2], __fmul_rn(d[2], t)), g.lo[2], g.scale[2], res);
             unsigned long long* w = vox + ((size_t)iz * res + iy) * res + ix;
             if (!(__ldcg(w) & bit)) atomicOr(w, bit);
         }
@@ -710,7 +731,8 @@ rc_status rc_hg_voxels_mark(rc_hg* hg, const rc_hg_vertex* d_vertices, const int
     if (!hg || npaths < 0 || stride < 1 || (npaths > 0 && (!d_vertices || !d_len))) return RC_ERR_ARG;
     if (!hg->vres) return fail(hg, RC_ERR_STATE, "no voxel masks (rc_hg_voxels_init)");
     if (npaths == 0) return RC_OK;
-    k_vox_mark<<<grid_for(npaths, HG_BLOCK), HG_BLOCK, 0, hg->stream>>>(dev_of(hg), d_vertices, d_len, stride, npaths, hg->vox, hg->vres);
+    k_vox_mark<<<grid_for(npaths, HG_BLOCK), HG_BLOCK, 0, hg->stream>>>(dev_of(hg), vox_dev(hg), d_vertices, d_len, stride, npaths,
+                                                                         hg->vox);
     HGCK(cudaGetLastError());
     return RC_OK;
 }
@@ -719,12 +741,11 @@ rc_status rc_hg_voxels_box_lights(rc_hg* hg, const float lo[3], const float hi[3
     if (!hg || !lo || !hi || !lights) return RC_ERR_ARG;
     if (!hg->vres) return fail(hg, RC_ERR_STATE, "no voxel masks (rc_hg_voxels_init)");
     const int res = hg->vres;
+    const VoxDev g = vox_dev(hg);
     int a[3], b[3];
     for (int k = 0; k < 3; ++k) {   // the host restatement of vox_axis
-        const float zl = hg->cfg.zone_lo[k], zh = hg->cfg.zone_hi[k];
-        volatile float e = zh - zl;
-        volatile float u0 = (lo[k] - zl) / e, u1 = (hi[k] - zl) / e;
-        volatile float f0 = u0 * (float)res, f1 = u1 * (float)res;
+        volatile float d0 = lo[k] - g.lo[k], d1 = hi[k] - g.lo[k];
+        volatile float f0 = d0 * g.scale[k], f1 = d1 * g.scale[k];
         a[k] = std::min(std::max((int)f0, 0), res - 1);
         b[k] = std::min(std::max((int)f1, 0), res - 1);
         if (b[k] < a[k]) std::swap(a[k], b[k]);

@@ -29,6 +29,7 @@ struct DState {
 // State-independent scene data (format 3 static mesh and spatial hash, per-point albedo/regions).
 struct DStatic {
     const float* ST;           // static triangles v0, e1, e2
+    const float4* ST4;         // the same, three float4 per triangle: (v0, e1.x), (e1.yz, e2.xy), (e2.z, 0, 0, 0)
     const float4* STN;         // geometric normal + flags (w bit 0 = double sided)
     const float4* BN;          // BVH nodes, 2 float4 each
     const unsigned long long* HK;

@@ -332,10 +332,10 @@ static __device__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int&
         int lf = __float_as_int(a.w), cnt = __float_as_int(b.w);
         if (cnt > 0) {
             for (int j = lf; j < lf + cnt; ++j) {
-                const float* T = g.ST + 9 * (size_t)j;
-                f3 v0 = mk(__ldg(T), __ldg(T + 1), __ldg(T + 2));
-                f3 e1 = mk(__ldg(T + 3), __ldg(T + 4), __ldg(T + 5));
-                f3 e2 = mk(__ldg(T + 6), __ldg(T + 7), __ldg(T + 8));
+                const float4 x = __ldg(g.ST4 + 3 * (size_t)j), y = __ldg(g.ST4 + 3 * (size_t)j + 1), z = __ldg(g.ST4 + 3 * (size_t)j + 2);
+                f3 v0 = mk(x.x, x.y, x.z);
+                f3 e1 = mk(x.w, y.x, y.y);
+                f3 e2 = mk(y.z, y.w, z.x);
                 f3 p = cross(d, e2);
                 float det = dot(e1, p);
                 if (fabsf(det) <= 1e-12f) continue;
@@ -1153,6 +1153,15 @@ __global__ void __launch_bounds__(BLOCK) k_camera(const DState s, const DStatic 
 // no camera).  Same trace, hit resolution and cosine sampling as the frames; RGB light.
 __device__ __forceinline__ float lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
 
+// a 64-byte vertex record as four 16-byte stores
+__device__ __forceinline__ void store_vertex(rc_hg_vertex* dst, const rc_hg_vertex& v) {
+    static_assert(sizeof(rc_hg_vertex) == 64, "vertex record: 64 bytes");
+    const float4* src = reinterpret_cast<const float4*>(&v);
+    float4* d = reinterpret_cast<float4*>(dst);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) d[k] = src[k];
+}
+
 // closest hit distance along a shadow ray (no cache-point resolution)
 __device__ __forceinline__ float shadow_t(const TraceSmem& sm, const DState& s, const DStatic& g, f3 O, f3 D, unsigned* flags) {
     float t;
@@ -1196,7 +1205,7 @@ __global__ void __launch_bounds__(BLOCK) k_paths(const DState s, const DStatic g
         if (h.q == -1) {   // escaped: the sky
             vx.hit[0] = O.x; vx.hit[1] = O.y; vx.hit[2] = O.z;
             vx.flags = RC_HG_MISS;
-            vtx[base + k] = vx;
+            store_vertex(vtx + base + k, vx);
             escaped = true;
             n = k + 1;
             break;
@@ -1235,65 +1244,66 @@ __global__ void __launch_bounds__(BLOCK) k_paths(const DState s, const DStatic g
         const float Wt = W + wa + ws;
         float e3[3] = {0.f, 0.f, 0.f};
         if (Wt > 0.f) {
+            // the sampled light: direction, distance, unshadowed contribution over its probability
+            f3 w = mk(0.f, 0.f, 1.f);
+            float r = 0.f, c3[3] = {0.f, 0.f, 0.f};
+            bool open = true, sun = false;
+            int li = -1;
             const float u = rnd(rs) * Wt;
             if (u < W) {   // a point light
                 int l = 0;
                 float acc = 0.f, wl = 0.f;
-                f3 d;
-                float r = 0.f, cs = 0.f;
+                f3 d = mk(0.f, 0.f, 0.f);
                 for (l = 0; l < pd.nl; ++l) {
                     d = mk(pd.lpos[l][0], pd.lpos[l][1], pd.lpos[l][2]) - H;
                     r = sqrtf(dot(d, d));
                     const float rr = fmaxf(r, 0.05f);
-                    cs = fmaxf(dot(nn, d) / r, 0.f);
+                    const float cs = fmaxf(dot(nn, d) / r, 0.f);
                     wl = pd.lint[l] * lum(pd.lrgb[l][0], pd.lrgb[l][1], pd.lrgb[l][2]) * cs / (rr * rr);
                     acc += wl;
                     if (u < acc && wl > 0.f) break;
                 }
                 l = min(l, pd.nl - 1);
-                const f3 w = d * (1.f / r);
-                const bool vis = shadow_t(tsm, s, g, Os, w, c.flags) >= r - 1e-3f;
-                vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
-                vx.light_dist = r;
-                vx.light_index = l;
-                if (vis && wl > 0.f) {
-                    vx.flags |= RC_HG_LIGHT_VISIBLE;
-                    const float ln = lum(pd.lrgb[l][0], pd.lrgb[l][1], pd.lrgb[l][2]);
-                    for (int ch = 0; ch < 3; ++ch) e3[ch] = Wt * pd.lrgb[l][ch] / ln;
-                }
+                w = d * (1.f / r);
+                li = l;
+                open = wl > 0.f;
+                const float ln = lum(pd.lrgb[l][0], pd.lrgb[l][1], pd.lrgb[l][2]);
+                for (int ch = 0; ch < 3; ++ch) c3[ch] = Wt * pd.lrgb[l][ch] / ln;
             } else if (u < W + wa) {   // a point of the rectangle
                 const float u1 = rnd(rs);
                 const float u2 = rnd(rs);
                 const f3 Y = mk(pd.ac[0] + u1 * pd.au[0] + u2 * pd.av[0], pd.ac[1] + u1 * pd.au[1] + u2 * pd.av[1],
                                 pd.ac[2] + u1 * pd.au[2] + u2 * pd.av[2]);
                 const f3 d = Y - H;
-                const float r = sqrtf(dot(d, d)), rr = fmaxf(r, 0.05f);
-                const f3 w = d * (1.f / r);
+                r = sqrtf(dot(d, d));
+                const float rr = fmaxf(r, 0.05f);
+                w = d * (1.f / r);
                 const float cs = fmaxf(dot(nn, w), 0.f), ca = fmaxf(-(pd.an[0] * w.x + pd.an[1] * w.y + pd.an[2] * w.z), 0.f);
-                const bool vis = cs > 0.f && ca > 0.f && shadow_t(tsm, s, g, Os, w, c.flags) >= r - 1e-3f;
-                vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
-                vx.light_dist = r;
-                vx.light_index = pd.nl;
-                if (vis) {
-                    vx.flags |= RC_HG_LIGHT_VISIBLE;
-                    const float geo = pd.aarea * cs * ca / (rr * rr) * (Wt / wa);
-                    for (int ch = 0; ch < 3; ++ch) e3[ch] = pd.argb[ch] * geo;
-                }
+                open = cs > 0.f && ca > 0.f;
+                li = pd.nl;
+                const float geo = pd.aarea * cs * ca / (rr * rr) * (Wt / wa);
+                for (int ch = 0; ch < 3; ++ch) c3[ch] = pd.argb[ch] * geo;
             } else {   // the sun
-                const f3 w = mk(pd.sdir[0], pd.sdir[1], pd.sdir[2]);
-                const bool vis = shadow_t(tsm, s, g, Os, w, c.flags) == INFINITY;
-                vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
-                vx.light_dist = pd.td;
-                vx.light_index = pd.nl + 1;
-                if (vis) {
-                    vx.flags |= RC_HG_LIGHT_VISIBLE;
-                    const float ln = lum(pd.srgb[0], pd.srgb[1], pd.srgb[2]);
-                    for (int ch = 0; ch < 3; ++ch) e3[ch] = Wt * pd.srgb[ch] / ln;
-                }
+                w = mk(pd.sdir[0], pd.sdir[1], pd.sdir[2]);
+                r = pd.td;
+                sun = true;
+                li = pd.nl + 1;
+                const float ln = lum(pd.srgb[0], pd.srgb[1], pd.srgb[2]);
+                for (int ch = 0; ch < 3; ++ch) c3[ch] = Wt * pd.srgb[ch] / ln;
+            }
+            // one shadow ray for whichever light was chosen
+            const float ts = open ? shadow_t(tsm, s, g, Os, w, c.flags) : 0.f;
+            const bool vis = open && (sun ? ts == INFINITY : ts >= r - 1e-3f);
+            vx.to_light[0] = w.x; vx.to_light[1] = w.y; vx.to_light[2] = w.z;
+            vx.light_dist = r;
+            vx.light_index = li;
+            if (vis) {
+                vx.flags |= RC_HG_LIGHT_VISIBLE;
+                for (int ch = 0; ch < 3; ++ch) e3[ch] = c3[ch];
             }
         }
         vx.hit[0] = H.x; vx.hit[1] = H.y; vx.hit[2] = H.z;
-        vtx[base + k] = vx;
+        store_vertex(vtx + base + k, vx);
         pos[3 * (base + k)] = H.x; pos[3 * (base + k) + 1] = H.y; pos[3 * (base + k) + 2] = H.z;
         nrm[3 * (base + k)] = nn.x; nrm[3 * (base + k) + 1] = nn.y; nrm[3 * (base + k) + 2] = nn.z;
         A[k] = alb;

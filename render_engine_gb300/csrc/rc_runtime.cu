@@ -211,6 +211,15 @@ __global__ void k_load_pack4(const float* __restrict__ src, float4* __restrict__
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f);
 }
+// static triangles (9 floats: v0, e1, e2) as three float4 each, for 16-byte loads
+__global__ void k_load_tri4(const float* __restrict__ src, float4* __restrict__ dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float* t = src + 9 * i;
+        dst[3 * i] = make_float4(t[0], t[1], t[2], t[3]);
+        dst[3 * i + 1] = make_float4(t[4], t[5], t[6], t[7]);
+        dst[3 * i + 2] = make_float4(t[8], 0.f, 0.f, 0.f);
+    }
+}
 __global__ void k_load_pad(const float* __restrict__ src, float* __restrict__ dst, size_t n, int nl, int lcs) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         for (int l = 0; l < lcs; ++l) dst[(size_t)lcs * i + l] = l < nl ? src[(size_t)nl * i + l] : 0.f;
@@ -464,6 +473,13 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
             (s = dput_raw(ctx, pool, (const float**)&g.BN, BN, 8 * (size_t)m[1])) ||
             (s = dput_raw(ctx, pool, &g.HK, HK, (size_t)m[2])) || (s = dput_raw(ctx, pool, &g.HV, HV, (size_t)m[2])))
             return s;
+        {
+            float4* st4 = nullptr;
+            if ((s = dalloc(ctx, pool, &st4, 3 * (size_t)m[0]))) return s;
+            k_load_tri4<<<load_grid((size_t)m[0]), 256, 0, ctx->stream>>>(g.ST, st4, (size_t)m[0]);
+            CKR(cudaGetLastError());
+            g.ST4 = st4;
+        }
         // hash values are cache point ids or -1; checked on the device, read back before the load returns
         k_load_check<<<load_grid((size_t)m[2]), 256, 0, ctx->stream>>>(g.HV, (size_t)m[2], -1, S.Np, ctx->flags_dev + 2, LOAD_BAD_HASH);
         CKR(cudaGetLastError());
@@ -1971,8 +1987,13 @@ rc_status ctx_probe_free_space(rc_ctx* ctx, const std::vector<float>& ST, const 
         (s = dput(ctx, tmp, &dBN, std::vector<float>(BN, BN + 8 * (size_t)nnodes))) || (s = dput(ctx, tmp, &dC, C)) ||
         (s = dalloc(ctx, tmp, &dO, C.size())))
         return s;
+    float4* dST4 = nullptr;
+    if ((s = dalloc(ctx, tmp, &dST4, 3 * (ST.size() / 9)))) return s;
+    k_load_tri4<<<load_grid(ST.size() / 9), 256, 0, ctx->stream>>>(dST, dST4, ST.size() / 9);
+    CKR(cudaGetLastError());
     DStatic g{};
     g.ST = dST;
+    g.ST4 = dST4;
     g.STN = reinterpret_cast<const float4*>(dSTN);
     g.BN = reinterpret_cast<const float4*>(dBN);
     g.has_bvh = 1;

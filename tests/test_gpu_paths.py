@@ -83,8 +83,9 @@ def test_camera_paths_vs_oracle(scene_main_bytes):
     assert np.array_equal(g["vox"], vox_o)
     assert g["vox"].any()
     v3 = g["vox"].reshape(32, 32, 32)
-    xs = slice(int(3.0 / 8 * 32), int(4.5 / 8 * 32) + 1)
-    ys = slice(int(1.0 / 4 * 32), int(2.5 / 4 * 32) + 1)
+    sx, sy = np.float32(32) / np.float32(8), np.float32(32) / np.float32(4)
+    xs = slice(int(np.float32(3.0) * sx), int(np.float32(4.5) * sx) + 1)
+    ys = slice(int(np.float32(1.0) * sy), int(np.float32(2.5) * sy) + 1)
     m = np.bitwise_or.reduce(v3[:, ys, xs].reshape(-1))
     assert g["box"] == int(m)
 
