@@ -204,35 +204,47 @@ __device__ __forceinline__ void encode(const MlpArgs& a, int pt, int half, Emit&
     emit(21, f);
 }
 
-// Forward pass over tiles of 128 samples (persistent CTAs of two warpgroups: thread t works on
-// sample row t % 128, the two threads of a row split the input features and the columns of
-// each accumulator -- warp w reads the tensor-memory lanes of its quarter w % 4).
-// TRAIN: also keeps X0^T, H_l^T and dY (with dY^T) of each tile in global memory and adds the
-// loss; otherwise writes the n_out outputs.
-constexpr int FWD_THREADS = 256;
-template <bool TRAIN>
-__global__ void __launch_bounds__(FWD_THREADS) k_mlp_forward(const MlpArgs a) {
+// Forward pass over tiles of 128 samples.  A CTA holds the bf16 weights once and runs GROUPS
+// tiles at a time, each on its own group of two warpgroups (thread t of a group works on sample
+// row t % 128; the two threads of a row split the input features and the columns of each
+// accumulator, warp w reading the tensor-memory lanes of its quarter w % 4), with its own
+// activation tile, mbarrier, named barrier and 64 tensor-memory columns; the groups overlap
+// one tile's products with another's encoding and epilogues.
+// TRAIN (one group): also keeps X0^T, H_l^T and dY (with dY^T) of each tile in global memory
+// and adds the loss; otherwise writes the n_out outputs.
+constexpr int FWD_THREADS = 256;                               // threads of one group
+constexpr int INFER_GROUPS = 4;                                // tiles in flight per inference CTA
+constexpr size_t GROUP_SMEM_INFER = (size_t)128 * K0 * 2;      // activation tile
+constexpr size_t GROUP_SMEM_TRAIN = GROUP_SMEM_INFER + (size_t)K0 * 128 * 2;   // + transposed staging
+template <bool TRAIN, int GROUPS>
+__global__ void __launch_bounds__(FWD_THREADS * GROUPS) k_mlp_forward(const MlpArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[GROUPS];
     __shared__ uint32_t tmem_base;
+    __shared__ int gflag[GROUPS];
+    constexpr uint32_t TCOLS = GROUPS == 1 ? 64u : (GROUPS == 2 ? 128u : 256u);
     uint8_t* sw = smem;                               // forward weight tiles, WF_BYTES
-    // one activation tile: X0 (128 x 176) and then each H_l (128 x 64) in its place, H_{l+1}
-    // written once the product that reads H_l has completed
-    uint8_t* sx = smem + WF_BYTES;
+    const int grp = threadIdx.x / FWD_THREADS, tid = threadIdx.x % FWD_THREADS;
+    // this group's activation tile: X0 (128 x 176) and then each H_l (128 x 64) in its place,
+    // H_{l+1} written once the product that reads H_l has completed
+    uint8_t* sx = smem + WF_BYTES + (size_t)grp * (TRAIN ? GROUP_SMEM_TRAIN : GROUP_SMEM_INFER);
     uint8_t* st = sx + 128 * K0 * 2;                  // TRAIN: transposed staging, 176 x 128
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int warp = tid >> 5, lane = tid & 31;
     const int row = tid & 127, half = tid >> 7, quarter = warp & 3;
-    for (int i = tid; i < WF_BYTES / 16; i += FWD_THREADS) reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(a.wbf)[i];
-    if (tid == 0) mbar_init(&mbar, 1);
-    if (warp == 0) tmem_alloc(&tmem_base, 64);
+    for (int i = threadIdx.x; i < WF_BYTES / 16; i += FWD_THREADS * GROUPS)
+        reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(a.wbf)[i];
+    if (threadIdx.x < GROUPS) mbar_init(&mbar[threadIdx.x], 1);
+    if (threadIdx.x < 32) tmem_alloc(&tmem_base, TCOLS);
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    const uint32_t tmem = tmem_base;
+    const uint32_t tmem = tmem_base + 64u * (uint32_t)grp;
+    // the group's barrier (named barrier 1 + group; barrier 0 is the whole CTA's)
+    auto gsync = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(FWD_THREADS) : "memory"); };
     uint32_t phase = 0;
     bool ok = true;
     const int ntiles = (a.n + 127) / 128;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    for (int tile = blockIdx.x * GROUPS + grp; tile < ntiles && ok; tile += gridDim.x * GROUPS) {
         const int s = tile * 128 + row;
         const bool live = s < a.n;
         const int pt = live ? (a.idx ? a.idx[s] : s) : 0;
@@ -247,11 +259,11 @@ __global__ void __launch_bounds__(FWD_THREADS) k_mlp_forward(const MlpArgs a) {
                 for (int j = 0; j < 8; ++j) st_bf16(st, kmajor_offset(8 * k8 + j, row, 128), f[j]);
         });
         fence_proxy_async();
-        __syncthreads();
+        gsync();
         if (TRAIN) {
             uint4* dst = reinterpret_cast<uint4*>(a.act + (size_t)tile * ACT_BYTES + ACT_X0T);
             for (int i = tid; i < K0 * 128 * 2 / 16; i += FWD_THREADS) dst[i] = reinterpret_cast<const uint4*>(st)[i];
-            __syncthreads();
+            gsync();
         }
         for (int l = 0; l < NLAYER && ok; ++l) {
             const int K = in_dim(l), N = out_dim(l);
@@ -262,16 +274,18 @@ __global__ void __launch_bounds__(FWD_THREADS) k_mlp_forward(const MlpArgs a) {
                 for (int kk = 0; kk < K / 16; ++kk)
                     mma_bf16(tmem, smem_desc(a0 + 256u * kk, 128u, 16u * K), smem_desc(b0 + 256u * kk, 128u, 16u * K),
                              idesc_bf16_f32(128, N), kk > 0);
-                mma_commit(&mbar);
+                mma_commit(&mbar[grp]);
             }
-            // one warp watches the barrier; the others wait at the block barrier without issuing
-            // (the fence orders the products before the block barrier for every thread)
+            // one warp watches the barrier; the others wait at the group barrier without issuing
+            // (the fence orders the products before the barrier for every thread of the group)
             if (warp == 0) {
-                ok = mbar_wait(&mbar, phase, WAIT_LIMIT);
+                ok = mbar_wait(&mbar[grp], phase, WAIT_LIMIT);
                 fence_before_sync();
+                if (lane == 0) gflag[grp] = ok ? 1 : 0;
             }
             phase ^= 1u;
-            ok = __syncthreads_and(ok);   // the whole block leaves together
+            gsync();
+            ok = gflag[grp] != 0;   // the whole group leaves together
             if (!ok) {
                 if (tid == 0) atomicOr(a.err, 1u);
                 break;
@@ -323,18 +337,18 @@ __global__ void __launch_bounds__(FWD_THREADS) k_mlp_forward(const MlpArgs a) {
             }
             fence_before_sync();
             fence_proxy_async();
-            __syncthreads();
+            gsync();
             if (TRAIN && l < NLAYER - 1) {
                 uint4* dst = reinterpret_cast<uint4*>(a.act + (size_t)tile * ACT_BYTES + act_ht(l + 1));
                 for (int i = tid; i < HID * 128 * 2 / 16; i += FWD_THREADS) dst[i] = reinterpret_cast<const uint4*>(st)[i];
-                __syncthreads();
+                gsync();
             }
             fence_after_sync();
         }
     }
     fence_before_sync();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 64);
+    if (threadIdx.x < 32) tmem_dealloc(tmem_base, TCOLS);
 }
 
 // Backward pass of one tile (128 threads): for l = 4 .. 0, dW_l = dZ_l^T A_l over the tile's
@@ -483,8 +497,8 @@ __global__ void k_mlp_adam(const float* __restrict__ slices, float* __restrict__
     if (l >= 1) st_bf16(wbf + wb_off(l), kmajor_offset(k, r, out_dim(l)), x);
 }
 
-constexpr size_t FWD_SMEM_INFER = (size_t)WF_BYTES + 128 * K0 * 2;
-constexpr size_t FWD_SMEM_TRAIN = FWD_SMEM_INFER + (size_t)K0 * 128 * 2;
+constexpr size_t FWD_SMEM_INFER = (size_t)WF_BYTES + INFER_GROUPS * GROUP_SMEM_INFER;   // 224 KB: one CTA per SM
+constexpr size_t FWD_SMEM_TRAIN = (size_t)WF_BYTES + GROUP_SMEM_TRAIN;
 constexpr size_t BWD_SMEM = (size_t)K0 * 128 * 2 + 128 * HID * 2 + 128 * 128 * 2 + HID * HID * 2;
 }  // namespace
 
@@ -585,8 +599,8 @@ rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out) {
     if (cudaMemsetAsync(m->m1, 0, 4 * NWEIGHT, m->stream) || cudaMemsetAsync(m->m2, 0, 4 * NWEIGHT, m->stream) ||
         cudaMemsetAsync(m->err, 0, 4, m->stream) || cudaStreamSynchronize(m->stream))
         return bad(RC_ERR_CUDA);
-    if (cudaFuncSetAttribute(k_mlp_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_TRAIN) ||
-        cudaFuncSetAttribute(k_mlp_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_INFER) ||
+    if (cudaFuncSetAttribute(k_mlp_forward<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_TRAIN) ||
+        cudaFuncSetAttribute(k_mlp_forward<false, INFER_GROUPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_INFER) ||
         cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_SMEM))
         return bad(RC_ERR_CUDA);
     *out = m;
@@ -643,7 +657,7 @@ rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.loss_scale = 1.f / ((float)n * (float)m->cfg.n_out);
     const int ntiles = n / 128;
     if (!d_loss && cudaMemsetAsync(m->loss, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "loss");
-    k_mlp_forward<true><<<std::min(ntiles, m->sms), FWD_THREADS, FWD_SMEM_TRAIN, m->stream>>>(a);
+    k_mlp_forward<true, 1><<<std::min(ntiles, m->sms), FWD_THREADS, FWD_SMEM_TRAIN, m->stream>>>(a);
     k_mlp_backward<<<ntiles, 128, BWD_SMEM, m->stream>>>(a);
     m->step++;
     const float b1 = 0.9f, b2 = 0.99f;
@@ -664,7 +678,8 @@ rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.out = d_out;
     a.ostride = ostride;
     const int ntiles = (n + 127) / 128;
-    k_mlp_forward<false><<<std::min(ntiles, 2 * m->sms), FWD_THREADS, FWD_SMEM_INFER, m->stream>>>(a);   // two per SM fit
+    k_mlp_forward<false, INFER_GROUPS><<<std::min((ntiles + INFER_GROUPS - 1) / INFER_GROUPS, m->sms), FWD_THREADS * INFER_GROUPS,
+                                         FWD_SMEM_INFER, m->stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
 }
 
