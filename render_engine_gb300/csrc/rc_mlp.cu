@@ -210,8 +210,8 @@ __device__ __forceinline__ void encode(const MlpArgs& a, int pt, int half, Emit&
 // accumulator, warp w reading the tensor-memory lanes of its quarter w % 4), with its own
 // activation tile, mbarrier, named barrier and 64 tensor-memory columns; the groups overlap
 // one tile's products with another's encoding and epilogues.
-// TRAIN (one group): also keeps X0^T, H_l^T and dY (with dY^T) of each tile in global memory
-// and adds the loss; otherwise writes the n_out outputs.
+// TRAIN: also keeps X0^T, H_l^T and dY (with dY^T) of each tile in global memory and adds the
+// loss; otherwise writes the n_out outputs.
 constexpr int FWD_THREADS = 256;                               // threads of one group
 constexpr int INFER_GROUPS = 4;                                // tiles in flight per inference CTA
 constexpr size_t GROUP_SMEM_INFER = (size_t)128 * K0 * 2;      // activation tile
@@ -351,6 +351,14 @@ __global__ void __launch_bounds__(FWD_THREADS * GROUPS) k_mlp_forward(const MlpA
     if (threadIdx.x < 32) tmem_dealloc(tmem_base, TCOLS);
 }
 
+// 16-byte asynchronous copies global -> shared (no register staging), all in flight at once
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // Backward pass of one tile (128 threads): for l = 4 .. 0, dW_l = dZ_l^T A_l over the tile's
 // samples (rows of dZ^T beyond the layer's outputs are zero) and, for l >= 1,
 // dZ_{l-1} = (dZ_l W_l) masked by ReLU'(H_l).  Tensor memory: dW in columns 0..175, dA in
@@ -368,8 +376,9 @@ __global__ void __launch_bounds__(128) k_mlp_backward(const MlpArgs a) {
     const uint8_t* act = a.act + (size_t)tile * ACT_BYTES;
     for (int i = tid; i < 128 * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sdzt)[i] = make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
-    for (int i = tid; i < 128 * OUTP * 2 / 16; i += 128) reinterpret_cast<uint4*>(sdz)[i] = reinterpret_cast<const uint4*>(act + ACT_DY)[i];
-    for (int i = tid; i < OUTP * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sdzt)[i] = reinterpret_cast<const uint4*>(act + ACT_DYT)[i];
+    for (int i = tid; i < 128 * OUTP * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sdz) + i, reinterpret_cast<const uint4*>(act + ACT_DY) + i);
+    for (int i = tid; i < OUTP * 128 * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sdzt) + i, reinterpret_cast<const uint4*>(act + ACT_DYT) + i);
+    cp_async_wait_all();
     if (tid == 0) mbar_init(&mbar, 1);
     if (warp == 0) tmem_alloc(&tmem_base, 256);
     fence_before_sync();
@@ -381,11 +390,12 @@ __global__ void __launch_bounds__(128) k_mlp_backward(const MlpArgs a) {
     for (int l = NLAYER - 1; l >= 0; --l) {
         const int Kin = in_dim(l), Nout = out_dim(l);
         const uint4* src = reinterpret_cast<const uint4*>(act + (l == 0 ? ACT_X0T : act_ht(l)));
-        for (int i = tid; i < Kin * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sat)[i] = src[i];
+        for (int i = tid; i < Kin * 128 * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sat) + i, src + i);
         if (l >= 1) {
             const uint4* w = reinterpret_cast<const uint4*>(a.wbf + wb_off(l));
-            for (int i = tid; i < Kin * Nout * 2 / 16; i += 128) reinterpret_cast<uint4*>(swt)[i] = w[i];
+            for (int i = tid; i < Kin * Nout * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(swt) + i, w + i);
         }
+        cp_async_wait_all();
         fence_proxy_async();
         __syncthreads();
         if (tid == 0) {
@@ -498,7 +508,8 @@ __global__ void k_mlp_adam(const float* __restrict__ slices, float* __restrict__
 }
 
 constexpr size_t FWD_SMEM_INFER = (size_t)WF_BYTES + INFER_GROUPS * GROUP_SMEM_INFER;   // 224 KB: one CTA per SM
-constexpr size_t FWD_SMEM_TRAIN = (size_t)WF_BYTES + GROUP_SMEM_TRAIN;
+constexpr int TRAIN_GROUPS = 2;                                  // tiles in flight per training-forward CTA
+constexpr size_t FWD_SMEM_TRAIN = (size_t)WF_BYTES + TRAIN_GROUPS * GROUP_SMEM_TRAIN;   // 224 KB
 constexpr size_t BWD_SMEM = (size_t)K0 * 128 * 2 + 128 * HID * 2 + 128 * 128 * 2 + HID * HID * 2;
 }  // namespace
 
@@ -599,7 +610,7 @@ rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out) {
     if (cudaMemsetAsync(m->m1, 0, 4 * NWEIGHT, m->stream) || cudaMemsetAsync(m->m2, 0, 4 * NWEIGHT, m->stream) ||
         cudaMemsetAsync(m->err, 0, 4, m->stream) || cudaStreamSynchronize(m->stream))
         return bad(RC_ERR_CUDA);
-    if (cudaFuncSetAttribute(k_mlp_forward<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_TRAIN) ||
+    if (cudaFuncSetAttribute(k_mlp_forward<true, TRAIN_GROUPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_TRAIN) ||
         cudaFuncSetAttribute(k_mlp_forward<false, INFER_GROUPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM_INFER) ||
         cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_SMEM))
         return bad(RC_ERR_CUDA);
@@ -657,7 +668,8 @@ rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.loss_scale = 1.f / ((float)n * (float)m->cfg.n_out);
     const int ntiles = n / 128;
     if (!d_loss && cudaMemsetAsync(m->loss, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "loss");
-    k_mlp_forward<true, 1><<<std::min(ntiles, m->sms), FWD_THREADS, FWD_SMEM_TRAIN, m->stream>>>(a);
+    k_mlp_forward<true, TRAIN_GROUPS><<<std::min((ntiles + TRAIN_GROUPS - 1) / TRAIN_GROUPS, m->sms), FWD_THREADS * TRAIN_GROUPS,
+                                        FWD_SMEM_TRAIN, m->stream>>>(a);
     k_mlp_backward<<<ntiles, 128, BWD_SMEM, m->stream>>>(a);
     m->step++;
     const float b1 = 0.9f, b2 = 0.99f;
