@@ -259,13 +259,17 @@ __global__ void __launch_bounds__(HG_BLOCK) k_vox_mark(const HgDev c, const VoxD
             a[k] = x.hit[k];
             d[k] = __fmul_rn(x.to_light[k], r);
         }
+        size_t last = ~(size_t)0;   // consecutive samples in one voxel mark it once
 #pragma unroll 4
         for (int k = 0; k < 20; ++k) {
             const float t = c_seg19[k];
             const int ix = vox_axis(__fadd_rn(a[0], __fmul_rn(d[0], t)), g.lo[0], g.scale[0], res);
             const int iy = vox_axis(__fadd_rn(a[1], __fmul_rn(d[1], t)), g.lo[1], g.scale[1], res);
             const int iz = vox_axis(__fadd_rn(a[2], __fmul_rn(d[2], t)), g.lo[2], g.scale[2], res);
-            unsigned long long* w = vox + ((size_t)iz * res + iy) * res + ix;
+            const size_t vi = ((size_t)iz * res + iy) * res + ix;
+            if (vi == last) continue;
+            last = vi;
+            unsigned long long* w = vox + vi;
             if (!(__ldcg(w) & bit)) atomicOr(w, bit);
         }
     }
@@ -354,19 +358,29 @@ __device__ __forceinline__ uint32_t to_fixed(float x) {
     return __float2uint_rn(y);
 }
 
-// Radiance samples in 1/1024 units and a sample count, added with integer atomics.
+// Radiance samples in 1/1024 units and a sample count, added with integer atomics; lanes of a
+// warp that share an entry add theirs first (integer sums: the result does not depend on it).
 __global__ void __launch_bounds__(HG_BLOCK) k_hg_accum(const uint32_t* __restrict__ entry, const float* __restrict__ rgb, int n,
                                                        uint4* __restrict__ accum) {
     const int i = blockIdx.x * HG_BLOCK + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t e = entry[i];
-    if (e == RC_HG_INVALID) return;
+    const uint32_t e = i < n ? entry[i] : RC_HG_INVALID;
+    uint32_t r = 0u, g = 0u, b = 0u;
+    if (e != RC_HG_INVALID) {
+        r = to_fixed(rgb[3 * (size_t)i]);
+        g = to_fixed(rgb[3 * (size_t)i + 1]);
+        b = to_fixed(rgb[3 * (size_t)i + 2]);
+    }
+    // lanes with the same entry (each group reduces over its own mask)
+    const unsigned peers = __match_any_sync(0xffffffffu, e);
+    const int lane = threadIdx.x & 31, lead = __ffs(peers) - 1;
+    const uint32_t sr = __reduce_add_sync(peers, r), sg = __reduce_add_sync(peers, g), sb = __reduce_add_sync(peers, b);
+    const uint32_t sc = (uint32_t)__popc(peers);
+    if (e == RC_HG_INVALID || lane != lead) return;
     unsigned* w = reinterpret_cast<unsigned*>(accum + e);
-    const uint32_t r = to_fixed(rgb[3 * (size_t)i]), g = to_fixed(rgb[3 * (size_t)i + 1]), b = to_fixed(rgb[3 * (size_t)i + 2]);
-    if (r) atomicAdd(w + 0, r);
-    if (g) atomicAdd(w + 1, g);
-    if (b) atomicAdd(w + 2, b);
-    atomicAdd(w + 3, 1u);
+    if (sr) atomicAdd(w + 0, sr);
+    if (sg) atomicAdd(w + 1, sg);
+    if (sb) atomicAdd(w + 2, sb);
+    atomicAdd(w + 3, sc);
 }
 
 __device__ __forceinline__ float h2f(uint32_t bits) { return __half2float(__ushort_as_half((unsigned short)bits)); }

@@ -121,6 +121,10 @@ struct rc_ctx {
         cudaEvent_t ready = nullptr;
     } cam;
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
+    int adj_cap_np = 0, adj_cap_k = 0, adj_cap_nl = 0;   // sizes the adjoint buffers were allocated for
+    float4* adj_aeu = nullptr;                  // unit-emission direct light of the last adjoint
+    uint32_t* adj_svu = nullptr;
+    const float* adj_ones = nullptr;
     rc::adj::Bufs adj{};
     Scene S;
     bool have_scene = false;
@@ -1160,6 +1164,7 @@ rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
     free_pool(ctx->taa_bufs);
     ctx->taa = TaaRun{};
     ctx->adj_np = ctx->adj_k = 0;
+    ctx->adj_cap_np = ctx->adj_cap_k = ctx->adj_cap_nl = 0;
     ctx->have_scene = false;
     ctx->run.active = false;
     ctx->c = DevCache{};
@@ -1653,31 +1658,41 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
     if (S.NL + 1 > adj::MAX_COLS) return fail(ctx, RC_ERR_UNSUPPORTED, "%d lights", S.NL);
     CKR(cudaSetDevice(ctx->cfg.device));
     cudaStream_t st = ctx->stream;
-    CKR(cudaStreamSynchronize(st));
-    free_pool(ctx->adj_bufs);
-    ctx->adj_np = ctx->adj_k = 0;
     const size_t Np = (size_t)S.Np, K = (size_t)prm->K;
     const int NL = S.NL, AES = aes_of(NL), iters = prm->iterations ? prm->iterations : 64;
-    auto& pool = ctx->adj_bufs;
-    adj::Bufs b{};
+    adj::Bufs b = ctx->adj;
     rc_status s;
-    if ((s = dalloc(ctx, pool, &b.hits, Np * K)) || (s = dalloc(ctx, pool, &b.cnt, Np + 1)) || (s = dalloc(ctx, pool, &b.off, Np + 1)) ||
-        (s = dalloc(ctx, pool, &b.fill, Np)) || (s = dalloc(ctx, pool, &b.src, Np * K)) ||
-        (s = dalloc(ctx, pool, &b.scratch, adj::scan_scratch_ints((long long)Np + 1))) || (s = dalloc(ctx, pool, &b.da, Np)) ||
-        (s = dalloc(ctx, pool, &b.L[0], Np)) || (s = dalloc(ctx, pool, &b.L[1], Np)) || (s = dalloc(ctx, pool, &b.g[0], Np)) ||
-        (s = dalloc(ctx, pool, &b.g[1], Np)) || (s = dalloc(ctx, pool, &b.u[0], Np)) ||
-        (s = dalloc(ctx, pool, &b.u[1], Np)) || (s = dalloc(ctx, pool, &b.w, Np)) ||
-        (s = dalloc(ctx, pool, &b.part, (size_t)adj::GRAD_BLOCKS * (NL + 1))) || (s = dalloc(ctx, pool, &b.stats, 1)))
-        return s;
-    // scratch of this call only: the unordered ray lists and the unit-emission direct light
-    std::vector<DevBuf> tmp;
-    struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
-    float4* AEu = nullptr;
-    uint32_t* SVu = nullptr;
-    const float* ones = nullptr;
-    if ((s = dalloc(ctx, tmp, &b.unordered, Np * K)) || (s = dalloc(ctx, tmp, &AEu, (size_t)AES / 4 * Np)) ||
-        (s = dalloc(ctx, tmp, &SVu, (size_t)ctx->NW * Np)) || (s = dput(ctx, tmp, &ones, std::vector<float>((size_t)NL, 1.f))))
-        return s;
+    // buffers kept from call to call while the point count, K and the light count stay
+    if (ctx->adj_cap_np != S.Np || ctx->adj_cap_k != prm->K || ctx->adj_cap_nl != NL) {
+        CKR(cudaStreamSynchronize(st));
+        free_pool(ctx->adj_bufs);
+        ctx->adj_np = ctx->adj_k = 0;
+        ctx->adj_cap_np = ctx->adj_cap_k = ctx->adj_cap_nl = 0;
+        auto& pool = ctx->adj_bufs;
+        b = adj::Bufs{};
+        float4* AEu = nullptr;
+        uint32_t* SVu = nullptr;
+        const float* ones = nullptr;
+        if ((s = dalloc(ctx, pool, &b.hits, Np * K)) || (s = dalloc(ctx, pool, &b.cnt, Np + 1)) || (s = dalloc(ctx, pool, &b.off, Np + 1)) ||
+            (s = dalloc(ctx, pool, &b.fill, Np)) || (s = dalloc(ctx, pool, &b.src, Np * K)) || (s = dalloc(ctx, pool, &b.unordered, Np * K)) ||
+            (s = dalloc(ctx, pool, &b.scratch, adj::scan_scratch_ints((long long)Np + 1))) || (s = dalloc(ctx, pool, &b.da, Np)) ||
+            (s = dalloc(ctx, pool, &b.L[0], Np)) || (s = dalloc(ctx, pool, &b.L[1], Np)) || (s = dalloc(ctx, pool, &b.g[0], Np)) ||
+            (s = dalloc(ctx, pool, &b.g[1], Np)) || (s = dalloc(ctx, pool, &b.u[0], Np)) ||
+            (s = dalloc(ctx, pool, &b.u[1], Np)) || (s = dalloc(ctx, pool, &b.w, Np)) ||
+            (s = dalloc(ctx, pool, &b.part, (size_t)adj::GRAD_BLOCKS * (NL + 1))) || (s = dalloc(ctx, pool, &b.stats, 1)) ||
+            (s = dalloc(ctx, pool, &AEu, (size_t)AES / 4 * Np)) || (s = dalloc(ctx, pool, &SVu, (size_t)ctx->NW * Np)) ||
+            (s = dput(ctx, pool, &ones, std::vector<float>((size_t)NL, 1.f))))
+            return s;
+        ctx->adj_aeu = AEu;
+        ctx->adj_svu = SVu;
+        ctx->adj_ones = ones;
+        ctx->adj_cap_np = S.Np;
+        ctx->adj_cap_k = prm->K;
+        ctx->adj_cap_nl = NL;
+    }
+    float4* AEu = ctx->adj_aeu;
+    uint32_t* SVu = ctx->adj_svu;
+    const float* ones = ctx->adj_ones;
     const DState& d = S.st[prm->state].d;
     FrameParams p{};
     p.Np = S.Np;
@@ -1706,7 +1721,6 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
         res->back = (long long)hs.back;
         res->max_incoming = hs.max_incoming;
     }
-    b.unordered = nullptr;
     ctx->adj = b;
     ctx->adj_np = S.Np;
     ctx->adj_k = prm->K;
