@@ -116,6 +116,8 @@ typedef struct rc_ray_rec {
     int pi;      /* cache point of the hit (the tracing point when the hit does not count) */
     int back;    /* 1 when the hit does not count (no hit, back face, cell absent) */
     float t;     /* hit distance (+inf when no hit) */
+    float dir[3];  /* ray direction */
+    float hit[3];  /* the end of the ray's dependency walk: origin + dir * t, the origin when no hit */
 } rc_ray_rec;
 
 /* Arrays of the run state (rc_array_*).  Layouts follow the reference Cache

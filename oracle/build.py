@@ -38,7 +38,7 @@ def build_refrun(force: bool = False) -> str:
 def build_reference_cubins(force: bool = False) -> bool:
     """Compile the reference kernels when the reference checkout is present."""
     src = os.path.join(REFERENCE, "cuda", "poc_gpu.cu")
-    outs = [os.path.join(HERE, "_ref", "ref_l%d.cubin" % n) for n in (3, 8)]
+    outs = [os.path.join(HERE, "_ref", n) for n in ("ref_l3.cubin", "ref_l8.cubin", "ref_l3_g16x8x6.cubin")]
     if not os.path.exists(src):
         return all(os.path.exists(o) for o in outs)
     if force or any(_stale(o, [src, os.path.join(HERE, "build_ref.sh")]) for o in outs):

@@ -11,12 +11,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "librefrun.so")
 
 
-def cubin_path(nl: int) -> str:
-    return os.path.join(HERE, "_ref", "ref_l%d.cubin" % nl)
+def cubin_path(nl: int, grid=(8, 4, 4)) -> str:
+    if tuple(grid) == (8, 4, 4):
+        return os.path.join(HERE, "_ref", "ref_l%d.cubin" % nl)
+    return os.path.join(HERE, "_ref", "ref_l%d_g%dx%dx%d.cubin" % (nl, *grid))
 
 
-def available(nl: int = 3) -> bool:
-    return os.path.exists(cubin_path(nl))
+def available(nl: int = 3, grid=(8, 4, 4)) -> bool:
+    return os.path.exists(cubin_path(nl, grid))
 
 
 _lib = None
@@ -31,6 +33,8 @@ def lib():
         vp, i, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
         L.ref_create.restype = vp
         L.ref_create.argtypes = [ctypes.c_char_p, i, ctypes.c_char_p, i]
+        L.ref_create_grid.restype = vp
+        L.ref_create_grid.argtypes = [ctypes.c_char_p, i, i, i, i, ctypes.c_char_p, i]
         L.ref_destroy.argtypes = [vp]
         L.ref_last_error.restype = ctypes.c_char_p
         L.ref_last_error.argtypes = [vp]
@@ -66,10 +70,10 @@ _DT = {0: np.float32, 1: np.float32, 2: np.float32, 3: np.float32, 4: np.float32
 class RefRunner:
     """The reference's kernels on the GPU with the reference's frame driver logic."""
 
-    def __init__(self, nl: int, data: bytes):
+    def __init__(self, nl: int, data: bytes, grid=(8, 4, 4)):
         L = lib()
         err = ctypes.create_string_buffer(256)
-        p = L.ref_create(cubin_path(nl).encode(), nl, err, 256)
+        p = L.ref_create_grid(cubin_path(nl, grid).encode(), nl, grid[0], grid[1], grid[2], err, 256)
         if not p:
             raise RuntimeError("reference kernels: " + err.value.decode())
         self.p = p
@@ -78,7 +82,7 @@ class RefRunner:
         if L.ref_load(p, self._data.ctypes.data_as(ctypes.c_void_p), self._data.nbytes) != 0:
             raise RuntimeError("reference load: " + L.ref_last_error(p).decode())
         h = np.frombuffer(data[:32], np.int32)
-        self.Np, self.NS, self.NL, self.NW = int(h[0]), int(h[3]), int(h[4]), 4
+        self.Np, self.NS, self.NL, self.NW = int(h[0]), int(h[3]), int(h[4]), grid[0] * grid[1] * grid[2] // 32
 
     def begin(self, method, s0: int, seed: int):
         from render_engine_gb300.methods import to_c

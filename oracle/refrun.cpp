@@ -211,12 +211,18 @@ extern "C" {
 
 const char* ref_last_error(ref_ctx* r) { return r ? r->err.c_str() : "no context"; }
 
-ref_ctx* ref_create(const char* cubin, int nl, char* err, int errlen) {
+// The cubin's transit grid (its -DGX/-DGY/-DGZ) is vx x vy x vz; NW = vx vy vz / 32.
+ref_ctx* ref_create_grid(const char* cubin, int nl, int vx, int vy, int vz, char* err, int errlen) {
     auto seterr = [&](const char* m) { if (err && errlen > 0) { strncpy(err, m, errlen - 1); err[errlen - 1] = 0; } };
     if (nl <= 0 || nl > MAXNL) { seterr("light count"); return nullptr; }
+    if (vx <= 0 || vy <= 0 || vz <= 0 || (vx * vy * vz) % 128) { seterr("transit grid"); return nullptr; }
     if (cuInit(0) != CUDA_SUCCESS) { seterr("cuInit failed"); return nullptr; }
     ref_ctx* r = new ref_ctx();
     r->NL = nl;
+    r->VX = vx;
+    r->VY = vy;
+    r->VZ = vz;
+    r->NW = vx * vy * vz / 32;
     CUdevice dev;
     if (cuDeviceGet(&dev, 0) != CUDA_SUCCESS || cuDevicePrimaryCtxRetain(&r->cu, dev) != CUDA_SUCCESS ||
         cuCtxSetCurrent(r->cu) != CUDA_SUCCESS) { seterr("no CUDA context"); delete r; return nullptr; }
@@ -255,6 +261,8 @@ ref_ctx* ref_create(const char* cubin, int nl, char* err, int errlen) {
     for (auto& e : r->ev) cuEventCreate(&e, CU_EVENT_DEFAULT);
     return r;
 }
+
+ref_ctx* ref_create(const char* cubin, int nl, char* err, int errlen) { return ref_create_grid(cubin, nl, 8, 4, 4, err, errlen); }
 
 void ref_destroy(ref_ctx* r) {
     if (!r) return;

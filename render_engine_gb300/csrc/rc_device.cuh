@@ -89,20 +89,29 @@ __device__ __forceinline__ void set_bit(uint32_t (&m)[NW], int v) {
 
 // Amanatides-Woo walk of segment a->b over the transit grid, same float sequence as
 // dda_reg (poc_gpu.cu:171-190).  The loop bound vx+vy+vz is the reference's.
+//
+// Every product and sum is rounded on its own (__fmul_rn / __fadd_rn / __fsub_rn are never
+// fused into an FMA): the grid coordinate ax = (a.x - lo) * sx must be rounded before ix is
+// subtracted from it.  A fused (a.x - lo) * sx - ix keeps the product's low bits, and a
+// cache point lying on a voxel face (z = 2.25 with sz = 4/3: the product is 3.0000001,
+// rounded 3.0) then starts with tmz = 1e-7 * tdz instead of 0 and breaks the tie at a voxel
+// edge the other way.
 template <int NW>
 __device__ __forceinline__ void dda_walk(const Grid& g, f3 a, f3 b, uint32_t (&m)[NW]) {
     const int VX = g.vx, VY = g.vy, VZ = g.vz;
     const float sx = g.scale[0], sy = g.scale[1], sz = g.scale[2];
-    float ax = (a.x - g.lo[0]) * sx, ay = (a.y - g.lo[1]) * sy, az = (a.z - g.lo[2]) * sz;
-    float bx = (b.x - g.lo[0]) * sx, by = (b.y - g.lo[1]) * sy, bz = (b.z - g.lo[2]) * sz;
+    const float ax = __fmul_rn(__fsub_rn(a.x, g.lo[0]), sx), ay = __fmul_rn(__fsub_rn(a.y, g.lo[1]), sy),
+                az = __fmul_rn(__fsub_rn(a.z, g.lo[2]), sz);
+    const float bx = __fmul_rn(__fsub_rn(b.x, g.lo[0]), sx), by = __fmul_rn(__fsub_rn(b.y, g.lo[1]), sy),
+                bz = __fmul_rn(__fsub_rn(b.z, g.lo[2]), sz);
     int ix = min(max(int(ax), 0), VX - 1), iy = min(max(int(ay), 0), VY - 1), iz = min(max(int(az), 0), VZ - 1);
     int ex = min(max(int(bx), 0), VX - 1), ey = min(max(int(by), 0), VY - 1), ez = min(max(int(bz), 0), VZ - 1);
-    float dx = bx - ax, dy = by - ay, dz = bz - az;
+    const float dx = __fsub_rn(bx, ax), dy = __fsub_rn(by, ay), dz = __fsub_rn(bz, az);
     int stx = dx > 0 ? 1 : -1, sty = dy > 0 ? 1 : -1, stz = dz > 0 ? 1 : -1;
     float tdx = dx != 0 ? fabsf(1.f / dx) : 1e30f, tdy = dy != 0 ? fabsf(1.f / dy) : 1e30f, tdz = dz != 0 ? fabsf(1.f / dz) : 1e30f;
-    float tmx = dx != 0 ? ((dx > 0 ? (ix + 1 - ax) : (ax - ix)) * tdx) : 1e30f;
-    float tmy = dy != 0 ? ((dy > 0 ? (iy + 1 - ay) : (ay - iy)) * tdy) : 1e30f;
-    float tmz = dz != 0 ? ((dz > 0 ? (iz + 1 - az) : (az - iz)) * tdz) : 1e30f;
+    float tmx = dx != 0 ? __fmul_rn(dx > 0 ? __fsub_rn((float)(ix + 1), ax) : __fsub_rn(ax, (float)ix), tdx) : 1e30f;
+    float tmy = dy != 0 ? __fmul_rn(dy > 0 ? __fsub_rn((float)(iy + 1), ay) : __fsub_rn(ay, (float)iy), tdy) : 1e30f;
+    float tmz = dz != 0 ? __fmul_rn(dz > 0 ? __fsub_rn((float)(iz + 1), az) : __fsub_rn(az, (float)iz), tdz) : 1e30f;
     const int steps = VX + VY + VZ;
     // The voxel index v and the steps left before each axis leaves the grid are carried along
     // instead of the three coordinates: the same voxels in the same order, and the same exits
@@ -131,9 +140,9 @@ __device__ __forceinline__ void dda_walk(const Grid& g, f3 a, f3 b, uint32_t (&m
         ry -= sy ? 1 : 0;
         rz -= (!sx && !sy) ? 1 : 0;
         v += sx ? dvx : (sy ? dvy : dvz);
-        tmx = sx ? tmx + tdx : tmx;
-        tmy = sy ? tmy + tdy : tmy;
-        tmz = (!sx && !sy) ? tmz + tdz : tmz;
+        tmx = sx ? __fadd_rn(tmx, tdx) : tmx;
+        tmy = sy ? __fadd_rn(tmy, tdy) : tmy;
+        tmz = (!sx && !sy) ? __fadd_rn(tmz, tdz) : tmz;
     }
     if (NW == 4) {
         m[0] |= (uint32_t)lo;

@@ -1337,7 +1337,7 @@ __global__ void __launch_bounds__(BLOCK) k_paths(const DState s, const DStatic g
 }
 
 // ------------------------------------------------------------------ probe
-struct RayRecD { int point, ray, q, pi, back; float t; };
+struct RayRecD { int point, ray, q, pi, back; float t; float dir[3], hit[3]; };
 
 template <int NL, int NW>
 __global__ void __launch_bounds__(BLOCK) k_probe(const DState s, const DStatic g, const Grid grid, const DevCache c,
@@ -1365,6 +1365,8 @@ __global__ void __launch_bounds__(BLOCK) k_probe(const DState s, const DStatic g
             RayRecD x;
             x.point = i; x.ray = r; x.q = h.q; x.pi = h.pi; x.back = h.back ? 1 : 0;
             x.t = h.q != -1 ? h.t : __int_as_float(0x7f800000);
+            x.dir[0] = D.x; x.dir[1] = D.y; x.dir[2] = D.z;
+            x.hit[0] = h.H.x; x.hit[1] = h.H.y; x.hit[2] = h.H.z;
             out[slot] = x;
         }
     }

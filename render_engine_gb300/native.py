@@ -86,7 +86,7 @@ class RunStats(ctypes.Structure):
 
 class RayRec(ctypes.Structure):
     _fields_ = [("point", ctypes.c_int), ("ray", ctypes.c_int), ("q", ctypes.c_int), ("pi", ctypes.c_int),
-                ("back", ctypes.c_int), ("t", ctypes.c_float)]
+                ("back", ctypes.c_int), ("t", ctypes.c_float), ("dir", ctypes.c_float * 3), ("hit", ctypes.c_float * 3)]
 
 
 _lib = None
@@ -348,6 +348,17 @@ class Context:
         n = ctypes.c_int()
         self._chk(self.L.rc_probe_rays(self.h, state, pts, len(points), out, cap, ctypes.byref(n)))
         return sorted((r.point, r.ray, r.q, r.pi, r.back, r.t) for r in out[: n.value])
+
+    def probe_full(self, state: int, points) -> list[dict]:
+        """rc_probe_rays with every field: also the direction and the end point of each ray."""
+        pts = (ctypes.c_int * len(points))(*[int(x) for x in points])
+        cap = 64 * len(points) + 64
+        out = (RayRec * cap)()
+        n = ctypes.c_int()
+        self._chk(self.L.rc_probe_rays(self.h, state, pts, len(points), out, cap, ctypes.byref(n)))
+        recs = [dict(point=r.point, ray=r.ray, q=r.q, pi=r.pi, back=r.back, t=r.t,
+                     dir=np.array(r.dir[:], np.float32), hit=np.array(r.hit[:], np.float32)) for r in out[: n.value]]
+        return sorted(recs, key=lambda d: (d["point"], d["ray"]))
 
     def check_count(self) -> tuple[int, int]:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
