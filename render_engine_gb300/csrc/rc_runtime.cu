@@ -85,6 +85,10 @@ struct TaaRun {
     double *part = nullptr, *out = nullptr;
     std::vector<const int*> dV;     // event voxels per state pair (device), and their counts
     std::vector<int> nV;
+    // per state: the sum of the references over the valid points and their count (the error's
+    // denominators), computed once per run and state
+    std::vector<double> ref_sum, ref_cnt;
+    std::vector<char> have_sums;
 };
 
 struct Run {
@@ -137,6 +141,7 @@ struct rc_ctx {
     float* img = nullptr;
     size_t img_cap = 0;
     cudaEvent_t ev[8] = {};
+    double* pinned = nullptr;   // page-locked scratch for per-frame scalar read-backs (8 doubles)
 };
 
 namespace {
@@ -1130,6 +1135,7 @@ void rc_destroy(rc_ctx* ctx) {
     free_pool(ctx->cam_bufs);
     if (ctx->cam.ready) cudaEventDestroy(ctx->cam.ready);
     if (ctx->flags_dev) cudaFree(ctx->flags_dev);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1560,6 +1566,8 @@ rc_status rc_reference_build(rc_ctx* ctx, const rc_ref_params* prm, double* nois
     const size_t Np = (size_t)S.Np;
     const int NL = S.NL, LCS = lcs_of(NL);
     cudaStream_t st = ctx->stream;
+    // the references change: a taa run recomputes its per-state error denominators
+    std::fill(ctx->taa.have_sums.begin(), ctx->taa.have_sums.end(), (char)0);
     std::vector<DevBuf> tmp;
     struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
     float *chain[2], *acc[2], *out = nullptr, *closec = nullptr;
@@ -1762,6 +1770,9 @@ rc_status rc_taa_begin(rc_ctx* ctx, const rc_taa_method* m, int first_state, uin
     t.M = *m;
     t.seed = seed;
     t.f = 0;
+    t.ref_sum.assign(S.NS, 0.0);
+    t.ref_cnt.assign(S.NS, 0.0);
+    t.have_sums.assign(S.NS, 0);
     t.prev_state = first_state;
     t.verify_left = 0;
     t.active = true;
@@ -1817,6 +1828,16 @@ rc_status rc_taa_frame(rc_ctx* ctx, int state, float* err) {
             ++kernels;
         }
     }
+    if (err && !t.have_sums[state]) {
+        double h[3];
+        CKR(taa::ref_sums(d.ref, d.valid, Np, t.part, t.out, st));
+        kernels += 2;
+        CKR(cudaMemcpyAsync(h, t.out, sizeof h, cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));
+        t.ref_sum[state] = h[1];
+        t.ref_cnt[state] = h[2];
+        t.have_sums[state] = 1;
+    }
     CKR(taa::post(t.x, t.qid, t.quad, t.H, t.H2, t.mu, t.sg, t.react, Np, M.alpha, TAA_ALPHA_R, M.gamma, d.ref, d.valid, err ? t.part : nullptr,
                   t.out, st));
     kernels += err ? 2 : 1;
@@ -1825,10 +1846,13 @@ rc_status rc_taa_frame(rc_ctx* ctx, int state, float* err) {
     t.prev_state = state;
     t.f = f + 1;
     if (err) {
-        double h[3];
-        CKR(cudaMemcpyAsync(h, t.out, sizeof h, cudaMemcpyDeviceToHost, st));
+        // the squared error through page-locked memory: one DMA, no staging copy
+        if (!ctx->pinned) CKR(cudaMallocHost(&ctx->pinned, 8 * sizeof(double)));
+        CKR(cudaMemcpyAsync(ctx->pinned, t.out, sizeof(double), cudaMemcpyDeviceToHost, st));
         CKR(cudaStreamSynchronize(st));
-        *err = (float)(h[2] > 0 && h[1] > 0 ? std::sqrt(h[0] / h[2]) / (h[1] / h[2]) : 0.0);
+        const double d2 = ctx->pinned[0];
+        const double rs = t.ref_sum[state], cn = t.ref_cnt[state];
+        *err = (float)(cn > 0 && rs > 0 ? std::sqrt(d2 / cn) / (rs / cn) : 0.0);
     }
     return RC_OK;
 }

@@ -99,9 +99,25 @@ __global__ void k_zone_decide(const float* __restrict__ rs, const float* __restr
     if (clear_pending) pend[i] = 0;
 }
 
+// Block partial of one FP64 value per thread, in a fixed order: the warp butterfly, then the
+// block's 8 warp sums in warp order by thread 0.
+__device__ __forceinline__ void block_partial(double v, double* sh, double* dst) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < B / 32; ++w) t += sh[w];
+        *dst = t;
+    }
+}
+
 // k_taa_stats + k_taa_update + k_taa_err (poc_gpu.cu:1100-1108, 1152-1166) for one point:
 // 3x3 mean and deviation of the samples, the clamped and blended history, and this block's
-// FP64 partial error sums over the new history (summed in a fixed order).  The 3x3
+// FP64 partial of the squared error of the new history (summed in a fixed order; the sums
+// of the references and of the valid points, which do not change within a state, come from
+// k_ref_sums).  The 3x3
 // neighbourhood on the point's quad grid (run_taa_mode's table, poc_gpu.cu:1192-1203) is
 // derived from the point's quad: quad[q] = (first point, nu, nv), neighbours in the table's
 // order (dv outer, du inner), -1 outside the grid; a point of no quad has no neighbours.
@@ -110,9 +126,9 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
                                             float* __restrict__ H2, float* __restrict__ mu_out, float* __restrict__ sg_out,
                                             int* __restrict__ react, int Np, float alpha, float alpha_r, float gamma,
                                             const float* __restrict__ ref, const uint8_t* __restrict__ valid, double* __restrict__ part) {
-    __shared__ double sh[3][B / 32];
+    __shared__ double sh[B / 32];
     const int i = blockIdx.x * B + threadIdx.x;
-    double d2 = 0.0, rsum = 0.0, c = 0.0;
+    double d2 = 0.0;
     if (i < Np) {
         float s1 = 0.f, s2 = 0.f;
         int n = 0;
@@ -151,28 +167,20 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
         if (ref && valid[i]) {
             const double e = hn - ref[i];
             d2 = e * e;
-            rsum = ref[i];
-            c = 1.0;
         }
     }
     if (!part) return;
-    for (int o = 16; o > 0; o >>= 1) {
-        d2 += __shfl_xor_sync(0xffffffffu, d2, o);
-        rsum += __shfl_xor_sync(0xffffffffu, rsum, o);
-        c += __shfl_xor_sync(0xffffffffu, c, o);
-    }
-    const int warp = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        sh[0][warp] = d2;
-        sh[1][warp] = rsum;
-        sh[2][warp] = c;
-    }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        double t = 0.0;
-        for (int w = 0; w < B / 32; ++w) t += sh[threadIdx.x][w];
-        part[3 * (size_t)blockIdx.x + threadIdx.x] = t;
-    }
+    block_partial(d2, sh, part + 3 * (size_t)blockIdx.x);
+}
+
+// The other two error sums of k_post's tree: the references and the count of the valid points.
+__global__ void __launch_bounds__(B) k_ref_sums(const float* __restrict__ ref, const uint8_t* __restrict__ valid, int Np,
+                                                double* __restrict__ part) {
+    __shared__ double sh[2][B / 32];
+    const int i = blockIdx.x * B + threadIdx.x;
+    const bool on = i < Np && valid[i];
+    block_partial(on ? (double)ref[i] : 0.0, sh[0], part + 3 * (size_t)blockIdx.x + 1);
+    block_partial(on ? 1.0 : 0.0, sh[1], part + 3 * (size_t)blockIdx.x + 2);
 }
 
 // the block partials in block order
@@ -228,6 +236,12 @@ cudaError_t post(const float* x, const int* qid, const int4* quad, const float* 
                  float alpha, float alpha_r, float gamma, const float* ref, const uint8_t* valid, double* part, double* out, cudaStream_t st) {
     k_post<<<blocks(Np), B, 0, st>>>(x, qid, quad, H, H2, mu, sg, react, Np, alpha, alpha_r, gamma, ref, valid, part);
     if (part) k_err_final<<<1, B, 0, st>>>(part, blocks(Np), out);
+    return cudaGetLastError();
+}
+
+cudaError_t ref_sums(const float* ref, const uint8_t* valid, int Np, double* part, double* out, cudaStream_t st) {
+    k_ref_sums<<<blocks(Np), B, 0, st>>>(ref, valid, Np, part);
+    k_err_final<<<1, B, 0, st>>>(part, blocks(Np), out);
     return cudaGetLastError();
 }
 

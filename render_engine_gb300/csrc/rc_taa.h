@@ -19,6 +19,9 @@ cudaError_t zone_decide(const float* rs, const float* cnt, uint8_t* pend, const 
 // quad of each point (-1: none), quad[q] = (first point, nu, nv, 0)
 cudaError_t post(const float* x, const int* qid, const int4* quad, const float* H, float* H2, float* mu, float* sg, int* react, int Np,
                  float alpha, float alpha_r, float gamma, const float* ref, const uint8_t* valid, double* part, double* out, cudaStream_t st);
+// out[1] = the sum of the references over the valid points, out[2] = their count, in post's
+// fixed order (out[0], the squared error, is post's).  They depend only on the state.
+cudaError_t ref_sums(const float* ref, const uint8_t* valid, int Np, double* part, double* out, cudaStream_t st);
 
 }  // namespace taa
 }  // namespace rc
