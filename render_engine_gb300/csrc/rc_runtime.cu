@@ -142,6 +142,8 @@ struct rc_ctx {
     size_t img_cap = 0;
     cudaEvent_t ev[8] = {};
     double* pinned = nullptr;   // page-locked scratch for per-frame scalar read-backs (8 doubles)
+    void* stage = nullptr;      // device staging of padded arrays packed for one host copy
+    size_t stage_cap = 0;
 };
 
 namespace {
@@ -238,6 +240,26 @@ __global__ void k_load_check(const int* __restrict__ v, size_t n, int lo, int hi
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         out |= v[i] < lo || v[i] >= hi;
     if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31) == 0) atomicOr(bad, bit);
+}
+__global__ void k_fill(float* __restrict__ dst, size_t n, float v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = v;
+}
+// Rows of 4-byte elements between a padded device layout (ss per row) and a packed one (ds per
+// row, ds <= ss): one contiguous host copy of the packed rows instead of a 2-D copy of
+// millions of 12-byte rows.  Unpacking leaves the padding of each row as it was.
+__global__ void k_pack_rows(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, size_t rows, int ds, int ss) {
+    const size_t n = rows * (size_t)ds;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = t / (size_t)ds, k = t - r * ds;
+        dst[t] = src[r * ss + k];
+    }
+}
+__global__ void k_unpack_rows(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, size_t rows, int ds, int ss) {
+    const size_t n = rows * (size_t)ds;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = t / (size_t)ds, k = t - r * ds;
+        dst[r * ss + k] = src[t];
+    }
 }
 constexpr unsigned LOAD_BAD_REGION = 1u, LOAD_BAD_HASH = 2u;
 int load_grid(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 4096); }
@@ -1136,6 +1158,7 @@ void rc_destroy(rc_ctx* ctx) {
     if (ctx->cam.ready) cudaEventDestroy(ctx->cam.ready);
     if (ctx->flags_dev) cudaFree(ctx->flags_dev);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->stage) cudaFree(ctx->stage);
     if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1240,9 +1263,9 @@ rc_status rc_run_begin(rc_ctx* ctx, const rc_method* m, int s0, uint32_t seed) {
     else CKR(cudaMemsetAsync(c.Lc, 0, LCS * Np * 4, st));
     R.nmax = m->nmax * m->rays;
     {
-        std::vector<float> nm(Np, R.nmax), ag(Np, 1e4f);
-        CKR(cudaMemcpyAsync(c.n, nm.data(), Np * 4, cudaMemcpyHostToDevice, st));
-        CKR(cudaMemcpyAsync(c.age, ag.data(), Np * 4, cudaMemcpyHostToDevice, st));
+        k_fill<<<load_grid(Np), 256, 0, st>>>(c.n, Np, R.nmax);
+        k_fill<<<load_grid(Np), 256, 0, st>>>(c.age, Np, 1e4f);
+        CKR(cudaGetLastError());
         CKR(cudaMemsetAsync(c.pending, 0, Np, st));
         CKR(cudaMemsetAsync(c.cur, 0, (size_t)ctx->NW * Np * 4, st));
         CKR(cudaMemsetAsync(c.prev, 0, (size_t)ctx->NW * Np * 4, st));
@@ -1252,7 +1275,7 @@ rc_status rc_run_begin(rc_ctx* ctx, const rc_method* m, int s0, uint32_t seed) {
         CKR(cudaMemcpyAsync(c.sumpr, sp, 8, cudaMemcpyHostToDevice, st));
         CKR(cudaMemcpyAsync(c.npend, z2, 8, cudaMemcpyHostToDevice, st));
         CKR(cudaMemsetAsync(c.rays, 0, 8, st));
-        CKR(cudaStreamSynchronize(st));   // host vectors above are about to go out of scope
+        CKR(cudaStreamSynchronize(st));   // sp and z2 are about to go out of scope
     }
     R.p.seed = seed;
     for (int k = 0; k < KSNAP; ++k) R.slot_state[k] = -1;
@@ -1396,6 +1419,33 @@ rc_status rc_array_info(rc_ctx* ctx, int which, size_t* nbytes, void** dev_ptr) 
     return RC_OK;
 }
 
+// `rows` rows of 4-byte elements between host (ds per row, packed) and device (ss per row,
+// the first ds copied): packed on the device into the staging buffer, then one contiguous copy
+// (or the reverse).  Asynchronous on the context's stream.
+static rc_status copy_rows(rc_ctx* ctx, void* host, void* dev, size_t rows, int ds, int ss, bool to_device) {
+    const size_t nbytes = rows * (size_t)ds * 4;
+    cudaStream_t st = ctx->stream;
+    if (ctx->stage_cap < nbytes) {
+        CKR(cudaStreamSynchronize(st));
+        if (ctx->stage) cudaFree(ctx->stage);
+        ctx->stage = nullptr;
+        ctx->stage_cap = 0;
+        CKR(cudaMalloc(&ctx->stage, nbytes));
+        ctx->stage_cap = nbytes;
+    }
+    uint32_t* sb = static_cast<uint32_t*>(ctx->stage);
+    if (to_device) {
+        CKR(cudaMemcpyAsync(sb, host, nbytes, cudaMemcpyHostToDevice, st));
+        k_unpack_rows<<<load_grid(rows * ds), 256, 0, st>>>(sb, static_cast<uint32_t*>(dev), rows, ds, ss);
+        CKR(cudaGetLastError());
+    } else {
+        k_pack_rows<<<load_grid(rows * ds), 256, 0, st>>>(static_cast<const uint32_t*>(dev), sb, rows, ds, ss);
+        CKR(cudaGetLastError());
+        CKR(cudaMemcpyAsync(host, sb, nbytes, cudaMemcpyDeviceToHost, st));
+    }
+    return RC_OK;
+}
+
 rc_status rc_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, int to_device) {
     if (!ctx || !host) return RC_ERR_ARG;
     if (!ctx->have_scene) return RC_ERR_STATE;
@@ -1417,8 +1467,14 @@ rc_status rc_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, int t
     if (ss) {
         // padded device rows of ss elements, packed host rows of ds elements
         const size_t rows = count / ds;
-        if (to_device) CKR(cudaMemcpy2DAsync(dev, ss * elem, host, ds * elem, ds * elem, rows, cudaMemcpyHostToDevice, ctx->stream));
-        else CKR(cudaMemcpy2DAsync(host, ds * elem, dev, ss * elem, ds * elem, rows, cudaMemcpyDeviceToHost, ctx->stream));
+        rc_status s2;
+        if (elem == 4) {
+            if ((s2 = copy_rows(ctx, host, dev, rows, (int)ds, (int)ss, to_device != 0)) != RC_OK) return s2;
+        } else if (to_device) {
+            CKR(cudaMemcpy2DAsync(dev, ss * elem, host, ds * elem, ds * elem, rows, cudaMemcpyHostToDevice, ctx->stream));
+        } else {
+            CKR(cudaMemcpy2DAsync(host, ds * elem, dev, ss * elem, ds * elem, rows, cudaMemcpyDeviceToHost, ctx->stream));
+        }
     } else {
         CKR(cudaMemcpyAsync(to_device ? dev : host, to_device ? host : dev, nbytes,
                             to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, ctx->stream));
@@ -1476,7 +1532,10 @@ rc_status rc_state_array_copy(rc_ctx* ctx, int state, int which, void* host, siz
     switch (which) {
         case RC_SA_EDIR:
             if (nbytes != 4 * NL * Np) return RC_ERR_ARG;
-            CKR(cudaMemcpy2DAsync(host, NL * 4, (const float*)d.AE + 1, AES * 4, NL * 4, Np, cudaMemcpyDeviceToHost, st));
+            {
+                rc_status s2 = copy_rows(ctx, host, const_cast<float*>(reinterpret_cast<const float*>(d.AE)) + 1, Np, (int)NL, (int)AES, false);
+                if (s2 != RC_OK) return s2;
+            }
             break;
         case RC_SA_SV:
             if (nbytes != 4 * (size_t)ctx->NW * Np) return RC_ERR_ARG;
@@ -1492,7 +1551,10 @@ rc_status rc_state_array_copy(rc_ctx* ctx, int state, int which, void* host, siz
             break;
         case RC_SA_PW:
             if (!S.has_ref || nbytes != 4 * NL * Np) return RC_ERR_ARG;
-            CKR(cudaMemcpy2DAsync(host, NL * 4, S.st[state].pw, (size_t)lcs_of(S.NL) * 4, NL * 4, Np, cudaMemcpyDeviceToHost, st));
+            {
+                rc_status s2 = copy_rows(ctx, host, const_cast<float*>(S.st[state].pw), Np, (int)NL, lcs_of(S.NL), false);
+                if (s2 != RC_OK) return s2;
+            }
             break;
         default:
             return RC_ERR_ARG;
