@@ -113,11 +113,26 @@ __device__ __forceinline__ void block_partial(double v, double* sh, double* dst)
     }
 }
 
+// Double-float sum (hi + lo, |lo| <= ulp(hi) / 2) of two such pairs: TwoSum of the high parts,
+// then the low parts, renormalised; about 48 significant bits, all on the FP32 pipe.  Adds
+// and subtractions only (nothing to fuse), and symmetric in a and b, so every lane of an xor
+// butterfly ends with the same pair.
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float s = __fadd_rn(a.x, b.x);
+    const float bv = __fsub_rn(s, a.x);
+    const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bv)), __fsub_rn(b.x, bv));
+    const float lo = __fadd_rn(__fadd_rn(a.y, b.y), err);
+    const float hi = __fadd_rn(s, lo);
+    return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+
 // k_taa_stats + k_taa_update + k_taa_err (poc_gpu.cu:1100-1108, 1152-1166) for one point:
 // 3x3 mean and deviation of the samples, the clamped and blended history, and this block's
-// FP64 partial of the squared error of the new history (summed in a fixed order; the sums
-// of the references and of the valid points, which do not change within a state, come from
-// k_ref_sums).  The 3x3
+// partial of the squared error of the new history in a fixed order: each e^2 exactly as a
+// pair of floats, the warp's sum as a double-float butterfly (the FP64 pipe of this GPU is a
+// small fraction of its FP32 rate), the 8 warp sums in FP64 in warp order.  The sums of the
+// references and of the valid points, which do not change within a state, come from
+// k_ref_sums.  The 3x3
 // neighbourhood on the point's quad grid (run_taa_mode's table, poc_gpu.cu:1192-1203) is
 // derived from the point's quad: quad[q] = (first point, nu, nv), neighbours in the table's
 // order (dv outer, du inner), -1 outside the grid; a point of no quad has no neighbours.
@@ -128,7 +143,7 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
                                             const float* __restrict__ ref, const uint8_t* __restrict__ valid, double* __restrict__ part) {
     __shared__ double sh[B / 32];
     const int i = blockIdx.x * B + threadIdx.x;
-    double d2 = 0.0;
+    float2 d2 = make_float2(0.f, 0.f);
     if (i < Np) {
         float s1 = 0.f, s2 = 0.f;
         int n = 0;
@@ -165,12 +180,23 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
         const float hn = h + a * (target - h);
         H2[i] = hn;
         if (ref && valid[i]) {
-            const double e = hn - ref[i];
-            d2 = e * e;
+            const float e = hn - ref[i];
+            const float hi = __fmul_rn(e, e);
+            d2 = make_float2(hi, __fmaf_rn(e, e, -hi));   // e^2 = hi + lo exactly
         }
     }
     if (!part) return;
-    block_partial(d2, sh, part + 3 * (size_t)blockIdx.x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        d2 = df_add(d2, make_float2(__shfl_xor_sync(0xffffffffu, d2.x, o), __shfl_xor_sync(0xffffffffu, d2.y, o)));
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) sh[warp] = (double)d2.x + (double)d2.y;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < B / 32; ++w) t += sh[w];
+        part[3 * (size_t)blockIdx.x] = t;
+    }
 }
 
 // The other two error sums of k_post's tree: the references and the count of the valid points.
