@@ -129,8 +129,9 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
 // k_taa_stats + k_taa_update + k_taa_err (poc_gpu.cu:1100-1108, 1152-1166) for one point:
 // 3x3 mean and deviation of the samples, the clamped and blended history, and this block's
 // partial of the squared error of the new history in a fixed order: each e^2 exactly as a
-// pair of floats, the warp's sum as a double-float butterfly (the FP64 pipe of this GPU is a
-// small fraction of its FP32 rate), the 8 warp sums in FP64 in warp order.  The sums of the
+// pair of floats, the warp's sum as a double-float butterfly and the block's 8 warp sums
+// added in warp order the same way (the FP64 pipe of this GPU is a small fraction of its
+// FP32 rate), one conversion to FP64 per block.  The sums of the
 // references and of the valid points, which do not change within a state, come from
 // k_ref_sums.  The 3x3
 // neighbourhood on the point's quad grid (run_taa_mode's table, poc_gpu.cu:1192-1203) is
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
                                             float* __restrict__ H2, float* __restrict__ mu_out, float* __restrict__ sg_out,
                                             int* __restrict__ react, int Np, float alpha, float alpha_r, float gamma,
                                             const float* __restrict__ ref, const uint8_t* __restrict__ valid, double* __restrict__ part) {
-    __shared__ double sh[B / 32];
+    __shared__ float2 sh[B / 32];
     const int i = blockIdx.x * B + threadIdx.x;
     float2 d2 = make_float2(0.f, 0.f);
     if (i < Np) {
@@ -151,15 +152,24 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
         if (q >= 0) {
             const int4 g = quad[q];   // first point, nu, nv
             const int r = i - g.x, iu = r % g.y, iv = r / g.y;
-            for (int dv = -1; dv <= 1; ++dv)
-                for (int du = -1; du <= 1; ++du) {
-                    const int a = iu + du, b = iv + dv;
-                    if (a < 0 || a >= g.y || b < 0 || b >= g.z) continue;
-                    const float v = x[g.x + b * g.y + a];
-                    s1 += v;
-                    s2 += v * v;
-                    n++;
-                }
+            // the nine loads are issued together: a neighbour outside the grid reads the point
+            // itself and adds an exact +0 (samples are >= 0, so the sums never hold -0), which
+            // leaves the sums of the in-grid neighbours in the table's order unchanged
+            float v[9];
+            bool ok[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const int a = iu + k % 3 - 1, b = iv + k / 3 - 1;
+                ok[k] = a >= 0 && a < g.y && b >= 0 && b < g.z;
+                v[k] = x[ok[k] ? g.x + b * g.y + a : i];
+            }
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float vv = ok[k] ? v[k] : 0.f;
+                s1 += vv;
+                s2 += vv * vv;
+                n += ok[k] ? 1 : 0;
+            }
         }
         const float mu = s1 / n;
         const float sg = sqrtf(fmaxf(s2 / n - mu * mu, 0.f));
@@ -190,12 +200,12 @@ __global__ void __launch_bounds__(B) k_post(const float* __restrict__ x, const i
     for (int o = 16; o > 0; o >>= 1)
         d2 = df_add(d2, make_float2(__shfl_xor_sync(0xffffffffu, d2.x, o), __shfl_xor_sync(0xffffffffu, d2.y, o)));
     const int warp = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) sh[warp] = (double)d2.x + (double)d2.y;
+    if ((threadIdx.x & 31) == 0) sh[warp] = d2;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < B / 32; ++w) t += sh[w];
-        part[3 * (size_t)blockIdx.x] = t;
+        float2 t = sh[0];
+        for (int w = 1; w < B / 32; ++w) t = df_add(t, sh[w]);
+        part[3 * (size_t)blockIdx.x] = (double)t.x + (double)t.y;
     }
 }
 
