@@ -106,6 +106,36 @@ VERTEX_DTYPE = np.dtype([("origin", "<f4", 3), ("dir", "<f4", 3), ("hit", "<f4",
                          ("light_dist", "<f4"), ("light_index", "<i4"), ("entry", "<u4"), ("flags", "<u4")])
 
 
+def dda_voxels(a, b, lo=(0.0, 0.0, 0.0), ext=(8.0, 4.0, 3.0), dims=(8, 4, 4)) -> list[int]:
+    """Voxels of the dependency walk of segment a -> b (poc_gpu.cu:171-190), in order, in float32
+    with every operation rounded on its own (numpy float32 scalars): the reference's sequence
+    as written, against which a GPU walk is checked bit for bit.  Small cases only (pure
+    Python)."""
+    f = np.float32
+    V = [int(x) for x in dims]
+    sc = [f(V[k]) / f(ext[k]) for k in range(3)]
+    A = [(f(a[k]) - f(lo[k])) * sc[k] for k in range(3)]
+    B = [(f(b[k]) - f(lo[k])) * sc[k] for k in range(3)]
+    i = [min(max(int(A[k]), 0), V[k] - 1) for k in range(3)]
+    e = [min(max(int(B[k]), 0), V[k] - 1) for k in range(3)]
+    d = [B[k] - A[k] for k in range(3)]
+    st = [1 if d[k] > 0 else -1 for k in range(3)]
+    with np.errstate(over="ignore", divide="ignore"):
+        td = [abs(f(1) / d[k]) if d[k] != 0 else f(1e30) for k in range(3)]
+        tm = [((f(i[k] + 1) - A[k]) if d[k] > 0 else (A[k] - f(i[k]))) * td[k] if d[k] != 0 else f(1e30) for k in range(3)]
+    out = []
+    for _ in range(sum(V)):
+        out.append((i[2] * V[1] + i[1]) * V[0] + i[0])
+        if i == e:
+            break
+        ax = 0 if (tm[0] < tm[1] and tm[0] < tm[2]) else (1 if tm[1] < tm[2] else 2)
+        i[ax] += st[ax]
+        tm[ax] = f(tm[ax] + td[ax])
+        if i[ax] < 0 or i[ax] >= V[ax]:
+            break
+    return out
+
+
 class _PathParams(ctypes.Structure):
     _fields_ = [("eye", ctypes.c_float * 3), ("fwd", ctypes.c_float * 3), ("right", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
                 ("tx", ctypes.c_float), ("ty", ctypes.c_float), ("w", ctypes.c_int), ("h", ctypes.c_int), ("bounces", ctypes.c_int),

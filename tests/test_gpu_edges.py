@@ -69,3 +69,37 @@ def test_fine_transit_grid():
     info = _compare(data, "v3 complet", grid=(16, 8, 6))
     assert info["nw"] == 24
     _compare(data, "v3 complet", grid=(16, 8, 6), frames=[0] * 12, mask_check=True)
+
+
+@pytest.mark.parametrize("points", [40, 300])
+def test_dependency_masks_replay_probe_records(points):
+    """Frame 0 of a method tracked every frame writes, per point, the OR of its rays' shadow-voxel
+    masks (at the hit point, or the point's own for a ray that does not count) and of the walks
+    O -> H.  Replayed on the CPU from the rc_probe_rays records (direction, end point) with the
+    float restatement of the walk, it equals the GPU's mask bit for bit, on rooms whose cache
+    points lie on voxel faces (ties at voxel edges included)."""
+    data = S.write(S.box_room(points=points, seed=5))
+    ctx = N.Context()
+    info = ctx.load_bytes(data)
+    Np, NW = info["np"], info["nw"]
+    m = M.by_name(M.timing_methods(), "v3 complet")
+    ctx.begin(m, 0, 13)
+    recs = ctx.probe_full(0, list(range(Np)))
+    ctx.frame(0)
+    cur = ctx.array(N.A_CUR).reshape(NW, Np)
+    sv = ctx.state_array(0, N.SA_SV).reshape(Np, NW)
+    st = S.read(data).states[0]
+    eps = np.float64(np.float32(1e-3))
+    by_point = {}
+    for r in recs:
+        by_point.setdefault(r["point"], []).append(r)
+    for i in range(Np):
+        want = np.zeros(NW, np.uint32)
+        rays = by_point.get(i, [])
+        # O = P + N * 1e-3 as one fused multiply-add: exact product and sum in double, one rounding
+        O = (st.P[i].astype(np.float64) + st.N[i].astype(np.float64) * eps).astype(np.float32)
+        for r in rays:
+            want |= sv[i if r["back"] else r["pi"]]
+            for v in po.dda_voxels(O, r["hit"]):
+                want[v >> 5] |= np.uint32(1 << (v & 31))
+        np.testing.assert_array_equal(cur[:, i], want, err_msg="point %d, %d rays" % (i, len(rays)))

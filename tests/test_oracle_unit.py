@@ -119,3 +119,13 @@ def test_street_scene_runs_in_oracle():
     assert np.isfinite(lc).all() and lc.max() > 0
     recs = run.probe(0, list(range(0, o.Np, 11)))
     assert any(r[2] <= -2 for r in recs)   # static (BVH) hits resolved through the hash table
+
+
+def test_walk_restatement_breaks_edge_ties_like_the_reference():
+    """A walk starting exactly on a voxel edge (x = 5, z = 2.25 -> grid z 3.0 with sz = 4/3)
+    going -x and -z: both crossing distances are 0 and the reference's if / else-if chain steps
+    z first (voxel 101 -> 69), which needs the grid coordinate rounded before the voxel index
+    is subtracted from it."""
+    v = po.dda_voxels((5.0, 0.001, 2.25), (3.5884497, 3.9999998, 1.8764427))
+    assert v[:2] == [101, 69]
+    assert po.dda_voxels((1.0, 0.5, 0.375), (1.0, 0.5, 0.375)) == [1]   # a point: its own voxel
