@@ -486,7 +486,8 @@ __device__ __forceinline__ int ray_count(const FrameParams& p, const DevCache& c
 
 // ------------------------------------------------------------------ state build
 // poc_gpu.cu:369-391: per point and light, a shadow ray gives the direct light; 20 samples
-// along each shadow segment give the static voxel mask.
+// along each shadow segment give the static voxel mask (skipped when SV is null: the direct
+// light alone).
 template <int NL, int NW>
 __global__ void __launch_bounds__(BLOCK) k_build(const DState s, const DStatic g, const Grid grid, const float* __restrict__ L,
                                                  const float* __restrict__ inten, float4* __restrict__ AE,
@@ -519,13 +520,17 @@ __global__ void __launch_bounds__(BLOCK) k_build(const DState s, const DStatic g
         bool vis = t >= r - 1e-3f;
         float rr = fmaxf(r, 0.05f);
         rec[1 + l] = inten[l] * fmaxf(cc, 0.f) / (rr * rr) * (vis ? 1.f : 0.f);
-        f3 a = O, b = O + D * fminf(t, r);
-        for (int k = 0; k < 20; ++k) set_bit<NW>(m, vox_of(grid, a + (b - a) * (k / 19.f)));
+        if (SV != nullptr) {
+            f3 a = O, b = O + D * fminf(t, r);
+            for (int k = 0; k < 20; ++k) set_bit<NW>(m, vox_of(grid, a + (b - a) * (k / 19.f)));
+        }
     }
 #pragma unroll
     for (int k = 0; k < AES / 4; ++k) AE[(size_t)i * (AES / 4) + k] = make_float4(rec[4 * k], rec[4 * k + 1], rec[4 * k + 2], rec[4 * k + 3]);
+    if (SV != nullptr) {
 #pragma unroll
-    for (int w = 0; w < NW; ++w) SV[(size_t)NW * i + w] = m[w];
+        for (int w = 0; w < NW; ++w) SV[(size_t)NW * i + w] = m[w];
+    }
 }
 
 // ------------------------------------------------------------------ frame kernel

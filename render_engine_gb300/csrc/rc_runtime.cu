@@ -127,7 +127,7 @@ struct rc_ctx {
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
     int adj_cap_np = 0, adj_cap_k = 0, adj_cap_nl = 0;   // sizes the adjoint buffers were allocated for
     float4* adj_aeu = nullptr;                  // unit-emission direct light of the last adjoint
-    uint32_t* adj_svu = nullptr;
+    int adj_aeu_state = -1;                     // the state adj_aeu holds (-1: none)
     const float* adj_ones = nullptr;
     rc::adj::Bufs adj{};
     Scene S;
@@ -1741,7 +1741,6 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
         auto& pool = ctx->adj_bufs;
         b = adj::Bufs{};
         float4* AEu = nullptr;
-        uint32_t* SVu = nullptr;
         const float* ones = nullptr;
         if ((s = dalloc(ctx, pool, &b.hits, Np * K)) || (s = dalloc(ctx, pool, &b.cnt, Np + 1)) || (s = dalloc(ctx, pool, &b.off, Np + 1)) ||
             (s = dalloc(ctx, pool, &b.fill, Np)) || (s = dalloc(ctx, pool, &b.src, Np * K)) || (s = dalloc(ctx, pool, &b.unordered, Np * K)) ||
@@ -1750,31 +1749,36 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
             (s = dalloc(ctx, pool, &b.g[1], Np)) || (s = dalloc(ctx, pool, &b.u[0], Np)) ||
             (s = dalloc(ctx, pool, &b.u[1], Np)) || (s = dalloc(ctx, pool, &b.w, Np)) ||
             (s = dalloc(ctx, pool, &b.part, (size_t)adj::GRAD_BLOCKS * (NL + 1))) || (s = dalloc(ctx, pool, &b.stats, 1)) ||
-            (s = dalloc(ctx, pool, &AEu, (size_t)AES / 4 * Np)) || (s = dalloc(ctx, pool, &SVu, (size_t)ctx->NW * Np)) ||
-            (s = dput(ctx, pool, &ones, std::vector<float>((size_t)NL, 1.f))))
+            (s = dalloc(ctx, pool, &AEu, (size_t)AES / 4 * Np)) || (s = dput(ctx, pool, &ones, std::vector<float>((size_t)NL, 1.f))))
             return s;
         ctx->adj_aeu = AEu;
-        ctx->adj_svu = SVu;
+        ctx->adj_aeu_state = -1;
         ctx->adj_ones = ones;
         ctx->adj_cap_np = S.Np;
         ctx->adj_cap_k = prm->K;
         ctx->adj_cap_nl = NL;
     }
     float4* AEu = ctx->adj_aeu;
-    uint32_t* SVu = ctx->adj_svu;
     const float* ones = ctx->adj_ones;
     const DState& d = S.st[prm->state].d;
     FrameParams p{};
     p.Np = S.Np;
     CKR(cudaMemcpyAsync(b.w, weights, Np * 4, cudaMemcpyHostToDevice, st));
     CKR(RC_DISPATCH(NL, frozen_hits(d, S.g, S.grid, ctx->c, p, prm->seed, prm->K, b.hits, st)));
-    CKR(RC_DISPATCH(NL, build(ctx->NW, d, S.g, S.grid, S.L, ones, AEu, SVu, S.Np, ctx->flags_dev, st)));
+    int launched = 0;
+    if (ctx->adj_aeu_state != prm->state) {
+        // G_l, the direct light of every light at unit emission, depends only on the state's
+        // geometry and the light positions: built once per state (no voxel masks)
+        CKR(RC_DISPATCH(NL, build(ctx->NW, d, S.g, S.grid, S.L, ones, AEu, nullptr, S.Np, ctx->flags_dev, st)));
+        ctx->adj_aeu_state = prm->state;
+        launched = 1;
+    }
     CKR(adj::build_transpose(b, S.Np, prm->K, st));
     CKR(adj::solve(&b, S.Np, prm->K, NL, AES, reinterpret_cast<const float*>(d.AE), reinterpret_cast<const float*>(AEu), iters, st));
     adj::Stats hs{};
     CKR(cudaMemcpyAsync(&hs, b.stats, sizeof hs, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
-    ctx->launches += 10 + 2 * iters;
+    ctx->launches += 9 + launched + 2 * iters;
     const std::vector<float>& E = S.st[prm->state].inten;
     double jg = 0.0;
     for (int l = 0; l < NL; ++l) {

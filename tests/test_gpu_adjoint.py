@@ -109,3 +109,25 @@ def test_gpu_references_agree_with_the_path_tracer(scene_main_bytes):
         assert abs((m - r).mean()) / r.mean() < 0.02, si
         assert (z * z).mean() < 1.5 and np.abs(z).max() < 4.5, si
     ctx.close()
+
+
+def test_adjoint_unit_build_kept_per_state(scene_main_bytes):
+    """The context keeps the unit-emission direct light of the last state it built: calls that
+    alternate states give, bit for bit, what fresh contexts give."""
+    n = S.read(scene_main_bytes).states[0].P.shape[0]
+    w = _weights(n, 256, 11)
+
+    def fresh(state):
+        c = N.Context()
+        c.load_bytes(scene_main_bytes)
+        g, _ = c.adjoint(state, w, K=8, seed=3, iterations=32)
+        c.close()
+        return g
+
+    want = {s: fresh(s) for s in (0, 2)}
+    ctx = N.Context()
+    ctx.load_bytes(scene_main_bytes)
+    for s in (0, 2, 2, 0):
+        g, _ = ctx.adjoint(s, w, K=8, seed=3, iterations=32)
+        assert np.array_equal(g, want[s]), s
+    ctx.close()
