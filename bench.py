@@ -48,11 +48,12 @@ def parse():
     ap.add_argument("--method", default=METHOD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=12)
-    ap.add_argument("--profile", choices=["frame", "hashgrid", "mlp", "adjoint", "taa", "paths"], default=None,
+    ap.add_argument("--profile", choices=["frame", "street", "hashgrid", "mlp", "adjoint", "taa", "paths"], default=None,
                     help="no timing: run --steps frames of state 0 (frame), three resolve passes of the "
                          "hash-grid table (hashgrid), two inference and training passes of the MLP (mlp) or "
                          "one 16-sweep adjoint of a 16-light room of --points points (adjoint), --steps "
-                         "frames of the taa mode (taa) or --steps 1080p camera-path passes (paths), for an ncu "
+                         "frames of the taa mode (taa), --steps 1080p camera-path passes (paths) or --steps "
+                         "frames of state 0 of the format-3 street of --points points (street), for an ncu "
                          "capture, and exit")
     return ap.parse_args()
 
@@ -66,6 +67,15 @@ def profile_run(args):
     if args.profile == "frame":
         ctx = N.Context()
         ctx.load_bytes(S.write(S.box_room(points=args.points, seed=0)))
+        ctx.begin(M.by_name(M.timing_methods(), args.method), 0, 11)
+        for _ in range(args.steps):
+            ctx.frame(0)
+        ctx.sync()
+        ctx.close()
+        return
+    if args.profile == "street":
+        ctx = N.Context()
+        ctx.load_bytes(S.write(street_scene(args.points)))
         ctx.begin(M.by_name(M.timing_methods(), args.method), 0, 11)
         for _ in range(args.steps):
             ctx.frame(0)
@@ -111,6 +121,13 @@ def profile_run(args):
         hg.resolve()
     torch.cuda.synchronize()
     hg.close()
+
+
+def street_scene(points: int):
+    """Format-3 street: ground, 40 buildings with facades subdivided into 0.58 m cells
+    (about 200 k triangles, median-split tree), three lamp-post lights, the movable cube."""
+    from render_engine_gb300 import scene as S
+    return S.street_scene(points=points, buildings=40, facade_cell=0.58, size=200.0)
 
 
 def sequence(n: int, ns: int = 5) -> list[int]:

@@ -59,6 +59,10 @@ typedef struct rc_config {
 
 #define RC_FLAG_BRUTE_FORCE 1u  /* test every dynamic triangle (no plane culling) */
 #define RC_FLAG_CHECK_TRACE 2u  /* trace both ways and count disagreements (slow; tests) */
+#define RC_FLAG_WATERTIGHT 4u   /* static-mesh triangles by the watertight test (Woop, Benthin,
+                                   Wald 2013) instead of the reference's Moller-Trumbore
+                                   (poc_gpu.cu:318-331): no ray leaks between triangles that
+                                   share an edge; hits differ from the reference's at edges */
 
 /* Reference Method (poc_gpu.cu:803-805) plus the BENCH_RAYONS multiplier (poc_gpu.cu:69). */
 typedef struct rc_method {
@@ -190,6 +194,13 @@ rc_status rc_state_array_copy(rc_ctx* ctx, int state, int which, void* host, siz
  * the run, and return one record per ray. */
 rc_status rc_probe_rays(rc_ctx* ctx, int state, const int* points, int npoints,
                         rc_ray_rec* out, int maxrec, int* nrec);
+/* Closest hit of caller-given rays against the geometry of state `state`: its dynamic
+ * triangles first, then the static mesh, as the reference's trace_full (poc_gpu.cu:340-344).
+ * rays: 6 floats per ray in host memory (origin, direction; the direction need not be unit
+ * length).  prim[i] = quad id (>= 0), -2 - j for static triangle j, -1 for no hit; t[i] =
+ * hit distance in units of the direction (+inf when no hit).  Follows the context's
+ * RC_FLAG_WATERTIGHT and RC_FLAG_BRUTE_FORCE.  Synchronous; needs a scene, not a run. */
+rc_status rc_trace_rays(rc_ctx* ctx, int state, const float* rays, int nrays, int* prim, float* t);
 /* Disagreements counted by RC_FLAG_CHECK_TRACE since the last call (then reset). */
 rc_status rc_trace_check_count(rc_ctx* ctx, long long* mismatches, long long* rays);
 /* Run counters (synchronises to read the ray count). */

@@ -91,6 +91,9 @@ def lib():
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.osc_frozen_hits.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p]
         L.osc_direct_unit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.osc_trace_rays.restype = ctypes.c_int
+        L.osc_trace_rays.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.c_void_p]
         L.osc_path_trace.restype = ctypes.c_int
         L.osc_path_trace.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
@@ -215,6 +218,16 @@ class Scene:
         out = np.empty((self.Np, K), np.int32)
         lib().osc_frozen_hits(self.p, state, seed & 0xFFFFFFFF, K, out.ctypes.data)
         return out
+
+    def trace_rays(self, state: int, rays, watertight: bool = False):
+        """Closest hit of (n, 6) rays (origin, direction) in state `state`: (prim, t) as
+        rc_trace_rays returns them (prim -2 - j for static triangle j, t = +inf when no hit)."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        prim = np.empty(len(r), np.int32)
+        t = np.empty(len(r), np.float32)
+        if lib().osc_trace_rays(self.p, state, r.ctypes.data, len(r), 1 if watertight else 0, prim.ctypes.data, t.ctypes.data):
+            raise ValueError("state out of range")
+        return prim, t
 
     def direct_unit(self, state: int) -> np.ndarray:
         """(Np, NL) direct light of each light at unit emission (FP32)."""

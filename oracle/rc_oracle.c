@@ -325,17 +325,61 @@ static int trace_dyn(v3 o, v3 d, const float* T, const int* TQ, int nt, float* t
     }
     return *q >= 0;
 }
-/* poc_gpu.cu:288-295 */
-static inline float aabb_enter(const float* a, const float* b, v3 o, v3 inv, float tmax) {
+/* poc_gpu.cu:288-295; fs scales the exit distance (1 = the reference; the watertight mode
+ * uses 1 + 4 ulp, Ize's conservative slab test, JCGT 2(2), 2013) */
+static inline float aabb_enter(const float* a, const float* b, v3 o, v3 inv, float tmax, float fs) {
     float tx1 = (a[0] - o.x) * inv.x, tx2 = (b[0] - o.x) * inv.x;
     float ty1 = (a[1] - o.y) * inv.y, ty2 = (b[1] - o.y) * inv.y;
     float tz1 = (a[2] - o.z) * inv.z, tz2 = (b[2] - o.z) * inv.z;
     float tn = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fmaxf(fminf(tz1, tz2), 0.f));
     float tf = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fminf(fmaxf(tz1, tz2), tmax));
-    return tn <= tf ? tn : 1e30f;
+    return tn <= tf * fs ? tn : 1e30f;
 }
-/* poc_gpu.cu:297-338 stack BVH traversal over the static mesh; q = -2 - triangle */
-static void trace_bvh(const osc_scene* s, v3 o, v3 d, float* tmin, int* q) {
+/* Watertight ray/triangle test (Woop, Benthin and Wald, JCGT 2(1), 2013), the
+ * RC_FLAG_WATERTIGHT alternative of the GPU traversal: permute the ray's largest direction
+ * component to z, shear the triangle into the ray frame, 2-D edge functions U, V, W (each
+ * product and difference rounded on its own: this file is built without contraction), all
+ * three recomputed in double when one is exactly zero; hit when they share a sign; t = T / det.
+ * Vertices: v0, v0 + e1, v0 + e2.  Returns the hit distance or +inf. */
+typedef struct { int kx, ky, kz; float sx, sy, sz; } wt_ray_t;
+static inline float sel3(v3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+static wt_ray_t wt_ray(v3 d) {
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    wt_ray_t r;
+    r.kz = ax >= ay ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
+    r.kx = r.kz == 2 ? 0 : r.kz + 1;
+    r.ky = r.kx == 2 ? 0 : r.kx + 1;
+    float dz = sel3(d, r.kz);
+    if (dz < 0.f) { int x = r.kx; r.kx = r.ky; r.ky = x; }
+    r.sx = sel3(d, r.kx) / dz;
+    r.sy = sel3(d, r.ky) / dz;
+    r.sz = 1.f / dz;
+    return r;
+}
+static inline float edge64(float ax, float by, float ay, float bx) { return (float)((double)ax * (double)by - (double)ay * (double)bx); }
+static float wt_tri(const wt_ray_t* r, v3 o, v3 v0, v3 e1, v3 e2) {
+    v3 A = vsub(v0, o), B = vsub(vadd(v0, e1), o), C = vsub(vadd(v0, e2), o);
+    float az = sel3(A, r->kz), bz = sel3(B, r->kz), cz = sel3(C, r->kz);
+    float Ax = sel3(A, r->kx) - r->sx * az, Ay = sel3(A, r->ky) - r->sy * az;
+    float Bx = sel3(B, r->kx) - r->sx * bz, By = sel3(B, r->ky) - r->sy * bz;
+    float Cx = sel3(C, r->kx) - r->sx * cz, Cy = sel3(C, r->ky) - r->sy * cz;
+    float U = Cx * By - Cy * Bx, Vv = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.f || Vv == 0.f || W == 0.f) {
+        U = edge64(Cx, By, Cy, Bx);
+        Vv = edge64(Ax, Cy, Ay, Cx);
+        W = edge64(Bx, Ay, By, Ax);
+    }
+    if ((U < 0.f || Vv < 0.f || W < 0.f) && (U > 0.f || Vv > 0.f || W > 0.f)) return INFINITY;
+    float det = (U + Vv) + W;
+    if (det == 0.f) return INFINITY;
+    float T = (U * (r->sz * az) + Vv * (r->sz * bz)) + W * (r->sz * cz);
+    return T / det;
+}
+/* poc_gpu.cu:297-338 stack BVH traversal over the static mesh; q = -2 - triangle.  With
+ * watertight set, leaves use wt_tri instead of the reference's Moller-Trumbore. */
+static void trace_bvh_m(const osc_scene* s, v3 o, v3 d, float* tmin, int* q, int watertight);
+static void trace_bvh(const osc_scene* s, v3 o, v3 d, float* tmin, int* q) { trace_bvh_m(s, o, d, tmin, q, 0); }
+static void trace_bvh_m(const osc_scene* s, v3 o, v3 d, float* tmin, int* q, int watertight) {
     v3 inv = V(fabsf(d.x) > 1e-12f ? 1.f / d.x : copysignf(1e30f, d.x),
                fabsf(d.y) > 1e-12f ? 1.f / d.y : copysignf(1e30f, d.y),
                fabsf(d.z) > 1e-12f ? 1.f / d.z : copysignf(1e30f, d.z));
@@ -344,7 +388,14 @@ static void trace_bvh(const osc_scene* s, v3 o, v3 d, float* tmin, int* q) {
         const float* a = s->BN + 8 * (size_t)node;
         const float* b = a + 4;
         int lf = f2i(a[3]), cnt = f2i(b[3]);
-        if (cnt > 0) {
+        if (cnt > 0 && watertight) {
+            wt_ray_t wr = wt_ray(d);
+            for (int j = lf; j < lf + cnt; ++j) {
+                const float* T = s->ST + 9 * (size_t)j;
+                float t = wt_tri(&wr, o, V(T[0], T[1], T[2]), V(T[3], T[4], T[5]), V(T[6], T[7], T[8]));
+                if (t > 1e-4f && t < *tmin) { *tmin = t; *q = -2 - j; }
+            }
+        } else if (cnt > 0) {
             for (int j = lf; j < lf + cnt; ++j) {
                 const float* T = s->ST + 9 * (size_t)j;
                 v3 v0 = V(T[0], T[1], T[2]), e1 = V(T[3], T[4], T[5]), e2 = V(T[6], T[7], T[8]);
@@ -363,7 +414,8 @@ static void trace_bvh(const osc_scene* s, v3 o, v3 d, float* tmin, int* q) {
             }
         } else {
             const float* la = s->BN + 8 * (size_t)lf;
-            float tl = aabb_enter(la, la + 4, o, inv, *tmin), tr = aabb_enter(la + 8, la + 12, o, inv, *tmin);
+            const float fs = watertight ? 1.00000048f : 1.f;
+            float tl = aabb_enter(la, la + 4, o, inv, *tmin, fs), tr = aabb_enter(la + 8, la + 12, o, inv, *tmin, fs);
             int first = lf, second = lf + 1;
             if (tr < tl) { float x = tl; tl = tr; tr = x; first = lf + 1; second = lf; }
             if (tl < 1e30f) {
@@ -381,6 +433,24 @@ static int trace_full(const osc_scene* s, const ostate* st, v3 o, v3 d, float* t
     int h = trace_dyn(o, d, st->T, st->TQ, s->Nt, t, q);
     if (s->BN) { trace_bvh(s, o, d, t, q); h = *q != -1; }
     return h;
+}
+/* Caller-given rays (origin, direction) through trace_full of state si; prim = quad id,
+ * -2 - static triangle, or -1; t = +inf when no hit (rc_trace_rays of the library). */
+int osc_trace_rays(const osc_scene* s, int si, const float* rays, int n, int watertight, int* prim, float* t) {
+    if (si < 0 || si >= s->NS) return -1;
+    const ostate* st = &s->st[si];
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < n; ++i) {
+        const float* r = rays + 6 * (size_t)i;
+        v3 o = V(r[0], r[1], r[2]), d = V(r[3], r[4], r[5]);
+        float tt;
+        int q;
+        trace_dyn(o, d, st->T, st->TQ, s->Nt, &tt, &q);
+        if (s->BN) trace_bvh_m(s, o, d, &tt, &q, watertight);
+        prim[i] = q;
+        t[i] = q != -1 ? tt : INFINITY;
+    }
+    return 0;
 }
 /* poc_gpu.cu:239-246 */
 static int point_index(const ostate* st, v3 H, int q) {

@@ -74,6 +74,11 @@ void osc_set_threads(int n);
 typedef struct { int point, ray, q, pi, back; float t; } osc_ray_rec;
 int osc_probe_rays(osc_run* r, int si, const int* pts, int npts, osc_ray_rec* out, int maxrec);
 
+/* Closest hit of caller-given rays (6 floats each: origin, direction) against state si:
+ * dynamic triangles, then the static mesh (Moller-Trumbore as the reference, or the watertight
+ * test when watertight != 0).  prim = quad id, -2 - static triangle or -1; t = +inf when none. */
+int osc_trace_rays(const osc_scene* s, int si, const float* rays, int n, int watertight, int* prim, float* t);
+
 /* Image pass (pinhole camera, one ray per pixel), see rc_render in include/rc_api.h. */
 int osc_render(osc_run* r, int si, const float* eye, const float* fwd, const float* right, const float* up, float tx, float ty,
                int w, int h, float* out);

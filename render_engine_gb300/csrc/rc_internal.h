@@ -41,6 +41,7 @@ struct DStatic {
     int has_bvh;
     int nnodes;
     int max_visits;            // traversal guard (4 x nodes)
+    int watertight;            // static triangles by the watertight test (RC_FLAG_WATERTIGHT)
 };
 
 struct DevCache {
@@ -186,6 +187,11 @@ struct Ops {
 // static mesh of g): out[3 i] = closest hit, out[3 i + 1] = fraction of hits closer than diag,
 // out[3 i + 2] = fraction of single-sided back faces.
 cudaError_t probe_free_space(const DStatic& g, const float* C, int nc, float diag, float* out, unsigned* flags, cudaStream_t st);
+// Closest hit of n caller-given rays (6 floats each: origin, direction) against state s's
+// dynamic triangles and g's static mesh: prim = quad id, -2 - static triangle or -1; t = hit
+// distance (+inf when none).
+cudaError_t trace_rays(const DState& s, const DStatic& g, int brute, const float* rays, int n, int* prim, float* t,
+                       unsigned* flags, cudaStream_t st);
 
 // Light counts and mask widths with compiled kernels.
 #define RC_NL_VALUES(X) X(1) X(2) X(3) X(4) X(8) X(16) X(32)

@@ -309,28 +309,108 @@ __device__ __forceinline__ void trace_dyn(const TraceSmem& sm, const DState& s, 
     else trace_groups<unsigned long long>(sm, s, o, d, tmin, q, jb);
 }
 
-// poc_gpu.cu:288-295
-__device__ __forceinline__ float aabb_enter(float4 a, float4 b, f3 o, f3 inv, float tmax) {
+// poc_gpu.cu:288-295.  fs scales the exit distance: 1 reproduces the reference exactly (a
+// product by 1 is exact); the watertight mode passes 1 + 4 ulp, which covers the rounding of
+// the slab distances (Ize, "Robust BVH Ray Traversal", JCGT 2(2), 2013: 1 + 2 gamma_3), so a
+// ray through a box's edge or corner is not culled by every box that touches it.
+__device__ __forceinline__ float aabb_enter(float4 a, float4 b, f3 o, f3 inv, float tmax, float fs = 1.f) {
     float tx1 = (a.x - o.x) * inv.x, tx2 = (b.x - o.x) * inv.x;
     float ty1 = (a.y - o.y) * inv.y, ty2 = (b.y - o.y) * inv.y;
     float tz1 = (a.z - o.z) * inv.z, tz2 = (b.z - o.z) * inv.z;
     float tn = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fmaxf(fminf(tz1, tz2), 0.f));
     float tf = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fminf(fmaxf(tz1, tz2), tmax));
-    return tn <= tf ? tn : 1e30f;
+    return tn <= tf * fs ? tn : 1e30f;
 }
+// ------------------------------------------------------------------ watertight test
+// Watertight ray/triangle test (Woop, Benthin and Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2(1), 2013), the RC_FLAG_WATERTIGHT alternative to the reference's
+// Moller-Trumbore for the static mesh.  The ray frame is permuted so that the ray's largest
+// direction component becomes z and sheared so that the ray runs along +z from the origin;
+// the triangle's three 2-D edge functions U, V, W are then evaluated with every product and
+// difference rounded on its own, so the triangle on the other side of a shared edge gets the
+// same value negated, and all three are recomputed in FP64 (exact products, one rounding) when
+// one of them is exactly zero.  A hit needs U, V, W of one sign (either side faces the ray).
+// The vertices are those of the stored triangle: v0, v0 + e1, v0 + e2.
+struct WtRay {
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+__device__ __forceinline__ float sel3(f3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+__device__ __forceinline__ WtRay wt_ray(f3 d) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    WtRay r;
+    r.kz = ax >= ay ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
+    r.kx = r.kz == 2 ? 0 : r.kz + 1;
+    r.ky = r.kx == 2 ? 0 : r.kx + 1;
+    const float dz = sel3(d, r.kz);
+    if (dz < 0.f) { const int x = r.kx; r.kx = r.ky; r.ky = x; }   // keep the winding
+    r.sx = __fdiv_rn(sel3(d, r.kx), dz);
+    r.sy = __fdiv_rn(sel3(d, r.ky), dz);
+    r.sz = __fdiv_rn(1.f, dz);
+    return r;
+}
+__device__ __forceinline__ f3 sub_rn(f3 a, f3 b) { return mk(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)); }
+__device__ __forceinline__ f3 add_rn(f3 a, f3 b) { return mk(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)); }
+__device__ __forceinline__ float edge64(float ax, float by, float ay, float bx) {
+    return (float)__dsub_rn(__dmul_rn((double)ax, (double)by), __dmul_rn((double)ay, (double)bx));
+}
+// Hit distance in units of d, or +inf when the ray misses the triangle.
+__device__ __forceinline__ float wt_tri(const WtRay& r, f3 o, f3 v0, f3 e1, f3 e2) {
+    const f3 A = sub_rn(v0, o), B = sub_rn(add_rn(v0, e1), o), C = sub_rn(add_rn(v0, e2), o);
+    const float az = sel3(A, r.kz), bz = sel3(B, r.kz), cz = sel3(C, r.kz);
+    const float Ax = __fsub_rn(sel3(A, r.kx), __fmul_rn(r.sx, az)), Ay = __fsub_rn(sel3(A, r.ky), __fmul_rn(r.sy, az));
+    const float Bx = __fsub_rn(sel3(B, r.kx), __fmul_rn(r.sx, bz)), By = __fsub_rn(sel3(B, r.ky), __fmul_rn(r.sy, bz));
+    const float Cx = __fsub_rn(sel3(C, r.kx), __fmul_rn(r.sx, cz)), Cy = __fsub_rn(sel3(C, r.ky), __fmul_rn(r.sy, cz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        U = edge64(Cx, By, Cy, Bx);
+        V = edge64(Ax, Cy, Ay, Cx);
+        W = edge64(Bx, Ay, By, Ax);
+    }
+    const float inf = __int_as_float(0x7f800000);
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return inf;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.f) return inf;
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, __fmul_rn(r.sz, az)), __fmul_rn(V, __fmul_rn(r.sz, bz))),
+                              __fmul_rn(W, __fmul_rn(r.sz, cz)));
+    return __fdiv_rn(T, det);
+}
+// One leaf of the static mesh by the watertight test (kept out of line so that the default
+// Moller-Trumbore traversal keeps its registers); returns (tmin, q) after the leaf's triangles.
+static __device__ __noinline__ float2 wt_leaf(const float4* __restrict__ ST4, int lf, int cnt, f3 o, f3 d, float tmin, int q) {
+    const WtRay wr = wt_ray(d);
+    for (int j = lf; j < lf + cnt; ++j) {
+        const float4 x = __ldg(ST4 + 3 * (size_t)j), y = __ldg(ST4 + 3 * (size_t)j + 1), z = __ldg(ST4 + 3 * (size_t)j + 2);
+        const float t = wt_tri(wr, o, mk(x.x, x.y, x.z), mk(x.w, y.x, y.y), mk(y.z, y.w, z.x));
+        if (t > 1e-4f && t < tmin) { tmin = t; q = -2 - j; }
+    }
+    return make_float2(tmin, __int_as_float(q));
+}
+
 // Static-mesh traversal, the reference's stack algorithm (poc_gpu.cu:297-338), with a visit
-// guard against malformed node links.
+// guard against malformed node links.  Nodes are visited in the reference's order (nearest
+// child first, far child pushed, same pruning against the running tmin).  A node's link word
+// (first child or first triangle, in a.w) and triangle count (b.w) arrive with its bounds
+// when its parent tests it, so the stack keeps that pair instead of the node index: a visit
+// then waits on one load (the children's bounds) instead of two in a row (the node, then
+// its children).
 static __device__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int& q, unsigned* flags) {
     f3 inv = mk(fabsf(d.x) > 1e-12f ? 1.f / d.x : copysignf(1e30f, d.x),
                 fabsf(d.y) > 1e-12f ? 1.f / d.y : copysignf(1e30f, d.y),
                 fabsf(d.z) > 1e-12f ? 1.f / d.z : copysignf(1e30f, d.z));
-    int stack[64];
-    int sp = 0, node = 0, visits = 0;
+    int2 stack[64];
+    int sp = 0, visits = 0;
+    int lf = __float_as_int(__ldg(&g.BN[0].w)), cnt = __float_as_int(__ldg(&g.BN[1].w));
+    const float fs = g.watertight ? __int_as_float(0x3f800004) : 1.f;
     while (true) {
         if (++visits > g.max_visits) { atomicOr(flags, (unsigned)FLAG_BVH_VISITS); break; }
-        float4 a = __ldg(g.BN + 2 * node), b = __ldg(g.BN + 2 * node + 1);
-        int lf = __float_as_int(a.w), cnt = __float_as_int(b.w);
-        if (cnt > 0) {
+        if (cnt > 0 && g.watertight) {
+            const float2 r = wt_leaf(g.ST4, lf, cnt, o, d, tmin, q);
+            tmin = r.x;
+            q = __float_as_int(r.y);
+        } else if (cnt > 0) {
             for (int j = lf; j < lf + cnt; ++j) {
                 const float4 x = __ldg(g.ST4 + 3 * (size_t)j), y = __ldg(g.ST4 + 3 * (size_t)j + 1), z = __ldg(g.ST4 + 3 * (size_t)j + 2);
                 f3 v0 = mk(x.x, x.y, x.z);
@@ -352,17 +432,21 @@ static __device__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int&
         } else {
             float4 la = __ldg(g.BN + 2 * lf), lb = __ldg(g.BN + 2 * lf + 1);
             float4 ra = __ldg(g.BN + 2 * lf + 2), rb = __ldg(g.BN + 2 * lf + 3);
-            float tl = aabb_enter(la, lb, o, inv, tmin), tr = aabb_enter(ra, rb, o, inv, tmin);
-            int first = lf, second = lf + 1;
-            if (tr < tl) { float x = tl; tl = tr; tr = x; first = lf + 1; second = lf; }
+            float tl = aabb_enter(la, lb, o, inv, tmin, fs), tr = aabb_enter(ra, rb, o, inv, tmin, fs);
+            int2 first = make_int2(__float_as_int(la.w), __float_as_int(lb.w));
+            int2 second = make_int2(__float_as_int(ra.w), __float_as_int(rb.w));
+            if (tr < tl) { float x = tl; tl = tr; tr = x; int2 y = first; first = second; second = y; }
             if (tl < 1e30f) {
                 if (tr < 1e30f && sp < 64) stack[sp++] = second;
-                node = first;
+                lf = first.x;
+                cnt = first.y;
                 continue;
             }
         }
         if (sp == 0) break;
-        node = stack[--sp];
+        const int2 e = stack[--sp];
+        lf = e.x;
+        cnt = e.y;
     }
 }
 
@@ -1752,6 +1836,35 @@ __global__ void __launch_bounds__(BLOCK) k_free_space(const DStatic g, const flo
 
 cudaError_t probe_free_space(const DStatic& g, const float* C, int nc, float diag, float* out, unsigned* flags, cudaStream_t st) {
     k_free_space<<<(nc + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(g, C, nc, diag, out, flags);
+    return cudaGetLastError();
+}
+
+// Closest hit of caller-given rays against one state's geometry: the dynamic triangles, then
+// the static mesh (trace_full, poc_gpu.cu:340-344).  rays = (origin, direction) per ray.
+__global__ void __launch_bounds__(BLOCK) k_trace_rays(const DState s, const DStatic g, int brute, const float* __restrict__ rays,
+                                                      int n, int* __restrict__ prim, float* __restrict__ tout, unsigned* flags) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= n) return;
+    const float* r = rays + 6 * (size_t)i;
+    const f3 o = mk(r[0], r[1], r[2]), d = mk(r[3], r[4], r[5]);
+    float t;
+    int q, jb;
+    trace_dyn(tsm, s, brute != 0, o, d, t, q, jb);
+    if (g.has_bvh) trace_bvh(g, o, d, t, q, flags);
+    prim[i] = q;
+    tout[i] = q != -1 ? t : __int_as_float(0x7f800000);
+}
+
+cudaError_t trace_rays(const DState& s, const DStatic& g, int brute, const float* rays, int n, int* prim, float* t,
+                       unsigned* flags, cudaStream_t st) {
+    const size_t smem = frame_smem_bytes(s);
+    cudaError_t e = prep_smem(k_trace_rays, smem);
+    if (e != cudaSuccess) return e;
+    k_trace_rays<<<(n + BLOCK - 1) / BLOCK, BLOCK, smem, st>>>(s, g, brute, rays, n, prim, t, flags);
     return cudaGetLastError();
 }
 #endif

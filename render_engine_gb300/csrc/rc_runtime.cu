@@ -519,6 +519,7 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         g.has_bvh = 1;
         g.nnodes = m[1];
         g.max_visits = 4 * m[1] + 64;
+        g.watertight = (ctx->cfg.flags & RC_FLAG_WATERTIGHT) != 0;
     }
     set_grid_scale(S.grid);
     auto L = r.vec<float>(3 * (size_t)NL);
@@ -1590,6 +1591,35 @@ rc_status rc_probe_rays(rc_ctx* ctx, int state, const int* points, int npoints, 
     cudaFree(drec);
     if (e != cudaSuccess) return fail(ctx, RC_ERR_CUDA, "probe: %s", cudaGetErrorString(e));
     *nrec = std::min(n, maxrec);
+    return RC_OK;
+}
+
+rc_status rc_trace_rays(rc_ctx* ctx, int state, const float* rays, int nrays, int* prim, float* t) {
+    if (!ctx || nrays < 0 || (nrays > 0 && (!rays || !prim || !t))) return RC_ERR_ARG;
+    if (!ctx->have_scene) return fail(ctx, RC_ERR_STATE, "no scene loaded");
+    const Scene& S = ctx->S;
+    if (state < 0 || state >= S.NS) return RC_ERR_ARG;
+    if (nrays == 0) return RC_OK;
+    CKR(cudaSetDevice(ctx->cfg.device));
+    std::vector<DevBuf> tmp;
+    struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
+    float* dr = nullptr;
+    float* dt = nullptr;
+    int* dq = nullptr;
+    rc_status s;
+    if ((s = dalloc(ctx, tmp, &dr, 6 * (size_t)nrays)) || (s = dalloc(ctx, tmp, &dq, (size_t)nrays)) ||
+        (s = dalloc(ctx, tmp, &dt, (size_t)nrays)))
+        return s;
+    cudaStream_t st = ctx->stream;
+    unsigned flags = 0;
+    CKR(cudaMemcpyAsync(dr, rays, 24 * (size_t)nrays, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemsetAsync(ctx->flags_dev, 0, 4, st));
+    CKR(trace_rays(S.st[state].d, S.g, (ctx->cfg.flags & RC_FLAG_BRUTE_FORCE) != 0, dr, nrays, dq, dt, ctx->flags_dev, st));
+    CKR(cudaMemcpyAsync(prim, dq, 4 * (size_t)nrays, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(t, dt, 4 * (size_t)nrays, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(&flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    if (flags) return fail(ctx, RC_ERR_DEVICE, "trace: BVH traversal guard tripped (flags %u)", flags);
     return RC_OK;
 }
 

@@ -31,13 +31,14 @@ ARRAY_DTYPE = {A_LC: np.float32, A_LC2: np.float32, A_M: np.float32, A_N: np.flo
 SA_EDIR, SA_SV, SA_REF, SA_VALID, SA_PW = range(5)
 FLAG_BRUTE_FORCE = 1
 FLAG_CHECK_TRACE = 2
+FLAG_WATERTIGHT = 4
 
 # Exported symbols, one per declaration of include/rc_api.h.
 EXPORTS = [
     "rc_abi_version", "rc_status_string", "rc_create", "rc_destroy", "rc_last_error", "rc_device_info_get",
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
     "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
-    "rc_state_array_copy", "rc_probe_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
+    "rc_state_array_copy", "rc_probe_rays", "rc_trace_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
     "rc_error_sums_noalloc", "rc_reference_build", "rc_adjoint", "rc_adjoint_arrays", "rc_taa_begin", "rc_taa_frame",
     "rc_taa_array_copy", "rc_prep_mesh",
 ]
@@ -147,6 +148,8 @@ def load_library():
     L.rc_trace_check_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
     L.rc_run_stats_get.restype = i
     L.rc_run_stats_get.argtypes = [vp, ctypes.POINTER(RunStats)]
+    L.rc_trace_rays.restype = i
+    L.rc_trace_rays.argtypes = [vp, i, vp, i, vp, vp]
     L.rc_device_flags.restype = i
     L.rc_device_flags.argtypes = [vp, ctypes.POINTER(ctypes.c_uint)]
     L.rc_reference_build.restype = i
@@ -348,6 +351,15 @@ class Context:
         n = ctypes.c_int()
         self._chk(self.L.rc_probe_rays(self.h, state, pts, len(points), out, cap, ctypes.byref(n)))
         return sorted((r.point, r.ray, r.q, r.pi, r.back, r.t) for r in out[: n.value])
+
+    def trace_rays(self, state: int, rays):
+        """rc_trace_rays: closest hit of (n, 6) rays (origin, direction) in state `state`;
+        returns (prim, t) with prim -2 - j for static triangle j and t = +inf when no hit."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        prim = np.empty(len(r), np.int32)
+        t = np.empty(len(r), np.float32)
+        self._chk(self.L.rc_trace_rays(self.h, state, r.ctypes.data, len(r), prim.ctypes.data, t.ctypes.data))
+        return prim, t
 
     def probe_full(self, state: int, points) -> list[dict]:
         """rc_probe_rays with every field: also the direction and the end point of each ray."""
