@@ -377,18 +377,6 @@ __device__ __forceinline__ float wt_tri(const WtRay& r, f3 o, f3 v0, f3 e1, f3 e
                               __fmul_rn(W, __fmul_rn(r.sz, cz)));
     return __fdiv_rn(T, det);
 }
-// One leaf of the static mesh by the watertight test (kept out of line so that the default
-// Moller-Trumbore traversal keeps its registers); returns (tmin, q) after the leaf's triangles.
-static __device__ __noinline__ float2 wt_leaf(const float4* __restrict__ ST4, int lf, int cnt, f3 o, f3 d, float tmin, int q) {
-    const WtRay wr = wt_ray(d);
-    for (int j = lf; j < lf + cnt; ++j) {
-        const float4 x = __ldg(ST4 + 3 * (size_t)j), y = __ldg(ST4 + 3 * (size_t)j + 1), z = __ldg(ST4 + 3 * (size_t)j + 2);
-        const float t = wt_tri(wr, o, mk(x.x, x.y, x.z), mk(x.w, y.x, y.y), mk(y.z, y.w, z.x));
-        if (t > 1e-4f && t < tmin) { tmin = t; q = -2 - j; }
-    }
-    return make_float2(tmin, __int_as_float(q));
-}
-
 // Static-mesh traversal, the reference's stack algorithm (poc_gpu.cu:297-338), with a visit
 // guard against malformed node links.  Nodes are visited in the reference's order (nearest
 // child first, far child pushed, same pruning against the running tmin).  A node's link word
@@ -396,23 +384,29 @@ static __device__ __noinline__ float2 wt_leaf(const float4* __restrict__ ST4, in
 // when its parent tests it, so the stack keeps that pair instead of the node index: a visit
 // then waits on one load (the children's bounds) instead of two in a row (the node, then
 // its children).
-static __device__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int& q, unsigned* flags) {
+// WT selects the watertight mode: its triangle test and a slab exit scaled by 1 + 4 ulp.
+template <bool WT>
+__device__ __forceinline__ void trace_bvh_t(const float4* __restrict__ BN, const float4* __restrict__ ST4, int max_visits, f3 o,
+                                            f3 d, float& tmin, int& q, unsigned* flags) {
     f3 inv = mk(fabsf(d.x) > 1e-12f ? 1.f / d.x : copysignf(1e30f, d.x),
                 fabsf(d.y) > 1e-12f ? 1.f / d.y : copysignf(1e30f, d.y),
                 fabsf(d.z) > 1e-12f ? 1.f / d.z : copysignf(1e30f, d.z));
     int2 stack[64];
     int sp = 0, visits = 0;
-    int lf = __float_as_int(__ldg(&g.BN[0].w)), cnt = __float_as_int(__ldg(&g.BN[1].w));
-    const float fs = g.watertight ? __int_as_float(0x3f800004) : 1.f;
+    int lf = __float_as_int(__ldg(&BN[0].w)), cnt = __float_as_int(__ldg(&BN[1].w));
+    const float fs = WT ? __int_as_float(0x3f800004) : 1.f;
     while (true) {
-        if (++visits > g.max_visits) { atomicOr(flags, (unsigned)FLAG_BVH_VISITS); break; }
-        if (cnt > 0 && g.watertight) {
-            const float2 r = wt_leaf(g.ST4, lf, cnt, o, d, tmin, q);
-            tmin = r.x;
-            q = __float_as_int(r.y);
+        if (++visits > max_visits) { atomicOr(flags, (unsigned)FLAG_BVH_VISITS); break; }
+        if (WT && cnt > 0) {
+            const WtRay wr = wt_ray(d);
+            for (int j = lf; j < lf + cnt; ++j) {
+                const float4 x = __ldg(ST4 + 3 * (size_t)j), y = __ldg(ST4 + 3 * (size_t)j + 1), z = __ldg(ST4 + 3 * (size_t)j + 2);
+                const float t = wt_tri(wr, o, mk(x.x, x.y, x.z), mk(x.w, y.x, y.y), mk(y.z, y.w, z.x));
+                if (t > 1e-4f && t < tmin) { tmin = t; q = -2 - j; }
+            }
         } else if (cnt > 0) {
             for (int j = lf; j < lf + cnt; ++j) {
-                const float4 x = __ldg(g.ST4 + 3 * (size_t)j), y = __ldg(g.ST4 + 3 * (size_t)j + 1), z = __ldg(g.ST4 + 3 * (size_t)j + 2);
+                const float4 x = __ldg(ST4 + 3 * (size_t)j), y = __ldg(ST4 + 3 * (size_t)j + 1), z = __ldg(ST4 + 3 * (size_t)j + 2);
                 f3 v0 = mk(x.x, x.y, x.z);
                 f3 e1 = mk(x.w, y.x, y.y);
                 f3 e2 = mk(y.z, y.w, z.x);
@@ -430,8 +424,8 @@ static __device__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int&
                 if (t > 1e-4f && t < tmin) { tmin = t; q = -2 - j; }
             }
         } else {
-            float4 la = __ldg(g.BN + 2 * lf), lb = __ldg(g.BN + 2 * lf + 1);
-            float4 ra = __ldg(g.BN + 2 * lf + 2), rb = __ldg(g.BN + 2 * lf + 3);
+            float4 la = __ldg(BN + 2 * lf), lb = __ldg(BN + 2 * lf + 1);
+            float4 ra = __ldg(BN + 2 * lf + 2), rb = __ldg(BN + 2 * lf + 3);
             float tl = aabb_enter(la, lb, o, inv, tmin, fs), tr = aabb_enter(ra, rb, o, inv, tmin, fs);
             int2 first = make_int2(__float_as_int(la.w), __float_as_int(lb.w));
             int2 second = make_int2(__float_as_int(ra.w), __float_as_int(rb.w));
@@ -447,6 +441,22 @@ static __device__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int&
         const int2 e = stack[--sp];
         lf = e.x;
         cnt = e.y;
+    }
+}
+// The two modes are separate instantiations chosen once per ray, so the default one runs the
+// reference's traversal with no per-node branch or exit factor.
+static __device__ __forceinline__ float2 trace_bvh_wt(const float4* BN, const float4* ST4, int max_visits, f3 o, f3 d, float tmin,
+                                                   int q, unsigned* flags) {
+    trace_bvh_t<true>(BN, ST4, max_visits, o, d, tmin, q, flags);
+    return make_float2(tmin, __int_as_float(q));
+}
+__device__ __forceinline__ void trace_bvh(const DStatic& g, f3 o, f3 d, float& tmin, int& q, unsigned* flags) {
+    if (g.watertight) {
+        const float2 r = trace_bvh_wt(g.BN, g.ST4, g.max_visits, o, d, tmin, q, flags);
+        tmin = r.x;
+        q = __float_as_int(r.y);
+    } else {
+        trace_bvh_t<false>(g.BN, g.ST4, g.max_visits, o, d, tmin, q, flags);
     }
 }
 
