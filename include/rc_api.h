@@ -61,8 +61,13 @@ typedef struct rc_config {
 #define RC_FLAG_CHECK_TRACE 2u  /* trace both ways and count disagreements (slow; tests) */
 #define RC_FLAG_WATERTIGHT 4u   /* static-mesh triangles by the watertight test (Woop, Benthin,
                                    Wald 2013) instead of the reference's Moller-Trumbore
-                                   (poc_gpu.cu:318-331): no ray leaks between triangles that
-                                   share an edge; hits differ from the reference's at edges */
+                                   (poc_gpu.cu:318-331); hits differ from the reference's at
+                                   edges.  Format 3 stores each triangle as v0 and two edge
+                                   vectors, and the test rebuilds v1 = v0 + e1, v2 = v0 + e2 in
+                                   FP32: no ray leaks through an edge when both triangles
+                                   rebuild its endpoints to the same floats (meshes whose
+                                   edge vectors are exact differences, e.g. on a lattice);
+                                   elsewhere a leak through a gap of one rounding is possible */
 
 /* Reference Method (poc_gpu.cu:803-805) plus the BENCH_RAYONS multiplier (poc_gpu.cu:69). */
 typedef struct rc_method {
@@ -314,7 +319,10 @@ rc_status rc_prep_mesh(rc_ctx* ctx, const char* mesh_path, const char* scene_pat
  * stream), asynchronously.  Scratch space is a fixed array in the library (393,224 bytes on
  * every GPU that loads it, held until the process exits), so np may not exceed
  * RC_NOALLOC_MAX_POINTS (RC_ERR_ARG otherwise).  The first call on a device looks up that
- * array's address for the device; make that first call before any stream capture.  Every
+ * array's address for the device and keeps it for the life of the process; make that first
+ * call before any stream capture.  A cudaDeviceReset (or any teardown of the device's primary
+ * context) unloads the array, and the kept address then points at freed memory: do not call
+ * this entry point on a device after resetting it.  Every
  * call uses the same array: calls whose work overlaps on the GPU (on different streams, or
  * from different threads) race and give wrong sums.  Allocates nothing: no cudaMalloc,
  * no cudaFree, no allocating library routine. */

@@ -13,7 +13,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+# the reference checkout: $RC_REFERENCE_DIR, else a directory named "reference" beside this repository
+REFERENCE = os.environ.get("RC_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 CUDA = "/usr/local/cuda"
 
 

@@ -6,10 +6,11 @@
 # with the transit grid of the reference's build script (cuda/build.sh: -DGX=8 -DGY=4
 # -DGZ=4) and its optimisation flags (-O3 -lineinfo -std=c++17).  Only the device code is
 # compiled (the host side of poc_gpu.cu is driven by oracle/refrun.cpp).
-# Usage: oracle/build_ref.sh [reference checkout, default /root/reference]
+# Usage: oracle/build_ref.sh [reference checkout]; default $RC_REFERENCE_DIR, else the
+# directory "reference" beside this repository
 set -e
-REF="${1:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${1:-${RC_REFERENCE_DIR:-$HERE/../../reference}}"
 SRC="$REF/cuda/poc_gpu.cu"
 [ -f "$SRC" ] || { echo "reference source not found: $SRC" >&2; exit 1; }
 mkdir -p "$HERE/_ref"

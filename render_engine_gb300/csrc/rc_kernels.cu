@@ -395,10 +395,11 @@ __device__ __forceinline__ void trace_bvh_t(const float4* __restrict__ BN, const
     int sp = 0, visits = 0;
     int lf = __float_as_int(__ldg(&BN[0].w)), cnt = __float_as_int(__ldg(&BN[1].w));
     const float fs = WT ? __int_as_float(0x3f800004) : 1.f;
+    WtRay wr{};
+    if constexpr (WT) wr = wt_ray(d);    // the ray's frame, once per ray (the direction never changes)
     while (true) {
         if (++visits > max_visits) { atomicOr(flags, (unsigned)FLAG_BVH_VISITS); break; }
         if (WT && cnt > 0) {
-            const WtRay wr = wt_ray(d);
             for (int j = lf; j < lf + cnt; ++j) {
                 const float4 x = __ldg(ST4 + 3 * (size_t)j), y = __ldg(ST4 + 3 * (size_t)j + 1), z = __ldg(ST4 + 3 * (size_t)j + 2);
                 const float t = wt_tri(wr, o, mk(x.x, x.y, x.z), mk(x.w, y.x, y.y), mk(y.z, y.w, z.x));

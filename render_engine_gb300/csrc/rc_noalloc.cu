@@ -98,7 +98,9 @@ __global__ void __launch_bounds__(NA_BLOCK) k_error_noalloc(const float* __restr
     }
 }
 
-// Address of this file's scratch array on the current device, looked up once per device.
+// Address of this file's scratch array on the current device, looked up once per device and kept
+// for the life of the process (a cudaDeviceReset unloads the array and leaves the kept address
+// stale: the entry point is not for use on a device after a reset).
 cudaError_t scratch_for_current_device(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

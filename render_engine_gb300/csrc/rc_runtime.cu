@@ -137,6 +137,8 @@ struct rc_ctx {
     Run run;
     double cache_bytes = 0;
     long long launches = 0;
+    // device guard words: [0] raised by the run's kernels (read and cleared by rc_device_flags),
+    // [1] by one-shot calls that trace (rc_trace_rays, the preparation's probes), [2] the loader's checks
     unsigned* flags_dev = nullptr;
     float* img = nullptr;
     size_t img_cap = 0;
@@ -1613,11 +1615,12 @@ rc_status rc_trace_rays(rc_ctx* ctx, int state, const float* rays, int nrays, in
     cudaStream_t st = ctx->stream;
     unsigned flags = 0;
     CKR(cudaMemcpyAsync(dr, rays, 24 * (size_t)nrays, cudaMemcpyHostToDevice, st));
-    CKR(cudaMemsetAsync(ctx->flags_dev, 0, 4, st));
-    CKR(trace_rays(S.st[state].d, S.g, (ctx->cfg.flags & RC_FLAG_BRUTE_FORCE) != 0, dr, nrays, dq, dt, ctx->flags_dev, st));
+    // word 1 is this call's own guard word: word 0 keeps what the run's frames raised
+    CKR(cudaMemsetAsync(ctx->flags_dev + 1, 0, 4, st));
+    CKR(trace_rays(S.st[state].d, S.g, (ctx->cfg.flags & RC_FLAG_BRUTE_FORCE) != 0, dr, nrays, dq, dt, ctx->flags_dev + 1, st));
     CKR(cudaMemcpyAsync(prim, dq, 4 * (size_t)nrays, cudaMemcpyDeviceToHost, st));
     CKR(cudaMemcpyAsync(t, dt, 4 * (size_t)nrays, cudaMemcpyDeviceToHost, st));
-    CKR(cudaMemcpyAsync(&flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(&flags, ctx->flags_dev + 1, 4, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
     if (flags) return fail(ctx, RC_ERR_DEVICE, "trace: BVH traversal guard tripped (flags %u)", flags);
     return RC_OK;
@@ -2133,12 +2136,12 @@ rc_status ctx_probe_free_space(rc_ctx* ctx, const std::vector<float>& ST, const 
     g.has_bvh = 1;
     g.nnodes = nnodes;
     g.max_visits = 4 * nnodes + 64;
-    CKR(cudaMemsetAsync(ctx->flags_dev, 0, 4, ctx->stream));
-    CKR(probe_free_space(g, dC, (int)(C.size() / 3), diag, dO, ctx->flags_dev, ctx->stream));
+    CKR(cudaMemsetAsync(ctx->flags_dev + 1, 0, 4, ctx->stream));
+    CKR(probe_free_space(g, dC, (int)(C.size() / 3), diag, dO, ctx->flags_dev + 1, ctx->stream));
     out.resize(C.size());
     unsigned flags = 0;
     CKR(cudaMemcpyAsync(out.data(), dO, out.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    CKR(cudaMemcpyAsync(&flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CKR(cudaMemcpyAsync(&flags, ctx->flags_dev + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
     CKR(cudaStreamSynchronize(ctx->stream));
     if (flags) return fail(ctx, RC_ERR_DEVICE, "prep: BVH traversal guard tripped (flags %u)", flags);
     return RC_OK;

@@ -8,7 +8,8 @@ Reads, from the reference (falcon123212/render_engine):
   cuda/scenes/scenarios_stress.txt
 and writes gzip copies of the scenes and the curves as JSON next to this script.
 
-Usage: python tests/golden/make_golden.py [reference checkout, default /root/reference]
+Usage: python tests/golden/make_golden.py [reference checkout]
+(default $RC_REFERENCE_DIR, else the directory "reference" beside this repository)
 """
 import gzip
 import json
@@ -16,8 +17,9 @@ import os
 import shutil
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
+REF = (sys.argv[1] if len(sys.argv) > 1 else
+       os.environ.get("RC_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference"))
 
 
 def curves(path):

@@ -71,3 +71,37 @@ def test_trace_rays_arguments():
     p, t = ctx.trace_rays(0, np.array([[5.0, 5.0, 50.0, 0.0, 0.0, 1.0]], np.float32))
     assert p[0] == -1 and np.isinf(t[0])
     ctx.close()
+
+
+def _dag_tree(lo, hi, depth: int = 14) -> np.ndarray:
+    """A node array in the format-3 layout whose inner nodes share their children: nodes
+    2j+1 and 2j+2 both link to 2j+3 and 2j+4, so a ray that enters the root box visits 2^depth
+    leaves, far beyond the traversal guard of 4 x nodes + 64 visits.  Every link and leaf range
+    is in bounds (the loader accepts it); the guard ends the walk and raises FLAG_BVH_VISITS."""
+    n = 2 * depth + 1
+    out = np.zeros((n, 8), np.float32)
+    for k in range(n):
+        out[k, 0:3] = lo
+        out[k, 4:7] = hi
+        leaf = k >= n - 2
+        link = 0 if leaf else (1 if k == 0 else 2 * ((k - 1) // 2) + 3)
+        out[k, 3] = np.array([link], np.int32).view(np.float32)[0]
+        out[k, 7] = np.array([4 if leaf else 0], np.int32).view(np.float32)[0]
+    return out
+
+
+def test_trace_rays_keeps_frame_guard_flags():
+    """rc_trace_rays between frames leaves the guard word of the run's kernels alone: a flag that
+    the state build raised (traversal guard on a shared-child tree) is still reported by
+    rc_device_flags after a trace_rays call that raised nothing itself."""
+    sc = S.read(lattice_scene_bytes())
+    V = np.asarray(sc.mesh["ST"], np.float32).reshape(-1, 9)
+    v0 = V[:, 0:3]
+    pts = np.concatenate([v0, v0 + V[:, 3:6], v0 + V[:, 6:9]])
+    sc.mesh["BN"] = _dag_tree(pts.min(0) - 0.01, pts.max(0) + 0.01)
+    ctx = _gpu(S.write(sc), 0)       # the state build's shadow rays trip the guard (word of the run)
+    p, t = ctx.trace_rays(0, np.array([[5.0, 5.0, 50.0, 0.0, 0.0, 1.0]], np.float32))   # misses the root box
+    assert p[0] == -1 and np.isinf(t[0])
+    assert ctx.device_flags() & 1      # FLAG_BVH_VISITS, raised before the call, survives it
+    assert ctx.device_flags() == 0     # read once, then cleared
+    ctx.close()
