@@ -2,15 +2,19 @@
 """Benchmark of the dependency-tracked radiance cache on GB300.
 
 Workload: the reference's headline timing case (cuda/poc_gpu.cu `timing` mode, published as
-reference/cuda_rtx4060/timing_1M.jsonl) on a seeded stand-in for its 1,082,802-point box
-scene: an 8 x 4 x 3 m room with four static boxes and a movable one (31 quads, 62 triangles),
-3 point lights, 5 states switched every 60 frames (light off, box moved, light back on, ...),
-method "v4-A2C suivi 1/4" (adaptive ray allocation, dependency masks on a 8 x 4 x 4 transit
-grid tracked one frame in four, verified dormant-light memory, history ramp).
+reference/cuda_rtx4060/timing_1M.jsonl) on the reference's own timing scene
+cuda/scenes/scene_scale_1M.bin (1,082,802 cache points, 58 triangles, 3 point lights, 5 states
+switched every 60 frames; shipped gzip-compressed in tests/golden/), method "v4-A2C suivi 1/4"
+(adaptive ray allocation, dependency masks on a 8 x 4 x 4 transit grid tracked one frame in
+four, verified dormant-light memory, history ramp).  A seeded stand-in room of the same size
+(render_engine_gb300/scene.py: box_room) is measured the same way as a second line.
 
 One step = one frame of the whole cache (trace + update of every cache point, plus the
-event kernels when the state changes).  Timed frames are separated by an L2 flush (a 512 MB
-write) and timed with CUDA events on the stream the kernels run on.
+event kernels when the state changes).  With fewer than 120 timed frames the timed window is
+centred on the first state change (frame 60): the frames before the warm-up run untimed, so
+that both arms time an event frame and the verification frames after it.  Timed frames are
+separated by an L2 flush (a 512 MB write) and timed with CUDA events on the stream the
+kernels run on.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -21,6 +25,7 @@ frames, timed the same way.
 from __future__ import annotations
 
 import argparse
+import gzip
 import json
 import os
 import statistics
@@ -36,6 +41,8 @@ POINTS = 1_082_802
 METHOD = "v4-A2C suivi 1/4"
 FRAMES_PER_STATE = 60
 PUBLISHED_FPS = 1000.0 / 1.44806   # timing_1M.jsonl:10 (RTX 4060): trace+decide+update+swap = 1.448 ms
+SCENE_1M = os.path.join(ROOT, "tests", "golden", "scene_scale_1M.bin.gz")
+POST_FRAMES, PRE_FRAMES = 30, 20     # the reference's post / pre windows (poc_gpu.cu:1428-1429)
 
 
 def parse():
@@ -132,6 +139,24 @@ def street_scene(points: int):
 
 def sequence(n: int, ns: int = 5) -> list[int]:
     return [(f // FRAMES_PER_STATE) % ns for f in range(n)]
+
+
+def window_start(warmup: int, steps: int) -> int:
+    """First timed frame.  Fewer than 120 timed frames are centred on the first state change
+    (frame 60), so that the window holds an event frame and the verification frames after it;
+    the frames before the warm-up run untimed.  Longer runs start right after the warm-up."""
+    return max(warmup, FRAMES_PER_STATE - steps // 2)
+
+
+def headline_scene(points: int) -> tuple[bytes, str]:
+    """The reference's own 1,082,802-point timing scene when it is present and the size asked
+    for, else the seeded stand-in room of that size."""
+    from render_engine_gb300 import scene as S
+    if points == POINTS and os.path.exists(SCENE_1M):
+        return gzip.decompress(open(SCENE_1M, "rb").read()), \
+            "the reference's timing scene cuda/scenes/scene_scale_1M.bin (1082802 cache points, 58 triangles, 3 point lights, 5 states)"
+    return S.write(S.box_room(points=points, seed=0)), \
+        "seeded stand-in for the reference's scene_scale_1M.bin (box room, %d cache points, 62 triangles, 3 point lights, 5 states)" % points
 
 
 class Clocks:
@@ -232,41 +257,29 @@ def setup_dist(args):
     return world, rank, local, dist
 
 
-def run_ours(args, world, rank, local, dist):
+def time_frames(ctx, method, seq, s0, args, stream, flush, dist=None):
+    """Frames [0, s0 - W) untimed, W warm-up frames, then the timed frames [s0, s0 + K), each
+    after an L2 flush, between CUDA events on the library's stream.  Returns per-frame times
+    and the kind of each timed frame (event: the state changed; fused: one fused kernel;
+    split: trace and update as separate kernels)."""
     import torch
-
-    from render_engine_gb300 import methods as M
     from render_engine_gb300 import native as N
-    from render_engine_gb300 import scene as S
-
-    torch.cuda.set_device(local)
-    # a dedicated stream: the library's kernels, the L2 flush and the timing events all go on it
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    data = S.write(S.box_room(points=args.points, seed=0))
-    method = M.by_name(M.timing_methods(), args.method)
-    ctx = N.Context(device=local, stream=stream.cuda_stream)
-    info = ctx.load_bytes(data)
-    seq = sequence(args.warmup + args.steps)
-    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     ctx.begin(method, seq[0], 11)
-    for f in range(args.warmup):
+    for f in range(s0):
         ctx.frame(seq[f])
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    fused = []
-    kinds = []
-    tracked = []
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    fused, kinds, tracked = [], [], []
     l0 = ctx.stats()
-    r0 = l0["rays"]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = Clocks(local)
+    clocks = Clocks(torch.cuda.current_device())
     wall0 = time.perf_counter()
-    for k in range(args.steps):
-        f = args.warmup + k
+    for k in range(K):
+        f = s0 + k
         flush.zero_()
         starts[k].record(stream)
         ctx.frame(seq[f])
@@ -279,14 +292,44 @@ def run_ours(args, world, rank, local, dist):
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
     st = ctx.stats()
-    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    return {"ms": ms, "fused": fused, "kinds": kinds, "tracked": tracked, "rays": st["rays"] - l0["rays"],
+            "launches": st["launches"] - l0["launches"], "wall_s": wall, "clocks": clk}
+
+
+def kinds_table(ms, kinds):
+    return {kd: {"frames": sum(1 for x in kinds if x == kd),
+                 "mean_ms": sum(m for m, x in zip(ms, kinds) if x == kd) / max(1, sum(1 for x in kinds if x == kd))}
+            for kd in sorted(set(kinds) | {"event"})}
+
+
+def run_ours(args, world, rank, local, dist):
+    import torch
+
+    from render_engine_gb300 import methods as M
+    from render_engine_gb300 import native as N
+    from render_engine_gb300 import scene as S
+
+    torch.cuda.set_device(local)
+    # a dedicated stream: the library's kernels, the L2 flush and the timing events all go on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    data, scene_desc = headline_scene(args.points)
+    method = M.by_name(M.timing_methods(), args.method)
+    s0 = window_start(args.warmup, args.steps)
+    seq = sequence(s0 + args.steps)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    ctx = N.Context(device=local, stream=stream.cuda_stream)
+    info = ctx.load_bytes(data)
+    t = time_frames(ctx, method, seq, s0, args, stream, flush, dist)
+    ms, fused, tracked = t["ms"], t["fused"], t["tracked"]
     total_ms = sum(ms)
     if dist:
         total_ms = max_over_ranks(total_ms, dist, "cuda")
         dist.barrier()
     # the 1920x1080 image pass of the same cache (one primary ray per pixel), timed the same way
     cam = N.camera(eye=(0.4, 0.4, 1.7), at=(7.6, 3.6, 0.8), fov_y_deg=75.0, width=1920, height=1080)
-    state_now = seq[args.warmup + args.steps - 1]
+    state_now = seq[-1]
     ctx.render(state_now, cam, copy=False)
     nimg = 20
     cams = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nimg)]
@@ -298,11 +341,10 @@ def run_ours(args, world, rank, local, dist):
     torch.cuda.synchronize()
     camera_ms = sum(e0.elapsed_time(e1) for e0, e1 in cams) / nimg
     frames = args.steps * world
-    rays = st["rays"] - r0
+    rays = t["rays"]
     np_ = info["np"]
     # dominant kernel: frames that are exactly one fused launch
     fk = [m for m, fu in zip(ms, fused) if fu]
-    fk_tr = [m for m, fu, tr in zip(ms, fused, tracked) if fu]
     fk_bytes = [algorithmic_bytes(np_, tr, method.ramp) for fu, tr in zip(fused, tracked) if fu]
     kern_ms = sum(fk) / max(len(fk), 1)
     kern_bytes = sum(fk_bytes) / max(len(fk_bytes), 1)
@@ -315,78 +357,141 @@ def run_ours(args, world, rank, local, dist):
         "mrays_per_s": rays * world / (total_ms * 1e-3) / 1e6,
         "cache_updates_per_s": np_ * frames / (total_ms * 1e-3),
         "rays_per_frame": rays / args.steps,
-        "launches": st["launches"] - l0["launches"],
-        "wall_s": wall,
-        "clocks": clk,
+        "launches": t["launches"],
+        "wall_s": t["wall_s"],
+        "clocks": t["clocks"],
+        "scene": scene_desc,
+        "window": {"first_timed_frame": s0, "untimed_lead_in_frames": s0 - args.warmup, "state_changes_timed":
+                   sum(1 for f in range(s0, s0 + args.steps) if seq[f] != seq[f - 1])},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic,
                      "kernel": "rc::k_frame<3,4,DEPS,FUSED=true>", "kernel_ms": kern_ms, "kernel_launches": len(fk),
                      "peak_source": peak_kind},
         "np": np_,
         "nt": info["nt"],
-        "frame_kinds_ms": {kd: {"frames": sum(1 for x in kinds if x == kd),
-                                "mean_ms": sum(m for m, x in zip(ms, kinds) if x == kd) / max(1, sum(1 for x in kinds if x == kd))}
-                           for kd in ("fused", "split", "event")},
+        "frame_kinds_ms": kinds_table(ms, t["kinds"]),
         "frame_1080p": {"cache_ms": total_ms / args.steps, "image_ms": camera_ms,
                         "frames_per_s": 1000.0 / (total_ms / args.steps + camera_ms),
                         "mrays_per_s": (rays / args.steps + 1920 * 1080) / ((total_ms / args.steps + camera_ms) * 1e-3) / 1e6,
                         "note": "cache-point frame + one primary ray per pixel at 1920x1080 shaded from the cache"},
     }
-    # end to end through the C ABI from host memory: scene upload + build, the frames, and the
-    # final cache read back
-    ctx2 = N.Context(device=local, stream=stream.cuda_stream)
-    host = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
-    nl = ctx.info()["nl"]
-    lc_host = torch.empty(nl * ctx.info()["np"], dtype=torch.float32).pin_memory()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    e0.record(stream)
-    ctx2.load_bytes(host.numpy())
-    ctx2.begin(method, seq[0], 11)
-    for f in range(args.steps):
-        ctx2.frame(seq[f])
-    lc = ctx2.array(N.A_LC, out=lc_host.numpy())
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    out["e2e"] = {"value": args.steps * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": len(data) / args.steps,
-                  "d2h_bytes_per_step": lc.nbytes / args.steps,
-                  "includes": "scene upload + per-state build + %d frames + final cache download" % args.steps}
-    ctx2.close()
+    out["e2e"] = e2e_run(data, method, seq, local, stream, world)
     ctx.close()
-    out["quality"] = quality(args, data, method, seq, local, stream)
+    # the seeded stand-in room of the same size, the same frames
+    if args.points == POINTS and os.path.exists(SCENE_1M):
+        c2 = N.Context(device=local, stream=stream.cuda_stream)
+        c2.load_bytes(S.write(S.box_room(points=args.points, seed=0)))
+        t2 = time_frames(c2, method, seq, s0, args, stream, flush)
+        c2.close()
+        out["standin_room"] = {"scene": "seeded box room (render_engine_gb300/scene.py: box_room, %d points, 62 triangles)" % args.points,
+                               "frames_per_s": args.steps / (sum(t2["ms"]) * 1e-3), "ms_per_step": sum(t2["ms"]) / args.steps,
+                               "frame_kinds_ms": kinds_table(t2["ms"], t2["kinds"]), "clocks": t2["clocks"]}
+    del flush
+    out["quality"], refs = quality(data, method, local, stream)
     out["hashgrid"] = hashgrid_bench(stream, peak)
     out["mlp"] = mlp_bench(stream)
     out["adjoint"] = adjoint_bench(peak)
     out["taa"] = taa_bench()
     out["camera_paths"] = paths_bench()
-    return out, data, method
+    return out, data, method, refs
 
 
-def quality(args, data, method, seq, local, stream):
-    """The metric's error part: the per-frame luminance error of the cache against converged
-    references (the error formula of the reference, sqrt(sum (est - ref)^2 / n) / (sum ref / n)
-    over valid points), averaged over the 30 frames after each event and the 20 before it.
-    The scene carries no references, so they are computed first on the GPU by the stochastic
-    Jacobi of the reference's scene preparation (rc_reference_build)."""
+def e2e_run(data, method, seq, local, stream, world):
+    """End to end through the C ABI from host memory: the scene upload from a pinned buffer and
+    its load, the run's frames from frame 0 through the last timed frame, and the cache read
+    back into pinned memory, all inside one host-clock interval."""
+    import torch
+    from render_engine_gb300 import native as N
+    from render_engine_gb300 import scene as S
+    host = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
+    hdr = S.header(data)
+    lc_host = torch.empty(hdr["nl"] * hdr["np"], dtype=torch.float32).pin_memory()
+    ctx = N.Context(device=local, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.load_bytes(host.numpy())
+    ctx.sync()
+    t1 = time.perf_counter()
+    ctx.begin(method, seq[0], 11)
+    for s in seq:
+        ctx.frame(s)
+    lc = ctx.array(N.A_LC, out=lc_host.numpy())
+    ctx.sync()
+    t2 = time.perf_counter()
+    ctx.close()
+    nf = len(seq)
+    return {"value": nf * world / (t2 - t0), "unit": "frames/s", "h2d_bytes_per_step": len(data) / nf,
+            "d2h_bytes_per_step": lc.nbytes / nf, "frames": nf, "load_ms": (t1 - t0) * 1e3, "frames_ms": (t2 - t1) * 1e3,
+            "includes": "scene upload from pinned host memory + load and state builds + frames 0-%d + final cache download" % (nf - 1)}
+
+
+def quality(data, method, local, stream):
+    """The metric's error part over the reference's whole timing sequence (5 states x 60
+    frames, 4 state changes), whatever the number of timed steps: the per-frame luminance error
+    sqrt(sum (est - ref)^2 / n) / (sum ref / n) of the reference (poc_gpu.cu:683-696, 1005-1010)
+    against converged references, averaged over the 30 frames after each change
+    (poc_gpu.cu:1428-1429) and the 20 before it, over all valid points (as the reference reports
+    it) and over the event region: the valid points whose reference changes by more than 5 %
+    between the two states, |new - old| / (old + 0.01) > 0.05 (the two upper recon categories,
+    poc_gpu.cu:1520-1526).  The scene carries no references, so they are computed first on the
+    GPU by the stochastic Jacobi of the reference's scene preparation (rc_reference_build); the
+    CPU leg checks them against the FP64 path tracer.  The event-region sums come from
+    rc_error_sums_noalloc on the run's own cache buffer after each frame."""
+    import math
+    import numpy as np
+    import torch
     from render_engine_gb300 import native as N
     q = N.Context(device=local, stream=stream.cuda_stream)
-    q.load_bytes(data)
+    info = q.load_bytes(data)
+    np_, nl, ns = info["np"], info["nl"], info["ns"]
     t0 = time.perf_counter()
     noise, iters = q.build_reference()
     tref = time.perf_counter() - t0
-    errs = [float(x) for x in q.run(method, seq, 11, want_err=True)]
-    q.close()
+    refs = [q.state_array(k, N.SA_REF) for k in range(ns)]
+    valid = [q.state_array(k, N.SA_VALID) for k in range(ns)]
+    seq = sequence(ns * FRAMES_PER_STATE, ns)
     events = [f for f in range(1, len(seq)) if seq[f] != seq[f - 1]]
-    post = [statistics.mean(errs[e:e + 30]) for e in events if e + 30 <= len(errs)]
-    pre = [statistics.mean(errs[e - 20:e]) for e in events if e >= 20]
-    return {"luma_err_post_event_pct": 100 * statistics.mean(post) if post else None,
-            "luma_err_pre_event_pct": 100 * statistics.mean(pre) if pre else None,
-            "events": len(post), "reference_noise": [float(x) for x in noise], "reference_iterations": [int(x) for x in iters],
-            "reference_build_s": tref,
-            "note": "references from the GPU stochastic Jacobi of the reference's scene preparation (K=32, two chains, 3 % noise)"}
+    dev = torch.device("cuda", local)
+    region = {}
+    for e in events:
+        a, b = seq[e - 1], seq[e]
+        rel = np.abs(refs[b] - refs[a]).astype(np.float64) / (refs[a].astype(np.float64) + 1e-2)
+        mask = (valid[b] != 0) & (rel > 0.05)
+        region[e] = (torch.from_numpy(mask.astype(np.uint8)).to(dev), torch.from_numpy(refs[b]).to(dev), int(mask.sum()))
+    out3 = torch.zeros((len(events) * POST_FRAMES, 3), dtype=torch.float64, device=dev)
+    lc_stride = (nl + 3) // 4 * 4
+    q.begin(method, seq[0], 11)
+    slot = 0
+    for f, s in enumerate(seq):
+        q.frame(s, want_err=True)
+        e = max([x for x in events if x <= f], default=None)
+        if e is not None and f < e + POST_FRAMES:
+            m, r, _ = region[e]
+            N.error_sums_noalloc(q.device_ptr(N.A_LC), lc_stride, nl, q.scalar(N.S_DORMANT), r.data_ptr(), m.data_ptr(), np_,
+                                 out3[slot].data_ptr(), stream.cuda_stream)
+            slot += 1
+    errs = [float(x) for x in q.errors()]
+    sums = out3.cpu().numpy()
+    q.close()
+    post = [statistics.mean(errs[e:e + POST_FRAMES]) for e in events]
+    pre = [statistics.mean(errs[e - PRE_FRAMES:e]) for e in events]
+    post_region = []
+    for k, e in enumerate(events):
+        v = []
+        for j in range(POST_FRAMES):
+            d2, rs, cnt = sums[k * POST_FRAMES + j]
+            v.append(math.sqrt(d2 / cnt) / (rs / cnt) if cnt > 0 and rs > 0 else 0.0)
+        post_region.append(statistics.mean(v))
+    res = {"luma_err_post_event_pct": 100 * statistics.mean(post), "luma_err_pre_event_pct": 100 * statistics.mean(pre),
+           "luma_err_post_event_region_pct": 100 * statistics.mean(post_region),
+           "per_event": [{"frame": e, "from": seq[e - 1], "to": seq[e], "region_points": region[e][2],
+                          "post_pct": 100 * p, "post_region_pct": 100 * pr, "pre_pct": 100 * pe}
+                         for e, p, pr, pe in zip(events, post, post_region, pre)],
+           "events": len(events), "frames": len(seq), "reference_noise": [float(x) for x in noise],
+           "reference_iterations": [int(x) for x in iters], "reference_build_s": tref,
+           "note": "references from the GPU stochastic Jacobi of the reference's scene preparation (K=32, two chains, 3 % noise "
+                   "target); their gap to the FP64 path tracer is measured by the CPU leg (fp64_reference_check)"}
+    return res, {"refs": refs, "valid": valid}
 
 
 def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20, reps=10):
@@ -634,12 +739,28 @@ def tensor_peak() -> float:
     return 1900.0
 
 
-def cpu_baseline(args, data, method):
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
+def cpu_baseline(args, data, method, refs):
+    """The CPU leg: the oracle (plain-C restatement, OpenMP on all host cores) timed on the first
+    frames of the same workload, and the checker of the GPU references the quality leg used:
+    the oracle's FP64 path tracer at 128 sampled valid points per state (16,384 paths each)
+    against the GPU's stochastic-Jacobi values there."""
+    import numpy as np
     from oracle import pyoracle as po
     cores = os.cpu_count() or 1
     po.set_threads(cores)
     sc = po.Scene(data=data)
-    t = time.perf_counter()
     sc.build()
     run = po.Run(sc)
     seq = sequence(args.cpu_frames)
@@ -648,8 +769,26 @@ def cpu_baseline(args, data, method):
     for s in seq:
         run.frame(s)
     dt = time.perf_counter() - t
-    return {"value": args.cpu_frames / dt, "unit": "frames/s", "cores": cores, "kind": "port",
-            "sample": "frames 0-%d of the same sequence at full size (%d points), C restatement with OpenMP" % (args.cpu_frames - 1, sc.Np)}
+    out = {"value": args.cpu_frames / dt, "unit": "frames/s", "cores": cores, "cpu_model": cpu_model(), "kind": "port",
+           "sample": "frames 0-%d of the same sequence at full size (%d points), C restatement with OpenMP" % (args.cpu_frames - 1, sc.Np)}
+    if refs is not None:
+        rng = np.random.default_rng(31)
+        t = time.perf_counter()
+        gaps, z2 = [], []
+        for si, (ref, val) in enumerate(zip(refs["refs"], refs["valid"])):
+            ok = np.flatnonzero((val != 0) & (ref > 0))
+            pts = ok[rng.choice(len(ok), min(128, len(ok)), replace=False)]
+            m, se = sc.path_trace(si, pts, paths=16384, min_bounces=3, seed=50 + si)
+            r = ref[pts].astype(np.float64)
+            gaps.append(float((r - m).mean() / m.mean()))
+            z2.append(float((((r - m) / np.sqrt(se ** 2 + (0.03 * r) ** 2)) ** 2).mean()))
+        out["fp64_reference_check"] = {
+            "points_per_state": 128, "paths_per_point": 16384, "seconds": time.perf_counter() - t,
+            "mean_rel_gap_per_state": gaps, "mean_abs_rel_gap_pct": 100 * float(np.mean(np.abs(gaps))),
+            "z2_per_state": z2,
+            "note": "GPU FP32 stochastic-Jacobi references minus the FP64 path tracer, relative to the latter's mean; z2 = "
+                    "mean squared difference over the path tracer's standard error and the references' 3 % noise target"}
+    return out
 
 
 def run_reference(args, world, rank, local, dist):
@@ -657,20 +796,20 @@ def run_reference(args, world, rank, local, dist):
 
     from oracle import pyref
     from render_engine_gb300 import methods as M
-    from render_engine_gb300 import scene as S
 
     if not pyref.available(3):
         return None, "reference kernels not built (oracle/_ref/ref_l3.cubin missing: needs the reference checkout at build time)"
     torch.cuda.set_device(local)
     torch.cuda.init()
-    data = S.write(S.box_room(points=args.points, seed=0))
+    data, scene_desc = headline_scene(args.points)
     method = M.by_name(M.timing_methods(), args.method)
     ref = pyref.RefRunner(3, data)
-    seq = sequence(args.warmup + args.steps)
+    s0 = window_start(args.warmup, args.steps)
+    seq = sequence(s0 + args.steps)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     ref.begin(method, seq[0], 11)
-    for f in range(args.warmup):
+    for f in range(s0):
         ref.frame(seq[f])
     torch.cuda.synchronize()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -679,19 +818,20 @@ def run_reference(args, world, rank, local, dist):
     for k in range(args.steps):
         flush.zero_()
         starts[k].record(stream)
-        ref.frame(seq[args.warmup + k])
+        ref.frame(seq[s0 + k])
         ends[k].record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    kinds = ["event" if seq[s0 + k] != seq[s0 + k - 1] else "other" for k in range(args.steps)]
     total_ms = sum(ms)
     # the reference's own timing-mode figures (per-frame events, one sync per frame)
     import numpy as np
     tm = np.zeros(5)
     ref.begin(method, seq[0], 12)
-    for f in range(min(args.steps, 5 * FRAMES_PER_STATE)):
-        ref.frame(seq[f], timers=tm)
     nf = min(args.steps, 5 * FRAMES_PER_STATE)
+    for f in range(nf):
+        ref.frame(seq[f], timers=tm)
     ref.close()
     # the taa mode with the reference's own kernels, as taa_bench times the product's
     rt = pyref.RefRunner(3, taa_scene(args.points))
@@ -704,6 +844,8 @@ def run_reference(args, world, rank, local, dist):
     dt = time.perf_counter() - t0
     rt.close()
     return {"frames_per_s": args.steps / (total_ms * 1e-3), "ms_per_step": total_ms / args.steps, "clocks": clk,
+            "scene": scene_desc, "frame_kinds_ms": kinds_table(ms, kinds),
+            "window": {"first_timed_frame": s0, "untimed_lead_in_frames": s0 - args.warmup},
             "timing_mode": {"trace": tm[1] / nf, "decide": tm[2] / nf, "update": tm[3] / nf, "swap": tm[0] / nf,
                             "event_total": tm[4]},
             "taa": {"points": args.points, "frames": 200, "frames_per_s": 200 / dt, "ms_per_frame": dt * 1e3 / 200,
@@ -716,11 +858,13 @@ def main():
         profile_run(args)
         return
     world, rank, local, dist = setup_dist(args)
-    config = {"workload": "dependency-tracked radiance cache, %s, seeded box room (%d cache points, 62 triangles, 3 point lights, "
-                          "5 states x %d frames with events), one frame per step" % (args.method, args.points, FRAMES_PER_STATE),
+    s0 = window_start(args.warmup, args.steps)
+    config = {"workload": "dependency-tracked radiance cache, %s, the reference's scene_scale_1M timing case (%d cache points, "
+                          "3 point lights, 5 states x %d frames with events), one frame per step" % (args.method, args.points, FRAMES_PER_STATE),
               "method": args.method, "cache_points": args.points, "transit_grid": "8x4x4 (128-bit dependency masks)",
               "l2": "flushed between timed frames (512 MB write); per-frame working set ~140 MB",
-              "scene": "synthetic stand-in for the reference's scene_scale_1M.bin (same room, size and light count)",
+              "window": "timed frames %d-%d of the state sequence (state changes every %d frames); frames before the warm-up run untimed"
+                        % (s0, s0 + args.steps - 1, FRAMES_PER_STATE),
               "parallelism": "replicas" if world > 1 else "single GPU"}
     if args.impl == "reference":
         if rank != 0:
@@ -729,29 +873,36 @@ def main():
         if res is None:
             print(json.dumps({"impl": "reference", "unavailable": why}))
             return
+        config["scene"] = res["scene"]
         line = {"metric": METRIC, "value": res["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
-                "impl": "reference", "clocks": res["clocks"], "reference_timing_mode_ms": res["timing_mode"], "taa": res["taa"],
+                "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "the reference's own scene file",
+                "config": config, "impl": "reference", "clocks": res["clocks"], "frame_kinds_ms": res["frame_kinds_ms"],
+                "window": res["window"], "reference_timing_mode_ms": res["timing_mode"], "taa": res["taa"],
                 "cpu_baseline": {"value": res["frames_per_s"], "unit": "frames/s", "cores": 1, "kind": "reference",
                                  "sample": "the reference's own kernels (cuda/poc_gpu.cu for sm_103a) on the GB300, driven by one host thread; "
                                            "the reference has no CPU implementation of this path"},
                 "e2e": {"value": res["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
-    res, data, method = run_ours(args, world, rank, local, dist)
+    res, data, method, refs = run_ours(args, world, rank, local, dist)
     if rank != 0:
         return
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, data, method)
+        cpu = cpu_baseline(args, data, method, refs)
+        if "fp64_reference_check" in cpu:
+            res["quality"]["reference_vs_fp64_gap_pct"] = cpu["fp64_reference_check"]["mean_abs_rel_gap_pct"]
+    config["scene"] = res["scene"]
     line = {"metric": METRIC, "value": res["frames_per_s"], "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "synthetic", "config": config,
+            "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "the reference's own scene file",
+            "config": config, "window": res["window"],
             "mrays_per_s": res["mrays_per_s"], "cache_updates_per_s": res["cache_updates_per_s"],
-            "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"], "clocks": res["clocks"], "e2e": res["e2e"],
-            "gpu_launches": res["launches"], "roofline": res["roofline"], "cpu_baseline": cpu, "quality": res["quality"], "hashgrid": res["hashgrid"], "mlp": res["mlp"],
-            "adjoint": res["adjoint"], "taa": res["taa"], "camera_paths": res["camera_paths"]}
+            "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"],
+            "clocks": res["clocks"], "e2e": res["e2e"], "gpu_launches": res["launches"], "roofline": res["roofline"],
+            "cpu_baseline": cpu, "quality": res["quality"], "standin_room": res.get("standin_room"), "hashgrid": res["hashgrid"],
+            "mlp": res["mlp"], "adjoint": res["adjoint"], "taa": res["taa"], "camera_paths": res["camera_paths"]}
     print(json.dumps(line))
 
 

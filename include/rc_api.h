@@ -286,24 +286,37 @@ rc_status rc_taa_frame(rc_ctx* ctx, int state, float* err);
 enum { RC_T_X = 0, RC_T_H, RC_T_MU, RC_T_SG, RC_T_REACT, RC_T_PEND, RC_T_CUR, RC_T_PREV, RC_T_COUNT };
 rc_status rc_taa_array_copy(rc_ctx* ctx, int which, void* host, size_t nbytes, int to_device);
 
-/* Scene preparation: the reference's `prep` mode (prep_mesh.cuh:303-531).  Reads an MSH1 mesh
- * (triangles in metres, z up, albedo and a double-sided flag per triangle), builds the static
- * BVH (binned SAH), cache points on a cell grid sized towards target_points, places three
- * lamps and a movable cube in free space found by probe rays, makes the five states and the
- * events' transit voxels, normalises the direct light to a mean of 1 in state 0, computes the
- * converged references (rc_reference_build with the preparation's parameters; the environment
- * variables PREP_BRUIT_CIBLE and PREP_ITER_MAX as the reference reads them) and writes the
- * format-3 scene to scene_path.  The context ends with the prepared scene loaded.  The report
- * holds what the reference prints in its `{"type":"prep",...}` line. */
+/* Scene preparation on the GPU, in place of the reference's `prep` mode
+ * (prep_mesh.cuh:303-531): an MSH1 mesh (triangles in metres, z up, albedo and a double-sided
+ * flag per triangle) becomes a format-3 scene with converged references, written to
+ * scene_path.  The static BVH is a linear BVH over Morton codes with SAH leaf collapse (leaves
+ * of at most four triangles); cache points are cells of side h and one normal bucket, sampled
+ * on the triangles, h scaled towards target_points; `lamps` point lights and a movable cube are
+ * placed in free space found by probe rays; the five states follow the reference's state table
+ * for mesh scenes (cuda/scenes/scenarios_publiques.txt: 0 lamps 0-1 on, cube at A; 1 lamp 0
+ * off; 2 cube at B; 3 lamp 2 on too; 4 lamp 0 off, cube at B; lamps beyond the third always
+ * on); each lamp's intensity gives it a mean direct light of 1 / lamps over the points of state
+ * 0; references by rc_reference_build (environment variables PREP_BRUIT_CIBLE and
+ * PREP_ITER_MAX as the reference reads them).  The context ends with the prepared scene loaded.
+ * The report holds what the reference prints in its `{"type":"prep",...}` line. */
+typedef struct {
+    int target_points;   /* cache points aimed at (the cell count lands within 5 %) */
+    int lamps;           /* point lights, 1..32 (the reference places 3) */
+    uint32_t seed;       /* sampling and placement seed */
+} rc_prep_params;
 typedef struct {
     int triangles, np, zones, bvh_nodes, ns;
     float cell_m, diag_m, cube_m;
     double valid_fraction;   /* mean over states of the valid points' fraction */
     double noise[8];
     int iterations[8];
-    float lights[3][3];
+    int nl, bvh_depth;
+    float lights[32][3];
     double seconds;
 } rc_prep_report;
+rc_status rc_prep_mesh_params(rc_ctx* ctx, const char* mesh_path, const char* scene_path, const rc_prep_params* params,
+                              rc_prep_report* out);
+/* The reference's `prep <mesh> <scene> [points]`: three lamps, seed 1. */
 rc_status rc_prep_mesh(rc_ctx* ctx, const char* mesh_path, const char* scene_path, int target_points, rc_prep_report* out);
 
 /* Error sums without any device allocation.  No counterpart in the reference: it exists for

@@ -274,16 +274,20 @@ int main(int argc, char** argv) {
     if (const char* d = getenv("BENCH_DEBUG")) g_debug = atoi(d);
     if (const char* r = getenv("BENCH_RAYONS")) g_rays = std::max(0.25f, (float)atof(r));
     if (mode == "prep") {   // poc_gpu.cu:1304-1306, prep_mesh.cuh:303-531
-        if (RC_CLI_NLIGHTS != 3) { fprintf(stderr, "prep : utiliser poc_gpu_l3 (scenes maillees a 3 lampes)\n"); return 1; }
+        // poc_gpu_l3 places the reference's three lamps; poc_gpu_l8 places eight
         if (argc < 4) { fprintf(stderr, "usage : prep <maillage.mesh> <scene.bin> [points]\n"); return 1; }
         rc_config pc;
         memset(&pc, 0, sizeof pc);
-        pc.expect_lights = 3;
+        pc.expect_lights = RC_CLI_NLIGHTS;
         rc_ctx* pctx = nullptr;
         rc_status ps = rc_create(&pc, &pctx);
         if (ps != RC_OK) { fprintf(stderr, "CUDA: %s\n", rc_status_string(ps)); return 2; }
         rc_prep_report r;
-        ps = rc_prep_mesh(pctx, argv[2], argv[3], argc > 4 ? atoi(argv[4]) : 300000, &r);
+        rc_prep_params pp;
+        pp.target_points = argc > 4 ? atoi(argv[4]) : 300000;
+        pp.lamps = RC_CLI_NLIGHTS;
+        pp.seed = 1u;
+        ps = rc_prep_mesh_params(pctx, argv[2], argv[3], &pp, &r);
         if (ps != RC_OK) {
             fprintf(stderr, "prep: %s\n", rc_last_error(pctx));
             rc_destroy(pctx);
@@ -296,7 +300,7 @@ int main(int argc, char** argv) {
         printf("],\"iterations_ref\":[");
         for (int k = 0; k < r.ns; ++k) printf("%s%d", k ? "," : "", r.iterations[k]);
         printf("],\"lampes\":[");
-        for (int l = 0; l < 3; ++l) printf("%s[%.3f,%.3f,%.3f]", l ? "," : "", r.lights[l][0], r.lights[l][1], r.lights[l][2]);
+        for (int l = 0; l < r.nl; ++l) printf("%s[%.3f,%.3f,%.3f]", l ? "," : "", r.lights[l][0], r.lights[l][1], r.lights[l][2]);
         printf("],\"secondes\":%.1f}\n", r.seconds);
         rc_destroy(pctx);
         return 0;

@@ -183,10 +183,10 @@ struct Ops {
     static cudaError_t pretrace(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                                 float4* out, cudaStream_t st);
 };
-// Free-space probe of the scene preparation (64 directions per candidate point through the
-// static mesh of g): out[3 i] = closest hit, out[3 i + 1] = fraction of hits closer than diag,
-// out[3 i + 2] = fraction of single-sided back faces.
-cudaError_t probe_free_space(const DStatic& g, const float* C, int nc, float diag, float* out, unsigned* flags, cudaStream_t st);
+// Free-space probe of the scene preparation (48 directions per candidate point through the
+// static mesh of g): out[3 i] = closest hit (1e30 when none), out[3 i + 1] = fraction of rays
+// that hit, out[3 i + 2] = fraction that meet a one-sided face from behind.
+cudaError_t prep_probe(const DStatic& g, const float* C, int nc, float diag, float* out, unsigned* flags, cudaStream_t st);
 // Closest hit of n caller-given rays (6 floats each: origin, direction) against state s's
 // dynamic triangles and g's static mesh: prim = quad id, -2 - static triangle or -1; t = hit
 // distance (+inf when none).

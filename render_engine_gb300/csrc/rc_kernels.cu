@@ -1816,37 +1816,45 @@ cudaError_t Ops<NL>::preload(int NW) {
 template struct Ops<RC_NL_ONE>;
 #endif
 
-#if RC_NL_ONE == 3   // compiled once: free-space probe of the scene preparation
+#if RC_NL_ONE == 3   // compiled once: the preparation's probe, caller-given rays
 // k_probe of the reference's preparation (prep_mesh.cuh:160-178): from each candidate point, 64
 // Fibonacci directions through the static mesh; out = (closest hit, fraction of hits closer than
 // diag, fraction of single-sided back faces hit).
-__global__ void __launch_bounds__(BLOCK) k_free_space(const DStatic g, const float* __restrict__ C, int nc, float diag,
-                                                      float* __restrict__ out, unsigned* flags) {
+// Free-space probe of the scene preparation: 48 directions of a spherical Fibonacci lattice
+// from each candidate point through the static mesh.  out = (clearance: the nearest hit, 1e30
+// when every ray escapes; the fraction of rays that hit; the fraction that meet a one-sided
+// face from behind, i.e. the candidate is inside closed geometry).
+__global__ void __launch_bounds__(BLOCK) k_prep_probe(const DStatic g, const float* __restrict__ C, int nc, float* __restrict__ out,
+                                                      unsigned* flags) {
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     if (i >= nc) return;
     const f3 o = mk(C[3 * i], C[3 * i + 1], C[3 * i + 2]);
-    float clr = 1e30f, enc = 0.f, back = 0.f;
-    const int ND = 64;
+    constexpr int ND = 48;
+    float clr = 1e30f;
+    int hits = 0, behind = 0;
     for (int k = 0; k < ND; ++k) {
-        const float z = 1.f - (2.f * k + 1.f) / ND, r = sqrtf(fmaxf(0.f, 1.f - z * z)), ph = 2.39996323f * k;
-        const f3 d = mk(r * cosf(ph), r * sinf(ph), z);
+        const float z = 1.f - (2.f * k + 1.f) * (1.f / ND);
+        const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+        float sp, cp;
+        sincosf(2.39996323f * (float)k, &sp, &cp);   // golden angle
+        const f3 d = mk(r * cp, r * sp, z);
         float t = 1e30f;
         int q = -1;
         trace_bvh(g, o, d, t, q, flags);
-        if (q != -1) {
-            clr = fminf(clr, t);
-            if (t < diag) enc += 1.f;
-            const float4 n4 = __ldg(g.STN + (-2 - q));
-            if (n4.x * d.x + n4.y * d.y + n4.z * d.z > 0.f && !(__float_as_int(n4.w) & 1)) back += 1.f;
-        }
+        if (q == -1) continue;
+        ++hits;
+        clr = fminf(clr, t);
+        const float4 n4 = __ldg(g.STN + (-2 - q));
+        if (n4.x * d.x + n4.y * d.y + n4.z * d.z > 0.f && !(__float_as_int(n4.w) & 1)) ++behind;
     }
     out[3 * i] = clr;
-    out[3 * i + 1] = enc / ND;
-    out[3 * i + 2] = back / ND;
+    out[3 * i + 1] = (float)hits / ND;
+    out[3 * i + 2] = (float)behind / ND;
 }
 
-cudaError_t probe_free_space(const DStatic& g, const float* C, int nc, float diag, float* out, unsigned* flags, cudaStream_t st) {
-    k_free_space<<<(nc + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(g, C, nc, diag, out, flags);
+cudaError_t prep_probe(const DStatic& g, const float* C, int nc, float diag, float* out, unsigned* flags, cudaStream_t st) {
+    (void)diag;
+    k_prep_probe<<<(nc + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(g, C, nc, out, flags);
     return cudaGetLastError();
 }
 

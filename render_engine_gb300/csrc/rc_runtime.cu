@@ -138,7 +138,7 @@ struct rc_ctx {
     double cache_bytes = 0;
     long long launches = 0;
     // device guard words: [0] raised by the run's kernels (read and cleared by rc_device_flags),
-    // [1] by one-shot calls that trace (rc_trace_rays, the preparation's probes), [2] the loader's checks
+    // [1] by one-shot calls that trace (rc_trace_rays), [2] the loader's checks
     unsigned* flags_dev = nullptr;
     float* img = nullptr;
     size_t img_cap = 0;
@@ -2109,42 +2109,6 @@ rc_status ctx_fail(rc_ctx* ctx, rc_status s, const char* fmt, ...) {
     va_end(a);
     if (ctx) ctx->err = buf;
     return s;
-}
-
-// the free-space probe of the scene preparation over a BVH not yet in any scene
-rc_status ctx_probe_free_space(rc_ctx* ctx, const std::vector<float>& ST, const std::vector<float>& STN, const float* BN, int nnodes,
-                               const std::vector<float>& C, float diag, std::vector<float>& out) {
-    CKR(cudaSetDevice(ctx->cfg.device));
-    std::vector<DevBuf> tmp;
-    struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
-    const float *dST = nullptr, *dSTN = nullptr, *dBN = nullptr, *dC = nullptr;
-    float* dO = nullptr;
-    rc_status s;
-    if ((s = dput(ctx, tmp, &dST, ST)) || (s = dput(ctx, tmp, &dSTN, STN)) ||
-        (s = dput(ctx, tmp, &dBN, std::vector<float>(BN, BN + 8 * (size_t)nnodes))) || (s = dput(ctx, tmp, &dC, C)) ||
-        (s = dalloc(ctx, tmp, &dO, C.size())))
-        return s;
-    float4* dST4 = nullptr;
-    if ((s = dalloc(ctx, tmp, &dST4, 3 * (ST.size() / 9)))) return s;
-    k_load_tri4<<<load_grid(ST.size() / 9), 256, 0, ctx->stream>>>(dST, dST4, ST.size() / 9);
-    CKR(cudaGetLastError());
-    DStatic g{};
-    g.ST = dST;
-    g.ST4 = dST4;
-    g.STN = reinterpret_cast<const float4*>(dSTN);
-    g.BN = reinterpret_cast<const float4*>(dBN);
-    g.has_bvh = 1;
-    g.nnodes = nnodes;
-    g.max_visits = 4 * nnodes + 64;
-    CKR(cudaMemsetAsync(ctx->flags_dev + 1, 0, 4, ctx->stream));
-    CKR(probe_free_space(g, dC, (int)(C.size() / 3), diag, dO, ctx->flags_dev + 1, ctx->stream));
-    out.resize(C.size());
-    unsigned flags = 0;
-    CKR(cudaMemcpyAsync(out.data(), dO, out.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    CKR(cudaMemcpyAsync(&flags, ctx->flags_dev + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    CKR(cudaStreamSynchronize(ctx->stream));
-    if (flags) return fail(ctx, RC_ERR_DEVICE, "prep: BVH traversal guard tripped (flags %u)", flags);
-    return RC_OK;
 }
 
 }  // namespace rc

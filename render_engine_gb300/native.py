@@ -40,7 +40,7 @@ EXPORTS = [
     "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
     "rc_state_array_copy", "rc_probe_rays", "rc_trace_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
     "rc_error_sums_noalloc", "rc_reference_build", "rc_adjoint", "rc_adjoint_arrays", "rc_taa_begin", "rc_taa_frame",
-    "rc_taa_array_copy", "rc_prep_mesh",
+    "rc_taa_array_copy", "rc_prep_mesh", "rc_prep_mesh_params",
 ]
 NOALLOC_MAX_POINTS = 4194304
 
@@ -163,6 +163,8 @@ def load_library():
     L.rc_adjoint_arrays.argtypes = [vp, vp, vp, vp]
     L.rc_prep_mesh.restype = i
     L.rc_prep_mesh.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, i, ctypes.POINTER(PrepReport)]
+    L.rc_prep_mesh_params.restype = i
+    L.rc_prep_mesh_params.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(PrepParams), ctypes.POINTER(PrepReport)]
     L.rc_taa_begin.restype = i
     L.rc_taa_begin.argtypes = [vp, ctypes.POINTER(TaaMethod), i, u32]
     L.rc_taa_frame.restype = i
@@ -191,7 +193,11 @@ class PrepReport(ctypes.Structure):
     _fields_ = [("triangles", ctypes.c_int), ("np", ctypes.c_int), ("zones", ctypes.c_int), ("bvh_nodes", ctypes.c_int),
                 ("ns", ctypes.c_int), ("cell_m", ctypes.c_float), ("diag_m", ctypes.c_float), ("cube_m", ctypes.c_float),
                 ("valid_fraction", ctypes.c_double), ("noise", ctypes.c_double * 8), ("iterations", ctypes.c_int * 8),
-                ("lights", (ctypes.c_float * 3) * 3), ("seconds", ctypes.c_double)]
+                ("nl", ctypes.c_int), ("bvh_depth", ctypes.c_int), ("lights", (ctypes.c_float * 3) * 32), ("seconds", ctypes.c_double)]
+
+
+class PrepParams(ctypes.Structure):
+    _fields_ = [("target_points", ctypes.c_int), ("lamps", ctypes.c_int), ("seed", ctypes.c_uint32)]
 
 
 class AdjointParams(ctypes.Structure):
@@ -415,14 +421,16 @@ class Context:
         self._chk(self.L.rc_adjoint_arrays(self.h, L.ctypes.data, u.ctypes.data, h.ctypes.data))
         return L, u, h
 
-    def prep_mesh(self, mesh_path: str, scene_path: str, points: int = 300000) -> dict:
-        """Prepare a format-3 scene from an MSH1 mesh (rc_prep_mesh); the scene stays loaded."""
+    def prep_mesh(self, mesh_path: str, scene_path: str, points: int = 300000, lamps: int = 3, seed: int = 1) -> dict:
+        """Prepare a format-3 scene from an MSH1 mesh (rc_prep_mesh_params); the scene stays loaded."""
         r = PrepReport()
-        self._chk(self.L.rc_prep_mesh(self.h, mesh_path.encode(), scene_path.encode(), points, ctypes.byref(r)))
+        p = PrepParams(points, lamps, seed & 0xFFFFFFFF)
+        self._chk(self.L.rc_prep_mesh_params(self.h, mesh_path.encode(), scene_path.encode(), ctypes.byref(p), ctypes.byref(r)))
         self.info()
-        return {"triangles": r.triangles, "np": r.np, "zones": r.zones, "bvh_nodes": r.bvh_nodes, "cell_m": r.cell_m,
-                "diag_m": r.diag_m, "cube_m": r.cube_m, "valid_fraction": r.valid_fraction, "noise": list(r.noise[:r.ns]),
-                "iterations": list(r.iterations[:r.ns]), "lights": [list(r.lights[l]) for l in range(3)], "seconds": r.seconds}
+        return {"triangles": r.triangles, "np": r.np, "zones": r.zones, "bvh_nodes": r.bvh_nodes, "bvh_depth": r.bvh_depth,
+                "cell_m": r.cell_m, "diag_m": r.diag_m, "cube_m": r.cube_m, "valid_fraction": r.valid_fraction,
+                "noise": list(r.noise[:r.ns]), "iterations": list(r.iterations[:r.ns]),
+                "lights": [list(r.lights[l]) for l in range(r.nl)], "seconds": r.seconds}
 
     def taa_begin(self, alpha: float, gamma: float, mask: int, s0: int, seed: int):
         """Start a run of the taa mode (rc_taa_begin)."""

@@ -99,6 +99,12 @@ def write(scene: Scene) -> bytes:
     return b.getvalue()
 
 
+def header(data: bytes) -> dict:
+    """The eight header integers of a scene file."""
+    h = np.frombuffer(data, dtype=np.int32, count=8)
+    return dict(zip(("np", "nq", "nt", "ns", "nl", "nr", "has_ref", "fmt"), (int(x) for x in h)))
+
+
 def read(data: bytes) -> Scene:
     off = 0
 

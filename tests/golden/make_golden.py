@@ -2,6 +2,7 @@
 
 Reads, from the reference (falcon123212/render_engine):
   cuda/scenes/scene_main.bin, cuda/scenes/scene_stress.bin     (its box-scene fixtures)
+  cuda/scenes/scene_scale_1M.bin.gz                            (its 1,082,802-point timing scene)
   reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl    (its published RTX 4060
       per-frame error curves: `poc_gpu_l3 scen scene_main.bin 10` and
       `poc_gpu_l8 scenf scene_stress.bin 10 scenarios_stress.txt`)
@@ -37,6 +38,8 @@ for name in ("scene_main.bin", "scene_stress.bin"):
     with open(os.path.join(REF, "cuda", "scenes", name), "rb") as f, gzip.open(os.path.join(HERE, name + ".gz"), "wb", 9) as g:
         shutil.copyfileobj(f, g)
 shutil.copy(os.path.join(REF, "cuda", "scenes", "scenarios_stress.txt"), os.path.join(HERE, "scenarios_stress.txt"))
+# the reference's 1,082,802-point timing scene (its throughput case, cuda/run_cuda.sh), already gzip
+shutil.copy(os.path.join(REF, "cuda", "scenes", "scene_scale_1M.bin.gz"), os.path.join(HERE, "scene_scale_1M.bin.gz"))
 json.dump({"mode": "scen", "seed0": 2000, "nseeds": 10, "rows": curves(os.path.join(REF, "reference", "cuda_rtx4060", "scen_main.jsonl"))},
           open(os.path.join(HERE, "golden_scen_main.json"), "w"))
 json.dump({"mode": "scenf", "seed0": 3000, "nseeds": 10, "rows": curves(os.path.join(REF, "reference", "cuda_rtx4060", "scen_stress.jsonl"))},
