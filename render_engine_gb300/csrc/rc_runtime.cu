@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -47,12 +48,44 @@ constexpr int PRE_K = 4;          // rays per point traced ahead on static-mesh 
 struct DevBuf {
     void* p = nullptr;
     size_t n = 0;
+    cudaStream_t s = nullptr;   // the stream the buffer was allocated on (and is freed on)
 };
+
+// Device memory of contexts comes from one stream-ordered pool per device that keeps the pages
+// it has mapped (release threshold: never): a context that is destroyed and created again, or
+// a scene loaded after another, reuses them instead of mapping fresh memory (mapping costs
+// about as much as copying the scene).
+cudaMemPool_t device_pool(int dev) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+        cudaMemPoolProps pp{};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.handleTypes = cudaMemHandleTypeNone;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        if (cudaMemPoolCreate(&p, &pp) != cudaSuccess) return nullptr;
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        pools[dev] = p;
+    }
+    return pools[dev];
+}
 
 struct HostState {
     std::vector<float> inten;
     const float* pw = nullptr;      // device warm start (padded cache layout)
     DState d{};
+    // Built on first use (ensure_state): until then the state's positions, normals and warm
+    // start wait on the device as the file lays them out (xyz triples, NL floats per point).
+    bool built = false;             // build issued (on the side stream, or on the context's stream)
+    bool wait = false;              // the context's stream has yet to wait for the side stream's build
+    const float* raw = nullptr;     // 6 Np floats (P, N) then NL Np (Pw, scenes with references)
+    const float* dint = nullptr;    // device light intensities
+    size_t raw_buf = 0;             // index of the raw buffer in the scene's pool
 };
 
 struct Scene {
@@ -124,6 +157,8 @@ struct rc_ctx {
         int stride = 0, npaths = 0;
         cudaEvent_t ready = nullptr;
     } cam;
+    cudaStream_t side = nullptr;                // state builds after a load (issue_state_builds)
+    std::vector<cudaEvent_t> state_ev;          // per state: its build on the side stream is done
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
     int adj_cap_np = 0, adj_cap_k = 0, adj_cap_nl = 0;   // sizes the adjoint buffers were allocated for
     float4* adj_aeu = nullptr;                  // unit-emission direct light of the last adjoint
@@ -165,13 +200,18 @@ rc_status fail(rc_ctx* ctx, rc_status s, const char* fmt, ...) {
         if (e_ != cudaSuccess) return fail(ctx, RC_ERR_CUDA, "CUDA %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
+// A buffer of n elements from the device's pool, ordered on the context's stream (usable on it
+// at once, on other streams after they wait for it).
 template <class T>
-rc_status dalloc(rc_ctx* ctx, std::vector<DevBuf>& pool, T** out, size_t n) {
+rc_status dalloc(rc_ctx* ctx, std::vector<DevBuf>& pool, T** out, size_t n, cudaStream_t on = nullptr) {
     void* p = nullptr;
     size_t bytes = n * sizeof(T) + 16;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e != cudaSuccess) return fail(ctx, RC_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
-    pool.push_back({p, bytes});
+    cudaMemPool_t mp = device_pool(ctx->cfg.device);
+    if (!mp) return fail(ctx, RC_ERR_CUDA, "no memory pool on device %d", ctx->cfg.device);
+    cudaStream_t st = on ? on : ctx->stream;
+    cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, mp, st);
+    if (e != cudaSuccess) return fail(ctx, RC_ERR_NOMEM, "device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
+    pool.push_back({p, bytes, st});
     *out = (T*)p;
     return RC_OK;
 }
@@ -184,8 +224,10 @@ rc_status dput(rc_ctx* ctx, std::vector<DevBuf>& pool, const T** out, const std:
     *out = p;
     return RC_OK;
 }
+// Back to the device's pool once the work queued on the buffer's stream so far is done.
 void free_pool(std::vector<DevBuf>& pool) {
-    for (auto& b : pool) cudaFree(b.p);
+    for (auto& b : pool)
+        if (b.p) cudaFreeAsync(b.p, b.s);
     pool.clear();
 }
 
@@ -539,11 +581,6 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     // the load has read the result back)
     k_load_check<<<load_grid(Np), 256, 0, ctx->stream>>>(g.region, Np, 0, S.NR, ctx->flags_dev + 2, LOAD_BAD_REGION);
     CKR(cudaGetLastError());
-    // staging for one state's per-point arrays as they lie in the file
-    float* stage = nullptr;
-    std::vector<DevBuf> stage_pool;
-    struct StageFree { std::vector<DevBuf>& p; ~StageFree() { free_pool(p); } } stage_free{stage_pool};
-    if ((s = dalloc(ctx, stage_pool, &stage, (size_t)(6 + (S.has_ref ? NL : 0)) * Np))) return s;
     S.st.resize(S.NS);
     for (int k = 0; k < S.NS; ++k) {
         HostState& hs = S.st[k];
@@ -576,44 +613,29 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         DState& d = hs.d;
         memset(&d, 0, sizeof d);
         if ((s = dput(ctx, pool, &d.Q, Q)) || (s = dput(ctx, pool, &d.dims, dims)) || (s = dput(ctx, pool, &d.off, off)) ||
-            (s = dput(ctx, pool, &d.tri, tri)) || (s = dput(ctx, pool, &d.grp, G.grp)) || (s = dput(ctx, pool, &d.misc, G.misc)))
+            (s = dput(ctx, pool, &d.tri, tri)) || (s = dput(ctx, pool, &d.grp, G.grp)) || (s = dput(ctx, pool, &d.misc, G.misc)) ||
+            (s = dput(ctx, pool, &hs.dint, hs.inten)))
             return s;
         {
-            // positions and normals: xyz triples copied as they are, packed to float4 on the device
-            float4 *P4 = nullptr, *N4 = nullptr;
-            if ((s = dalloc(ctx, pool, &P4, Np)) || (s = dalloc(ctx, pool, &N4, Np))) return s;
-            CKR(cudaMemcpyAsync(stage, P, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
-            CKR(cudaMemcpyAsync(stage + 3 * Np, N, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
-            k_load_pack4<<<load_grid(Np), 256, 0, ctx->stream>>>(stage, P4, Np);
-            k_load_pack4<<<load_grid(Np), 256, 0, ctx->stream>>>(stage + 3 * Np, N4, Np);
-            CKR(cudaGetLastError());
-            d.P4 = P4;
-            d.N4 = N4;
+            // the per-point arrays are copied now (the caller's buffer is not kept) and re-laid
+            // out when the state is first used
+            float* raw = nullptr;
+            const size_t nraw = (size_t)(6 + (S.has_ref ? NL : 0)) * Np;
+            if ((s = dalloc(ctx, pool, &raw, nraw))) return s;
+            hs.raw_buf = pool.size() - 1;
+            CKR(cudaMemcpyAsync(raw, P, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
+            CKR(cudaMemcpyAsync(raw + 3 * Np, N, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
+            if (S.has_ref) CKR(cudaMemcpyAsync(raw + 6 * Np, Pw, 4 * (size_t)NL * Np, cudaMemcpyHostToDevice, ctx->stream));
+            hs.raw = raw;
         }
-        if (S.has_ref) {
+        if (S.has_ref)
             if ((s = dput_raw(ctx, pool, &d.ref, ref, Np)) || (s = dput_raw(ctx, pool, &d.valid, valid, Np))) return s;
-            // warm start of every run beginning in this state (poc_gpu.cu:832), padded like the cache
-            float* pw = nullptr;
-            if ((s = dalloc(ctx, pool, &pw, (size_t)lcs_of(NL) * Np))) return s;
-            CKR(cudaMemcpyAsync(stage + 6 * Np, Pw, 4 * (size_t)NL * Np, cudaMemcpyHostToDevice, ctx->stream));
-            k_load_pad<<<load_grid(Np), 256, 0, ctx->stream>>>(stage + 6 * Np, pw, Np, NL, lcs_of(NL));
-            CKR(cudaGetLastError());
-            hs.pw = pw;
-        }
         d.nt = S.Nt;
         d.ng = G.gr.g0[3];
         d.nmisc = (int)G.misc.size();
         d.gr = G.gr;
         size_t smem = frame_smem_bytes(d);
         if (smem > 200 * 1024) return fail(ctx, RC_ERR_UNSUPPORTED, "%d dynamic triangles exceed shared memory", S.Nt);
-        float4* AE = nullptr;
-        uint32_t* SV = nullptr;
-        if ((s = dalloc(ctx, pool, &AE, (size_t)aes_of(NL) / 4 * Np)) || (s = dalloc(ctx, pool, &SV, (size_t)NW * Np))) return s;
-        const float* dint = nullptr;
-        if ((s = dput(ctx, pool, &dint, hs.inten))) return s;
-        CKR(RC_DISPATCH(NL, build(NW, d, g, S.grid, dL, dint, AE, SV, S.Np, ctx->flags_dev, ctx->stream)));
-        d.AE = AE;
-        d.SV = SV;
     }
     const int npairs = S.NS * S.NS;
     S.ev.resize((size_t)npairs * (1 + NL));
@@ -652,6 +674,93 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
 }  // namespace
 
 namespace {
+
+// A state's device build: positions and normals packed to float4, the warm start padded like
+// the cache, the direct light and shadow-voxel masks (k_build); the raw copy is then released.
+// Issued on stream `st`.
+rc_status build_state(rc_ctx* ctx, int k, cudaStream_t st) {
+    Scene& S = ctx->S;
+    HostState& hs = S.st[k];
+    const int NL = S.NL, NW = ctx->NW;
+    const size_t Np = (size_t)S.Np;
+    auto& pool = ctx->scene_bufs;
+    DState& d = hs.d;
+    float4 *P4 = nullptr, *N4 = nullptr, *AE = nullptr;
+    uint32_t* SV = nullptr;
+    rc_status s;
+    if ((s = dalloc(ctx, pool, &P4, Np, st)) || (s = dalloc(ctx, pool, &N4, Np, st)) ||
+        (s = dalloc(ctx, pool, &AE, (size_t)aes_of(NL) / 4 * Np, st)) || (s = dalloc(ctx, pool, &SV, (size_t)NW * Np, st)))
+        return s;
+    k_load_pack4<<<load_grid(Np), 256, 0, st>>>(hs.raw, P4, Np);
+    k_load_pack4<<<load_grid(Np), 256, 0, st>>>(hs.raw + 3 * Np, N4, Np);
+    CKR(cudaGetLastError());
+    d.P4 = P4;
+    d.N4 = N4;
+    if (S.has_ref) {
+        // warm start of every run beginning in this state (poc_gpu.cu:832), padded like the cache
+        float* pw = nullptr;
+        if ((s = dalloc(ctx, pool, &pw, (size_t)lcs_of(NL) * Np, st))) return s;
+        k_load_pad<<<load_grid(Np), 256, 0, st>>>(hs.raw + 6 * Np, pw, Np, NL, lcs_of(NL));
+        CKR(cudaGetLastError());
+        hs.pw = pw;
+    }
+    CKR(RC_DISPATCH(NL, build(NW, d, S.g, S.grid, S.L, hs.dint, AE, SV, S.Np, ctx->flags_dev, st)));
+    d.AE = AE;
+    d.SV = SV;
+    DevBuf& rb = pool[hs.raw_buf];
+    if (rb.p == hs.raw) {
+        cudaFreeAsync(rb.p, st);
+        rb.p = nullptr;
+        rb.n = 0;
+    }
+    hs.raw = nullptr;
+    hs.built = true;
+    ctx->launches += 3 + (S.has_ref ? 1 : 0);
+    return RC_OK;
+}
+// Before the context's stream uses state k: wait for its build on the side stream, or build it.
+rc_status ensure_state(rc_ctx* ctx, int k) {
+    Scene& S = ctx->S;
+    if (k < 0 || k >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", k);
+    HostState& hs = S.st[k];
+    if (hs.built) {
+        if (hs.wait) {
+            CKR(cudaStreamWaitEvent(ctx->stream, ctx->state_ev[k], 0));
+            hs.wait = false;
+        }
+        return RC_OK;
+    }
+    return build_state(ctx, k, ctx->stream);
+}
+rc_status ensure_all_states(rc_ctx* ctx) {
+    for (int k = 0; k < ctx->S.NS; ++k) {
+        rc_status s = ensure_state(ctx, k);
+        if (s != RC_OK) return s;
+    }
+    return RC_OK;
+}
+// After a load: every state's build issued on the side stream behind the load's copies, in
+// state order, each followed by an event that the context's stream waits for at first use.
+// The builds overlap whatever the context's stream does next (the first frames, mostly).
+rc_status issue_state_builds(rc_ctx* ctx) {
+    Scene& S = ctx->S;
+    if (!ctx->side) CKR(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    while ((int)ctx->state_ev.size() < S.NS) {
+        cudaEvent_t e = nullptr;
+        CKR(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->state_ev.push_back(e);
+    }
+    cudaEvent_t copies = ctx->state_ev[0];
+    CKR(cudaEventRecord(copies, ctx->stream));
+    CKR(cudaStreamWaitEvent(ctx->side, copies, 0));
+    for (int k = 0; k < S.NS; ++k) {
+        rc_status s = build_state(ctx, k, ctx->side);
+        if (s != RC_OK) return s;
+        CKR(cudaEventRecord(ctx->state_ev[k], ctx->side));
+        S.st[k].wait = true;
+    }
+    return RC_OK;
+}
 
 rc_status alloc_cache(rc_ctx* ctx) {
     free_pool(ctx->cache_bufs);
@@ -699,15 +808,15 @@ rc_status ensure_err(rc_ctx* ctx, size_t frames) {
     if (frames <= ctx->err_cap) return RC_OK;
     size_t cap = std::max<size_t>(1024, frames * 2);
     double* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, cap * 3 * sizeof(double));
-    if (e != cudaSuccess) return fail(ctx, RC_ERR_NOMEM, "error buffer: %s", cudaGetErrorString(e));
+    std::vector<DevBuf> fresh;
+    rc_status s = dalloc(ctx, fresh, &p, cap * 3);
+    if (s != RC_OK) return s;
     if (ctx->c.err) {
         CKR(cudaMemcpyAsync(p, ctx->c.err, ctx->err_cap * 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-        CKR(cudaStreamSynchronize(ctx->stream));
         for (auto it = ctx->cache_bufs.begin(); it != ctx->cache_bufs.end(); ++it)
-            if (it->p == ctx->c.err) { cudaFree(it->p); ctx->cache_bufs.erase(it); break; }
+            if (it->p == ctx->c.err) { cudaFreeAsync(it->p, it->s); ctx->cache_bufs.erase(it); break; }
     }
-    ctx->cache_bufs.push_back({p, cap * 3 * sizeof(double)});
+    ctx->cache_bufs.push_back(fresh[0]);
     ctx->c.err = p;
     ctx->err_cap = cap;
     return RC_OK;
@@ -930,6 +1039,7 @@ FrameParams base_params(rc_ctx* ctx) {
 }
 
 rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
+    if (rc_status es = ensure_state(ctx, si)) return es;
     Scene& S = ctx->S;
     Run& R = ctx->run;
     const rc_method& M = R.M;
@@ -1153,6 +1263,7 @@ rc_status rc_create(const rc_config* cfg, rc_ctx** out) {
 void rc_destroy(rc_ctx* ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
     free_pool(ctx->cache_bufs);
     free_pool(ctx->scene_bufs);
     free_pool(ctx->adj_bufs);
@@ -1164,6 +1275,8 @@ void rc_destroy(rc_ctx* ctx) {
     if (ctx->stage) cudaFree(ctx->stage);
     if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->state_ev) cudaEventDestroy(e);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1190,6 +1303,7 @@ rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
     if (!ctx || !data) return RC_ERR_ARG;
     CKR(cudaSetDevice(ctx->cfg.device));
     CKR(cudaStreamSynchronize(ctx->stream));
+    if (ctx->side) CKR(cudaStreamSynchronize(ctx->side));
     free_pool(ctx->cache_bufs);
     free_pool(ctx->scene_bufs);
     free_pool(ctx->adj_bufs);
@@ -1204,12 +1318,14 @@ rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
     rc_status s = load_scene(ctx, (const uint8_t*)data, nbytes);
     // copies from the caller's buffer may still be in flight after a failed load
     if (s != RC_OK) { cudaStreamSynchronize(ctx->stream); free_pool(ctx->scene_bufs); return s; }
-    double b = 0;
-    for (auto& x : ctx->scene_bufs) b += (double)x.n;
-    ctx->S.scene_bytes = b;
     if ((s = alloc_cache(ctx)) != RC_OK) return s;
     CKR(cudaStreamSynchronize(ctx->stream));
     ctx->have_scene = true;
+    // the states' device builds run behind the load on the side stream
+    if ((s = issue_state_builds(ctx)) != RC_OK) { ctx->have_scene = false; return s; }
+    double b = 0;
+    for (auto& x : ctx->scene_bufs) b += (double)x.n;
+    ctx->S.scene_bytes = b;
     return RC_OK;
 }
 
@@ -1254,6 +1370,8 @@ rc_status rc_run_begin(rc_ctx* ctx, const rc_method* m, int s0, uint32_t seed) {
     Scene& S = ctx->S;
     if (s0 < 0 || s0 >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", s0);
     if (!(m->rays > 0.f)) return fail(ctx, RC_ERR_ARG, "rays must be > 0");
+    rc_status es = ensure_state(ctx, s0);
+    if (es != RC_OK) return es;
     Run& R = ctx->run;
     R = Run{};
     R.M = *m;
@@ -1326,6 +1444,7 @@ rc_status rc_run(rc_ctx* ctx, const rc_method* m, const int* seq, int nframes, u
 rc_status rc_sync(rc_ctx* ctx) {
     if (!ctx) return RC_ERR_ARG;
     CKR(cudaStreamSynchronize(ctx->stream));
+    if (ctx->side) CKR(cudaStreamSynchronize(ctx->side));
     return RC_OK;
 }
 
@@ -1363,6 +1482,7 @@ rc_status rc_render(rc_ctx* ctx, int state, const rc_camera* cam, float* image, 
         return fail(ctx, RC_ERR_ARG, "bad camera");
     const size_t npx = (size_t)cam->width * cam->height;
     if (image && image_floats != npx) return fail(ctx, RC_ERR_ARG, "image holds %zu floats, not %zu", image_floats, npx);
+    if (rc_status es = ensure_state(ctx, state)) return es;
     if (npx > ctx->img_cap) {
         if (ctx->img) { CKR(cudaStreamSynchronize(ctx->stream)); cudaFree(ctx->img); ctx->img = nullptr; }
         cudaError_t e = cudaMalloc(&ctx->img, npx * sizeof(float));
@@ -1530,6 +1650,7 @@ rc_status rc_state_array_copy(rc_ctx* ctx, int state, int which, void* host, siz
     const Scene& S = ctx->S;
     if (state < 0 || state >= S.NS) return RC_ERR_ARG;
     const size_t Np = (size_t)S.Np, NL = (size_t)S.NL, AES = (size_t)aes_of(S.NL);
+    if (rc_status es = ensure_state(ctx, state)) return es;
     const DState& d = S.st[state].d;
     cudaStream_t st = ctx->stream;
     switch (which) {
@@ -1573,6 +1694,7 @@ rc_status rc_probe_rays(rc_ctx* ctx, int state, const int* points, int npoints, 
     if (state < 0 || state >= S.NS) return RC_ERR_ARG;
     *nrec = 0;
     if (npoints == 0) return RC_OK;
+    if (rc_status es = ensure_state(ctx, state)) return es;
     int* dpts = nullptr;
     int* dn = nullptr;
     void* drec = nullptr;
@@ -1603,6 +1725,7 @@ rc_status rc_trace_rays(rc_ctx* ctx, int state, const float* rays, int nrays, in
     if (state < 0 || state >= S.NS) return RC_ERR_ARG;
     if (nrays == 0) return RC_OK;
     CKR(cudaSetDevice(ctx->cfg.device));
+    if (rc_status es = ensure_state(ctx, state)) return es;
     std::vector<DevBuf> tmp;
     struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
     float* dr = nullptr;
@@ -1661,6 +1784,7 @@ rc_status rc_reference_build(rc_ctx* ctx, const rc_ref_params* prm, double* nois
     const size_t Np = (size_t)S.Np;
     const int NL = S.NL, LCS = lcs_of(NL);
     cudaStream_t st = ctx->stream;
+    if (rc_status es = ensure_all_states(ctx)) return es;
     // the references change: a taa run recomputes its per-state error denominators
     std::fill(ctx->taa.have_sums.begin(), ctx->taa.have_sums.end(), (char)0);
     std::vector<DevBuf> tmp;
@@ -1760,6 +1884,7 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
     if ((long long)S.Np * prm->K >= (1ll << 31)) return fail(ctx, RC_ERR_ARG, "Np * K must stay below 2^31");
     if (S.NL + 1 > adj::MAX_COLS) return fail(ctx, RC_ERR_UNSUPPORTED, "%d lights", S.NL);
     CKR(cudaSetDevice(ctx->cfg.device));
+    if (rc_status es = ensure_state(ctx, prm->state)) return es;
     cudaStream_t st = ctx->stream;
     const size_t Np = (size_t)S.Np, K = (size_t)prm->K;
     const int NL = S.NL, AES = aes_of(NL), iters = prm->iterations ? prm->iterations : 64;
@@ -1856,6 +1981,7 @@ rc_status rc_taa_begin(rc_ctx* ctx, const rc_taa_method* m, int first_state, uin
     if (first_state < 0 || first_state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", first_state);
     CKR(cudaSetDevice(ctx->cfg.device));
     rc_status s;
+    if ((s = ensure_state(ctx, first_state))) return s;
     if (!ctx->taa.x && (s = taa_alloc(ctx))) return s;
     TaaRun& t = ctx->taa;
     const size_t Np = (size_t)S.Np, NW = (size_t)ctx->NW;
@@ -1885,6 +2011,7 @@ rc_status rc_taa_frame(rc_ctx* ctx, int state, float* err) {
     if (!t.active) return fail(ctx, RC_ERR_STATE, "no taa run begun");
     const Scene& S = ctx->S;
     if (state < 0 || state >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", state);
+    if (rc_status es = ensure_state(ctx, state)) return es;
     const int Np = S.Np, NW = ctx->NW, f = t.f;
     const size_t nbytes_mask = (size_t)NW * Np * 4;
     cudaStream_t st = ctx->stream;
@@ -1998,6 +2125,7 @@ rc_status rc_hg_camera_paths(rc_hg* hg, rc_ctx* ctx, int state, const rc_hg_path
     auto& C = ctx->cam;
     CKR(cudaSetDevice(ctx->cfg.device));
     cudaStream_t hs = rc::hg_stream(hg);
+    if ((st = ensure_state(ctx, state))) return st;
     if (nslots > C.slots_cap || npix > C.pix_cap) {
         CKR(cudaStreamSynchronize(hs));
         CKR(cudaStreamSynchronize(ctx->stream));
@@ -2117,6 +2245,7 @@ extern "C" {
 
 rc_status rc_device_flags(rc_ctx* ctx, unsigned* flags) {
     if (!ctx || !flags) return RC_ERR_ARG;
+    if (ctx->side) CKR(cudaStreamSynchronize(ctx->side));   // state builds raise guards too
     CKR(cudaMemcpyAsync(flags, ctx->flags_dev, 4, cudaMemcpyDeviceToHost, ctx->stream));
     CKR(cudaMemsetAsync(ctx->flags_dev, 0, 4, ctx->stream));
     CKR(cudaStreamSynchronize(ctx->stream));

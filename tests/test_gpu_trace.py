@@ -99,7 +99,8 @@ def test_trace_rays_keeps_frame_guard_flags():
     v0 = V[:, 0:3]
     pts = np.concatenate([v0, v0 + V[:, 3:6], v0 + V[:, 6:9]])
     sc.mesh["BN"] = _dag_tree(pts.min(0) - 0.01, pts.max(0) + 0.01)
-    ctx = _gpu(S.write(sc), 0)       # the state build's shadow rays trip the guard (word of the run)
+    ctx = _gpu(S.write(sc), 0)       # the state builds' shadow rays trip the guard (word of the run)
+    ctx.sync()                       # the builds run behind the load
     p, t = ctx.trace_rays(0, np.array([[5.0, 5.0, 50.0, 0.0, 0.0, 1.0]], np.float32))   # misses the root box
     assert p[0] == -1 and np.isinf(t[0])
     assert ctx.device_flags() & 1      # FLAG_BVH_VISITS, raised before the call, survives it
