@@ -62,6 +62,8 @@ struct DevCache {
     float* rstat;              // NR x 4
     float* dstat;              // NR x 3
     float4* pre_hit;           // static-mesh scenes: hits traced ahead, PRE_K per point
+    float4* rayq;              // static-mesh scenes: the ray queue of the traced-ahead rays, 2 float4 per ray
+    unsigned* rayctr;          // [0, 8) rays per direction octant, [8, 16) octant cursors, [16] queue head
     float* sumpr;              // 2 slots
     int* npend;                // [0] current, [1] accumulator
     double* err;               // 3 doubles per frame of the run
@@ -98,6 +100,7 @@ struct FrameParams {
     float half_inv_np;         // 0.5f / Np, the float quotient the ray count uses
     const float4* pre_hit;     // rays traced ahead by k_pretrace (pre_k per point), or null
     int pre_k;
+    int wavefront;             // traced-ahead rays through the ray queue (k_trace_queue), else one thread per point
 };
 
 // Pinhole camera of the image pass: pixel (x, y) looks along
@@ -207,7 +210,7 @@ RC_NL_VALUES(X)
 #undef X
 // The group buffer: 3 float4 per group, then 3 float4 per pair of groups (pass-1 records).
 __host__ __device__ inline int grp_float4s(int ng) { return 3 * ng + 3 * (ng / 2); }
-inline size_t frame_smem_bytes(const DState& s) {
+__host__ __device__ inline size_t frame_smem_bytes(const DState& s) {
     return sizeof(float4) * (3 * (size_t)s.nt + (size_t)grp_float4s(s.ng)) + sizeof(int) * (size_t)s.nmisc + 16;
 }
 __host__ __device__ constexpr int lcs_of(int NL) { return (NL + 3) / 4 * 4; }

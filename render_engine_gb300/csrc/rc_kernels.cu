@@ -506,6 +506,29 @@ struct Hit {
     f3 H;
 };
 
+// The cache point a traced ray reached (poc_gpu.cu:345-358, 466-469): with h.t and h.q set,
+// fills the hit point, the point index and whether the hit counts.
+__device__ __forceinline__ void resolve_hit(const DState& s, const DStatic& g, const Grid& grid, f3 O, f3 D, int i, Hit& h) {
+    const bool hit = h.q != -1;
+    h.H = hit ? O + D * h.t : O;
+    if (!hit) { h.pi = i; h.back = true; return; }
+    if (h.q >= 0) {
+        h.pi = point_index(s, h.H, h.q);
+        const float* Q = s.Q + 12 * h.q;
+        h.back = dot(mk(__ldg(Q + 9), __ldg(Q + 10), __ldg(Q + 11)), D) > 0.f;
+        return;
+    }
+    float4 n4 = __ldg(g.STN + (-2 - h.q));
+    f3 n = mk(n4.x, n4.y, n4.z);
+    if (dot(n, D) > 0.f) {
+        if (!(__float_as_int(n4.w) & 1)) { h.pi = i; h.back = true; return; }
+        n = n * -1.f;
+    }
+    h.pi = hash_point(g, grid, h.H, n);
+    h.back = false;
+    if (h.pi < 0) { h.pi = i; h.back = true; }
+}
+
 // Trace one ray and resolve its cache point (poc_gpu.cu:340-358, 466-469).
 __device__ __forceinline__ Hit trace_resolve(const TraceSmem& sm, const DState& s, const DStatic& g, const Grid& grid,
                                              const FrameParams& p, const DevCache& c, f3 O, f3 D, int i) {
@@ -519,24 +542,7 @@ __device__ __forceinline__ Hit trace_resolve(const TraceSmem& sm, const DState& 
         if (qb != h.q || __float_as_int(tb) != __float_as_int(h.t)) atomicAdd(c.check, 1ull);
     }
     if (g.has_bvh) trace_bvh(g, O, D, h.t, h.q, c.flags);
-    const bool hit = h.q != -1;
-    h.H = hit ? O + D * h.t : O;
-    if (!hit) { h.pi = i; h.back = true; return h; }
-    if (h.q >= 0) {
-        h.pi = point_index(s, h.H, h.q);
-        const float* Q = s.Q + 12 * h.q;
-        h.back = dot(mk(__ldg(Q + 9), __ldg(Q + 10), __ldg(Q + 11)), D) > 0.f;
-        return h;
-    }
-    float4 n4 = __ldg(g.STN + (-2 - h.q));
-    f3 n = mk(n4.x, n4.y, n4.z);
-    if (dot(n, D) > 0.f) {
-        if (!(__float_as_int(n4.w) & 1)) { h.pi = i; h.back = true; return h; }
-        n = n * -1.f;
-    }
-    h.pi = hash_point(g, grid, h.H, n);
-    h.back = false;
-    if (h.pi < 0) { h.pi = i; h.back = true; }
+    resolve_hit(s, g, grid, O, D, i, h);
     return h;
 }
 
@@ -936,6 +942,246 @@ __global__ void __launch_bounds__(BLOCK, RC_PRETRACE_MINB) k_pretrace(const DSta
         const Hit h = trace_resolve(tsm, s, g, grid, p, c, O, D, i);
         out[(size_t)i * p.pre_k + r] = make_float4(h.H.x, h.H.y, h.H.z, __int_as_float(h.back ? -1 : h.pi));
     }
+}
+
+// ------------------------------------------------------------------ wavefront traversal
+// The traced-ahead rays of static-mesh scenes go through a ray queue instead of one thread per
+// point (k_pretrace above, kept behind RC_FLAG_THREAD_TRACE):
+//   k_ray_octants  counts the rays of each direction octant (warp sums, one atomic per warp and
+//                  octant);
+//   k_ray_scatter  writes every ray (origin + output slot, direction + point) into the queue,
+//                  grouped by octant: per warp and octant a warp scan of the lanes' counts and
+//                  one atomicAdd on the octant's cursor;
+//   k_trace_queue  persistent warps: a warp refills its idle lanes from the queue head with one
+//                  atomicAdd once at least WQ_REFILL of them are idle (warp ballot, rank by
+//                  popcount); each lane walks its ray in the traversal's visit order (inner
+//                  nodes until a leaf, then the leaf: Aila and Laine's while-while), its stack's
+//                  top WQ_STACK entries in shared memory, deeper ones in local memory (64 in all,
+//                  as the reference), and writes the resolved hit where k_pretrace would.
+// Same rays, same per-ray visit order and pruning: the hits equal k_pretrace's bit for bit.
+constexpr int WQ_BLOCK = 128;
+constexpr int WQ_STACK = 16;
+constexpr int WQ_REFILL = 8;
+constexpr int WQ_MAXSTACK = 64;
+
+static __device__ __forceinline__ int octant_of(f3 d) { return (d.x < 0.f ? 1 : 0) | (d.y < 0.f ? 2 : 0) | (d.z < 0.f ? 4 : 0); }
+
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_ray_octants(const DState s, const DevCache c, const FrameParams p) {
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    unsigned long long mine = 0ull;   // 8 bits per octant (at most 4 rays per lane, 128 per warp)
+    if (i < p.Np) {
+        uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
+        const bool pend = p.pend_left > 0 && c.pending[i];
+        const int k = min(ray_count(p, c, c.n[i], pend, c.sumpr[p.sum_in], c.npend[0], rs), p.pre_k);
+        const f3 N = xyz(s.N4[i]);
+        for (int r = 0; r < k; ++r) {
+            const float u1 = rnd(rs);
+            const float u2 = rnd(rs);
+            mine += 1ull << (8 * octant_of(cosine_dir(N, u1, u2)));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+    if ((threadIdx.x & 31) == 0)
+        for (int o = 0; o < 8; ++o) {
+            const unsigned n = (unsigned)((mine >> (8 * o)) & 255ull);
+            if (n) atomicAdd(c.rayctr + o, n);
+        }
+}
+
+template <int NL>
+__global__ void __launch_bounds__(BLOCK) k_ray_scatter(const DState s, const DevCache c, const FrameParams p) {
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    f3 O = mk(0.f, 0.f, 0.f);
+    f3 D[4] = {mk(0.f, 0.f, 1.f), mk(0.f, 0.f, 1.f), mk(0.f, 0.f, 1.f), mk(0.f, 0.f, 1.f)};
+    int oc[4] = {-1, -1, -1, -1};   // -1: no ray (lanes past the last point write nothing)
+    if (i < p.Np) {
+        uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
+        const bool pend = p.pend_left > 0 && c.pending[i];
+        const int k = min(ray_count(p, c, c.n[i], pend, c.sumpr[p.sum_in], c.npend[0], rs), p.pre_k);
+        const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]);
+        O = P + N * 1e-3f;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            if (r < k) {
+                const float u1 = rnd(rs);
+                const float u2 = rnd(rs);
+                D[r] = cosine_dir(N, u1, u2);
+                oc[r] = octant_of(D[r]);
+            }
+    }
+    const unsigned cap = (unsigned)(p.Np * p.pre_k);
+    unsigned start = 0;   // the octant's first queue position
+#pragma unroll 1
+    for (int o = 0; o < 8; ++o) {
+        int n = 0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) n += oc[r] == o;
+        int x = n;   // warp inclusive scan
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, x, 31);
+        unsigned base = 0;
+        if (lane == 31 && total) base = atomicAdd(c.rayctr + 8 + o, (unsigned)total);
+        unsigned at = __shfl_sync(0xffffffffu, base, 31) + start + (unsigned)(x - n);
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            if (oc[r] == o && at < cap) {
+                c.rayq[2 * (size_t)at] = make_float4(O.x, O.y, O.z, __int_as_float(i * p.pre_k + r));
+                c.rayq[2 * (size_t)at + 1] = make_float4(D[r].x, D[r].y, D[r].z, __int_as_float(i));
+                ++at;
+            }
+        start += __ldcg(c.rayctr + o);
+    }
+}
+
+template <bool WT>
+__global__ void __launch_bounds__(WQ_BLOCK) k_trace_queue(const DState s, const DStatic g, const Grid grid, const DevCache c,
+                                                          const FrameParams p, float4* __restrict__ out) {
+    extern __shared__ float4 sm[];
+    stage_smem(sm, s);
+    __syncthreads();
+    const TraceSmem tsm = smem_view(sm, s);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int dyn4 = (int)((frame_smem_bytes(s) + 15) / 16);
+    int2* sstk = reinterpret_cast<int2*>(sm + dyn4) + warp * (WQ_STACK * 32) + lane;   // entry e at sstk[32 e]
+    int2 deep[WQ_MAXSTACK - WQ_STACK];
+    unsigned nrays = 0;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) nrays += __ldcg(c.rayctr + o);
+    const unsigned lt = (1u << lane) - 1u;
+    const float fs = WT ? __int_as_float(0x3f800004) : 1.f;
+    bool active = false, drained = false;
+    f3 O = mk(0.f, 0.f, 0.f), D = mk(0.f, 0.f, 1.f), inv = mk(0.f, 0.f, 0.f);
+    float tmin = 0.f;
+    int q = -1, lf = 0, cnt = 0, sp = 0, visits = 0, slot = 0, pt = 0;
+    WtRay wr{};
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (!drained && __popc(idle) >= WQ_REFILL) {
+            const int leader = __ffs(idle) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(c.rayctr + 16, (unsigned)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            drained = base + (unsigned)__popc(idle) >= nrays;
+            if (!active) {
+                const unsigned r = base + (unsigned)__popc(idle & lt);
+                if (r < nrays) {
+                    const float4 a = __ldcs(c.rayq + 2 * (size_t)r), b = __ldcs(c.rayq + 2 * (size_t)r + 1);
+                    O = mk(a.x, a.y, a.z);
+                    slot = __float_as_int(a.w);
+                    D = mk(b.x, b.y, b.z);
+                    pt = __float_as_int(b.w);
+                    int jb;
+                    trace_dyn(tsm, s, p.brute != 0, O, D, tmin, q, jb);
+                    if (p.check) {
+                        float tb;
+                        int qb, jbb;
+                        trace_dyn(tsm, s, true, O, D, tb, qb, jbb);
+                        atomicAdd(c.check + 1, 1ull);
+                        if (qb != q || __float_as_int(tb) != __float_as_int(tmin)) atomicAdd(c.check, 1ull);
+                    }
+                    inv = mk(fabsf(D.x) > 1e-12f ? 1.f / D.x : copysignf(1e30f, D.x),
+                             fabsf(D.y) > 1e-12f ? 1.f / D.y : copysignf(1e30f, D.y),
+                             fabsf(D.z) > 1e-12f ? 1.f / D.z : copysignf(1e30f, D.z));
+                    if constexpr (WT) wr = wt_ray(D);
+                    lf = __float_as_int(__ldg(&g.BN[0].w));
+                    cnt = __float_as_int(__ldg(&g.BN[1].w));
+                    sp = 0;
+                    visits = 0;
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (drained) break;
+            continue;
+        }
+        bool done = false;
+        if (active) {
+            // inner nodes until a leaf (its visit counted) or the end of the walk
+            while (true) {
+                if (++visits > g.max_visits) { atomicOr(c.flags, (unsigned)FLAG_BVH_VISITS); done = true; break; }
+                if (cnt > 0) break;
+                const float4 la = __ldg(g.BN + 2 * lf), lb = __ldg(g.BN + 2 * lf + 1);
+                const float4 ra = __ldg(g.BN + 2 * lf + 2), rb = __ldg(g.BN + 2 * lf + 3);
+                float tl = aabb_enter(la, lb, O, inv, tmin, fs), tr = aabb_enter(ra, rb, O, inv, tmin, fs);
+                int2 first = make_int2(__float_as_int(la.w), __float_as_int(lb.w));
+                int2 second = make_int2(__float_as_int(ra.w), __float_as_int(rb.w));
+                if (tr < tl) { const float x = tl; tl = tr; tr = x; const int2 y = first; first = second; second = y; }
+                if (tl < 1e30f) {
+                    if (tr < 1e30f && sp < WQ_MAXSTACK) {
+                        if (sp < WQ_STACK) sstk[32 * sp] = second;
+                        else deep[sp - WQ_STACK] = second;
+                        ++sp;
+                    }
+                    lf = first.x;
+                    cnt = first.y;
+                    continue;
+                }
+                if (sp == 0) { done = true; break; }
+                --sp;
+                const int2 e = sp < WQ_STACK ? sstk[32 * sp] : deep[sp - WQ_STACK];
+                lf = e.x;
+                cnt = e.y;
+            }
+            if (!done) {
+                // the leaf
+                if constexpr (WT) {
+                    for (int j = lf; j < lf + cnt; ++j) {
+                        const float4 x = __ldg(g.ST4 + 3 * (size_t)j), y = __ldg(g.ST4 + 3 * (size_t)j + 1), z = __ldg(g.ST4 + 3 * (size_t)j + 2);
+                        const float t = wt_tri(wr, O, mk(x.x, x.y, x.z), mk(x.w, y.x, y.y), mk(y.z, y.w, z.x));
+                        if (t > 1e-4f && t < tmin) { tmin = t; q = -2 - j; }
+                    }
+                } else {
+                    for (int j = lf; j < lf + cnt; ++j) {
+                        const float4 x = __ldg(g.ST4 + 3 * (size_t)j), y = __ldg(g.ST4 + 3 * (size_t)j + 1), z = __ldg(g.ST4 + 3 * (size_t)j + 2);
+                        const f3 v0 = mk(x.x, x.y, x.z), e1 = mk(x.w, y.x, y.y), e2 = mk(y.z, y.w, z.x);
+                        const f3 pv = cross(D, e2);
+                        const float det = dot(e1, pv);
+                        if (fabsf(det) <= 1e-12f) continue;
+                        const float iv = 1.f / det;
+                        const f3 tv = O - v0;
+                        const float u = dot(tv, pv) * iv;
+                        if (u < 0.f || u > 1.f) continue;
+                        const f3 qv = cross(tv, e1);
+                        const float v = dot(D, qv) * iv;
+                        if (v < 0.f || u + v > 1.f) continue;
+                        const float t = dot(e2, qv) * iv;
+                        if (t > 1e-4f && t < tmin) { tmin = t; q = -2 - j; }
+                    }
+                }
+                if (sp == 0) done = true;
+                else {
+                    --sp;
+                    const int2 e = sp < WQ_STACK ? sstk[32 * sp] : deep[sp - WQ_STACK];
+                    lf = e.x;
+                    cnt = e.y;
+                }
+            }
+        }
+        if (done) {
+            if ((unsigned)slot < (unsigned)(p.Np * p.pre_k) && (unsigned)pt < (unsigned)p.Np) {
+                Hit h;
+                h.t = tmin;
+                h.q = q;
+                resolve_hit(s, g, grid, O, D, pt, h);
+                out[slot] = make_float4(h.H.x, h.H.y, h.H.z, __int_as_float(h.back ? -1 : h.pi));
+            } else {
+                atomicOr(c.flags, (unsigned)FLAG_BAD_INDEX);   // a malformed queue record: skipped
+            }
+            active = false;
+        }
+    }
+}
+
+static size_t trace_queue_smem(const DState& s) {
+    return ((frame_smem_bytes(s) + 15) / 16) * 16 + (size_t)(WQ_BLOCK / 32) * WQ_STACK * 32 * sizeof(int2);
 }
 
 // ------------------------------------------------------------------ split update
@@ -1607,13 +1853,32 @@ static cudaError_t prep_smem(K kern, size_t smem) {
     return cudaSuccess;
 }
 
+static cudaError_t resident_grid(const void* kern, size_t smem, int& out, int threads);
+
 template <int NL>
 cudaError_t Ops<NL>::pretrace(const DState& s, const DStatic& g, const Grid& grid, const DevCache& c, const FrameParams& p,
                               float4* out, cudaStream_t st) {
-    const size_t smem = frame_smem_bytes(s);
-    cudaError_t e = prep_smem(k_pretrace<NL>, smem);
+    if (!p.wavefront || !c.rayq) {   // one thread per point
+        const size_t smem = frame_smem_bytes(s);
+        cudaError_t e = prep_smem(k_pretrace<NL>, smem);
+        if (e != cudaSuccess) return e;
+        k_pretrace<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, out);
+        return cudaGetLastError();
+    }
+    // ray queue: octant counts, scatter, persistent traversal
+    cudaError_t e = cudaMemsetAsync(c.rayctr, 0, 17 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_pretrace<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, out);
+    k_ray_octants<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(s, c, p);
+    k_ray_scatter<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(s, c, p);
+    const size_t smem = trace_queue_smem(s);
+    auto kern = g.watertight ? k_trace_queue<true> : k_trace_queue<false>;
+    if ((e = prep_smem(kern, smem)) != cudaSuccess) return e;
+    // persistent: as many blocks as are resident
+    int resident = 0;
+    if ((e = resident_grid((const void*)kern, smem, resident, WQ_BLOCK)) != cudaSuccess) return e;
+    const int maxrays = p.Np * p.pre_k;
+    const int blocks = std::max(1, std::min(resident, (maxrays + WQ_BLOCK - 1) / WQ_BLOCK));
+    kern<<<blocks, WQ_BLOCK, smem, st>>>(s, g, grid, c, p, out);
     return cudaGetLastError();
 }
 
@@ -1677,8 +1942,8 @@ cudaError_t Ops<NL>::build(int NW, const DState& s, const DStatic& g, const Grid
 
 // Blocks of `kern` (BLOCK threads, `smem` dynamic shared bytes) resident on the whole current
 // device at once, looked up once per device, kernel and shared-memory size.
-static cudaError_t resident_grid(const void* kern, size_t smem, int& out) {
-    struct Entry { int dev; const void* kern; size_t smem; int blocks; };
+static cudaError_t resident_grid(const void* kern, size_t smem, int& out, int threads) {
+    struct Entry { int dev; const void* kern; size_t smem; int threads; int blocks; };
     static std::mutex mu;
     static std::vector<Entry> cache;
     int dev = 0;
@@ -1686,12 +1951,12 @@ static cudaError_t resident_grid(const void* kern, size_t smem, int& out) {
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(mu);
     for (const Entry& x : cache)
-        if (x.dev == dev && x.kern == kern && x.smem == smem) { out = x.blocks; return cudaSuccess; }
+        if (x.dev == dev && x.kern == kern && x.smem == smem && x.threads == threads) { out = x.blocks; return cudaSuccess; }
     int per_sm = 0, sms = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    cache.push_back({dev, kern, smem, per_sm * sms});
+    cache.push_back({dev, kern, smem, threads, per_sm * sms});
     out = per_sm * sms;
     return cudaSuccess;
 }
@@ -1703,7 +1968,7 @@ static cudaError_t frame_t(const DState& s, const DStatic& g, const Grid& grid, 
     cudaError_t e = prep_smem(k_frame<NL, NW, DEPS, FUSED>, smem);
     if (e != cudaSuccess) return e;
     int resident = 0;
-    if ((e = resident_grid((const void*)k_frame<NL, NW, DEPS, FUSED>, smem, resident)) != cudaSuccess) return e;
+    if ((e = resident_grid((const void*)k_frame<NL, NW, DEPS, FUSED>, smem, resident, BLOCK)) != cudaSuccess) return e;
     const int blocks = std::min(grid_of(p.Np), resident);
     k_frame<NL, NW, DEPS, FUSED><<<blocks, BLOCK, smem, st>>>(s, g, grid, c, p);
     return cudaGetLastError();
@@ -1805,6 +2070,10 @@ cudaError_t Ops<NL>::preload(int NW) {
     touch((const void*)k_update<NL>);
     touch((const void*)k_event<NL>);
     touch((const void*)k_pretrace<NL>);
+    touch((const void*)k_ray_octants<NL>);
+    touch((const void*)k_ray_scatter<NL>);
+    touch((const void*)k_trace_queue<false>);
+    touch((const void*)k_trace_queue<true>);
     touch((const void*)k_ref<NL>);
     touch((const void*)k_error<NL>);
     touch((const void*)k_proj_apply<NL>);
