@@ -59,8 +59,9 @@ typedef struct rc_config {
 
 #define RC_FLAG_BRUTE_FORCE 1u  /* test every dynamic triangle (no plane culling) */
 #define RC_FLAG_CHECK_TRACE 2u  /* trace both ways and count disagreements (slow; tests) */
-#define RC_FLAG_THREAD_TRACE 8u /* static-mesh scenes: trace the rays one thread per point instead of
-                                   through the ray queue (same hits; for comparisons) */
+#define RC_FLAG_RAY_QUEUE 8u    /* static-mesh scenes: trace the rays traced ahead of the frame through a
+                                   compacted ray queue served to persistent warps instead of one
+                                   thread per point (same hits; slower at a few rays per point) */
 #define RC_FLAG_WATERTIGHT 4u   /* static-mesh triangles by the watertight test (Woop, Benthin,
                                    Wald 2013) instead of the reference's Moller-Trumbore
                                    (poc_gpu.cu:318-331); hits differ from the reference's at

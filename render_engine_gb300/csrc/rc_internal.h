@@ -63,7 +63,7 @@ struct DevCache {
     float* dstat;              // NR x 3
     float4* pre_hit;           // static-mesh scenes: hits traced ahead, PRE_K per point
     float4* rayq;              // static-mesh scenes: the ray queue of the traced-ahead rays, 2 float4 per ray
-    unsigned* rayctr;          // [0, 8) rays per direction octant, [8, 16) octant cursors, [16] queue head
+    unsigned* rayctr;          // [0] rays in the queue, [1] the next ray to hand out
     float* sumpr;              // 2 slots
     int* npend;                // [0] current, [1] accumulator
     double* err;               // 3 doubles per frame of the run
@@ -100,7 +100,7 @@ struct FrameParams {
     float half_inv_np;         // 0.5f / Np, the float quotient the ray count uses
     const float4* pre_hit;     // rays traced ahead by k_pretrace (pre_k per point), or null
     int pre_k;
-    int wavefront;             // traced-ahead rays through the ray queue (k_trace_queue), else one thread per point
+    int wavefront;             // traced-ahead rays through the ray queue (k_trace_queue) instead of k_pretrace
 };
 
 // Pinhole camera of the image pass: pixel (x, y) looks along

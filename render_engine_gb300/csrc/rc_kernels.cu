@@ -16,6 +16,7 @@
 //  * an event is one kernel applying the reference's per-point event kernels in order.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -944,99 +945,63 @@ __global__ void __launch_bounds__(BLOCK, RC_PRETRACE_MINB) k_pretrace(const DSta
     }
 }
 
-// ------------------------------------------------------------------ wavefront traversal
-// The traced-ahead rays of static-mesh scenes go through a ray queue instead of one thread per
-// point (k_pretrace above, kept behind RC_FLAG_THREAD_TRACE):
-//   k_ray_octants  counts the rays of each direction octant (warp sums, one atomic per warp and
-//                  octant);
-//   k_ray_scatter  writes every ray (origin + output slot, direction + point) into the queue,
-//                  grouped by octant: per warp and octant a warp scan of the lanes' counts and
-//                  one atomicAdd on the octant's cursor;
-//   k_trace_queue  persistent warps: a warp refills its idle lanes from the queue head with one
-//                  atomicAdd once at least WQ_REFILL of them are idle (warp ballot, rank by
-//                  popcount); each lane walks its ray in the traversal's visit order (inner
-//                  nodes until a leaf, then the leaf: Aila and Laine's while-while), its stack's
-//                  top WQ_STACK entries in shared memory, deeper ones in local memory (64 in all,
-//                  as the reference), and writes the resolved hit where k_pretrace would.
+// ------------------------------------------------------------------ ray-queue traversal
+// An alternative to k_pretrace for the traced-ahead rays of static-mesh scenes
+// (RC_FLAG_RAY_QUEUE):
+//   k_ray_queue    writes every ray (origin + output slot, direction + point) into a compacted
+//                  queue in point order: per warp a scan of the lanes' ray counts and one
+//                  atomicAdd on the queue's tail;
+//   k_trace_queue  persistent warps: a warp takes chunks of WQ_CHUNK consecutive rays with one
+//                  atomicAdd each and refills its idle lanes from its chunk once at least
+//                  WQ_REFILL of them are idle (warp ballot, rank by popcount); each lane walks
+//                  its ray in the traversal's visit order (inner nodes until a leaf, then the
+//                  leaf: Aila and Laine's while-while), the top WQ_STACK entries of its stack in
+//                  shared memory and deeper ones in local memory (64 in all, as the reference),
+//                  and writes the resolved hit where k_pretrace would.
 // Same rays, same per-ray visit order and pruning: the hits equal k_pretrace's bit for bit.
+// Measured slower than k_pretrace at about half a million rays per frame (a resident warp gets
+// only a few rays per lane per frame, so the refills do not pay for their own cost), hence not
+// the default.
 constexpr int WQ_BLOCK = 128;
 constexpr int WQ_STACK = 16;
-constexpr int WQ_REFILL = 8;
+constexpr int WQ_REFILL = 16;
+constexpr int WQ_CHUNK = 32;
 constexpr int WQ_MAXSTACK = 64;
 
-static __device__ __forceinline__ int octant_of(f3 d) { return (d.x < 0.f ? 1 : 0) | (d.y < 0.f ? 2 : 0) | (d.z < 0.f ? 4 : 0); }
-
 template <int NL>
-__global__ void __launch_bounds__(BLOCK) k_ray_octants(const DState s, const DevCache c, const FrameParams p) {
-    const int i = blockIdx.x * BLOCK + threadIdx.x;
-    unsigned long long mine = 0ull;   // 8 bits per octant (at most 4 rays per lane, 128 per warp)
-    if (i < p.Np) {
-        uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
-        const bool pend = p.pend_left > 0 && c.pending[i];
-        const int k = min(ray_count(p, c, c.n[i], pend, c.sumpr[p.sum_in], c.npend[0], rs), p.pre_k);
-        const f3 N = xyz(s.N4[i]);
-        for (int r = 0; r < k; ++r) {
-            const float u1 = rnd(rs);
-            const float u2 = rnd(rs);
-            mine += 1ull << (8 * octant_of(cosine_dir(N, u1, u2)));
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
-    if ((threadIdx.x & 31) == 0)
-        for (int o = 0; o < 8; ++o) {
-            const unsigned n = (unsigned)((mine >> (8 * o)) & 255ull);
-            if (n) atomicAdd(c.rayctr + o, n);
-        }
-}
-
-template <int NL>
-__global__ void __launch_bounds__(BLOCK) k_ray_scatter(const DState s, const DevCache c, const FrameParams p) {
+__global__ void __launch_bounds__(BLOCK) k_ray_queue(const DState s, const DevCache c, const FrameParams p) {
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    f3 O = mk(0.f, 0.f, 0.f);
-    f3 D[4] = {mk(0.f, 0.f, 1.f), mk(0.f, 0.f, 1.f), mk(0.f, 0.f, 1.f), mk(0.f, 0.f, 1.f)};
-    int oc[4] = {-1, -1, -1, -1};   // -1: no ray (lanes past the last point write nothing)
+    int k = 0;
+    f3 O = mk(0.f, 0.f, 0.f), N = mk(0.f, 0.f, 1.f);
+    uint32_t rs = 0;
     if (i < p.Np) {
-        uint32_t rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
+        rs = hash32(p.seed * 0x9E3779B9u ^ hash32(p.frame * 0x85EBCA6Bu ^ hash32(i + 1)));
         const bool pend = p.pend_left > 0 && c.pending[i];
-        const int k = min(ray_count(p, c, c.n[i], pend, c.sumpr[p.sum_in], c.npend[0], rs), p.pre_k);
-        const f3 P = xyz(s.P4[i]), N = xyz(s.N4[i]);
+        k = min(ray_count(p, c, c.n[i], pend, c.sumpr[p.sum_in], c.npend[0], rs), p.pre_k);
+        const f3 P = xyz(s.P4[i]);
+        N = xyz(s.N4[i]);
         O = P + N * 1e-3f;
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-            if (r < k) {
-                const float u1 = rnd(rs);
-                const float u2 = rnd(rs);
-                D[r] = cosine_dir(N, u1, u2);
-                oc[r] = octant_of(D[r]);
-            }
     }
+    int x = k;   // warp inclusive scan of the ray counts
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, x, 31);
+    unsigned base = 0;
+    if (lane == 31 && total) base = atomicAdd(c.rayctr, (unsigned)total);
+    unsigned at = __shfl_sync(0xffffffffu, base, 31) + (unsigned)(x - k);
     const unsigned cap = (unsigned)(p.Np * p.pre_k);
-    unsigned start = 0;   // the octant's first queue position
-#pragma unroll 1
-    for (int o = 0; o < 8; ++o) {
-        int n = 0;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) n += oc[r] == o;
-        int x = n;   // warp inclusive scan
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, x, d);
-            if (lane >= d) x += y;
+    for (int r = 0; r < k; ++r, ++at) {
+        const float u1 = rnd(rs);
+        const float u2 = rnd(rs);
+        const f3 D = cosine_dir(N, u1, u2);
+        if (at < cap) {
+            c.rayq[2 * (size_t)at] = make_float4(O.x, O.y, O.z, __int_as_float(i * p.pre_k + r));
+            c.rayq[2 * (size_t)at + 1] = make_float4(D.x, D.y, D.z, __int_as_float(i));
         }
-        const int total = __shfl_sync(0xffffffffu, x, 31);
-        unsigned base = 0;
-        if (lane == 31 && total) base = atomicAdd(c.rayctr + 8 + o, (unsigned)total);
-        unsigned at = __shfl_sync(0xffffffffu, base, 31) + start + (unsigned)(x - n);
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-            if (oc[r] == o && at < cap) {
-                c.rayq[2 * (size_t)at] = make_float4(O.x, O.y, O.z, __int_as_float(i * p.pre_k + r));
-                c.rayq[2 * (size_t)at + 1] = make_float4(D[r].x, D[r].y, D[r].z, __int_as_float(i));
-                ++at;
-            }
-        start += __ldcg(c.rayctr + o);
     }
 }
 
@@ -1051,12 +1016,11 @@ __global__ void __launch_bounds__(WQ_BLOCK) k_trace_queue(const DState s, const 
     const int dyn4 = (int)((frame_smem_bytes(s) + 15) / 16);
     int2* sstk = reinterpret_cast<int2*>(sm + dyn4) + warp * (WQ_STACK * 32) + lane;   // entry e at sstk[32 e]
     int2 deep[WQ_MAXSTACK - WQ_STACK];
-    unsigned nrays = 0;
-#pragma unroll
-    for (int o = 0; o < 8; ++o) nrays += __ldcg(c.rayctr + o);
+    const unsigned nrays = min(__ldcg(c.rayctr), (unsigned)(p.Np * p.pre_k));
     const unsigned lt = (1u << lane) - 1u;
     const float fs = WT ? __int_as_float(0x3f800004) : 1.f;
     bool active = false, drained = false;
+    unsigned cbase = 0, cend = 0;   // the warp's current chunk of the queue
     f3 O = mk(0.f, 0.f, 0.f), D = mk(0.f, 0.f, 1.f), inv = mk(0.f, 0.f, 0.f);
     float tmin = 0.f;
     int q = -1, lf = 0, cnt = 0, sp = 0, visits = 0, slot = 0, pt = 0;
@@ -1064,14 +1028,22 @@ __global__ void __launch_bounds__(WQ_BLOCK) k_trace_queue(const DState s, const 
     while (true) {
         const unsigned idle = __ballot_sync(0xffffffffu, !active);
         if (!drained && __popc(idle) >= WQ_REFILL) {
-            const int leader = __ffs(idle) - 1;
-            unsigned base = 0;
-            if (lane == leader) base = atomicAdd(c.rayctr + 16, (unsigned)__popc(idle));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            drained = base + (unsigned)__popc(idle) >= nrays;
+            const int nidle = __popc(idle);
+            if (cbase >= cend) {   // the warp's chunk is used up: one atomicAdd for the next
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(c.rayctr + 1, (unsigned)WQ_CHUNK);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base >= nrays) drained = true;
+                else { cbase = base; cend = min(base + WQ_CHUNK, nrays); }
+            }
+            const unsigned avail = cend - cbase;
+            const unsigned take = min((unsigned)nidle, avail);
+            const unsigned base = cbase;
+            cbase += take;
             if (!active) {
-                const unsigned r = base + (unsigned)__popc(idle & lt);
-                if (r < nrays) {
+                const unsigned rank = (unsigned)__popc(idle & lt);
+                const unsigned r = base + rank;
+                if (rank < take) {
                     const float4 a = __ldcs(c.rayq + 2 * (size_t)r), b = __ldcs(c.rayq + 2 * (size_t)r + 1);
                     O = mk(a.x, a.y, a.z);
                     slot = __float_as_int(a.w);
@@ -1865,11 +1837,10 @@ cudaError_t Ops<NL>::pretrace(const DState& s, const DStatic& g, const Grid& gri
         k_pretrace<NL><<<grid_of(p.Np), BLOCK, smem, st>>>(s, g, grid, c, p, out);
         return cudaGetLastError();
     }
-    // ray queue: octant counts, scatter, persistent traversal
-    cudaError_t e = cudaMemsetAsync(c.rayctr, 0, 17 * sizeof(unsigned), st);
+    // ray queue: compacted rays, then the persistent traversal
+    cudaError_t e = cudaMemsetAsync(c.rayctr, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_ray_octants<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(s, c, p);
-    k_ray_scatter<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(s, c, p);
+    k_ray_queue<NL><<<grid_of(p.Np), BLOCK, 0, st>>>(s, c, p);
     const size_t smem = trace_queue_smem(s);
     auto kern = g.watertight ? k_trace_queue<true> : k_trace_queue<false>;
     if ((e = prep_smem(kern, smem)) != cudaSuccess) return e;
@@ -2070,8 +2041,7 @@ cudaError_t Ops<NL>::preload(int NW) {
     touch((const void*)k_update<NL>);
     touch((const void*)k_event<NL>);
     touch((const void*)k_pretrace<NL>);
-    touch((const void*)k_ray_octants<NL>);
-    touch((const void*)k_ray_scatter<NL>);
+    touch((const void*)k_ray_queue<NL>);
     touch((const void*)k_trace_queue<false>);
     touch((const void*)k_trace_queue<true>);
     touch((const void*)k_ref<NL>);

@@ -786,7 +786,7 @@ rc_status alloc_cache(rc_ctx* ctx) {
     c.rayq = nullptr;
     c.rayctr = nullptr;
     if (S.g.has_bvh && ((s = dalloc(ctx, pool, &c.pre_hit, (size_t)PRE_K * Np)) || (s = dalloc(ctx, pool, &c.rayq, 2 * (size_t)PRE_K * Np)) ||
-                        (s = dalloc(ctx, pool, &c.rayctr, 17))))
+                        (s = dalloc(ctx, pool, &c.rayctr, 2))))
         return s;
     CKR(cudaMemsetAsync(c.ticket, 0, 16, ctx->stream));
     CKR(cudaMemsetAsync(c.check, 0, 16, ctx->stream));
@@ -1088,9 +1088,9 @@ rc_status frame_impl(rc_ctx* ctx, int si, int want_err, rc_timers* tm) {
         // static-mesh scene: the traversal runs ahead in its own kernel
         p.pre_hit = ctx->c.pre_hit;
         p.pre_k = PRE_K;
-        p.wavefront = !(ctx->cfg.flags & RC_FLAG_THREAD_TRACE);
+        p.wavefront = (ctx->cfg.flags & RC_FLAG_RAY_QUEUE) != 0;
         CKR(RC_DISPATCH(S.NL, pretrace(d, S.g, S.grid, ctx->c, p, ctx->c.pre_hit, st)));
-        R.last_kernels += p.wavefront ? 3 : 1;
+        R.last_kernels += p.wavefront ? 2 : 1;
     }
     if (fused) {
         CKR(RC_DISPATCH(S.NL, frame(ctx->NW, track, true, d, S.g, S.grid, ctx->c, p, st)));

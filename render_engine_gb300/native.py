@@ -32,7 +32,7 @@ SA_EDIR, SA_SV, SA_REF, SA_VALID, SA_PW = range(5)
 FLAG_BRUTE_FORCE = 1
 FLAG_CHECK_TRACE = 2
 FLAG_WATERTIGHT = 4
-FLAG_THREAD_TRACE = 8
+FLAG_RAY_QUEUE = 8
 
 # Exported symbols, one per declaration of include/rc_api.h.
 EXPORTS = [

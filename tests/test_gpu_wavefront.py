@@ -1,12 +1,12 @@
-"""The ray-queue traversal of static-mesh scenes (k_ray_octants, k_ray_scatter, k_trace_queue)
-against the one-thread-per-point traversal it replaces (RC_FLAG_THREAD_TRACE): the same rays
+"""The ray-queue traversal of static-mesh scenes (k_ray_queue, k_trace_queue; RC_FLAG_RAY_QUEUE)
+against the one-thread-per-point traversal (k_pretrace, the default): the same rays
 with the same per-ray visit order.  The two contexts run in lockstep, the second one given the
 first one's run state before every frame, as the parity tests do with the reference, so a frame
 is compared from identical inputs: bit for bit, except on the frames whose own outputs depend on
 float sums taken with atomics in an undefined order (verification and event frames of the
 adaptive methods), held to the parity tests' bound.  Reference mode and watertight mode, on a
 median-split tree and on the preparation's linear BVH.  Frames against the reference's own
-kernels are in test_gpu_parity.py (format-3 tests run the queue, the default)."""
+kernels are in test_gpu_parity.py."""
 import numpy as np
 import pytest
 
@@ -22,8 +22,8 @@ SYNC = [N.A_LC, N.A_N, N.A_C0, N.A_PENDING, N.A_CUR, N.A_PREV, N.A_STALE, N.A_AG
 
 
 def _lockstep(data, flags, method, seq, seed):
-    a = N.Context(flags=flags)
-    b = N.Context(flags=flags | N.FLAG_THREAD_TRACE)
+    a = N.Context(flags=flags | N.FLAG_RAY_QUEUE)
+    b = N.Context(flags=flags)
     for c in (a, b):
         c.load_bytes(data)
         c.begin(method, seq[0], seed)
