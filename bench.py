@@ -137,6 +137,47 @@ def street_scene(points: int):
     return S.street_scene(points=points, buildings=40, facade_cell=0.58, size=200.0)
 
 
+# The at-scale workloads: seeded procedural meshes made into format-3 scenes by the library's
+# GPU preparation (rc_prep_mesh_params, linear BVH, cell-grid cache points, lamps and cube placed
+# by probe rays), without references (timing only).  Both arms load the same scene file.
+SCALE_CONFIGS = {
+    "street": {"mesh": dict(kind="street", buildings=40, seed=0, facade_cell=0.58, size=200.0), "points": 530_000,
+               "lamps": 8, "method": "v4-A2C suivi 1/4",
+               "desc": "procedural street (ground + 40 buildings 5-30 m tall, facades in 0.58 m cells: 199,346 triangles), "
+                       "8 lamp lights, ~530 k cache points"},
+    "city": {"mesh": dict(kind="city", buildings=400, seed=0, facade_cell=1.6), "points": 1_000_000, "lamps": 32,
+             "method": "v3 complet",
+             "desc": "procedural city (400 buildings 5-60 m tall on a 20 x 20 block grid, facades in 1.6 m cells: ~1 M triangles), "
+                     "32 lamp lights, ~1 M cache points; a method without dormant-light memory (the reference's per-point stale "
+                     "mask holds 8 lights)"},
+}
+
+
+def scale_scene(name: str) -> bytes:
+    """The prepared scene of an at-scale workload, cached on the machine's temporary directory
+    (the two arms run as separate processes)."""
+    import tempfile
+    cfg = SCALE_CONFIGS[name]
+    d = os.path.join(tempfile.gettempdir(), "rc_bench_scenes")
+    os.makedirs(d, exist_ok=True)
+    key = "%s_%d_%d" % (name, cfg["points"], cfg["lamps"])
+    path = os.path.join(d, key + ".bin")
+    if not os.path.exists(path):
+        from render_engine_gb300 import native as N
+        from render_engine_gb300 import scene as S
+        m = dict(cfg["mesh"])
+        kind = m.pop("kind")
+        V, alb, ds = S.street_mesh(**m) if kind == "street" else S.city_mesh(**m)
+        mesh = os.path.join(d, key + ".msh")
+        with open(mesh, "wb") as f:
+            f.write(S.write_msh1(V, alb, ds))
+        ctx = N.Context()
+        ctx.prep_mesh(mesh, path + ".tmp", points=cfg["points"], lamps=cfg["lamps"], ref_iterations=-1)
+        ctx.close()
+        os.replace(path + ".tmp", path)
+    return open(path, "rb").read()
+
+
 def sequence(n: int, ns: int = 5) -> list[int]:
     return [(f // FRAMES_PER_STATE) % ns for f in range(n)]
 
@@ -168,6 +209,7 @@ class Clocks:
     def __init__(self, device: int):
         self.p = None
         self.device = device
+        self.t0 = time.perf_counter()
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
                                        "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
@@ -177,6 +219,11 @@ class Clocks:
     def stop(self) -> dict:
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        # at least one sampling period after the start (a short timed region would end before the
+        # first sample); the GPU idles meanwhile, so the samples taken then are marked idle
+        rest = 0.45 - (time.perf_counter() - self.t0)
+        if rest > 0:
+            time.sleep(rest)
         self.p.terminate()
         out, _ = self.p.communicate(timeout=10)
         sm, smax, reasons = [], [], set()
@@ -285,8 +332,9 @@ def time_frames(ctx, method, seq, s0, args, stream, flush, dist=None):
         ctx.frame(seq[f])
         ends[k].record(stream)
         nk = ctx.scalar(N.S_LAST_FRAME_KERNELS)
-        fused.append(ctx.scalar(N.S_LAST_FRAME_FUSED) == 1 and nk == 1)
-        kinds.append("event" if seq[f] != seq[f - 1] else ("fused" if fused[-1] else "split"))
+        fu = ctx.scalar(N.S_LAST_FRAME_FUSED) == 1
+        fused.append(fu and nk == 1)   # exactly one launch: the roofline's kernel
+        kinds.append("event" if seq[f] != seq[f - 1] else ("fused" if fu else "split"))
         tracked.append(f % method.track_every == 0)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
@@ -398,7 +446,51 @@ def run_ours(args, world, rank, local, dist):
     out["adjoint"] = adjoint_bench(peak)
     out["taa"] = taa_bench()
     out["camera_paths"] = paths_bench()
+    for name in SCALE_CONFIGS:
+        out[name] = scale_line_ours(name, args, local)
     return out, data, method, refs
+
+
+def scale_line_ours(name, args, local):
+    """An at-scale workload timed like the headline: the same window of frames around the first
+    state change, L2 flushed between frames, CUDA events on the library's stream, clocks
+    sampled.  The city line adds the 3840 x 2160 image pass from its cache."""
+    import numpy as np
+    import torch
+    from render_engine_gb300 import methods as M
+    from render_engine_gb300 import native as N
+    cfg = SCALE_CONFIGS[name]
+    data = scale_scene(name)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    method = M.by_name(M.timing_methods(), cfg["method"])
+    s0 = window_start(args.warmup, args.steps)
+    seq = sequence(s0 + args.steps)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    ctx = N.Context(device=local, stream=stream.cuda_stream, expect_lights=cfg["lamps"])
+    info = ctx.load_bytes(data)
+    t = time_frames(ctx, method, seq, s0, args, stream, flush)
+    total = sum(t["ms"])
+    out = {"scene": cfg["desc"], "triangles": info["nst"], "cache_points": info["np"], "lights": info["nl"],
+           "method": cfg["method"], "frames_per_s": args.steps / (total * 1e-3), "ms_per_step": total / args.steps,
+           "mrays_per_s": t["rays"] / (total * 1e-3) / 1e6, "frame_kinds_ms": kinds_table(t["ms"], t["kinds"]),
+           "clocks": t["clocks"], "bvh_nodes": info["nnodes"]}
+    if name == "city":
+        lo = np.frombuffer(data, np.float32, count=3, offset=32)   # the scene box's lower corner
+        cam = N.camera(eye=(float(lo[0]) * 0.9, float(lo[1]) * 0.9, 120.0), at=(0.0, 0.0, 0.0), fov_y_deg=60.0,
+                       width=3840, height=2160)
+        ctx.render(seq[-1], cam, copy=False)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            ctx.render(seq[-1], cam, copy=False)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        out["image_3840x2160_ms"] = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+    ctx.close()
+    del flush
+    return out
 
 
 def e2e_run(data, method, seq, local, stream, world):
@@ -860,8 +952,45 @@ def run_reference(args, world, rank, local, dist):
             "window": {"first_timed_frame": s0, "untimed_lead_in_frames": s0 - args.warmup},
             "timing_mode": {"trace": tm[1] / nf, "decide": tm[2] / nf, "update": tm[3] / nf, "swap": tm[0] / nf,
                             "event_total": tm[4]},
+            "street": scale_line_reference("street", args),
+            "city": scale_line_reference("city", args),
             "taa": {"points": args.points, "frames": 200, "frames_per_s": 200 / dt, "ms_per_frame": dt * 1e3 / 200,
                     "method": "TAA + masque dependances"}}, None
+
+
+def scale_line_reference(name, args):
+    """The reference's own kernels on an at-scale workload, timed as scale_line_ours times ours."""
+    import torch
+    from oracle import pyref
+    from render_engine_gb300 import methods as M
+    cfg = SCALE_CONFIGS[name]
+    if not pyref.available(cfg["lamps"]):
+        return {"unavailable": "reference kernels for %d lights not built" % cfg["lamps"]}
+    data = scale_scene(name)
+    method = M.by_name(M.timing_methods(), cfg["method"])
+    ref = pyref.RefRunner(cfg["lamps"], data)
+    s0 = window_start(args.warmup, args.steps)
+    seq = sequence(s0 + args.steps)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    ref.begin(method, seq[0], 11)
+    for f in range(s0):
+        ref.frame(seq[f])
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = Clocks(torch.cuda.current_device())
+    for k, (e0, e1) in enumerate(ev):
+        flush.zero_()
+        e0.record(stream)
+        ref.frame(seq[s0 + k])
+        e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ref.close()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    kinds = ["event" if seq[s0 + k] != seq[s0 + k - 1] else "other" for k in range(args.steps)]
+    return {"scene": cfg["desc"], "method": cfg["method"], "frames_per_s": args.steps / (sum(ms) * 1e-3),
+            "ms_per_step": sum(ms) / args.steps, "frame_kinds_ms": kinds_table(ms, kinds), "clocks": clk}
 
 
 def main():
@@ -891,6 +1020,7 @@ def main():
                 "vs_baseline": res["frames_per_s"] / PUBLISHED_FPS, "dtype": "f32", "data": "the reference's own scene file",
                 "config": config, "impl": "reference", "clocks": res["clocks"], "frame_kinds_ms": res["frame_kinds_ms"],
                 "window": res["window"], "reference_timing_mode_ms": res["timing_mode"], "taa": res["taa"],
+                "street": res["street"], "city": res["city"],
                 "cpu_baseline": {"value": res["frames_per_s"], "unit": "frames/s", "cores": 1, "kind": "reference",
                                  "sample": "the reference's own kernels (cuda/poc_gpu.cu for sm_103a) on the GB300, driven by one host thread; "
                                            "the reference has no CPU implementation of this path"},
@@ -914,7 +1044,8 @@ def main():
             "rays_per_frame": res["rays_per_frame"], "frame_kinds_ms": res["frame_kinds_ms"], "frame_1080p": res["frame_1080p"],
             "clocks": res["clocks"], "e2e": res["e2e"], "gpu_launches": res["launches"], "roofline": res["roofline"],
             "cpu_baseline": cpu, "quality": res["quality"], "standin_room": res.get("standin_room"), "hashgrid": res["hashgrid"],
-            "mlp": res["mlp"], "adjoint": res["adjoint"], "taa": res["taa"], "camera_paths": res["camera_paths"]}
+            "mlp": res["mlp"], "adjoint": res["adjoint"], "taa": res["taa"], "camera_paths": res["camera_paths"],
+            "street": res["street"], "city": res["city"]}
     print(json.dumps(line))
 
 

@@ -309,6 +309,9 @@ typedef struct {
     int target_points;   /* cache points aimed at (the cell count lands within 5 %) */
     int lamps;           /* point lights, 1..32 (the reference places 3) */
     uint32_t seed;       /* sampling and placement seed */
+    int ref_iterations;  /* most reference iterations per state: 0 = the preparation's default
+                            (2048, or PREP_ITER_MAX), < 0 = no references (a scene without them,
+                            for timing) */
 } rc_prep_params;
 typedef struct {
     int triangles, np, zones, bvh_nodes, ns;

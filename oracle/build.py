@@ -2,7 +2,7 @@
 
 * ``_build/liboracle.so``  -- the CPU restatement (rc_oracle.c), gcc -O3 -fopenmp;
 * ``_build/librefrun.so``  -- the driver of the reference's own kernels (refrun.cpp);
-* ``_ref/ref_l{3,8}.cubin`` -- the reference's cuda/poc_gpu.cu compiled for sm_103a by
+* ``_ref/ref_l{3,8,16,32}.cubin`` -- the reference's cuda/poc_gpu.cu compiled for sm_103a by
   build_ref.sh, only where the reference checkout is present (the cubins are device code,
   so the copies built here are used unchanged on the GPU machine).
 """
@@ -39,7 +39,8 @@ def build_refrun(force: bool = False) -> str:
 def build_reference_cubins(force: bool = False) -> bool:
     """Compile the reference kernels when the reference checkout is present."""
     src = os.path.join(REFERENCE, "cuda", "poc_gpu.cu")
-    outs = [os.path.join(HERE, "_ref", n) for n in ("ref_l3.cubin", "ref_l8.cubin", "ref_l3_g16x8x6.cubin")]
+    outs = [os.path.join(HERE, "_ref", n) for n in ("ref_l3.cubin", "ref_l8.cubin", "ref_l16.cubin", "ref_l32.cubin",
+                                                     "ref_l3_g16x8x6.cubin")]
     if not os.path.exists(src):
         return all(os.path.exists(o) for o in outs)
     if force or any(_stale(o, [src, os.path.join(HERE, "build_ref.sh")]) for o in outs):

@@ -24,7 +24,7 @@
 
 namespace {
 
-constexpr int KSNAP = 6, NEQ = 28, VERIF_FRAMES = 4, PROJ_FRAMES = 4, MAXNL = 8;
+constexpr int KSNAP = 6, NEQ = 28, VERIF_FRAMES = 4, PROJ_FRAMES = 4, MAXNL = 32;
 
 struct float4_ { float x, y, z, w; };
 

@@ -287,6 +287,7 @@ int main(int argc, char** argv) {
         pp.target_points = argc > 4 ? atoi(argv[4]) : 300000;
         pp.lamps = RC_CLI_NLIGHTS;
         pp.seed = 1u;
+        pp.ref_iterations = 0;
         ps = rc_prep_mesh_params(pctx, argv[2], argv[3], &pp, &r);
         if (ps != RC_OK) {
             fprintf(stderr, "prep: %s\n", rc_last_error(pctx));

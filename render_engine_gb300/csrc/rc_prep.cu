@@ -1163,11 +1163,13 @@ extern "C" rc_status rc_prep_mesh_params(rc_ctx* ctx, const char* mesh_path, con
     rc_ref_params rp{32, 16, 64, 2048, 0.03};
     if (const char* e = getenv("PREP_BRUIT_CIBLE")) rp.noise_target = atof(e);
     if (const char* e = getenv("PREP_ITER_MAX")) rp.max_iter = std::max(rp.block, atoi(e));
-    double noise[5];
-    int iters[5];
-    if ((stt = rc_reference_build(ctx, &rp, noise, iters)) != RC_OK) return stt;
+    if (prm->ref_iterations > 0) rp.max_iter = std::max(rp.block, prm->ref_iterations);
+    const bool with_ref = prm->ref_iterations >= 0;
+    double noise[5] = {0, 0, 0, 0, 0};
+    int iters[5] = {0, 0, 0, 0, 0};
+    if (with_ref && (stt = rc_reference_build(ctx, &rp, noise, iters)) != RC_OK) return stt;
     double vfrac = 0;
-    for (int si = 0; si < 5; ++si) {
+    for (int si = 0; si < 5 && with_ref; ++si) {
         std::vector<float> ref(Np), pw((size_t)NL * Np);
         std::vector<uint8_t> val(Np);
         if ((stt = rc_state_array_copy(ctx, si, RC_SA_REF, ref.data(), ref.size() * 4)) != RC_OK ||
@@ -1181,7 +1183,7 @@ extern "C" rc_status rc_prep_mesh_params(rc_ctx* ctx, const char* mesh_path, con
         m.valid.push_back(std::move(val));
         m.Pw.push_back(std::move(pw));
     }
-    if (!write_file(scene_path, scene_bytes(m, true))) return rc::ctx_fail(ctx, RC_ERR_IO, "prep: cannot write %s", scene_path);
+    if (!write_file(scene_path, scene_bytes(m, with_ref))) return rc::ctx_fail(ctx, RC_ERR_IO, "prep: cannot write %s", scene_path);
     if (rep) {
         memset(rep, 0, sizeof *rep);
         rep->triangles = n;
@@ -1204,6 +1206,6 @@ extern "C" rc_status rc_prep_mesh_params(rc_ctx* ctx, const char* mesh_path, con
 }
 
 extern "C" rc_status rc_prep_mesh(rc_ctx* ctx, const char* mesh_path, const char* scene_path, int target, rc_prep_report* rep) {
-    rc_prep_params p{target, 3, 1u};
+    rc_prep_params p{target, 3, 1u, 0};
     return rc_prep_mesh_params(ctx, mesh_path, scene_path, &p, rep);
 }

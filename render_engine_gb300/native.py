@@ -198,7 +198,8 @@ class PrepReport(ctypes.Structure):
 
 
 class PrepParams(ctypes.Structure):
-    _fields_ = [("target_points", ctypes.c_int), ("lamps", ctypes.c_int), ("seed", ctypes.c_uint32)]
+    _fields_ = [("target_points", ctypes.c_int), ("lamps", ctypes.c_int), ("seed", ctypes.c_uint32),
+                ("ref_iterations", ctypes.c_int)]
 
 
 class AdjointParams(ctypes.Structure):
@@ -422,10 +423,12 @@ class Context:
         self._chk(self.L.rc_adjoint_arrays(self.h, L.ctypes.data, u.ctypes.data, h.ctypes.data))
         return L, u, h
 
-    def prep_mesh(self, mesh_path: str, scene_path: str, points: int = 300000, lamps: int = 3, seed: int = 1) -> dict:
-        """Prepare a format-3 scene from an MSH1 mesh (rc_prep_mesh_params); the scene stays loaded."""
+    def prep_mesh(self, mesh_path: str, scene_path: str, points: int = 300000, lamps: int = 3, seed: int = 1,
+                  ref_iterations: int = 0) -> dict:
+        """Prepare a format-3 scene from an MSH1 mesh (rc_prep_mesh_params); the scene stays loaded.
+        ref_iterations < 0: no references."""
         r = PrepReport()
-        p = PrepParams(points, lamps, seed & 0xFFFFFFFF)
+        p = PrepParams(points, lamps, seed & 0xFFFFFFFF, ref_iterations)
         self._chk(self.L.rc_prep_mesh_params(self.h, mesh_path.encode(), scene_path.encode(), ctypes.byref(p), ctypes.byref(r)))
         self.info()
         return {"triangles": r.triangles, "np": r.np, "zones": r.zones, "bvh_nodes": r.bvh_nodes, "bvh_depth": r.bvh_depth,

@@ -551,6 +551,46 @@ def street_mesh(buildings: int = 40, seed: int = 0, facade_cell: float = 2.0, si
     return V, np.array(albs, np.float32), np.zeros(len(tris), np.uint8)
 
 
+def city_mesh(buildings: int = 400, seed: int = 0, facade_cell: float = 1.6, block: float = 32.0, street: float = 10.0):
+    """Seeded city: a square grid of sqrt(buildings)^2 blocks separated by streets, one box
+    building per block (footprint 50-90 % of the block, 5-60 m tall), facades subdivided into
+    cells of about `facade_cell` metres, on a ground plane split into 8 m quads.  About 1 M
+    triangles with the defaults.  Returns (V (n, 3, 3) float32, albedo per triangle,
+    double-sided flags)."""
+    rng = np.random.default_rng(seed)
+    g = int(round(np.sqrt(buildings)))
+    pitch = block + street
+    size = g * pitch + street
+    tris, albs = [], []
+
+    def quad(o, u, v, alb, nu, nv):
+        o, u, v = (np.asarray(x, np.float64) for x in (o, u, v))
+        i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="xy")
+        a = o + u * (i.reshape(-1, 1) / nu) + v * (j.reshape(-1, 1) / nv)
+        du, dv = u / nu, v / nv
+        t1 = np.stack([a, a + du, a + dv], 1)
+        t2 = np.stack([a + du + dv, a + dv, a + du], 1)
+        tris.append(np.stack([t1, t2], 1).reshape(-1, 3, 3))
+        albs.append(np.full(2 * nu * nv, alb))
+
+    cells = max(1, int(size / 8))
+    quad((-size / 2, -size / 2, 0), (size, 0, 0), (0, size, 0), 0.3, cells, cells)
+    for by in range(g):
+        for bx in range(g):
+            w = rng.uniform(0.5, 0.9) * block
+            d = rng.uniform(0.5, 0.9) * block
+            hgt = rng.uniform(5, 60)
+            x0 = -size / 2 + street + bx * pitch + rng.uniform(0, block - w)
+            y0 = -size / 2 + street + by * pitch + rng.uniform(0, block - d)
+            alb = rng.uniform(0.2, 0.8)
+            for o, u, v, n in _box_quads(np.array([x0, y0, 0.0]), np.array([x0 + w, y0 + d, hgt])):
+                nu = max(1, int(np.linalg.norm(u) / facade_cell))
+                nv = max(1, int(np.linalg.norm(v) / facade_cell))
+                quad(o, u, v, alb, nu, nv)
+    V = np.concatenate(tris).astype(np.float32)
+    return V, np.concatenate(albs).astype(np.float32), np.zeros(len(V), np.uint8)
+
+
 def street_scene(points: int = 20000, buildings: int = 8, seed: int = 0, facade_cell: float = 2.0, size: float = 60.0,
                  lights: int = 3) -> Scene:
     """Format-3 street scene: street_mesh + three lamp-post lights and the movable cube; five
