@@ -441,6 +441,7 @@ def run_ours(args, world, rank, local, dist):
                                "frame_kinds_ms": kinds_table(t2["ms"], t2["kinds"]), "clocks": t2["clocks"]}
     del flush
     out["quality"], refs = quality(data, method, local, stream)
+    out["learned_cache"] = learned_bench(data, refs, local)
     out["hashgrid"] = hashgrid_bench(stream, peak)
     out["mlp"] = mlp_bench(stream)
     out["adjoint"] = adjoint_bench(peak)
@@ -592,6 +593,109 @@ def quality(data, method, local, stream):
            "note": "references from the GPU stochastic Jacobi of the reference's scene preparation (K=32, two chains, 3 % noise "
                    "target); their gap to the FP64 path tracer is measured by the CPU leg (fp64_reference_check)"}
     return res, {"refs": refs, "valid": valid}
+
+
+def learned_bench(data, refs, local, batch=1 << 16):
+    """The learned cache (render_engine_gb300/learned.py: the network trained online every frame on
+    the tracer's one-bounce estimates, 2^16 samples per step, loss-scaled, and served as the
+    cache) against the per-point cache methods of the reference over the whole timing sequence
+    (5 states x 60 frames, 4 state changes): the 30-frame post-event luminance error over all
+    valid points and over the event region (as the quality leg), and each method's frame ms (CUDA
+    events around each frame's work; for the learned cache inference + frame + training step).
+    The per-point caches run at 1, 2, 4 and 8 rays per point, so that one of them spends at least
+    the learned cache's time per frame.  Every method starts from an empty cache (the scene file
+    carries no warm start) and runs 120 frames of the first state before the measured sequence."""
+    import math
+    import numpy as np
+    import torch
+    from render_engine_gb300 import learned as LC
+    from render_engine_gb300 import methods as M
+    from render_engine_gb300 import native as N
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev = torch.device("cuda", local)
+    hdr = __import__("render_engine_gb300.scene", fromlist=["header"]).header(data)
+    np_, nl, ns = hdr["np"], hdr["nl"], hdr["ns"]
+    seq = sequence(ns * FRAMES_PER_STATE, ns)
+    events = [f for f in range(1, len(seq)) if seq[f] != seq[f - 1]]
+    ref_d = [torch.from_numpy(r).to(dev) for r in refs["refs"]]
+    val_d = [torch.from_numpy(v.astype(np.uint8)).to(dev) for v in refs["valid"]]
+    reg_d = {}
+    for e in events:
+        a, b = seq[e - 1], seq[e]
+        rel = np.abs(refs["refs"][b] - refs["refs"][a]).astype(np.float64) / (refs["refs"][a].astype(np.float64) + 1e-2)
+        reg_d[e] = torch.from_numpy(((refs["valid"][b] != 0) & (rel > 0.05)).astype(np.uint8)).to(dev)
+    lcs = (nl + 3) // 4 * 4
+
+    warm = 120
+
+    def run(step, ctx, dormant_of):
+        for f in range(warm):
+            step(f, seq[0])
+        sums = torch.zeros((len(seq), 2, 3), dtype=torch.float64, device=dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in seq]
+        for f, s in enumerate(seq):
+            ev[f][0].record(stream)
+            served = step(warm + f, s)     # the cache's values for frame f are in the context's buffer
+            ev[f][1].record(stream)
+            e = max([x for x in events if x <= f], default=None)
+            N.error_sums_noalloc(served, lcs, nl, dormant_of(), ref_d[s].data_ptr(), val_d[s].data_ptr(), np_,
+                                 sums[f, 0].data_ptr(), stream.cuda_stream)
+            if e is not None and f < e + POST_FRAMES:
+                N.error_sums_noalloc(served, lcs, nl, dormant_of(), ref_d[s].data_ptr(), reg_d[e].data_ptr(), np_,
+                                     sums[f, 1].data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        h = sums.cpu().numpy()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        err = lambda x: math.sqrt(x[0] / x[2]) / (x[1] / x[2]) if x[2] > 0 and x[1] > 0 else 0.0
+        post = statistics.mean(statistics.mean(err(h[f, 0]) for f in range(e, e + POST_FRAMES)) for e in events)
+        post_r = statistics.mean(statistics.mean(err(h[f, 1]) for f in range(e, e + POST_FRAMES)) for e in events)
+        pre = statistics.mean(statistics.mean(err(h[f, 0]) for f in range(e - PRE_FRAMES, e)) for e in events)
+        return {"post_event_err_pct": 100 * post, "post_event_region_err_pct": 100 * post_r, "pre_event_err_pct": 100 * pre,
+                "frame_ms": statistics.median(ms[5:])}
+
+    out = {}
+    ctx = N.Context(device=local, stream=stream.cuda_stream)
+    ctx.load_bytes(data)
+    lc = LC.LearnedCache(ctx, data, stream.cuda_stream, batch=batch, lr=1e-2, seed=1)
+    lc.begin(seq[0], 11)
+    pending = {}
+
+    def learned_step(f, s):
+        if f > 0:
+            lc.frame(pending["s"], predicted=True)   # finish the previous frame: trace, gather, train
+        lc.predict(s)
+        pending["s"] = s
+        return ctx.device_ptr(N.A_LC)
+
+    r = run(learned_step, ctx, lambda: 0)
+    scale, steps, skipped = lc.mlp.loss_scale()
+    lc.close()
+    ctx.close()
+    r.update({"loss_scale": scale, "train_steps": steps, "skipped_steps": skipped, "batch": batch, "warm_frames": warm,
+              "note": "frame_ms = training step of the previous frame + inference of this one (the served values) + the rest "
+                      "of the frame loop"})
+    out["learned"] = r
+    for name in ("v4-A2C suivi 1/4", "Classique 1.0x"):
+        for rays in (1.0, 2.0, 4.0, 8.0):
+            m = M.by_name(M.timing_methods(), name).replace(rays=rays)
+            c = N.Context(device=local, stream=stream.cuda_stream)
+            c.load_bytes(data)
+            c.begin(m, seq[0], 11)
+
+            def cache_step(f, s, c=c):
+                c.frame(s)
+                return c.device_ptr(N.A_LC)
+
+            out["%s x%g" % (name, rays)] = run(cache_step, c, lambda c=c: c.scalar(N.S_DORMANT))
+            c.close()
+    best = None
+    for k, v in out.items():
+        if k != "learned" and v["frame_ms"] >= out["learned"]["frame_ms"]:
+            if best is None or v["post_event_err_pct"] < out[best]["post_event_err_pct"]:
+                best = k
+    out["per_point_cache_at_equal_or_more_ms"] = best
+    return out
 
 
 def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20, reps=10):
@@ -1045,7 +1149,7 @@ def main():
             "clocks": res["clocks"], "e2e": res["e2e"], "gpu_launches": res["launches"], "roofline": res["roofline"],
             "cpu_baseline": cpu, "quality": res["quality"], "standin_room": res.get("standin_room"), "hashgrid": res["hashgrid"],
             "mlp": res["mlp"], "adjoint": res["adjoint"], "taa": res["taa"], "camera_paths": res["camera_paths"],
-            "street": res["street"], "city": res["city"]}
+            "street": res["street"], "city": res["city"], "learned_cache": res["learned_cache"]}
     print(json.dumps(line))
 
 

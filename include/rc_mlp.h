@@ -40,6 +40,7 @@ typedef struct {
     int max_batch;              /* largest training batch (samples) */
     int device;
     void* stream;               /* cudaStream_t, NULL = a stream of the network */
+    float loss_scale;           /* initial loss scale, rounded down to a power of two; 0 = 1024 */
 } rc_mlp_config;
 
 rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out);
@@ -47,12 +48,19 @@ void rc_mlp_destroy(rc_mlp* m);
 const char* rc_mlp_last_error(const rc_mlp* m);
 
 /* One training step on n samples (a multiple of 128, at most max_batch): sample s is point
- * d_idx[s] (or s when d_idx is NULL) of d_pos4 / d_nrm4 / d_aux4, its target the first n_out
- * of the tstride floats at d_target + s * tstride.  Loss: relative L2,
+ * p = d_idx[s] (or s when d_idx is NULL) of d_pos4 / d_nrm4 / d_aux4, its target the first
+ * n_out of the tstride floats at d_target + p * tstride (per-point arrays throughout).  Loss: relative L2,
  * (y - t)^2 / (y^2 + 0.01) averaged over samples and outputs; its sum is added to *d_loss
  * (when not NULL).  Gradients are summed over the batch in a fixed order. */
 rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, const float* d_target, int tstride,
                        const int* d_idx, int n, float* d_loss);
+
+/* Loss scaling of the training steps: the output gradient is multiplied by a power-of-two
+ * scale before the bf16 backward pass and divided out of the summed weight gradient before
+ * Adam; a step whose gradient is not finite is skipped and the scale halved, and the scale
+ * doubles after 1000 finite steps in a row (at most 65536).  The current scale, the steps
+ * applied and the steps skipped (synchronises). */
+rc_status rc_mlp_loss_scale(rc_mlp* m, float* scale, long long* steps, long long* skipped);
 
 /* The network's n_out outputs for n points into d_out (ostride floats per point). */
 rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, int n, float* d_out, int ostride);

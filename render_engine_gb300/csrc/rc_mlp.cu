@@ -117,6 +117,7 @@ struct MlpArgs {
     float* dwpart;             // training: per-tile weight gradients, NWEIGHT per tile
     float* loss;               // training: sum of the relative L2 loss (for reporting)
     float loss_scale;          // 1 / (samples x n_out)
+    const float* scale;        // training: the loss scale of this step (device, MlpState::SCALE)
     unsigned* err;
 };
 
@@ -218,6 +219,7 @@ constexpr size_t GROUP_SMEM_INFER = (size_t)128 * K0 * 2;      // activation til
 constexpr size_t GROUP_SMEM_TRAIN = GROUP_SMEM_INFER + (size_t)K0 * 128 * 2;   // + transposed staging
 template <bool TRAIN, int GROUPS>
 __global__ void __launch_bounds__(FWD_THREADS * GROUPS) k_mlp_forward(const MlpArgs a) {
+    const float sc = TRAIN ? __ldg(a.scale) : 1.f;   // loss scale (a power of two)
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar[GROUPS];
     __shared__ uint32_t tmem_base;
@@ -323,10 +325,10 @@ __global__ void __launch_bounds__(FWD_THREADS * GROUPS) k_mlp_forward(const MlpA
                     for (int j = 0; j < OUTP; ++j) {
                         float g = 0.f;
                         if (live && j < a.n_out) {
-                            const float t = a.target[(size_t)s * a.tstride + j];
+                            const float t = a.target[(size_t)pt * a.tstride + j];   // the target of the sample's point
                             const float d = v[j] - t, den = v[j] * v[j] + 0.01f;
                             lsum += d * d / den;
-                            g = 2.f * d / den * a.loss_scale;
+                            g = 2.f * d / den * a.loss_scale * sc;
                         }
                         st_bf16(dy, kmajor_offset(row, j, OUTP), g);
                         st_bf16(dyt, kmajor_offset(j, row, 128), g);
@@ -486,13 +488,50 @@ __global__ void k_mlp_gsum(const float* __restrict__ part, int ntiles, float* __
     for (int t = s; t < ntiles; t += GSLICES) g += part[(size_t)t * NWEIGHT + i];
     slices[(size_t)s * NWEIGHT + i] = g;
 }
-__global__ void k_mlp_adam(const float* __restrict__ slices, float* __restrict__ w, float* __restrict__ m1, float* __restrict__ m2,
-                           float* __restrict__ grad, uint8_t* __restrict__ wbf, float lr, float b1, float b2, float eps, float c1,
-                           float c2) {
+// Loss scaling.  The output gradient is multiplied by a power-of-two scale before it goes
+// through the bf16 backward pass and divided out of the summed weight gradient (exact for a power
+// of two, barring overflow).  A step whose summed gradient is not finite is skipped and the
+// scale halved; after SCALE_RUN finite steps in a row it doubles, up to SCALE_MAX.
+// Device state, floats: scale for the next step, steps applied, finite steps in a row, steps
+// skipped, Adam's bias corrections c1 and c2 of this step, 1 / the scale of this step.
+enum MlpState { ST_SCALE = 0, ST_STEPS, ST_RUN, ST_SKIPPED, ST_C1, ST_C2, ST_INV, ST_COUNT };
+constexpr float SCALE_MAX = 65536.f;
+constexpr int SCALE_RUN = 1000;
+__global__ void k_mlp_gcheck(const float* __restrict__ slices, unsigned* __restrict__ nonfinite) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= NWEIGHT) return;
     float g = 0.f;
     for (int s = 0; s < GSLICES; ++s) g += slices[(size_t)s * NWEIGHT + i];
+    if (!isfinite(g)) atomicOr(nonfinite, 1u);
+}
+__global__ void k_mlp_step(float* __restrict__ st, const unsigned* __restrict__ nonfinite, float b1, float b2) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    st[ST_INV] = 1.f / st[ST_SCALE];
+    if (*nonfinite) {
+        st[ST_SCALE] = fmaxf(st[ST_SCALE] * 0.5f, 1.f);
+        st[ST_RUN] = 0.f;
+        st[ST_SKIPPED] += 1.f;
+        return;
+    }
+    const double s = (double)st[ST_STEPS] + 1.0;
+    st[ST_STEPS] = (float)s;
+    st[ST_C1] = (float)(1.0 / (1.0 - pow((double)b1, s)));
+    st[ST_C2] = (float)(1.0 / (1.0 - pow((double)b2, s)));
+    st[ST_RUN] += 1.f;
+    if (st[ST_RUN] >= (float)SCALE_RUN) {
+        st[ST_SCALE] = fminf(st[ST_SCALE] * 2.f, SCALE_MAX);
+        st[ST_RUN] = 0.f;
+    }
+}
+__global__ void k_mlp_adam(const float* __restrict__ slices, float* __restrict__ w, float* __restrict__ m1, float* __restrict__ m2,
+                           float* __restrict__ grad, uint8_t* __restrict__ wbf, float lr, float b1, float b2, float eps,
+                           const float* __restrict__ st, const unsigned* __restrict__ nonfinite) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NWEIGHT || *nonfinite) return;
+    const float c1 = st[ST_C1], c2 = st[ST_C2];
+    float g = 0.f;
+    for (int s = 0; s < GSLICES; ++s) g += slices[(size_t)s * NWEIGHT + i];
+    g *= st[ST_INV];
     grad[i] = g;
     const float m = b1 * m1[i] + (1.f - b1) * g;
     const float v = b2 * m2[i] + (1.f - b2) * g * g;
@@ -531,8 +570,10 @@ struct rc_mlp {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     float *w = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *part = nullptr, *slices = nullptr, *loss = nullptr;
+    float* state = nullptr;     // loss scale and Adam step state (MlpState)
     uint8_t *wbf = nullptr, *act = nullptr;
     unsigned* err = nullptr;
+    unsigned* nonfinite = nullptr;
     int cap_tiles = 0, sms = 0;
     long long step = 0;
     std::string msg;
@@ -590,8 +631,15 @@ rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out) {
         cudaMalloc(&m->grad, 4 * NWEIGHT) || cudaMalloc(&m->wbf, WF_BYTES + WB_BYTES) || cudaMalloc(&m->err, 4) ||
         cudaMalloc(&m->loss, 4) || cudaMalloc(&m->part, (size_t)4 * NWEIGHT * m->cap_tiles) ||
         cudaMalloc(&m->slices, (size_t)4 * NWEIGHT * GSLICES) ||
-        cudaMalloc(&m->act, (size_t)ACT_BYTES * m->cap_tiles))
+        cudaMalloc(&m->act, (size_t)ACT_BYTES * m->cap_tiles) || cudaMalloc(&m->state, 4 * ST_COUNT) ||
+        cudaMalloc(&m->nonfinite, 4))
         return bad(RC_ERR_NOMEM);
+    {
+        float st0[ST_COUNT] = {0};
+        float sc = cfg->loss_scale > 0.f ? cfg->loss_scale : 1024.f;
+        st0[ST_SCALE] = exp2f(floorf(log2f(sc)));   // a power of two
+        if (cudaMemcpy(m->state, st0, sizeof st0, cudaMemcpyHostToDevice) != cudaSuccess) return bad(RC_ERR_CUDA);
+    }
     // He-uniform initial weights, seeded
     std::vector<float> w(NWEIGHT);
     uint64_t st = 0x5EEDull ^ (uint64_t)cfg->seed * 0x100000001B3ull;
@@ -622,7 +670,7 @@ void rc_mlp_destroy(rc_mlp* m) {
     if (!m) return;
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->w); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad); cudaFree(m->part); cudaFree(m->slices);
-    cudaFree(m->loss); cudaFree(m->wbf); cudaFree(m->act); cudaFree(m->err);
+    cudaFree(m->loss); cudaFree(m->wbf); cudaFree(m->act); cudaFree(m->err); cudaFree(m->state); cudaFree(m->nonfinite);
     if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
     delete m;
 }
@@ -666,17 +714,20 @@ rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.dwpart = m->part;
     a.loss = d_loss ? d_loss : m->loss;
     a.loss_scale = 1.f / ((float)n * (float)m->cfg.n_out);
+    a.scale = m->state + ST_SCALE;
     const int ntiles = n / 128;
     if (!d_loss && cudaMemsetAsync(m->loss, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "loss");
+    if (cudaMemsetAsync(m->nonfinite, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "flag");
     k_mlp_forward<true, TRAIN_GROUPS><<<std::min((ntiles + TRAIN_GROUPS - 1) / TRAIN_GROUPS, m->sms), FWD_THREADS * TRAIN_GROUPS,
                                         FWD_SMEM_TRAIN, m->stream>>>(a);
     k_mlp_backward<<<ntiles, 128, BWD_SMEM, m->stream>>>(a);
     m->step++;
     const float b1 = 0.9f, b2 = 0.99f;
-    const float c1 = (float)(1.0 / (1.0 - pow(b1, (double)m->step))), c2 = (float)(1.0 / (1.0 - pow(b2, (double)m->step)));
     k_mlp_gsum<<<dim3((NWEIGHT + 255) / 256, GSLICES), 256, 0, m->stream>>>(m->part, ntiles, m->slices);
+    k_mlp_gcheck<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->nonfinite);
+    k_mlp_step<<<1, 32, 0, m->stream>>>(m->state, m->nonfinite, b1, b2);
     k_mlp_adam<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->w, m->m1, m->m2, m->grad, m->wbf, m->cfg.lr, b1, b2,
-                                                              1e-8f, c1, c2);
+                                                              1e-8f, m->state, m->nonfinite);
     return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
 }
 
@@ -693,6 +744,18 @@ rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     k_mlp_forward<false, INFER_GROUPS><<<std::min((ntiles + INFER_GROUPS - 1) / INFER_GROUPS, m->sms), FWD_THREADS * INFER_GROUPS,
                                          FWD_SMEM_INFER, m->stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
+}
+
+rc_status rc_mlp_loss_scale(rc_mlp* m, float* scale, long long* steps, long long* skipped) {
+    if (!m) return RC_ERR_ARG;
+    float st[ST_COUNT];
+    if (cudaMemcpyAsync(st, m->state, sizeof st, cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess)
+        return mfail(m, RC_ERR_CUDA, "copy");
+    if (scale) *scale = st[ST_SCALE];
+    if (steps) *steps = (long long)st[ST_STEPS];
+    if (skipped) *skipped = (long long)st[ST_SKIPPED];
+    return RC_OK;
 }
 
 rc_status rc_mlp_error_flags(rc_mlp* m, unsigned* flags) {

@@ -12,14 +12,15 @@ import numpy as np
 from . import native
 
 EXPORTS = ["rc_mlp_tile_product", "rc_mlp_create", "rc_mlp_destroy", "rc_mlp_last_error", "rc_mlp_train", "rc_mlp_infer",
-           "rc_mlp_weights", "rc_mlp_gradients", "rc_mlp_error_flags"]
+           "rc_mlp_weights", "rc_mlp_gradients", "rc_mlp_error_flags", "rc_mlp_loss_scale"]
 NWEIGHT = 24576
 LAYERS = [(176, 64), (64, 64), (64, 64), (64, 64), (64, 16)]   # (inputs, outputs)
 
 
 class Config(ctypes.Structure):
     _fields_ = [("box_lo", ctypes.c_float * 3), ("box_hi", ctypes.c_float * 3), ("n_out", ctypes.c_int), ("lr", ctypes.c_float),
-                ("seed", ctypes.c_uint32), ("max_batch", ctypes.c_int), ("device", ctypes.c_int), ("stream", ctypes.c_void_p)]
+                ("seed", ctypes.c_uint32), ("max_batch", ctypes.c_int), ("device", ctypes.c_int), ("stream", ctypes.c_void_p),
+                ("loss_scale", ctypes.c_float)]
 
 
 _bound = False
@@ -41,6 +42,8 @@ def _lib():
         L.rc_mlp_weights.argtypes = [vp, vp, ctypes.c_size_t, i]
         L.rc_mlp_gradients.argtypes = [vp, vp, ctypes.c_size_t]
         L.rc_mlp_error_flags.argtypes = [vp, ctypes.POINTER(ctypes.c_uint)]
+        L.rc_mlp_loss_scale.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_longlong),
+                                        ctypes.POINTER(ctypes.c_longlong)]
         _bound = True
     return L
 
@@ -70,11 +73,12 @@ class Mlp:
     """One network on one GPU (rc_mlp_create / rc_mlp_destroy)."""
 
     def __init__(self, box_lo=(0.0, 0.0, 0.0), box_hi=(8.0, 4.0, 3.0), n_out=3, lr=1e-2, seed=1, max_batch=1 << 16, device=0,
-                 stream=None):
+                 stream=None, loss_scale=0.0):
         c = Config()
         c.box_lo[:] = box_lo
         c.box_hi[:] = box_hi
         c.n_out, c.lr, c.seed, c.max_batch, c.device, c.stream = n_out, lr, seed, max_batch, device, stream
+        c.loss_scale = loss_scale
         self.L = _lib()
         h = ctypes.c_void_p()
         st = self.L.rc_mlp_create(ctypes.byref(c), ctypes.byref(h))
@@ -97,6 +101,21 @@ class Mlp:
     def train(self, pos4, nrm4, aux4, target, idx=None, loss=None):
         self._chk(self.L.rc_mlp_train(self.h, _ptr(pos4), _ptr(nrm4), _ptr(aux4), _ptr(target), int(target.shape[-1]), _ptr(idx),
                                       int(target.shape[0]) if idx is None else int(idx.shape[0]), _ptr(loss)))
+
+    def train_raw(self, pos4, nrm4, aux4, target_ptr: int, tstride: int, idx, n: int, loss=None):
+        """A training step whose targets are tstride floats per point at a raw device address
+        (for instance a context's cache buffer, rc_array_info)."""
+        self._chk(self.L.rc_mlp_train(self.h, _ptr(pos4), _ptr(nrm4), _ptr(aux4), target_ptr, int(tstride), _ptr(idx), int(n),
+                                      _ptr(loss)))
+
+    def infer_raw(self, pos4, nrm4, aux4, n: int, out_ptr: int, ostride: int):
+        self._chk(self.L.rc_mlp_infer(self.h, _ptr(pos4), _ptr(nrm4), _ptr(aux4), int(n), out_ptr, int(ostride)))
+
+    def loss_scale(self) -> tuple[float, int, int]:
+        """(current loss scale, steps applied, steps skipped for a non-finite gradient)."""
+        sc, st, sk = ctypes.c_float(), ctypes.c_longlong(), ctypes.c_longlong()
+        self._chk(self.L.rc_mlp_loss_scale(self.h, ctypes.byref(sc), ctypes.byref(st), ctypes.byref(sk)))
+        return sc.value, st.value, sk.value
 
     def infer(self, pos4, nrm4, aux4, out):
         self._chk(self.L.rc_mlp_infer(self.h, _ptr(pos4), _ptr(nrm4), _ptr(aux4), int(out.shape[0]), _ptr(out), int(out.shape[1])))
