@@ -550,6 +550,7 @@ def quality(data, method, local, stream):
     tref = time.perf_counter() - t0
     refs = [q.state_array(k, N.SA_REF) for k in range(ns)]
     valid = [q.state_array(k, N.SA_VALID) for k in range(ns)]
+    pw = [q.state_array(k, N.SA_PW) for k in range(ns)]
     seq = sequence(ns * FRAMES_PER_STATE, ns)
     events = [f for f in range(1, len(seq)) if seq[f] != seq[f - 1]]
     dev = torch.device("cuda", local)
@@ -592,7 +593,7 @@ def quality(data, method, local, stream):
            "reference_iterations": [int(x) for x in iters], "reference_build_s": tref,
            "note": "references from the GPU stochastic Jacobi of the reference's scene preparation (K=32, two chains, 3 % noise "
                    "target); their gap to the FP64 path tracer is measured by the CPU leg (fp64_reference_check)"}
-    return res, {"refs": refs, "valid": valid}
+    return res, {"refs": refs, "valid": valid, "pw": pw}
 
 
 def learned_bench(data, refs, local, batch=1 << 16):
@@ -603,8 +604,10 @@ def learned_bench(data, refs, local, batch=1 << 16):
     valid points and over the event region (as the quality leg), and each method's frame ms (CUDA
     events around each frame's work; for the learned cache inference + frame + training step).
     The per-point caches run at 1, 2, 4 and 8 rays per point, so that one of them spends at least
-    the learned cache's time per frame.  Every method starts from an empty cache (the scene file
-    carries no warm start) and runs 120 frames of the first state before the measured sequence."""
+    the learned cache's time per frame.  Every method starts from the converged cache of the first
+    state, as the reference's runs do (the per-point caches from the references' per-light warm
+    start written into the scene; the network by 120 training steps on that warm start), then
+    runs the sequence."""
     import math
     import numpy as np
     import torch
@@ -626,17 +629,19 @@ def learned_bench(data, refs, local, batch=1 << 16):
         rel = np.abs(refs["refs"][b] - refs["refs"][a]).astype(np.float64) / (refs["refs"][a].astype(np.float64) + 1e-2)
         reg_d[e] = torch.from_numpy(((refs["valid"][b] != 0) & (rel > 0.05)).astype(np.uint8)).to(dev)
     lcs = (nl + 3) // 4 * 4
-
     warm = 120
+    from render_engine_gb300 import scene as S
+    sc = S.read(data)
+    for k, st in enumerate(sc.states):
+        st.ref, st.valid, st.Pw = refs["refs"][k], refs["valid"][k].astype(np.uint8), refs["pw"][k].reshape(np_, nl)
+    data = S.write(sc)     # the scene with its references and warm start
 
     def run(step, ctx, dormant_of):
-        for f in range(warm):
-            step(f, seq[0])
         sums = torch.zeros((len(seq), 2, 3), dtype=torch.float64, device=dev)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in seq]
         for f, s in enumerate(seq):
             ev[f][0].record(stream)
-            served = step(warm + f, s)     # the cache's values for frame f are in the context's buffer
+            served = step(f, s)     # the cache's values for frame f are in the context's buffer
             ev[f][1].record(stream)
             e = max([x for x in events if x <= f], default=None)
             N.error_sums_noalloc(served, lcs, nl, dormant_of(), ref_d[s].data_ptr(), val_d[s].data_ptr(), np_,
@@ -659,6 +664,7 @@ def learned_bench(data, refs, local, batch=1 << 16):
     ctx.load_bytes(data)
     lc = LC.LearnedCache(ctx, data, stream.cuda_stream, batch=batch, lr=1e-2, seed=1)
     lc.begin(seq[0], 11)
+    lc.pretrain(seq[0], torch.from_numpy(refs["pw"][seq[0]].reshape(np_, nl)).to(dev).contiguous(), warm)
     pending = {}
 
     def learned_step(f, s):

@@ -252,6 +252,9 @@ typedef struct {
     int K;              /* frozen rays per point (1..1024, Np * K < 2^31) */
     uint32_t seed;      /* seed of the frozen rays */
     int iterations;     /* Jacobi sweeps of each solve (0 = 64) */
+    const float* emission;  /* NL light emissions of the forward solve (host; NULL = the state's
+                               intensities): its direct light is sum_l emission_l G_l.  The
+                               derivatives do not depend on it (L is linear in E); J and L do */
 } rc_adjoint_params;
 typedef struct {
     double J;           /* w . L from the forward solve (L summed over lights) */

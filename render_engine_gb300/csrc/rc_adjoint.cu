@@ -117,13 +117,20 @@ __global__ void k_rank(const int* __restrict__ off, int Np, const int* __restric
 }
 
 // per point: direct light summed over the lights (l ascending) and albedo; the first gathered
-// values A_j (d_j + L_j) with L = 0
-__global__ void k_prep(const float* __restrict__ AE, int aes, int NL, int Np, float2* __restrict__ da, float* __restrict__ g0) {
+// values A_j (d_j + L_j) with L = 0.  With `em` (NL emissions, device), the direct light is
+// sum_l em_l G_l from the unit-emission build AEu instead of the state's own.
+__global__ void k_prep(const float* __restrict__ AE, const float* __restrict__ AEu, const float* __restrict__ em, int aes, int NL,
+                       int Np, float2* __restrict__ da, float* __restrict__ g0) {
     const int j = blockIdx.x * B + threadIdx.x;
     if (j >= Np) return;
     const float* ae = AE + (size_t)aes * j;
     float d = 0.f;
-    for (int l = 0; l < NL; ++l) d += ae[1 + l];
+    if (em) {
+        const float* au = AEu + (size_t)aes * j;
+        for (int l = 0; l < NL; ++l) d += em[l] * au[1 + l];
+    } else {
+        for (int l = 0; l < NL; ++l) d += ae[1 + l];
+    }
     da[j] = make_float2(d, ae[0]);
     g0[j] = ae[0] * (d + 0.f);
 }
@@ -276,10 +283,11 @@ cudaError_t build_transpose(const Bufs& b, int Np, int K, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t solve(Bufs* bp, int Np, int K, int NL, int aes, const float* AE, const float* AEu, int iters, cudaStream_t st) {
+cudaError_t solve(Bufs* bp, int Np, int K, int NL, int aes, const float* AE, const float* AEu, const float* em, int iters,
+                  cudaStream_t st) {
     const Bufs& b = *bp;
     cudaError_t e;
-    k_prep<<<blocks_for(Np), B, 0, st>>>(AE, aes, NL, Np, b.da, b.g[0]);
+    k_prep<<<blocks_for(Np), B, 0, st>>>(AE, AEu, em, aes, NL, Np, b.da, b.g[0]);
     if ((e = cudaMemsetAsync(b.L[0], 0, sizeof(float) * (size_t)Np, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(b.u[0], b.w, sizeof(float) * (size_t)Np, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
     for (int t = 0; t < iters; ++t) {

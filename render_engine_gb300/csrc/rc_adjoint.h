@@ -42,7 +42,8 @@ size_t scan_scratch_ints(long long n);
 cudaError_t build_transpose(const Bufs& b, int Np, int K, cudaStream_t st);
 // `iters` forward and adjoint Jacobi sweeps from L = 0, u = w, then the gradient against the
 // unit-emission direct light AEu (same gather-record layout as AE, `aes` floats per point)
-cudaError_t solve(Bufs* b, int Np, int K, int NL, int aes, const float* AE, const float* AEu, int iters, cudaStream_t st);
+cudaError_t solve(Bufs* b, int Np, int K, int NL, int aes, const float* AE, const float* AEu, const float* em, int iters,
+                  cudaStream_t st);
 
 }  // namespace adj
 }  // namespace rc

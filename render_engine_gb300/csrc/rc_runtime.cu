@@ -1937,12 +1937,24 @@ rc_status rc_adjoint(rc_ctx* ctx, const rc_adjoint_params* prm, const float* wei
         launched = 1;
     }
     CKR(adj::build_transpose(b, S.Np, prm->K, st));
-    CKR(adj::solve(&b, S.Np, prm->K, NL, AES, reinterpret_cast<const float*>(d.AE), reinterpret_cast<const float*>(AEu), iters, st));
+    // the emissions of the forward solve: the state's, or the caller's
+    std::vector<float> E = S.st[prm->state].inten;
+    std::vector<DevBuf> tmp;
+    struct TmpFree { std::vector<DevBuf>& p; ~TmpFree() { free_pool(p); } } tmp_free{tmp};
+    const float* dem = nullptr;
+    if (prm->emission) {
+        for (int l = 0; l < NL; ++l) {
+            if (!std::isfinite(prm->emission[l])) return fail(ctx, RC_ERR_ARG, "emission %d not finite", l);
+            E[l] = prm->emission[l];
+        }
+        if ((s = dput(ctx, tmp, &dem, E))) return s;
+    }
+    CKR(adj::solve(&b, S.Np, prm->K, NL, AES, reinterpret_cast<const float*>(d.AE), reinterpret_cast<const float*>(AEu), dem, iters,
+                   st));
     adj::Stats hs{};
     CKR(cudaMemcpyAsync(&hs, b.stats, sizeof hs, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
     ctx->launches += 9 + launched + 2 * iters;
-    const std::vector<float>& E = S.st[prm->state].inten;
     double jg = 0.0;
     for (int l = 0; l < NL; ++l) {
         dJ_dE[l] = (float)hs.out[l];

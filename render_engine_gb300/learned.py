@@ -74,6 +74,15 @@ class LearnedCache:
     def begin(self, state: int, seed: int):
         self.ctx.begin(self.method, state, seed)
 
+    def pretrain(self, state: int, target, steps: int):
+        """`steps` training steps on fixed per-point targets (a (Np, NL) CUDA tensor), e.g. a converged
+        cache to start from."""
+        import torch
+        p4, n4, a4 = self.feat[state]
+        for _ in range(steps):
+            idx = torch.randint(0, self.np, (self.batch,), device=self.dev, generator=self.gen, dtype=torch.int32)
+            self.mlp.train(p4, n4, a4, target, idx=idx)
+
     def predict(self, state: int):
         """The network's radiance into the context's cache buffer (what the cache serves)."""
         p4, n4, a4 = self.feat[state]

@@ -203,7 +203,8 @@ class PrepParams(ctypes.Structure):
 
 
 class AdjointParams(ctypes.Structure):
-    _fields_ = [("state", ctypes.c_int), ("K", ctypes.c_int), ("seed", ctypes.c_uint32), ("iterations", ctypes.c_int)]
+    _fields_ = [("state", ctypes.c_int), ("K", ctypes.c_int), ("seed", ctypes.c_uint32), ("iterations", ctypes.c_int),
+                ("emission", ctypes.POINTER(ctypes.c_float))]
 
 
 class AdjointResult(ctypes.Structure):
@@ -400,16 +401,22 @@ class Context:
         self._info = self.info()
         return list(noise), list(iters)
 
-    def adjoint(self, state: int, weights, K: int = 32, seed: int = 0, iterations: int = 64):
+    def adjoint(self, state: int, weights, K: int = 32, seed: int = 0, iterations: int = 64, emission=None):
         """dJ/dE per light for J = sum_i w_i sum_l L_l[i] over K frozen rays per point (rc_adjoint);
-        returns (gradient, result dict)."""
+        returns (gradient, result dict).  emission: the lights' emissions of the forward solve
+        (None = the state's)."""
         nl, np_ = self._info["nl"], self._info["np"]
         w = np.ascontiguousarray(weights, np.float32)
         if w.shape != (np_,):
             raise ValueError("weights must have one entry per cache point")
         g = (ctypes.c_float * nl)()
         res = AdjointResult()
-        prm = AdjointParams(state, K, seed & 0xFFFFFFFF, iterations)
+        prm = AdjointParams(state, K, seed & 0xFFFFFFFF, iterations, None)
+        if emission is not None:
+            em = np.ascontiguousarray(emission, np.float32)
+            if em.shape != (nl,):
+                raise ValueError("emission must have one entry per light")
+            prm.emission = em.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
         self._chk(self.L.rc_adjoint(self.h, ctypes.byref(prm), w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), g, ctypes.byref(res)))
         self._adj_k = K
         return np.array(g[:], np.float32), {n: getattr(res, n) for n, _ in AdjointResult._fields_}
