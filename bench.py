@@ -56,12 +56,15 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=12)
     ap.add_argument("--profile", choices=["frame", "street", "hashgrid", "mlp", "adjoint", "taa", "paths"], default=None,
-                    help="no timing: run --steps frames of state 0 (frame), three resolve passes of the "
-                         "hash-grid table (hashgrid), two inference and training passes of the MLP (mlp) or "
-                         "one 16-sweep adjoint of a 16-light room of --points points (adjoint), --steps "
-                         "frames of the taa mode (taa), --steps 1080p camera-path passes (paths) or --steps "
-                         "frames of state 0 of the format-3 street of --points points (street), for an ncu "
-                         "capture, and exit")
+                    help="no timing: run --steps frames of state 0 of the headline scene (frame), three resolve "
+                         "passes of the hash-grid table (hashgrid), two inference and training passes of the MLP "
+                         "(mlp) or one 16-sweep adjoint of a 16-light room of --points points (adjoint), --steps "
+                         "frames of the taa mode (taa), --steps camera-path passes at --width x --height (paths) "
+                         "or --steps frames of state 0 of the prepared street workload (street; --ray-queue: "
+                         "through the ray queue), for an ncu capture, and exit")
+    ap.add_argument("--ray-queue", action="store_true")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
     return ap.parse_args()
 
 
@@ -73,7 +76,7 @@ def profile_run(args):
     from render_engine_gb300 import scene as S
     if args.profile == "frame":
         ctx = N.Context()
-        ctx.load_bytes(S.write(S.box_room(points=args.points, seed=0)))
+        ctx.load_bytes(headline_scene(args.points)[0])
         ctx.begin(M.by_name(M.timing_methods(), args.method), 0, 11)
         for _ in range(args.steps):
             ctx.frame(0)
@@ -81,9 +84,9 @@ def profile_run(args):
         ctx.close()
         return
     if args.profile == "street":
-        ctx = N.Context()
-        ctx.load_bytes(S.write(street_scene(args.points)))
-        ctx.begin(M.by_name(M.timing_methods(), args.method), 0, 11)
+        ctx = N.Context(flags=N.FLAG_RAY_QUEUE if args.ray_queue else 0, expect_lights=SCALE_CONFIGS["street"]["lamps"])
+        ctx.load_bytes(scale_scene("street"))
+        ctx.begin(M.by_name(M.timing_methods(), SCALE_CONFIGS["street"]["method"]), 0, 11)
         for _ in range(args.steps):
             ctx.frame(0)
         ctx.sync()
@@ -94,7 +97,7 @@ def profile_run(args):
         torch.cuda.synchronize()
         return
     if args.profile == "paths":
-        paths_bench(reps=args.steps, warm=0)
+        paths_bench(reps=args.steps, warm=0, width=args.width, height=args.height)
         torch.cuda.synchronize()
         return
     if args.profile == "taa":
@@ -252,8 +255,9 @@ def measured_peaks() -> tuple[float, str]:
 
 
 def profile_traffic() -> float | None:
-    """DRAM bytes per launch of the fused frame kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_frame_fused_room1m.md")
+    """DRAM bytes of one launch of the fused frame kernel (a tracked frame of the headline scene)
+    from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_frame_fused_scene_scale_1m.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -418,7 +422,7 @@ def run_ours(args, world, rank, local, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic,
                      "kernel": "rc::k_frame<3,4,DEPS,FUSED=true>", "kernel_ms": kern_ms, "kernel_launches": len(fk),
-                     "peak_source": peak_kind},
+                     "peak_source": peak_kind, "traffic_of": "one tracked frame (ncu, profiles/k_frame_fused_scene_scale_1m.md)"},
         "np": np_,
         "nt": info["nt"],
         "frame_kinds_ms": kinds_table(ms, t["kinds"]),
@@ -778,7 +782,7 @@ def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20,
             "mark_paths": {"paths": npaths, "vertices": n, "ms": mark_ms, "vertices_per_s": n / (mark_ms * 1e-3)}}
 
 
-def paths_bench(reps=10, points=1_082_802, warm=3):
+def paths_bench(reps=10, points=1_082_802, warm=3, width=1920, height=1080):
     """Secondary line: the 1080p camera-path pass feeding the hash-grid cache (rc_hg_camera_paths):
     1920 x 1080 paths with 2 bounces through the 1.08 M-point room, the room's 3 point lights
     plus a 1 x 1 m rectangle light and a sun, one light sample and shadow ray per vertex; 2^22
@@ -795,10 +799,10 @@ def paths_bench(reps=10, points=1_082_802, warm=3):
                         stream=st.cuda_stream)
     hg = H.HashGrid(cfg)
     hg.voxels_init(128)
-    cam = N.camera((0.5, 0.5, 1.6), (6.0, 3.0, 1.0), width=1920, height=1080, fov_y_deg=75.0)
+    cam = N.camera((0.5, 0.5, 1.6), (6.0, 3.0, 1.0), width=width, height=height, fov_y_deg=75.0)
     area = ((3.5, 1.5, 2.95), (1.0, 0.0, 0.0), (0.0, -1.0, 0.0), (4.0, 3.5, 3.0))
     sun = ((0.3, 0.2, 1.0), (0.5, 0.5, 0.45))
-    img = torch.zeros(1920 * 1080 * 3, device="cuda")
+    img = torch.zeros(width * height * 3, device="cuda")
     for f in range(warm):
         hg.begin_frame(f, 16)
         hg.camera_paths(ctx, 0, H.path_params(cam, bounces=2, seed=1, frame=f, area=area, sun=sun), img)
@@ -817,7 +821,7 @@ def paths_bench(reps=10, points=1_082_802, warm=3):
     hg.close()
     ctx.close()
     rays = used + int(((verts["light_index"] >= 0)).sum())   # path rays + shadow rays of the last pass
-    return {"width": 1920, "height": 1080, "bounces": 2, "ms": ms, "paths_per_s": 1920 * 1080 / (ms * 1e-3),
+    return {"width": width, "height": height, "bounces": 2, "ms": ms, "paths_per_s": width * height / (ms * 1e-3),
             "rays_per_pass": rays, "mrays_per_s": rays / (ms * 1e-3) / 1e6, "voxel_res": 128, "capacity": 1 << 22}
 
 
