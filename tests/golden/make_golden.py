@@ -6,7 +6,7 @@ Reads, from the reference (falcon123212/render_engine):
   reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl    (its published RTX 4060
       per-frame error curves: `poc_gpu_l3 scen scene_main.bin 10` and
       `poc_gpu_l8 scenf scene_stress.bin 10 scenarios_stress.txt`)
-  cuda/scenes/scenarios_stress.txt
+  cuda/scenes/scenarios_stress.txt, cuda/scenes/scenarios_main.txt
 and writes gzip copies of the scenes and the curves as JSON next to this script.
 
 Usage: python tests/golden/make_golden.py [reference checkout]
@@ -38,6 +38,7 @@ for name in ("scene_main.bin", "scene_stress.bin"):
     with open(os.path.join(REF, "cuda", "scenes", name), "rb") as f, gzip.open(os.path.join(HERE, name + ".gz"), "wb", 9) as g:
         shutil.copyfileobj(f, g)
 shutil.copy(os.path.join(REF, "cuda", "scenes", "scenarios_stress.txt"), os.path.join(HERE, "scenarios_stress.txt"))
+shutil.copy(os.path.join(REF, "cuda", "scenes", "scenarios_main.txt"), os.path.join(HERE, "scenarios_main.txt"))
 # the reference's 1,082,802-point timing scene (its throughput case, cuda/run_cuda.sh), already gzip
 shutil.copy(os.path.join(REF, "cuda", "scenes", "scene_scale_1M.bin.gz"), os.path.join(HERE, "scene_scale_1M.bin.gz"))
 json.dump({"mode": "scen", "seed0": 2000, "nseeds": 10, "rows": curves(os.path.join(REF, "reference", "cuda_rtx4060", "scen_main.jsonl"))},
