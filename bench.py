@@ -715,10 +715,11 @@ def learned_bench(data, refs, local, batch=1 << 16):
 def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20, reps=10):
     """Secondary lines: the hash-grid cache with dependency masks (include/rc_hashgrid.h).
 
-    resolve: one pass over a 2^24-entry table with 2^23 live entries that all received samples
-    this frame (each pass preceded, untimed, by the accumulation that refills them); per
-    entry it reads key 8 B + accumulation 16 B + resolved 16 B + two mask banks 32 B, and a
-    live entry writes its accumulation and resolved words (32 B): the HBM roofline.
+    resolve: one pass over a 2^24-entry table with about 2^23 live entries that all received
+    samples this frame (each pass preceded, untimed, by the accumulation that refills them); it
+    reads every slot's key (8 B) and, for a live entry only, its accumulation 16 B, resolved 16 B
+    and two mask banks 32 B, and writes its accumulation and resolved words (32 B): the HBM
+    roofline over those necessary bytes.
     mark: dependency marking of 2^20 random paths of 1-5 bounces in the zone box."""
     import numpy as np
     import torch
@@ -746,7 +747,9 @@ def hashgrid_bench(stream, peak, capacity=1 << 24, live=1 << 23, npaths=1 << 20,
         e1.record(stream)
     torch.cuda.synchronize()
     res_ms = sum(a.elapsed_time(b) for a, b in evs) / reps
-    res_bytes = 72.0 * capacity + 32.0 * nlive
+    # necessary bytes: every slot's key; the accumulation, resolved radiance and two mask banks
+    # (64 B) of each live entry; its accumulation and resolved words written (32 B)
+    res_bytes = 8.0 * capacity + 64.0 * nlive + 32.0 * nlive
     # path batch
     rng = np.random.default_rng(8)
     lens = rng.integers(1, 6, npaths)

@@ -177,6 +177,7 @@ void hgo_resolve(const hgo_config* c, hgo_state* s, const uint32_t inv[4], uint3
     const int any_inv = (inv[0] | inv[1] | inv[2] | inv[3]) != 0;
     counts[0] = counts[1] = counts[2] = 0;
     for (uint32_t e = 0; e < c->capacity; ++e) {
+        if (s->keys[e] == 0 || s->keys[e] == TOMB) continue;   /* empty or evicted: holds no data */
         uint32_t* a = s->accum + 4 * (size_t)e;
         uint32_t* r = s->resolved + 4 * (size_t)e;
         uint32_t* b0 = s->bank0 + 4 * (size_t)e;

@@ -399,6 +399,10 @@ __global__ void __launch_bounds__(HG_BLOCK) k_hg_resolve(const HgDev c, const ui
     uint32_t n_inv = 0, n_evict = 0, n_valid = 0;
     const bool any_inv = (inv.x | inv.y | inv.z | inv.w) != 0u;
     for (uint32_t e = blockIdx.x * HG_BLOCK + threadIdx.x; e < c.cap; e += gridDim.x * HG_BLOCK) {
+        // all five loads issued together: an empty or evicted slot holds no data (its arrays are
+        // zero: cleared when the entry is evicted, below, and not written while the slot has no
+        // key), but reading the key first and skipping the rest put a dependent load in front of
+        // every live entry and measured slower (0.268 against 0.235 ms at 2^24 slots, 47 % live)
         const unsigned long long key0 = keys[e];
         const uint4 m0 = b0[e], m1 = b1[e];
         uint4 a = accum[e], r = resolved[e];

@@ -96,6 +96,9 @@ def _rand_state(rng, cap, stale_frames):
     res[:, 0] = rgb[:, 0] | rgb[:, 1] << 16
     res[:, 1] = rgb[:, 2] | n0.astype(np.float16).view(np.uint16).astype(np.uint32) << 16
     res[:, 2] = n0 | rng.integers(0, stale_frames + 2, cap).astype(np.uint32) << 16
+    empty = keys == 0            # an empty slot holds no data (the cache keeps it so)
+    accum[empty] = 0
+    res[empty] = 0
     return keys, accum, res
 
 
@@ -108,6 +111,8 @@ def test_resolve_bitexact(inv):
     orc = pyhg.Cache(pyhg.config_from(cfg))
     keys, accum, res = _rand_state(rng, cap, 3)
     b0, b1 = _rand_banks(rng, cap, 0.5), _rand_banks(rng, cap, 0.5)
+    b0[keys == 0] = 0
+    b1[keys == 0] = 0
     for which, a in ((H.A_KEYS, keys), (H.A_ACCUM, accum), (H.A_RESOLVED, res), (H.A_BANK0, b0), (H.A_BANK1, b1)):
         hg.upload(which, a)
     orc.keys[:], orc.accum[:], orc.resolved[:], orc.bank0[:], orc.bank1[:] = keys, accum, res, b0, b1
