@@ -785,8 +785,9 @@ rc_status alloc_cache(rc_ctx* ctx) {
     c.pre_hit = nullptr;
     c.rayq = nullptr;
     c.rayctr = nullptr;
-    if (S.g.has_bvh && ((s = dalloc(ctx, pool, &c.pre_hit, (size_t)PRE_K * Np)) || (s = dalloc(ctx, pool, &c.rayq, 2 * (size_t)PRE_K * Np)) ||
-                        (s = dalloc(ctx, pool, &c.rayctr, 2))))
+    // the traced-ahead hits and the traversal's work counters; the ray queue only when asked for
+    if (S.g.has_bvh && ((s = dalloc(ctx, pool, &c.pre_hit, (size_t)PRE_K * Np)) || (s = dalloc(ctx, pool, &c.rayctr, 2)) ||
+                        ((ctx->cfg.flags & RC_FLAG_RAY_QUEUE) && (s = dalloc(ctx, pool, &c.rayq, 2 * (size_t)PRE_K * Np)))))
         return s;
     CKR(cudaMemsetAsync(c.ticket, 0, 16, ctx->stream));
     CKR(cudaMemsetAsync(c.check, 0, 16, ctx->stream));

@@ -38,7 +38,7 @@ def test_gradcheck_against_central_differences(scene_main_bytes):
     J = f(E0)
     J.backward()
     g = E0.grad.numpy()
-    assert float(J) == pytest.approx(float((E0.detach().numpy() * g).sum()), rel=1e-5)
+    assert float(J.detach()) == pytest.approx(float((E0.detach().numpy() * g).sum()), rel=1e-5)
     # other emissions: the same derivatives, J scaled accordingly
     E1 = torch.tensor([3.0, 0.5, 7.0], dtype=torch.float64, requires_grad=True)
     J1 = f(E1)
