@@ -114,7 +114,7 @@ struct MlpArgs {
     int n_out;
     float lo[3], inv_ext[3];   // encoding box
     uint8_t* act;              // training: activation tiles, ACT_BYTES per tile
-    float* dwpart;             // training: per-tile weight gradients, NWEIGHT per tile
+    float* dwpart;             // training: weight gradients of each backward CTA, NWEIGHT per CTA
     float* loss;               // training: sum of the relative L2 loss (for reporting)
     float loss_scale;          // 1 / (samples x n_out)
     const float* scale;        // training: the loss scale of this step (device, MlpState::SCALE)
@@ -361,107 +361,154 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
-// Backward pass of one tile (128 threads): for l = 4 .. 0, dW_l = dZ_l^T A_l over the tile's
-// samples (rows of dZ^T beyond the layer's outputs are zero) and, for l >= 1,
-// dZ_{l-1} = (dZ_l W_l) masked by ReLU'(H_l).  Tensor memory: dW in columns 0..175, dA in
-// 192..255.  Weight gradients go to this tile's slot of dwpart.
-__global__ void __launch_bounds__(128) k_mlp_backward(const MlpArgs a) {
+// Backward pass (128 threads per CTA, one CTA per SM, tiles blockIdx.x, blockIdx.x + gridDim.x,
+// ... in that order): for each tile and l = 4 .. 0, dW_l += dZ_l^T A_l over the tile's samples
+// (rows of dZ^T beyond the layer's outputs are zero) and, for l >= 1,
+// dZ_{l-1} = (dZ_l W_l) masked by ReLU'(H_l).  The weight gradients of all five layers stay in
+// tensor memory across the CTA's tiles (the MMAs accumulate into them; columns bw_dw_col(l),
+// 432 in all) and leave once, as the CTA's slot of dwpart; dZ_l W_l goes to columns BW_DA ..
+// BW_DA + 63, per tile.  The transposed weights stay in shared memory for the whole kernel;
+// each step's activation tile A_l^T is loaded into one of two buffers while the step before
+// runs its products and its epilogue (and the next tile's dY, dY^T while its layers 3 .. 0
+// run).  The tile order within a CTA and the number of CTAs are fixed, so the sums are
+// reproducible.
+constexpr uint32_t BW_COLS = 512;
+constexpr uint32_t BW_DA = 448;
+__host__ __device__ constexpr uint32_t bw_dw_col(int l) { return l == 0 ? 0u : (uint32_t)(K0 + (l - 1) * HID); }
+static_assert(bw_dw_col(NLAYER - 1) + HID <= BW_DA && BW_DA + HID <= BW_COLS, "tensor-memory columns of the backward pass");
+// shared-memory carve-up (bytes)
+constexpr int BS_SAT = K0 * 128 * 2;                 // one A_l^T buffer (the largest, layer 0)
+constexpr int BS_SWT = 2 * BS_SAT;                   // W_l^T of layers 1..4 (WB_BYTES)
+constexpr int BS_SDZ = BS_SWT + WB_BYTES;            // dZ, 128 x 64 (K-major)
+constexpr int BS_SDZT = BS_SDZ + 128 * HID * 2;      // dZ^T, 128 x 128 (rows 64.. zero)
+constexpr int BS_SDY = BS_SDZT + 128 * 128 * 2;      // dY, 128 x 16 (K-major)
+constexpr int BS_SDYT = BS_SDY + 128 * OUTP * 2;     // dY^T, 128 x 128 (rows 16.. zero)
+constexpr int BS_END = BS_SDYT + 128 * 128 * 2;      // 202,752
+__global__ void __launch_bounds__(128) k_mlp_backward(const MlpArgs a, int ntiles) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar;
     __shared__ uint32_t tmem_base;
-    uint8_t* sat = smem;                              // A_l^T, in_l x 128
-    uint8_t* sdz = sat + K0 * 128 * 2;                // dZ, 128 x out_l (K-major)
-    uint8_t* sdzt = sdz + 128 * HID * 2;              // dZ^T, 128 x 128 (rows >= out_l zero)
-    uint8_t* swt = sdzt + 128 * 128 * 2;              // W_l^T, in_l x out_l
+    uint8_t* sat[2] = {smem, smem + BS_SAT};
+    uint8_t* swt = smem + BS_SWT;
+    uint8_t* sdz = smem + BS_SDZ;
+    uint8_t* sdzt = smem + BS_SDZT;
+    uint8_t* sdy = smem + BS_SDY;
+    uint8_t* sdyt = smem + BS_SDYT;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tile = blockIdx.x;
-    const uint8_t* act = a.act + (size_t)tile * ACT_BYTES;
-    for (int i = tid; i < 128 * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sdzt)[i] = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = tid; i < 128 * 128 * 2 / 16; i += 128) {
+        reinterpret_cast<uint4*>(sdzt)[i] = make_uint4(0u, 0u, 0u, 0u);
+        reinterpret_cast<uint4*>(sdyt)[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
     __syncthreads();
-    for (int i = tid; i < 128 * OUTP * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sdz) + i, reinterpret_cast<const uint4*>(act + ACT_DY) + i);
-    for (int i = tid; i < OUTP * 128 * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sdzt) + i, reinterpret_cast<const uint4*>(act + ACT_DYT) + i);
-    cp_async_wait_all();
+    // the transposed weights, once; the first tile's dY, dY^T and A_4^T
+    for (int i = tid; i < WB_BYTES / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(swt) + i, reinterpret_cast<const uint4*>(a.wbf + WF_BYTES) + i);
+    auto load_dy = [&](int tile) {
+        const uint8_t* act = a.act + (size_t)tile * ACT_BYTES;
+        for (int i = tid; i < 128 * OUTP * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sdy) + i, reinterpret_cast<const uint4*>(act + ACT_DY) + i);
+        for (int i = tid; i < OUTP * 128 * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sdyt) + i, reinterpret_cast<const uint4*>(act + ACT_DYT) + i);
+    };
+    auto load_at = [&](int tile, int l, uint8_t* dst) {
+        const uint4* src = reinterpret_cast<const uint4*>(a.act + (size_t)tile * ACT_BYTES + (l == 0 ? ACT_X0T : act_ht(l)));
+        for (int i = tid; i < in_dim(l) * 128 * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(dst) + i, src + i);
+    };
+    load_dy(blockIdx.x);
+    load_at(blockIdx.x, NLAYER - 1, sat[0]);
+    asm volatile("cp.async.commit_group;" ::: "memory");
     if (tid == 0) mbar_init(&mbar, 1);
-    if (warp == 0) tmem_alloc(&tmem_base, 256);
+    if (warp == 0) tmem_alloc(&tmem_base, BW_COLS);
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = tmem_base;
     uint32_t phase = 0;
-    float* dw = a.dwpart + (size_t)tile * NWEIGHT;
-    for (int l = NLAYER - 1; l >= 0; --l) {
-        const int Kin = in_dim(l), Nout = out_dim(l);
-        const uint4* src = reinterpret_cast<const uint4*>(act + (l == 0 ? ACT_X0T : act_ht(l)));
-        for (int i = tid; i < Kin * 128 * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(sat) + i, src + i);
-        if (l >= 1) {
-            const uint4* w = reinterpret_cast<const uint4*>(a.wbf + wb_off(l));
-            for (int i = tid; i < Kin * Nout * 2 / 16; i += 128) cp_async16(reinterpret_cast<uint4*>(swt) + i, w + i);
-        }
-        cp_async_wait_all();
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            const uint32_t zt = smem_u32(sdzt), at = smem_u32(sat);
-            for (int kk = 0; kk < 8; ++kk)
-                mma_bf16(tmem, smem_desc(zt + 256u * kk, 128u, 16u * 128), smem_desc(at + 256u * kk, 128u, 16u * 128),
-                         idesc_bf16_f32(128, Kin), kk > 0);
-            if (l >= 1) {
-                const uint32_t z = smem_u32(sdz), w = smem_u32(swt);
-                for (int kk = 0; kk < Nout / 16; ++kk)
-                    mma_bf16(tmem + 192u, smem_desc(z + 256u * kk, 128u, 16u * Nout), smem_desc(w + 256u * kk, 128u, 16u * Nout),
-                             idesc_bf16_f32(128, HID), kk > 0);
+    int step = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const bool first = tile == (int)blockIdx.x;
+        for (int l = NLAYER - 1; l >= 0; --l, ++step) {
+            const int Kin = in_dim(l), Nout = out_dim(l);
+            uint8_t* cur = sat[step & 1];
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+            fence_proxy_async();
+            __syncthreads();
+            if (tid == 0) {
+                const uint32_t zt = smem_u32(l == NLAYER - 1 ? sdyt : sdzt), at = smem_u32(cur);
+                for (int kk = 0; kk < 8; ++kk)
+                    mma_bf16(tmem + bw_dw_col(l), smem_desc(zt + 256u * kk, 128u, 16u * 128), smem_desc(at + 256u * kk, 128u, 16u * 128),
+                             idesc_bf16_f32(128, Kin), (kk > 0 || !first) ? 1u : 0u);
+                if (l >= 1) {
+                    const uint32_t z = smem_u32(l == NLAYER - 1 ? sdy : sdz), w = smem_u32(swt + (wb_off(l) - WF_BYTES));
+                    for (int kk = 0; kk < Nout / 16; ++kk)
+                        mma_bf16(tmem + BW_DA, smem_desc(z + 256u * kk, 128u, 16u * Nout), smem_desc(w + 256u * kk, 128u, 16u * Nout),
+                                 idesc_bf16_f32(128, HID), kk > 0);
+                }
+                mma_commit(&mbar);
             }
-            mma_commit(&mbar);
-        }
-        bool seen = true;
-        if (warp == 0) {   // one warp watches the barrier (see k_mlp_forward)
-            seen = mbar_wait(&mbar, phase, WAIT_LIMIT);
+            // the next step's operands, into the other buffer, while this one runs
+            if (l > 0) {
+                load_at(tile, l - 1, sat[(step + 1) & 1]);
+            } else if (tile + (int)gridDim.x < ntiles) {
+                load_dy(tile + gridDim.x);
+                load_at(tile + gridDim.x, NLAYER - 1, sat[(step + 1) & 1]);
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            bool seen = true;
+            if (warp == 0) {   // one warp watches the barrier (see k_mlp_forward)
+                seen = mbar_wait(&mbar, phase, WAIT_LIMIT);
+                fence_before_sync();
+            }
+            ok = __syncthreads_and(seen);
+            phase ^= 1u;
+            if (!ok) {
+                if (tid == 0) atomicOr(a.err, 1u);
+                break;
+            }
+            fence_after_sync();
+            if (l >= 1) {
+                // dZ_{l-1} = (dZ_l W_l) * [H_l > 0], row = sample
+                const int m = tid;
+                for (int c = 0; c < HID; c += 16) {
+                    float v[16];
+                    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + BW_DA + (uint32_t)c, v);
+                    tmem_wait_ld();
+                    for (int j = 0; j < 16; ++j) {
+                        const int k = c + j;
+                        const float h = bf16_at(cur, kmajor_offset(k, m, 128));
+                        v[j] = h > 0.f ? v[j] : 0.f;
+                    }
+                    for (int j = 0; j < 16; ++j) {
+                        st_bf16(sdz, kmajor_offset(m, c + j, HID), v[j]);
+                        st_bf16(sdzt, kmajor_offset(c + j, m, 128), v[j]);
+                    }
+                }
+            }
             fence_before_sync();
+            fence_proxy_async();
+            __syncthreads();
+            fence_after_sync();
         }
-        const bool ok = __syncthreads_and(seen);
-        phase ^= 1u;
-        if (!ok) {
-            if (tid == 0) atomicOr(a.err, 1u);
-            break;
-        }
-        fence_after_sync();
-        // dW_l: rows = outputs (warps 0 and 1 hold rows 0..63)
-        if (warp < 2) {
-            const int row = warp * 32 + lane;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    // the CTA's weight gradients: rows = outputs (warps 0 and 1 hold rows 0..63), 16-byte stores
+    if (ok && warp < 2) {
+        const int row = warp * 32 + lane;
+        float* dw = a.dwpart + (size_t)blockIdx.x * NWEIGHT;
+        for (int l = 0; l < NLAYER; ++l) {
+            const int Kin = in_dim(l), Nout = out_dim(l);
             for (int c = 0; c < Kin; c += 16) {
                 float v[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + bw_dw_col(l) + (uint32_t)c, v);
                 tmem_wait_ld();
-                if (row < Nout)
-                    for (int j = 0; j < 16; ++j) dw[master_off(l) + row * Kin + c + j] = v[j];
-            }
-        }
-        if (l >= 1) {
-            // dZ_{l-1} = (dZ_l W_l) * [H_l > 0], row = sample
-            const int m = tid;
-            for (int c = 0; c < HID; c += 16) {
-                float v[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 192u + (uint32_t)c, v);
-                tmem_wait_ld();
-                for (int j = 0; j < 16; ++j) {
-                    const int k = c + j;
-                    const float h = bf16_at(sat, kmajor_offset(k, m, 128));
-                    v[j] = h > 0.f ? v[j] : 0.f;
-                }
-                for (int j = 0; j < 16; ++j) {
-                    st_bf16(sdz, kmajor_offset(m, c + j, HID), v[j]);
-                    st_bf16(sdzt, kmajor_offset(c + j, m, 128), v[j]);
+                if (row < Nout) {
+                    float4* d4 = reinterpret_cast<float4*>(dw + master_off(l) + row * Kin + c);
+                    for (int j = 0; j < 4; ++j) d4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                 }
             }
         }
-        fence_before_sync();
-        fence_proxy_async();
-        __syncthreads();
-        fence_after_sync();
     }
     fence_before_sync();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 256);
+    if (warp == 0) tmem_dealloc(tmem, BW_COLS);
 }
 
 // Master weights (FP32, [out][in] per layer) -> bf16 tiles: W_l (rows out, K in) and, for
@@ -549,7 +596,10 @@ __global__ void k_mlp_adam(const float* __restrict__ slices, float* __restrict__
 constexpr size_t FWD_SMEM_INFER = (size_t)WF_BYTES + INFER_GROUPS * GROUP_SMEM_INFER;   // 224 KB: one CTA per SM
 constexpr int TRAIN_GROUPS = 2;                                  // tiles in flight per training-forward CTA
 constexpr size_t FWD_SMEM_TRAIN = (size_t)WF_BYTES + TRAIN_GROUPS * GROUP_SMEM_TRAIN;   // 224 KB
-constexpr size_t BWD_SMEM = (size_t)K0 * 128 * 2 + 128 * HID * 2 + 128 * 128 * 2 + HID * HID * 2;
+// operands of the backward pass (more than half an SM's shared memory: one CTA per SM, each
+// holding all 512 tensor-memory columns)
+constexpr size_t BWD_SMEM = (size_t)BS_END;
+static_assert(BWD_SMEM > 114 * 1024 && BWD_SMEM <= 227 * 1024, "backward shared memory");
 }  // namespace
 
 extern "C" rc_status rc_mlp_tile_product(const uint16_t* d_a, const uint16_t* d_b, float* d_d, int K, int N, unsigned* d_err,
@@ -629,7 +679,7 @@ rc_status rc_mlp_create(const rc_mlp_config* cfg, rc_mlp** out) {
     m->cap_tiles = (cfg->max_batch + 127) / 128;
     if (cudaMalloc(&m->w, 4 * NWEIGHT) || cudaMalloc(&m->m1, 4 * NWEIGHT) || cudaMalloc(&m->m2, 4 * NWEIGHT) ||
         cudaMalloc(&m->grad, 4 * NWEIGHT) || cudaMalloc(&m->wbf, WF_BYTES + WB_BYTES) || cudaMalloc(&m->err, 4) ||
-        cudaMalloc(&m->loss, 4) || cudaMalloc(&m->part, (size_t)4 * NWEIGHT * m->cap_tiles) ||
+        cudaMalloc(&m->loss, 4) || cudaMalloc(&m->part, (size_t)4 * NWEIGHT * std::max(1, std::min(m->cap_tiles, m->sms))) ||
         cudaMalloc(&m->slices, (size_t)4 * NWEIGHT * GSLICES) ||
         cudaMalloc(&m->act, (size_t)ACT_BYTES * m->cap_tiles) || cudaMalloc(&m->state, 4 * ST_COUNT) ||
         cudaMalloc(&m->nonfinite, 4))
@@ -720,10 +770,11 @@ rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     if (cudaMemsetAsync(m->nonfinite, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "flag");
     k_mlp_forward<true, TRAIN_GROUPS><<<std::min((ntiles + TRAIN_GROUPS - 1) / TRAIN_GROUPS, m->sms), FWD_THREADS * TRAIN_GROUPS,
                                         FWD_SMEM_TRAIN, m->stream>>>(a);
-    k_mlp_backward<<<ntiles, 128, BWD_SMEM, m->stream>>>(a);
+    const int bwd_ctas = std::min(ntiles, m->sms);
+    k_mlp_backward<<<bwd_ctas, 128, BWD_SMEM, m->stream>>>(a, ntiles);
     m->step++;
     const float b1 = 0.9f, b2 = 0.99f;
-    k_mlp_gsum<<<dim3((NWEIGHT + 255) / 256, GSLICES), 256, 0, m->stream>>>(m->part, ntiles, m->slices);
+    k_mlp_gsum<<<dim3((NWEIGHT + 255) / 256, GSLICES), 256, 0, m->stream>>>(m->part, bwd_ctas, m->slices);
     k_mlp_gcheck<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->nonfinite);
     k_mlp_step<<<1, 32, 0, m->stream>>>(m->state, m->nonfinite, b1, b2);
     k_mlp_adam<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->w, m->m1, m->m2, m->grad, m->wbf, m->cfg.lr, b1, b2,
