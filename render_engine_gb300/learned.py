@@ -9,7 +9,8 @@ The network of include/rc_mlp.h stands where the per-point cache stands: every f
    A(hit) (Edir(hit) + L(hit)) with L(hit) the network's radiance at the hit point: paths the
    tracer itself generates, bootstrapped on the network as a neural radiance cache is;
 3. `steps_per_frame` Adam steps (rc_mlp_train, loss-scaled) on `batch` random points each, with
-   those estimates as targets.
+   those estimates as targets (`event_steps` more in each of the `event_frames` frames that
+   follow a state change).
 
 The network's inputs per point are its position and normal in the state's geometry and
 (albedo, direct light of lights 0..2) of that state, each light's direct light divided by a
@@ -35,7 +36,8 @@ class LearnedCache:
     network's inputs carry the direct light of lights 0..2)."""
 
     def __init__(self, ctx: N.Context, data: bytes, stream: int, batch: int = 1 << 16, lr: float = 1e-2, seed: int = 1,
-                 loss_scale: float = 0.0, steps_per_frame: int = 1, rays: float = 1.0):
+                 loss_scale: float = 0.0, steps_per_frame: int = 1, rays: float = 1.0, event_steps: int = 0,
+                 event_frames: int = 0):
         import torch
         info = ctx.info()
         self.ctx, self.np, self.nl = ctx, info["np"], info["nl"]
@@ -51,6 +53,9 @@ class LearnedCache:
                            loss_scale=loss_scale)
         self.batch = batch
         self.steps_per_frame = steps_per_frame
+        # after a state change: event_steps more steps per frame for event_frames frames
+        self.event_steps, self.event_frames = event_steps, event_frames
+        self.last_state, self.boost_left = None, 0
         self.method = LEARNED_METHOD.replace(budget=float(rays))
         dev = torch.device("cuda", torch.cuda.current_device())
         # the direct light enters scaled by one constant per light (its largest mean over the
@@ -94,8 +99,15 @@ class LearnedCache:
         if not predicted:
             self.predict(state)
         self.ctx.frame(state)
+        if self.last_state is not None and state != self.last_state:
+            self.boost_left = self.event_frames
+        self.last_state = state
+        steps = self.steps_per_frame
+        if self.boost_left > 0:
+            steps += self.event_steps
+            self.boost_left -= 1
         p4, n4, a4 = self.feat[state]
-        for _ in range(self.steps_per_frame):
+        for _ in range(steps):
             idx = torch.randint(0, self.np, (self.batch,), device=self.dev, generator=self.gen, dtype=torch.int32)
             self.mlp.train_raw(p4, n4, a4, self.ctx.device_ptr(N.A_LC), self.lcs, idx, self.batch)
 

@@ -44,7 +44,7 @@ def test_gradcheck_against_central_differences(scene_main_bytes):
     J1 = f(E1)
     J1.backward()
     np.testing.assert_allclose(E1.grad.numpy(), g, rtol=1e-6)
-    assert float(J1) == pytest.approx(float((E1.detach().numpy() * g).sum()), rel=1e-5)
+    assert float(J1.detach()) == pytest.approx(float((E1.detach().numpy() * g).sum()), rel=1e-5)
     ctx.close()
 
 
