@@ -514,8 +514,10 @@ def e2e_run(data, method, seq, local, stream, world):
     ctx = N.Context(device=local, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    # the load returns once the scene is on the device and checked; the five state builds it
+    # issued run on the context's second stream behind it, and each frame waits (on the device)
+    # only for its own state's build, as a caller that does not synchronise sees it
     ctx.load_bytes(host.numpy())
-    ctx.sync()
     t1 = time.perf_counter()
     ctx.begin(method, seq[0], 11)
     for s in seq:
@@ -527,7 +529,8 @@ def e2e_run(data, method, seq, local, stream, world):
     nf = len(seq)
     return {"value": nf * world / (t2 - t0), "unit": "frames/s", "h2d_bytes_per_step": len(data) / nf,
             "d2h_bytes_per_step": lc.nbytes / nf, "frames": nf, "load_ms": (t1 - t0) * 1e3, "frames_ms": (t2 - t1) * 1e3,
-            "includes": "scene upload from pinned host memory + load and state builds + frames 0-%d + final cache download" % (nf - 1)}
+            "includes": "scene upload from pinned host memory + load (returns when the scene is checked) + the state builds "
+                        "(second stream) + frames 0-%d + final cache download" % (nf - 1)}
 
 
 def quality(data, method, local, stream):
@@ -603,8 +606,9 @@ def quality(data, method, local, stream):
 def learned_bench(data, refs, local, batch=1 << 16):
     """The learned cache (render_engine_gb300/learned.py: the network trained online every frame on
     the tracer's one-bounce estimates, 2^16 samples per step, loss-scaled, and served as the
-    cache) against the per-point cache methods of the reference over the whole timing sequence
-    (5 states x 60 frames, 4 state changes): the 30-frame post-event luminance error over all
+    cache) against the reference's cache methods over the whole timing sequence (5 states x 60
+    frames, 4 state changes): the dependency-tracked `v4-A2C suivi 1/4`, the plain `Classique 1.0x`
+    and the SHaRC-style hash-grid cache `SHaRC responsive 1.0x`, the judge of the learned cache: the 30-frame post-event luminance error over all
     valid points and over the event region (as the quality leg), and each method's frame ms (CUDA
     events around each frame's work; for the learned cache inference + frame + training step).
     The per-point caches run at 1, 2, 4, 8 and 16 rays per point, so that one of them spends at least
@@ -695,7 +699,7 @@ def learned_bench(data, refs, local, batch=1 << 16):
               "note": "frame_ms = training step of the previous frame + inference of this one (the served values) + the rest "
                       "of the frame loop"})
     out["learned"] = r
-    for name in ("v4-A2C suivi 1/4", "Classique 1.0x"):
+    for name in ("v4-A2C suivi 1/4", "Classique 1.0x", "SHaRC responsive 1.0x"):
         for rays in (1.0, 2.0, 4.0, 8.0, 16.0):
             m = M.by_name(M.timing_methods(), name).replace(rays=rays)
             c = N.Context(device=local, stream=stream.cuda_stream)
@@ -714,6 +718,15 @@ def learned_bench(data, refs, local, batch=1 << 16):
             if best is None or v["post_event_err_pct"] < out[best]["post_event_err_pct"]:
                 best = k
     out["per_point_cache_at_equal_or_more_ms"] = best
+    # the judge the learned cache is held to: the SHaRC-style hash-grid cache (bench B's "SHaRC
+    # responsive": spatial-hash cache points, running mean reset where a light's contribution
+    # changes) at the cheapest ray budget whose frame costs at least the learned cache's
+    sharc = sorted((v["frame_ms"], k) for k, v in out.items() if k.startswith("SHaRC") and isinstance(v, dict))
+    judge = next((k for ms, k in sharc if ms >= out["learned"]["frame_ms"]), sharc[-1][1] if sharc else None)
+    if judge is not None:
+        out["hash_grid_judge"] = {"method": judge, "frame_ms": out[judge]["frame_ms"],
+                                  "post_event_err_pct": out[judge]["post_event_err_pct"],
+                                  "learned_post_event_le_judge": out["learned"]["post_event_err_pct"] <= out[judge]["post_event_err_pct"]}
     return out
 
 
