@@ -432,7 +432,11 @@ def run_ours(args, world, rank, local, dist):
                         "note": "cache-point frame + one primary ray per pixel at 1920x1080 shaded from the cache"},
     }
     ctx.close()
-    out["e2e"] = e2e_run(data, method, seq, local, stream, world)
+    # three end-to-end runs, the median reported (each maps no new memory unless the pool could
+    # not reuse a freed block in time: the spread is in `runs`)
+    e2e_runs = sorted((e2e_run(data, method, seq, local, stream, world) for _ in range(3)), key=lambda r: r["value"])
+    out["e2e"] = dict(e2e_runs[1])
+    out["e2e"]["runs"] = [round(r["value"], 1) for r in e2e_runs]
     out["e2e"]["first_load_in_process_ms"] = first_load_ms
     # the seeded stand-in room of the same size, the same frames
     if args.points == POINTS and os.path.exists(SCENE_1M):

@@ -161,9 +161,12 @@ rc_status rc_device_info_get(rc_ctx* ctx, rc_device_info* out);
 /* Load a scene, formats 2 and 3, and build every state's direct light and shadow-voxel
  * masks on the GPU.  Replaces load() + k_build (poc_gpu.cu:751-801, 369-391).  The memory
  * variant takes the same bytes from a host buffer (page-locked memory is copied by DMA).
- * The call returns once the bytes are on the device and checked; the states' builds then run
- * on a second stream of the context, and the context's stream waits for a state's build where
- * it first uses the state (no host synchronisation).  rc_sync waits for them too. */
+ * The call returns once the bytes are on the device and checked.  The states' builds run on a
+ * second stream of the context: state 0's is issued by the load, and the first use of a state
+ * issues the next state's, so a run moving through the states finds each one built; the
+ * context's stream waits for a state's build where it first uses the state (no host
+ * synchronisation), and builds the state itself if it was not issued.  rc_sync waits for
+ * them too. */
 rc_status rc_scene_load(rc_ctx* ctx, const char* path);
 rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes);
 rc_status rc_scene_info_get(const rc_ctx* ctx, rc_scene_info* out);

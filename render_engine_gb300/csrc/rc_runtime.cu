@@ -81,7 +81,7 @@ struct HostState {
     DState d{};
     // Built on first use (ensure_state): until then the state's positions, normals and warm
     // start wait on the device as the file lays them out (xyz triples, NL floats per point).
-    bool built = false;             // build issued (on the side stream, or on the context's stream)
+    bool built = false;             // build issued (on the side stream ahead of use, or on the context's stream)
     bool wait = false;              // the context's stream has yet to wait for the side stream's build
     const float* raw = nullptr;     // 6 Np floats (P, N) then NL Np (Pw, scenes with references)
     const float* dint = nullptr;    // device light intensities
@@ -157,7 +157,7 @@ struct rc_ctx {
         int stride = 0, npaths = 0;
         cudaEvent_t ready = nullptr;
     } cam;
-    cudaStream_t side = nullptr;                // state builds after a load (issue_state_builds)
+    cudaStream_t side = nullptr;                // state builds issued ahead of use (prebuild_state)
     std::vector<cudaEvent_t> state_ev;          // per state: its build on the side stream is done
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
     int adj_cap_np = 0, adj_cap_k = 0, adj_cap_nl = 0;   // sizes the adjoint buffers were allocated for
@@ -318,6 +318,32 @@ rc_status dput_raw(rc_ctx* ctx, std::vector<DevBuf>& pool, const T** out, const 
     *out = p;
     return RC_OK;
 }
+
+// The small host arrays of a scene (lights, quads, triangles, groups, intensities, event lists),
+// gathered into one host block and sent with one copy into one buffer of the pool: about a
+// hundred small copies from pageable memory cost more than the 139 MB of per-point arrays.
+struct Stage {
+    struct Item { void** slot; size_t off; };
+    std::vector<uint8_t> host;
+    std::vector<Item> items;
+    template <class T>
+    void add(const T** out, const std::vector<T>& v) {
+        const size_t off = (host.size() + 255) & ~(size_t)255;
+        host.resize(off + v.size() * sizeof(T));
+        if (!v.empty()) memcpy(host.data() + off, v.data(), v.size() * sizeof(T));
+        items.push_back({reinterpret_cast<void**>(const_cast<T**>(out)), off});
+    }
+    rc_status flush(rc_ctx* ctx, std::vector<DevBuf>& pool) {
+        if (items.empty()) return RC_OK;
+        uint8_t* p = nullptr;
+        rc_status s = dalloc(ctx, pool, &p, host.size());
+        if (s != RC_OK) return s;
+        if (!host.empty()) CKR(cudaMemcpyAsync(p, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->stream));
+        for (const Item& it : items) *it.slot = p + it.off;
+        items.clear();
+        return RC_OK;
+    }
+};
 
 // poc_gpu.cu:720-735: fine event grid (16 x 8 x 6 over the 8 x 4 x 3 m box) -> transit grid.
 std::vector<int> to_grid(const std::vector<int>& fine, int VX, int VY, int VZ) {
@@ -573,10 +599,9 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     if (r.bad) return fail(ctx, RC_ERR_FORMAT, "scene: truncated");
     rc_status s;
     CKR(RC_DISPATCH(NL, preload(NW)));
-    const float* dL = nullptr;
-    if ((s = dput(ctx, pool, &dL, L)) || (s = dput_raw(ctx, pool, &g.A, A, Np)) || (s = dput_raw(ctx, pool, &g.region, region, Np)))
-        return s;
-    S.L = dL;
+    Stage stage;
+    stage.add(&S.L, L);
+    if ((s = dput_raw(ctx, pool, &g.A, A, Np)) || (s = dput_raw(ctx, pool, &g.region, region, Np))) return s;
     // region ids index the per-region statistics; checked on the device (no frame runs before
     // the load has read the result back)
     k_load_check<<<load_grid(Np), 256, 0, ctx->stream>>>(g.region, Np, 0, S.NR, ctx->flags_dev + 2, LOAD_BAD_REGION);
@@ -612,10 +637,13 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         Groups G = build_groups(T, TQ, S.Nt);
         DState& d = hs.d;
         memset(&d, 0, sizeof d);
-        if ((s = dput(ctx, pool, &d.Q, Q)) || (s = dput(ctx, pool, &d.dims, dims)) || (s = dput(ctx, pool, &d.off, off)) ||
-            (s = dput(ctx, pool, &d.tri, tri)) || (s = dput(ctx, pool, &d.grp, G.grp)) || (s = dput(ctx, pool, &d.misc, G.misc)) ||
-            (s = dput(ctx, pool, &hs.dint, hs.inten)))
-            return s;
+        stage.add(&d.Q, Q);
+        stage.add(&d.dims, dims);
+        stage.add(&d.off, off);
+        stage.add(&d.tri, tri);
+        stage.add(&d.grp, G.grp);
+        stage.add(&d.misc, G.misc);
+        stage.add(&hs.dint, hs.inten);
         {
             // the per-point arrays are copied now (the caller's buffer is not kept) and re-laid
             // out when the state is first used
@@ -655,13 +683,10 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
             for (int v : dst) if (v < 0 || v >= S.grid.vx * S.grid.vy * S.grid.vz) return fail(ctx, RC_ERR_FORMAT, "event voxel out of range");
         }
     }
-    S.ev_dev.resize(S.ev.size());
-    for (size_t e = 0; e < S.ev.size(); ++e) {
-        if (S.ev[e].empty()) { S.ev_dev[e] = nullptr; continue; }
-        const int* p = nullptr;
-        if ((s = dput(ctx, pool, &p, S.ev[e]))) return s;
-        S.ev_dev[e] = p;
-    }
+    S.ev_dev.assign(S.ev.size(), nullptr);
+    for (size_t e = 0; e < S.ev.size(); ++e)
+        if (!S.ev[e].empty()) stage.add(&S.ev_dev[e], S.ev[e]);
+    if ((s = stage.flush(ctx, pool))) return s;
     unsigned bad = 0;
     CKR(cudaMemcpyAsync(&bad, ctx->flags_dev + 2, sizeof bad, cudaMemcpyDeviceToHost, ctx->stream));
     CKR(cudaStreamSynchronize(ctx->stream));
@@ -718,7 +743,21 @@ rc_status build_state(rc_ctx* ctx, int k, cudaStream_t st) {
     ctx->launches += 3 + (S.has_ref ? 1 : 0);
     return RC_OK;
 }
-// Before the context's stream uses state k: wait for its build on the side stream, or build it.
+// State k's build issued on the side stream (behind the load's copies, which the side stream
+// waits for once, at the load), unless it is built or issued already; the context's stream waits
+// for its event at first use.
+rc_status prebuild_state(rc_ctx* ctx, int k) {
+    HostState& hs = ctx->S.st[k];
+    if (hs.built || !ctx->side) return RC_OK;
+    rc_status s = build_state(ctx, k, ctx->side);
+    if (s != RC_OK) return s;
+    CKR(cudaEventRecord(ctx->state_ev[k], ctx->side));
+    hs.wait = true;
+    return RC_OK;
+}
+// Before the context's stream uses state k: wait for its build on the side stream, or build it;
+// then issue the next state's build on the side stream, so that a run moving through the states
+// in order finds each one built (a state that is never used is never built).
 rc_status ensure_state(rc_ctx* ctx, int k) {
     Scene& S = ctx->S;
     if (k < 0 || k >= S.NS) return fail(ctx, RC_ERR_ARG, "state %d out of range", k);
@@ -728,9 +767,11 @@ rc_status ensure_state(rc_ctx* ctx, int k) {
             CKR(cudaStreamWaitEvent(ctx->stream, ctx->state_ev[k], 0));
             hs.wait = false;
         }
-        return RC_OK;
+    } else {
+        rc_status s = build_state(ctx, k, ctx->stream);
+        if (s != RC_OK) return s;
     }
-    return build_state(ctx, k, ctx->stream);
+    return S.NS > 1 ? prebuild_state(ctx, (k + 1) % S.NS) : RC_OK;
 }
 rc_status ensure_all_states(rc_ctx* ctx) {
     for (int k = 0; k < ctx->S.NS; ++k) {
@@ -739,9 +780,8 @@ rc_status ensure_all_states(rc_ctx* ctx) {
     }
     return RC_OK;
 }
-// After a load: every state's build issued on the side stream behind the load's copies, in
-// state order, each followed by an event that the context's stream waits for at first use.
-// The builds overlap whatever the context's stream does next (the first frames, mostly).
+// After a load: the side stream waits for the load's copies, and state 0's build (where runs
+// usually begin) is issued on it; the other states are built ahead of their first use.
 rc_status issue_state_builds(rc_ctx* ctx) {
     Scene& S = ctx->S;
     if (!ctx->side) CKR(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
@@ -753,13 +793,7 @@ rc_status issue_state_builds(rc_ctx* ctx) {
     cudaEvent_t copies = ctx->state_ev[0];
     CKR(cudaEventRecord(copies, ctx->stream));
     CKR(cudaStreamWaitEvent(ctx->side, copies, 0));
-    for (int k = 0; k < S.NS; ++k) {
-        rc_status s = build_state(ctx, k, ctx->side);
-        if (s != RC_OK) return s;
-        CKR(cudaEventRecord(ctx->state_ev[k], ctx->side));
-        S.st[k].wait = true;
-    }
-    return RC_OK;
+    return prebuild_state(ctx, 0);
 }
 
 rc_status alloc_cache(rc_ctx* ctx) {
