@@ -71,11 +71,24 @@ inline void set_grid_scale(Grid& g) {
     g.scale[2] = (float)g.vz / g.ext[2];
 }
 
-// poc_gpu.cu:137-142
+// One axis of vox_of (poc_gpu.cu:137-142): int((x - lo) / ext * n), clamped to [0, n - 1].  The
+// reference's quotient q = (x - lo) / ext * n is only needed to the integer: qf = (x - lo) * s,
+// s = n / ext rounded, differs from it by a few ulps, far less than the 1e-3 margin asked of qf's
+// distance to the nearest integer, so truncating qf gives q's integer whenever qf is that far
+// from one.  Otherwise (and for a NaN or an infinity, whose comparisons are false) the
+// reference's own IEEE division decides.  The result is the reference's, without the division in
+// all but a few samples.
+__device__ __forceinline__ int vox_axis(float x, float lo, float ext, float s, int n) {
+    const float d = x - lo;
+    const float qf = d * s;
+    const float r = rintf(qf);
+    const int v = fabsf(qf - r) > 1e-3f * fmaxf(1.f, fabsf(qf)) ? int(qf) : int(d / ext * n);
+    return min(max(v, 0), n - 1);
+}
 __device__ __forceinline__ int vox_of(const Grid& g, f3 p) {
-    int i = min(max(int((p.x - g.lo[0]) / g.ext[0] * g.vx), 0), g.vx - 1);
-    int j = min(max(int((p.y - g.lo[1]) / g.ext[1] * g.vy), 0), g.vy - 1);
-    int k = min(max(int((p.z - g.lo[2]) / g.ext[2] * g.vz), 0), g.vz - 1);
+    const int i = vox_axis(p.x, g.lo[0], g.ext[0], g.scale[0], g.vx);
+    const int j = vox_axis(p.y, g.lo[1], g.ext[1], g.scale[1], g.vy);
+    const int k = vox_axis(p.z, g.lo[2], g.ext[2], g.scale[2], g.vz);
     return (k * g.vy + j) * g.vx + i;
 }
 
