@@ -159,6 +159,7 @@ struct rc_ctx {
     } cam;
     cudaStream_t side = nullptr;                // state builds issued ahead of use (prebuild_state)
     std::vector<cudaEvent_t> state_ev;          // per state: its build on the side stream is done
+    cudaEvent_t load_ev = nullptr;              // the load's copies, which the side stream waits for
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
     int adj_cap_np = 0, adj_cap_k = 0, adj_cap_nl = 0;   // sizes the adjoint buffers were allocated for
     float4* adj_aeu = nullptr;                  // unit-emission direct light of the last adjoint
@@ -320,7 +321,7 @@ rc_status dput_raw(rc_ctx* ctx, std::vector<DevBuf>& pool, const T** out, const 
 }
 
 // The small host arrays of a scene (lights, quads, triangles, groups, intensities, event lists),
-// gathered into one host block and sent with one copy into one buffer of the pool: about a
+// gathered into one host block and sent with one copy per flush into one buffer of the pool: about a
 // hundred small copies from pageable memory cost more than the 139 MB of per-point arrays.
 struct Stage {
     struct Item { void** slot; size_t off; };
@@ -341,6 +342,7 @@ struct Stage {
         if (!host.empty()) CKR(cudaMemcpyAsync(p, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->stream));
         for (const Item& it : items) *it.slot = p + it.off;
         items.clear();
+        host.clear();   // a copy from pageable memory has taken the bytes when it returns
         return RC_OK;
     }
 };
@@ -525,6 +527,10 @@ Groups build_groups(const std::vector<float>& T, const std::vector<int>& TQ, int
     return out;
 }
 
+rc_status build_state(rc_ctx* ctx, Scene& S, int k, cudaStream_t st);
+rc_status ensure_side(rc_ctx* ctx, int ns);
+rc_status side_after_stream(rc_ctx* ctx);
+
 rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     Reader r{data, n};
     int h[8];
@@ -664,6 +670,15 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         d.gr = G.gr;
         size_t smem = frame_smem_bytes(d);
         if (smem > 200 * 1024) return fail(ctx, RC_ERR_UNSUPPORTED, "%d dynamic triangles exceed shared memory", S.Nt);
+        if (k == 0) {
+            // state 0's build (where runs usually begin) starts on the side stream as soon as its
+            // arrays are on the device, while the other states' copies stream in
+            if ((s = stage.flush(ctx, pool)) || (s = ensure_side(ctx, S.NS)) || (s = side_after_stream(ctx)) ||
+                (s = build_state(ctx, S, 0, ctx->side)))
+                return s;
+            CKR(cudaEventRecord(ctx->state_ev[0], ctx->side));
+            hs.wait = true;
+        }
     }
     const int npairs = S.NS * S.NS;
     S.ev.resize((size_t)npairs * (1 + NL));
@@ -703,8 +718,7 @@ namespace {
 // A state's device build: positions and normals packed to float4, the warm start padded like
 // the cache, the direct light and shadow-voxel masks (k_build); the raw copy is then released.
 // Issued on stream `st`.
-rc_status build_state(rc_ctx* ctx, int k, cudaStream_t st) {
-    Scene& S = ctx->S;
+rc_status build_state(rc_ctx* ctx, Scene& S, int k, cudaStream_t st) {
     HostState& hs = S.st[k];
     const int NL = S.NL, NW = ctx->NW;
     const size_t Np = (size_t)S.Np;
@@ -749,7 +763,7 @@ rc_status build_state(rc_ctx* ctx, int k, cudaStream_t st) {
 rc_status prebuild_state(rc_ctx* ctx, int k) {
     HostState& hs = ctx->S.st[k];
     if (hs.built || !ctx->side) return RC_OK;
-    rc_status s = build_state(ctx, k, ctx->side);
+    rc_status s = build_state(ctx, ctx->S, k, ctx->side);
     if (s != RC_OK) return s;
     CKR(cudaEventRecord(ctx->state_ev[k], ctx->side));
     hs.wait = true;
@@ -768,7 +782,7 @@ rc_status ensure_state(rc_ctx* ctx, int k) {
             hs.wait = false;
         }
     } else {
-        rc_status s = build_state(ctx, k, ctx->stream);
+        rc_status s = build_state(ctx, S, k, ctx->stream);
         if (s != RC_OK) return s;
     }
     return S.NS > 1 ? prebuild_state(ctx, (k + 1) % S.NS) : RC_OK;
@@ -780,19 +794,29 @@ rc_status ensure_all_states(rc_ctx* ctx) {
     }
     return RC_OK;
 }
-// After a load: the side stream waits for the load's copies, and state 0's build (where runs
-// usually begin) is issued on it; the other states are built ahead of their first use.
-rc_status issue_state_builds(rc_ctx* ctx) {
-    Scene& S = ctx->S;
+// The side stream and the per-state events (created once per context, grown with the scene).
+rc_status ensure_side(rc_ctx* ctx, int ns) {
     if (!ctx->side) CKR(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
-    while ((int)ctx->state_ev.size() < S.NS) {
+    if (!ctx->load_ev) CKR(cudaEventCreateWithFlags(&ctx->load_ev, cudaEventDisableTiming));
+    while ((int)ctx->state_ev.size() < ns) {
         cudaEvent_t e = nullptr;
         CKR(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         ctx->state_ev.push_back(e);
     }
-    cudaEvent_t copies = ctx->state_ev[0];
-    CKR(cudaEventRecord(copies, ctx->stream));
-    CKR(cudaStreamWaitEvent(ctx->side, copies, 0));
+    return RC_OK;
+}
+// The side stream waits for everything the context's stream has queued (the load's copies).
+rc_status side_after_stream(rc_ctx* ctx) {
+    CKR(cudaEventRecord(ctx->load_ev, ctx->stream));
+    CKR(cudaStreamWaitEvent(ctx->side, ctx->load_ev, 0));
+    return RC_OK;
+}
+// After a load: the side stream waits for all of the load's copies (state 0's build was issued
+// by the load itself, behind its own copies); the other states are built ahead of first use.
+rc_status issue_state_builds(rc_ctx* ctx) {
+    rc_status s = ensure_side(ctx, ctx->S.NS);
+    if (s != RC_OK) return s;
+    if ((s = side_after_stream(ctx)) != RC_OK) return s;
     return prebuild_state(ctx, 0);
 }
 
@@ -1316,6 +1340,7 @@ void rc_destroy(rc_ctx* ctx) {
     if (ctx->img) cudaFree(ctx->img);
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
     for (auto& e : ctx->state_ev) cudaEventDestroy(e);
+    if (ctx->load_ev) cudaEventDestroy(ctx->load_ev);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
