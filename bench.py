@@ -45,6 +45,13 @@ SCENE_1M = os.path.join(ROOT, "tests", "golden", "scene_scale_1M.bin.gz")
 POST_FRAMES, PRE_FRAMES = 30, 20     # the reference's post / pre windows (poc_gpu.cu:1428-1429)
 
 
+def _json_default(o):
+    """numpy scalars (a bool or a float that came from an array) as Python values."""
+    if hasattr(o, "item"):
+        return o.item()
+    raise TypeError("not JSON serializable: %r" % (o,))
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -730,7 +737,7 @@ def learned_bench(data, refs, local, batch=1 << 16):
     if judge is not None:
         out["hash_grid_judge"] = {"method": judge, "frame_ms": out[judge]["frame_ms"],
                                   "post_event_err_pct": out[judge]["post_event_err_pct"],
-                                  "learned_post_event_le_judge": out["learned"]["post_event_err_pct"] <= out[judge]["post_event_err_pct"]}
+                                  "learned_post_event_le_judge": bool(out["learned"]["post_event_err_pct"] <= out[judge]["post_event_err_pct"])}
     return out
 
 
@@ -1168,7 +1175,7 @@ def main():
                                  "sample": "the reference's own kernels (cuda/poc_gpu.cu for sm_103a) on the GB300, driven by one host thread; "
                                            "the reference has no CPU implementation of this path"},
                 "e2e": {"value": res["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(line, default=_json_default))
         return
     res, data, method, refs = run_ours(args, world, rank, local, dist)
     if rank != 0:
@@ -1189,7 +1196,7 @@ def main():
             "cpu_baseline": cpu, "quality": res["quality"], "standin_room": res.get("standin_room"), "hashgrid": res["hashgrid"],
             "mlp": res["mlp"], "adjoint": res["adjoint"], "taa": res["taa"], "camera_paths": res["camera_paths"],
             "street": res["street"], "city": res["city"], "learned_cache": res["learned_cache"]}
-    print(json.dumps(line))
+    print(json.dumps(line, default=_json_default))
 
 
 if __name__ == "__main__":
