@@ -322,6 +322,9 @@ def time_frames(ctx, method, seq, s0, args, stream, flush, dist=None):
     split: trace and update as separate kernels)."""
     import torch
     from render_engine_gb300 import native as N
+    # every state built before the frames (as the reference's load does): no build shares the GPU
+    # with a timed frame
+    ctx.build_states()
     ctx.begin(method, seq[0], 11)
     for f in range(s0):
         ctx.frame(seq[f])
@@ -689,6 +692,8 @@ def learned_bench(data, refs, local, batch=1 << 16):
     steps_per_frame, event_steps, event_frames, lr = 4, 8, 10, 7e-3
     lc = LC.LearnedCache(ctx, data, stream.cuda_stream, batch=batch, lr=lr, seed=1, steps_per_frame=steps_per_frame,
                          event_steps=event_steps, event_frames=event_frames)
+    ctx.build_states()
+    ctx.sync()
     lc.begin(seq[0], 11)
     for _ in range(warm):
         lc.frame(seq[0])
@@ -715,6 +720,8 @@ def learned_bench(data, refs, local, batch=1 << 16):
             m = M.by_name(M.timing_methods(), name).replace(rays=rays)
             c = N.Context(device=local, stream=stream.cuda_stream)
             c.load_bytes(data)
+            c.build_states()
+            c.sync()
             c.begin(m, seq[0], 11)
 
             def cache_step(f, s, c=c):

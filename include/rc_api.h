@@ -187,6 +187,12 @@ rc_status rc_errors(rc_ctx* ctx, float* out, int max, int* n);
 rc_status rc_run(rc_ctx* ctx, const rc_method* m, const int* seq, int nframes, uint32_t seed,
                  int want_err, float* errs, rc_timers* tm);
 rc_status rc_sync(rc_ctx* ctx);
+/* Issue the build of every state of the loaded scene that is not built or issued yet, on the
+ * context's second stream (the context's stream waits for each where it first uses the state).
+ * No counterpart in the reference, whose load builds every state before returning: for a caller
+ * that wants every state ready before a section whose frames must not share the GPU with a
+ * build (rc_sync then waits for them). */
+rc_status rc_scene_build_states(rc_ctx* ctx);
 
 /* Image pass (no counterpart in the reference, whose bench B has no camera): one primary ray
  * per pixel through the geometry of `state`, shaded from the current cache with the light

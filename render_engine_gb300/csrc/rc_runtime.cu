@@ -1513,6 +1513,17 @@ rc_status rc_sync(rc_ctx* ctx) {
     return RC_OK;
 }
 
+rc_status rc_scene_build_states(rc_ctx* ctx) {
+    if (!ctx) return RC_ERR_ARG;
+    if (!ctx->have_scene) return fail(ctx, RC_ERR_STATE, "no scene loaded");
+    CKR(cudaSetDevice(ctx->cfg.device));
+    for (int k = 0; k < ctx->S.NS; ++k) {
+        rc_status s = prebuild_state(ctx, k);
+        if (s != RC_OK) return s;
+    }
+    return RC_OK;
+}
+
 static rc_status camera_basis(rc_ctx* ctx, const rc_camera* cam, CameraD* out) {
     // camera frame: forward to the target, right = forward x up, up re-orthogonalised
     double f[3], r[3], u[3];

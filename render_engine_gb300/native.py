@@ -38,7 +38,7 @@ FLAG_RAY_QUEUE = 8
 EXPORTS = [
     "rc_abi_version", "rc_status_string", "rc_create", "rc_destroy", "rc_last_error", "rc_device_info_get",
     "rc_scene_load", "rc_scene_load_memory", "rc_scene_info_get", "rc_state_lights", "rc_run_begin", "rc_frame",
-    "rc_errors", "rc_run", "rc_sync", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
+    "rc_errors", "rc_run", "rc_sync", "rc_scene_build_states", "rc_render", "rc_array_info", "rc_array_copy", "rc_scalar_get", "rc_scalar_set",
     "rc_state_array_copy", "rc_probe_rays", "rc_trace_rays", "rc_trace_check_count", "rc_run_stats_get", "rc_device_flags",
     "rc_error_sums_noalloc", "rc_reference_build", "rc_adjoint", "rc_adjoint_arrays", "rc_taa_begin", "rc_taa_frame",
     "rc_taa_array_copy", "rc_prep_mesh", "rc_prep_mesh_params",
@@ -131,6 +131,8 @@ def load_library():
     L.rc_run.argtypes = [vp, ctypes.POINTER(CMethod), ip, i, u32, i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(Timers)]
     L.rc_sync.restype = i
     L.rc_sync.argtypes = [vp]
+    L.rc_scene_build_states.restype = i
+    L.rc_scene_build_states.argtypes = [vp]
     L.rc_render.restype = i
     L.rc_render.argtypes = [vp, i, ctypes.POINTER(Camera), ctypes.POINTER(ctypes.c_float), sz]
     L.rc_array_info.restype = i
@@ -304,6 +306,10 @@ class Context:
 
     def sync(self):
         self._chk(self.L.rc_sync(self.h))
+
+    def build_states(self):
+        """Issue every state's build now (rc_scene_build_states); sync() waits for them."""
+        self._chk(self.L.rc_scene_build_states(self.h))
 
     def render(self, state: int, cam: Camera, copy: bool = True):
         """Image pass from the current cache; returns an (h, w) float32 image when copy."""

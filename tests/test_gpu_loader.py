@@ -65,3 +65,29 @@ def test_truncated_scene_rejected(scene_main_bytes):
             ctx.load_bytes(scene_main_bytes[:cut])
     ctx.load_bytes(scene_main_bytes)
     assert np.isfinite(_run_frames(ctx)).all()
+
+
+def test_states_built_ahead_of_use_give_the_same_frames(scene_main_bytes):
+    """States built ahead of use on the second stream in another order (rc_scene_build_states for
+    all of them before the run, against the load's build of state 0 and the look-ahead of the next
+    state during a run that jumps between states, where a state can be built on the context's
+    stream at first use) hold the same direct light and give the same frames, bit for bit."""
+    m = M.by_name(M.timing_methods(), "Classique 2.0x")   # no float-atomic sums: runs are bit-reproducible
+    seq = [0] * 6 + [3] * 5 + [1] * 5 + [4] * 4 + [2] * 4
+    out = []
+    for ahead in (False, True):
+        ctx = N.Context()
+        ctx.load_bytes(scene_main_bytes)
+        if ahead:
+            ctx.build_states()
+            ctx.sync()
+        ctx.begin(m, seq[0], 7)
+        for s in seq:
+            ctx.frame(s)
+        ctx.sync()
+        assert ctx.device_flags() == 0
+        out.append((ctx.array(N.A_LC).copy(), [ctx.state_array(k, N.SA_EDIR).copy() for k in range(5)]))
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
