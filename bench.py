@@ -625,8 +625,8 @@ def learned_bench(data, refs, local, batch=1 << 16):
     and the SHaRC-style hash-grid cache `SHaRC responsive 1.0x`, the judge of the learned cache: the 30-frame post-event luminance error over all
     valid points and over the event region (as the quality leg), and each method's frame ms (CUDA
     events around each frame's work; for the learned cache inference + frame + training step).
-    The per-point caches run at 1, 2, 4, 8 and 16 rays per point, so that one of them spends at least
-    the learned cache's time per frame.  The per-point caches start from the converged cache of the
+    The per-point caches run at 1, 2, 4, 8 and 16 rays per point (the hash-grid cache at 32 too), so
+    that one of them spends at least the learned cache's time per frame.  The per-point caches start from the converged cache of the
     first state, as the reference's runs do (the references' per-light warm start written into the
     scene); the network runs 120 frames of its own online training in the first state before the
     sequence (training it on that warm start first was measured worse: 46-49 % before events).
@@ -716,7 +716,7 @@ def learned_bench(data, refs, local, batch=1 << 16):
                       "of the frame loop"})
     out["learned"] = r
     for name in ("v4-A2C suivi 1/4", "Classique 1.0x", "SHaRC responsive 1.0x"):
-        for rays in (1.0, 2.0, 4.0, 8.0, 16.0):
+        for rays in (1.0, 2.0, 4.0, 8.0, 16.0) + ((32.0,) if name.startswith("SHaRC") else ()):
             m = M.by_name(M.timing_methods(), name).replace(rays=rays)
             c = N.Context(device=local, stream=stream.cuda_stream)
             c.load_bytes(data)
@@ -744,6 +744,7 @@ def learned_bench(data, refs, local, batch=1 << 16):
     if judge is not None:
         out["hash_grid_judge"] = {"method": judge, "frame_ms": out[judge]["frame_ms"],
                                   "post_event_err_pct": out[judge]["post_event_err_pct"],
+                                  "judge_frame_ms_ge_learned": bool(out[judge]["frame_ms"] >= out["learned"]["frame_ms"]),
                                   "learned_post_event_le_judge": bool(out["learned"]["post_event_err_pct"] <= out[judge]["post_event_err_pct"])}
     return out
 
