@@ -25,6 +25,13 @@ extern "C" {
 rc_status rc_mlp_tile_product(const uint16_t* d_a, const uint16_t* d_b, float* d_d, int K, int N, unsigned* d_err,
                               void* stream);
 
+/* Health check of the bounded completion waits every kernel of this library uses (an mbarrier
+ * polled at most a fixed number of times, then the error flag instead of a hang): one warp
+ * waits on an mbarrier for at most `polls` polls; `arrive` = 1 makes one thread arrive on it
+ * first (the wait must succeed), 0 leaves it without an arrival (the wait must give up).
+ * *d_err |= 1 when the wait gave up.  polls in [1, 2^24]. */
+rc_status rc_mlp_wait_check(uint32_t polls, int arrive, unsigned* d_err, void* stream);
+
 /* The network: 168 input features -> 64 -> 64 -> 64 -> 64 -> n_out (<= 16), ReLU between
  * layers, no biases, bf16 weights and activations, FP32 accumulation, Adam (beta 0.9 / 0.99).
  * Inputs per point (float4 each): position (xyz), normal (xyz), and (albedo, direct light of

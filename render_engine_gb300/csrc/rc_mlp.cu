@@ -76,6 +76,16 @@ __global__ void __launch_bounds__(128) k_tile_product(const uint16_t* __restrict
     if (warp == 0) tmem_dealloc(tmem, ncols);
 }
 
+// The bounded wait on its own: an mbarrier of one expected arrival, which one thread provides
+// or nobody does; one thread polls it at most `polls` times.
+__global__ void k_wait_check(uint32_t polls, int arrive, unsigned* __restrict__ err) {
+    __shared__ uint64_t mbar;
+    if (threadIdx.x == 0) mbar_init(&mbar, 1);
+    __syncwarp();
+    if (arrive && threadIdx.x == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&mbar)) : "memory");
+    __syncwarp();
+    if (threadIdx.x == 0 && !mbar_wait(&mbar, 0, polls)) atomicOr(err, 1u);
+}
 
 // ---------------------------------------------------------------- the network
 // 168 input features (padded to 176) -> 64 -> 64 -> 64 -> 64 -> 16 outputs (the first n_out
@@ -353,12 +363,9 @@ __global__ void __launch_bounds__(FWD_THREADS * GROUPS) k_mlp_forward(const MlpA
     if (threadIdx.x < 32) tmem_dealloc(tmem_base, TCOLS);
 }
 
-// 16-byte asynchronous copies global -> shared (no register staging), all in flight at once
+// 16-byte asynchronous copies global -> shared (no register staging)
 __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(sdst)), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
 // Backward pass (128 threads per CTA, one CTA per SM, tiles blockIdx.x, blockIdx.x + gridDim.x,
@@ -611,6 +618,12 @@ extern "C" rc_status rc_mlp_tile_product(const uint16_t* d_a, const uint16_t* d_
     if (smem > 48 * 1024 && cudaFuncSetAttribute(k_tile_product, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return RC_ERR_CUDA;
     k_tile_product<<<1, 128, smem, st>>>(d_a, d_b, d_d, K, N, d_err);
+    return cudaGetLastError() == cudaSuccess ? RC_OK : RC_ERR_CUDA;
+}
+
+extern "C" rc_status rc_mlp_wait_check(uint32_t polls, int arrive, unsigned* d_err, void* stream) {
+    if (!d_err || polls < 1 || polls > (1u << 24)) return RC_ERR_ARG;
+    k_wait_check<<<1, 32, 0, (cudaStream_t)stream>>>(polls, arrive != 0, d_err);
     return cudaGetLastError() == cudaSuccess ? RC_OK : RC_ERR_CUDA;
 }
 

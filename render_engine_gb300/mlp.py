@@ -11,7 +11,7 @@ import numpy as np
 
 from . import native
 
-EXPORTS = ["rc_mlp_tile_product", "rc_mlp_create", "rc_mlp_destroy", "rc_mlp_last_error", "rc_mlp_train", "rc_mlp_infer",
+EXPORTS = ["rc_mlp_tile_product", "rc_mlp_wait_check", "rc_mlp_create", "rc_mlp_destroy", "rc_mlp_last_error", "rc_mlp_train", "rc_mlp_infer",
            "rc_mlp_weights", "rc_mlp_gradients", "rc_mlp_error_flags", "rc_mlp_loss_scale"]
 NWEIGHT = 24576
 LAYERS = [(176, 64), (64, 64), (64, 64), (64, 64), (64, 16)]   # (inputs, outputs)
@@ -32,6 +32,7 @@ def _lib():
     if not _bound:
         vp, i = ctypes.c_void_p, ctypes.c_int
         L.rc_mlp_tile_product.argtypes = [vp, vp, vp, i, i, vp, vp]
+        L.rc_mlp_wait_check.argtypes = [ctypes.c_uint32, i, vp, vp]
         L.rc_mlp_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
         L.rc_mlp_destroy.argtypes = [vp]
         L.rc_mlp_destroy.restype = None
@@ -58,6 +59,14 @@ def tile_product(a, b, d, err, stream=None):
     st = _lib().rc_mlp_tile_product(_ptr(a), _ptr(b), _ptr(d), K, N, _ptr(err), stream)
     if st != native.RC_OK:
         raise native.RCError(st, "rc_mlp_tile_product")
+
+
+def wait_check(polls: int, arrive: bool, err, stream=None):
+    """The bounded mbarrier wait on its own (rc_mlp_wait_check): err (a CUDA uint32/int32 tensor)
+    gets bit 0 when the wait gave up."""
+    st = _lib().rc_mlp_wait_check(polls, 1 if arrive else 0, _ptr(err), stream)
+    if st != native.RC_OK:
+        raise native.RCError(st, "rc_mlp_wait_check")
 
 
 def split_weights(w: np.ndarray) -> list[np.ndarray]:

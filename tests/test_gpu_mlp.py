@@ -149,3 +149,22 @@ def test_training_fits_a_smooth_field():
     net.infer(P, N, aux, out)
     rel = ((out - target).norm() / target.norm()).item()
     assert rel < 0.2, rel   # 0.117 after 200 steps on the GB300
+
+
+def test_bounded_wait_gives_up_and_reports():
+    """Failure detection without a fault: a completion wait on an mbarrier that nothing arrives on
+    gives up after its poll limit and raises the error bit (the kernel ends, the context stays
+    usable); with one arrival the same wait succeeds."""
+    import torch
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    mlp.wait_check(1 << 12, True, err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    mlp.wait_check(1 << 12, False, err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 1
+    # the context still runs work
+    err.zero_()
+    mlp.wait_check(1 << 12, True, err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
