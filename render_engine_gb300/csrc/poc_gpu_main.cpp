@@ -316,6 +316,10 @@ int main(int argc, char** argv) {
     CHK(ctx, rc_device_info_get(ctx, &dev0), "device");
     double r0 = ram_mb();
     CHK(ctx, rc_scene_load(ctx, argv[2]), "scene");
+    // every state built before any mode runs, as the reference's load() does (the timing mode
+    // must not share the GPU with a state build, and res reports the whole scene's memory)
+    CHK(ctx, rc_scene_build_states(ctx), "state builds");
+    CHK(ctx, rc_sync(ctx), "sync");
     rc_scene_info si;
     CHK(ctx, rc_scene_info_get(ctx, &si), "scene info");
     const int NS = si.ns, NL = si.nl;
