@@ -642,6 +642,24 @@ struct rc_mlp {
     int cap_tiles = 0, sms = 0;
     long long step = 0;
     std::string msg;
+    // A training step's launches (2 memsets, 6 kernels) as CUDA graphs, one per set of arguments
+    // that came twice in a row (a caller that trains on the same buffers every frame replays one
+    // graph per call; arguments seen once are launched directly)
+    struct StepArgs {
+        const void *P = nullptr, *N = nullptr, *aux = nullptr, *target = nullptr, *idx = nullptr;
+        int tstride = 0, n = 0;
+        const float* loss = nullptr;
+        bool operator==(const StepArgs& o) const {
+            return P == o.P && N == o.N && aux == o.aux && target == o.target && idx == o.idx && tstride == o.tstride && n == o.n &&
+                   loss == o.loss;
+        }
+    };
+    struct StepGraph {
+        StepArgs args;
+        cudaGraphExec_t exec;
+    };
+    std::vector<StepGraph> graphs;
+    StepArgs last;
 };
 
 namespace {
@@ -736,6 +754,7 @@ void rc_mlp_destroy(rc_mlp* m) {
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->w); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad); cudaFree(m->part); cudaFree(m->slices);
     cudaFree(m->loss); cudaFree(m->wbf); cudaFree(m->act); cudaFree(m->err); cudaFree(m->state); cudaFree(m->nonfinite);
+    for (auto& g : m->graphs) cudaGraphExecDestroy(g.exec);
     if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
     delete m;
 }
@@ -763,6 +782,26 @@ rc_status rc_mlp_gradients(rc_mlp* m, float* host, size_t n) {
     return RC_OK;
 }
 
+namespace {
+// The launches of one training step on the network's stream.
+cudaError_t issue_train(rc_mlp* m, const MlpArgs& a, int ntiles, bool own_loss) {
+    cudaError_t e;
+    if (own_loss && (e = cudaMemsetAsync(m->loss, 0, 4, m->stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(m->nonfinite, 0, 4, m->stream)) != cudaSuccess) return e;
+    k_mlp_forward<true, TRAIN_GROUPS><<<std::min((ntiles + TRAIN_GROUPS - 1) / TRAIN_GROUPS, m->sms), FWD_THREADS * TRAIN_GROUPS,
+                                        FWD_SMEM_TRAIN, m->stream>>>(a);
+    const int bwd_ctas = std::min(ntiles, m->sms);
+    k_mlp_backward<<<bwd_ctas, 128, BWD_SMEM, m->stream>>>(a, ntiles);
+    const float b1 = 0.9f, b2 = 0.99f;
+    k_mlp_gsum<<<dim3((NWEIGHT + 255) / 256, GSLICES), 256, 0, m->stream>>>(m->part, bwd_ctas, m->slices);
+    k_mlp_gcheck<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->nonfinite);
+    k_mlp_step<<<1, 32, 0, m->stream>>>(m->state, m->nonfinite, b1, b2);
+    k_mlp_adam<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->w, m->m1, m->m2, m->grad, m->wbf, m->cfg.lr, b1, b2,
+                                                              1e-8f, m->state, m->nonfinite);
+    return cudaGetLastError();
+}
+}  // namespace
+
 rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, const float* d_target, int tstride,
                        const int* d_idx, int n, float* d_loss) {
     if (!m || !d_pos4 || !d_nrm4 || !d_aux4 || !d_target || n < 128 || n % 128 || n > 128 * m->cap_tiles || tstride < m->cfg.n_out)
@@ -781,20 +820,34 @@ rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, cons
     a.loss_scale = 1.f / ((float)n * (float)m->cfg.n_out);
     a.scale = m->state + ST_SCALE;
     const int ntiles = n / 128;
-    if (!d_loss && cudaMemsetAsync(m->loss, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "loss");
-    if (cudaMemsetAsync(m->nonfinite, 0, 4, m->stream) != cudaSuccess) return mfail(m, RC_ERR_CUDA, "flag");
-    k_mlp_forward<true, TRAIN_GROUPS><<<std::min((ntiles + TRAIN_GROUPS - 1) / TRAIN_GROUPS, m->sms), FWD_THREADS * TRAIN_GROUPS,
-                                        FWD_SMEM_TRAIN, m->stream>>>(a);
-    const int bwd_ctas = std::min(ntiles, m->sms);
-    k_mlp_backward<<<bwd_ctas, 128, BWD_SMEM, m->stream>>>(a, ntiles);
     m->step++;
-    const float b1 = 0.9f, b2 = 0.99f;
-    k_mlp_gsum<<<dim3((NWEIGHT + 255) / 256, GSLICES), 256, 0, m->stream>>>(m->part, bwd_ctas, m->slices);
-    k_mlp_gcheck<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->nonfinite);
-    k_mlp_step<<<1, 32, 0, m->stream>>>(m->state, m->nonfinite, b1, b2);
-    k_mlp_adam<<<(NWEIGHT + 255) / 256, 256, 0, m->stream>>>(m->slices, m->w, m->m1, m->m2, m->grad, m->wbf, m->cfg.lr, b1, b2,
-                                                              1e-8f, m->state, m->nonfinite);
-    return cudaGetLastError() == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
+    rc_mlp::StepArgs key;
+    key.P = d_pos4; key.N = d_nrm4; key.aux = d_aux4; key.target = d_target; key.idx = d_idx;
+    key.tstride = tstride; key.n = n; key.loss = d_loss;
+    for (const auto& g : m->graphs)
+        if (g.args == key) return cudaGraphLaunch(g.exec, m->stream) == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "graph launch");
+    // the same arguments twice in a row: capture the step (unless the stream is being captured
+    // already or cannot be); otherwise launch it directly
+    const bool repeat = key == m->last;
+    m->last = key;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (!repeat || m->graphs.size() >= 16 || cudaStreamIsCapturing(m->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone ||
+        cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return issue_train(m, a, ntiles, !d_loss) == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
+    }
+    const cudaError_t le = issue_train(m, a, ntiles, !d_loss);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
+    cudaGraphExec_t exec = nullptr;
+    const bool ok = le == cudaSuccess && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {   // the step did not run: launch it directly
+        cudaGetLastError();
+        return issue_train(m, a, ntiles, !d_loss) == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "launch");
+    }
+    m->graphs.push_back({key, exec});
+    return cudaGraphLaunch(exec, m->stream) == cudaSuccess ? RC_OK : mfail(m, RC_ERR_CUDA, "graph launch");
 }
 
 rc_status rc_mlp_infer(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, int n, float* d_out, int ostride) {

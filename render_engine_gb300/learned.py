@@ -75,6 +75,9 @@ class LearnedCache:
         self.gen = torch.Generator(device=dev)
         self.gen.manual_seed(seed)
         self.dev = dev
+        # one index buffer refilled every step: the training step's arguments stay the same, so
+        # the library replays its captured graph of the step
+        self.idx = torch.empty(batch, dtype=torch.int32, device=dev)
 
     def begin(self, state: int, seed: int):
         self.ctx.begin(self.method, state, seed)
@@ -108,8 +111,8 @@ class LearnedCache:
             self.boost_left -= 1
         p4, n4, a4 = self.feat[state]
         for _ in range(steps):
-            idx = torch.randint(0, self.np, (self.batch,), device=self.dev, generator=self.gen, dtype=torch.int32)
-            self.mlp.train_raw(p4, n4, a4, self.ctx.device_ptr(N.A_LC), self.lcs, idx, self.batch)
+            torch.randint(0, self.np, (self.batch,), generator=self.gen, out=self.idx)
+            self.mlp.train_raw(p4, n4, a4, self.ctx.device_ptr(N.A_LC), self.lcs, self.idx, self.batch)
 
     def close(self):
         self.mlp.close()
