@@ -58,7 +58,10 @@ const char* rc_mlp_last_error(const rc_mlp* m);
  * p = d_idx[s] (or s when d_idx is NULL) of d_pos4 / d_nrm4 / d_aux4, its target the first
  * n_out of the tstride floats at d_target + p * tstride (per-point arrays throughout).  Loss: relative L2,
  * (y - t)^2 / (y^2 + 0.01) averaged over samples and outputs; its sum is added to *d_loss
- * (when not NULL).  Gradients are summed over the batch in a fixed order. */
+ * (when not NULL).  Gradients are summed over the batch in a fixed order.  A call whose
+ * arguments (pointers, tstride, n) equal the previous call's is captured as a CUDA graph on the
+ * network's stream and later calls with those arguments replay it (at most 16 graphs; none while
+ * the stream is being captured by the caller): the same launches, fewer launch gaps. */
 rc_status rc_mlp_train(rc_mlp* m, const float* d_pos4, const float* d_nrm4, const float* d_aux4, const float* d_target, int tstride,
                        const int* d_idx, int n, float* d_loss);
 
