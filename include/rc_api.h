@@ -62,6 +62,11 @@ typedef struct rc_config {
 #define RC_FLAG_RAY_QUEUE 8u    /* static-mesh scenes: trace the rays traced ahead of the frame through a
                                    compacted ray queue served to persistent warps instead of one
                                    thread per point (same hits; slower at a few rays per point) */
+#define RC_FLAG_LOAD_ASYNC 16u  /* rc_scene_load_memory returns once the scene's global arrays and
+                                   state 0 are on the device and checked; the other states' arrays
+                                   keep streaming from the caller's buffer on the context's second
+                                   stream, so the buffer must stay valid and unchanged until
+                                   rc_sync, the next load or rc_destroy */
 #define RC_FLAG_WATERTIGHT 4u   /* static-mesh triangles by the watertight test (Woop, Benthin,
                                    Wald 2013) instead of the reference's Moller-Trumbore
                                    (poc_gpu.cu:318-331); hits differ from the reference's at

@@ -86,6 +86,7 @@ struct HostState {
     const float* raw = nullptr;     // 6 Np floats (P, N) then NL Np (Pw, scenes with references)
     const float* dint = nullptr;    // device light intensities
     size_t raw_buf = 0;             // index of the raw buffer in the scene's pool
+    bool copies_side = false;       // its per-point arrays were copied on the side stream (RC_FLAG_LOAD_ASYNC)
 };
 
 struct Scene {
@@ -160,6 +161,7 @@ struct rc_ctx {
     cudaStream_t side = nullptr;                // state builds issued ahead of use (prebuild_state)
     std::vector<cudaEvent_t> state_ev;          // per state: its build on the side stream is done
     cudaEvent_t load_ev = nullptr;              // the load's copies, which the side stream waits for
+    std::vector<cudaEvent_t> copies_ev;         // per state: its copies on the side stream are done (RC_FLAG_LOAD_ASYNC)
     int adj_np = 0, adj_k = 0;                  // sizes of the last rc_adjoint (0: none)
     int adj_cap_np = 0, adj_cap_k = 0, adj_cap_nl = 0;   // sizes the adjoint buffers were allocated for
     float4* adj_aeu = nullptr;                  // unit-emission direct light of the last adjoint
@@ -311,11 +313,11 @@ int load_grid(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 4096); }
 
 // Device copy of `bytes` bytes at `src` (host) into a new buffer of the pool.
 template <class T>
-rc_status dput_raw(rc_ctx* ctx, std::vector<DevBuf>& pool, const T** out, const uint8_t* src, size_t cnt) {
+rc_status dput_raw(rc_ctx* ctx, std::vector<DevBuf>& pool, const T** out, const uint8_t* src, size_t cnt, cudaStream_t on = nullptr) {
     T* p = nullptr;
-    rc_status s = dalloc(ctx, pool, &p, cnt);
+    rc_status s = dalloc(ctx, pool, &p, cnt, on);
     if (s != RC_OK) return s;
-    if (cnt) CKR(cudaMemcpyAsync(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    if (cnt) CKR(cudaMemcpyAsync(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice, on ? on : ctx->stream));
     *out = p;
     return RC_OK;
 }
@@ -651,19 +653,26 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         stage.add(&d.misc, G.misc);
         stage.add(&hs.dint, hs.inten);
         {
-            // the per-point arrays are copied now (the caller's buffer is not kept) and re-laid
-            // out when the state is first used
+            // the per-point arrays are copied now and re-laid out when the state is built; with
+            // RC_FLAG_LOAD_ASYNC the states after the first are copied on the side stream, behind
+            // state 0's build, and the load does not wait for them (the caller keeps its buffer)
+            const bool side = k > 0 && (ctx->cfg.flags & RC_FLAG_LOAD_ASYNC) && ctx->side;
+            cudaStream_t cs = side ? ctx->side : ctx->stream;
             float* raw = nullptr;
             const size_t nraw = (size_t)(6 + (S.has_ref ? NL : 0)) * Np;
-            if ((s = dalloc(ctx, pool, &raw, nraw))) return s;
+            if ((s = dalloc(ctx, pool, &raw, nraw, cs))) return s;
             hs.raw_buf = pool.size() - 1;
-            CKR(cudaMemcpyAsync(raw, P, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
-            CKR(cudaMemcpyAsync(raw + 3 * Np, N, 12 * Np, cudaMemcpyHostToDevice, ctx->stream));
-            if (S.has_ref) CKR(cudaMemcpyAsync(raw + 6 * Np, Pw, 4 * (size_t)NL * Np, cudaMemcpyHostToDevice, ctx->stream));
+            CKR(cudaMemcpyAsync(raw, P, 12 * Np, cudaMemcpyHostToDevice, cs));
+            CKR(cudaMemcpyAsync(raw + 3 * Np, N, 12 * Np, cudaMemcpyHostToDevice, cs));
+            if (S.has_ref) CKR(cudaMemcpyAsync(raw + 6 * Np, Pw, 4 * (size_t)NL * Np, cudaMemcpyHostToDevice, cs));
             hs.raw = raw;
+            if (S.has_ref)
+                if ((s = dput_raw(ctx, pool, &d.ref, ref, Np, cs)) || (s = dput_raw(ctx, pool, &d.valid, valid, Np, cs))) return s;
+            if (side) {
+                CKR(cudaEventRecord(ctx->copies_ev[k], cs));
+                hs.copies_side = true;
+            }
         }
-        if (S.has_ref)
-            if ((s = dput_raw(ctx, pool, &d.ref, ref, Np)) || (s = dput_raw(ctx, pool, &d.valid, valid, Np))) return s;
         d.nt = S.Nt;
         d.ng = G.gr.g0[3];
         d.nmisc = (int)G.misc.size();
@@ -782,6 +791,7 @@ rc_status ensure_state(rc_ctx* ctx, int k) {
             hs.wait = false;
         }
     } else {
+        if (hs.copies_side) CKR(cudaStreamWaitEvent(ctx->stream, ctx->copies_ev[k], 0));
         rc_status s = build_state(ctx, S, k, ctx->stream);
         if (s != RC_OK) return s;
     }
@@ -799,9 +809,11 @@ rc_status ensure_side(rc_ctx* ctx, int ns) {
     if (!ctx->side) CKR(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
     if (!ctx->load_ev) CKR(cudaEventCreateWithFlags(&ctx->load_ev, cudaEventDisableTiming));
     while ((int)ctx->state_ev.size() < ns) {
-        cudaEvent_t e = nullptr;
+        cudaEvent_t e = nullptr, c = nullptr;
         CKR(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         ctx->state_ev.push_back(e);
+        CKR(cudaEventCreateWithFlags(&c, cudaEventDisableTiming));
+        ctx->copies_ev.push_back(c);
     }
     return RC_OK;
 }
@@ -1341,6 +1353,7 @@ void rc_destroy(rc_ctx* ctx) {
     for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
     for (auto& e : ctx->state_ev) cudaEventDestroy(e);
     if (ctx->load_ev) cudaEventDestroy(ctx->load_ev);
+    for (auto& e : ctx->copies_ev) cudaEventDestroy(e);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -33,6 +33,7 @@ FLAG_BRUTE_FORCE = 1
 FLAG_CHECK_TRACE = 2
 FLAG_WATERTIGHT = 4
 FLAG_RAY_QUEUE = 8
+FLAG_LOAD_ASYNC = 16   # the caller keeps the loaded bytes valid until sync(); the states after the first stream in behind the load
 
 # Exported symbols, one per declaration of include/rc_api.h.
 EXPORTS = [

@@ -91,3 +91,28 @@ def test_states_built_ahead_of_use_give_the_same_frames(scene_main_bytes):
     assert np.array_equal(out[0][0], out[1][0])
     for a, b in zip(out[0][1], out[1][1]):
         assert np.array_equal(a, b)
+
+
+def test_async_load_gives_the_same_states_and_frames(scene_main_bytes):
+    """RC_FLAG_LOAD_ASYNC (the states after the first copied on the second stream behind the load,
+    from a buffer the caller keeps): the same state arrays and the same frames as a plain load,
+    whether a state is first built ahead of use or on demand."""
+    m = M.by_name(M.timing_methods(), "Classique 2.0x")
+    seq = [0] * 4 + [3] * 4 + [1] * 4 + [4] * 3 + [2] * 3
+    pinned = torch.frombuffer(bytearray(scene_main_bytes), dtype=torch.uint8).pin_memory()
+    out = []
+    for flags in (0, N.FLAG_LOAD_ASYNC):
+        ctx = N.Context(flags=flags)
+        ctx.load_bytes(pinned.numpy())
+        ctx.begin(m, seq[0], 9)
+        for s in seq:
+            ctx.frame(s)
+        ctx.sync()
+        assert ctx.device_flags() == 0
+        states = [[ctx.state_array(k, w).copy() for w in (N.SA_EDIR, N.SA_SV, N.SA_REF, N.SA_VALID, N.SA_PW)] for k in range(5)]
+        out.append((ctx.array(N.A_LC).copy(), states))
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, b in zip(out[0][1], out[1][1]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
