@@ -615,6 +615,10 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
     k_load_check<<<load_grid(Np), 256, 0, ctx->stream>>>(g.region, Np, 0, S.NR, ctx->flags_dev + 2, LOAD_BAD_REGION);
     CKR(cudaGetLastError());
     S.st.resize(S.NS);
+    // RC_FLAG_LOAD_ASYNC: every state's per-point arrays go on the side stream (the load returns
+    // once the global arrays are checked; the caller keeps its buffer until rc_sync)
+    const bool async = (ctx->cfg.flags & RC_FLAG_LOAD_ASYNC) != 0;
+    if (async && (s = ensure_side(ctx, S.NS))) return s;
     for (int k = 0; k < S.NS; ++k) {
         HostState& hs = S.st[k];
         hs.inten = r.vec<float>(NL);
@@ -654,9 +658,9 @@ rc_status load_scene(rc_ctx* ctx, const uint8_t* data, size_t n) {
         stage.add(&hs.dint, hs.inten);
         {
             // the per-point arrays are copied now and re-laid out when the state is built; with
-            // RC_FLAG_LOAD_ASYNC the states after the first are copied on the side stream, behind
-            // state 0's build, and the load does not wait for them (the caller keeps its buffer)
-            const bool side = k > 0 && (ctx->cfg.flags & RC_FLAG_LOAD_ASYNC) && ctx->side;
+            // RC_FLAG_LOAD_ASYNC they are copied on the side stream (state 0's first, then its
+            // build, then the other states') and the load does not wait for them
+            const bool side = async;
             cudaStream_t cs = side ? ctx->side : ctx->stream;
             float* raw = nullptr;
             const size_t nraw = (size_t)(6 + (S.has_ref ? NL : 0)) * Np;
@@ -1396,8 +1400,10 @@ rc_status rc_scene_load_memory(rc_ctx* ctx, const void* data, size_t nbytes) {
     rc_status s = load_scene(ctx, (const uint8_t*)data, nbytes);
     // copies from the caller's buffer may still be in flight after a failed load
     if (s != RC_OK) { cudaStreamSynchronize(ctx->stream); free_pool(ctx->scene_bufs); return s; }
+    // the cache's buffers and their clearing are ordered on the context's stream before any frame
+    // (no host wait: with RC_FLAG_LOAD_ASYNC the copy engine is still busy with the other states)
     if ((s = alloc_cache(ctx)) != RC_OK) return s;
-    CKR(cudaStreamSynchronize(ctx->stream));
+    CKR(cudaGetLastError());
     ctx->have_scene = true;
     // the states' device builds run behind the load on the side stream
     if ((s = issue_state_builds(ctx)) != RC_OK) { ctx->have_scene = false; return s; }
