@@ -626,7 +626,7 @@ def learned_bench(data, refs, local, batch=1 << 16):
     the tracer's one-bounce estimates, 2^16 samples per step, loss-scaled, and served as the
     cache) against the reference's cache methods over the whole timing sequence (5 states x 60
     frames, 4 state changes): the dependency-tracked `v4-A2C suivi 1/4`, the plain `Classique 1.0x`
-    and the SHaRC-style hash-grid cache `SHaRC responsive 1.0x`, the judge of the learned cache: the 30-frame post-event luminance error over all
+    and the SHaRC-style hash-grid cache `SHaRC responsive 1.0x`, the cache the learned one is held against: the 30-frame post-event luminance error over all
     valid points and over the event region (as the quality leg), and each method's frame ms (CUDA
     events around each frame's work; for the learned cache inference + frame + training step).
     The per-point caches run at 1, 2, 4, 8 and 16 rays per point (the hash-grid cache at 32 too), so
@@ -740,16 +740,16 @@ def learned_bench(data, refs, local, batch=1 << 16):
             if best is None or v["post_event_err_pct"] < out[best]["post_event_err_pct"]:
                 best = k
     out["per_point_cache_at_equal_or_more_ms"] = best
-    # the judge the learned cache is held to: the SHaRC-style hash-grid cache (bench B's "SHaRC
+    # the comparison the learned cache is held to: the SHaRC-style hash-grid cache (bench B's "SHaRC
     # responsive": spatial-hash cache points, running mean reset where a light's contribution
     # changes) at the cheapest ray budget whose frame costs at least the learned cache's
     sharc = sorted((v["frame_ms"], k) for k, v in out.items() if k.startswith("SHaRC") and isinstance(v, dict))
-    judge = next((k for ms, k in sharc if ms >= out["learned"]["frame_ms"]), sharc[-1][1] if sharc else None)
-    if judge is not None:
-        out["hash_grid_judge"] = {"method": judge, "frame_ms": out[judge]["frame_ms"],
-                                  "post_event_err_pct": out[judge]["post_event_err_pct"],
-                                  "judge_frame_ms_ge_learned": bool(out[judge]["frame_ms"] >= out["learned"]["frame_ms"]),
-                                  "learned_post_event_le_judge": bool(out["learned"]["post_event_err_pct"] <= out[judge]["post_event_err_pct"])}
+    ref_k = next((k for ms, k in sharc if ms >= out["learned"]["frame_ms"]), sharc[-1][1] if sharc else None)
+    if ref_k is not None:
+        out["vs_hash_grid"] = {"method": ref_k, "frame_ms": out[ref_k]["frame_ms"],
+                                  "post_event_err_pct": out[ref_k]["post_event_err_pct"],
+                                  "hash_grid_frame_ms_ge_learned": bool(out[ref_k]["frame_ms"] >= out["learned"]["frame_ms"]),
+                                  "learned_post_event_le_hash_grid": bool(out["learned"]["post_event_err_pct"] <= out[ref_k]["post_event_err_pct"])}
     return out
 
 
