@@ -73,16 +73,16 @@ inline void set_grid_scale(Grid& g) {
 
 // One axis of vox_of (poc_gpu.cu:137-142): int((x - lo) / ext * n), clamped to [0, n - 1].  The
 // reference's quotient q = (x - lo) / ext * n is only needed to the integer: qf = (x - lo) * s,
-// s = n / ext rounded, differs from it by a few ulps, far less than the 1e-3 margin asked of qf's
-// distance to the nearest integer, so truncating qf gives q's integer whenever qf is that far
-// from one.  Otherwise (and for a NaN or an infinity, whose comparisons are false) the
-// reference's own IEEE division decides.  The result is the reference's, without the division in
-// all but a few samples.
+// s = n / ext rounded, and q each carry two roundings, so |qf - q| <= 2.4e-7 |q|, forty times
+// less than the 1e-5 |qf| (or 1e-5) margin asked of qf's distance to the nearest integer; when qf
+// is that far from one, truncating it gives q's integer.  Otherwise (and for a NaN or an infinity,
+// whose comparisons are false) the reference's own IEEE division decides.  The result is the
+// reference's, without the division in all but a few samples.
 __device__ __forceinline__ int vox_axis(float x, float lo, float ext, float s, int n) {
     const float d = x - lo;
     const float qf = d * s;
     const float r = rintf(qf);
-    const int v = fabsf(qf - r) > 1e-3f * fmaxf(1.f, fabsf(qf)) ? int(qf) : int(d / ext * n);
+    const int v = fabsf(qf - r) > 1e-5f * fmaxf(1.f, fabsf(qf)) ? int(qf) : int(d / ext * n);
     return min(max(v, 0), n - 1);
 }
 __device__ __forceinline__ int vox_of(const Grid& g, f3 p) {
