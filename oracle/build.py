@@ -4,7 +4,9 @@
 * ``_build/librefrun.so``  -- the driver of the reference's own kernels (refrun.cpp);
 * ``_ref/ref_l{3,8,16,32}.cubin`` -- the reference's cuda/poc_gpu.cu compiled for sm_103a by
   build_ref.sh, only where the reference checkout is present (the cubins are device code,
-  so the copies built here are used unchanged on the GPU machine).
+  so the copies built here are used unchanged on the GPU machine);
+* ``_ref/libhlsl_dep.so`` -- the reference's dependency-marking shader functions compiled as
+  C++ by build_hlsl_ref.sh, where the reference checkout is present (CPU tests only).
 """
 from __future__ import annotations
 
@@ -48,11 +50,25 @@ def build_reference_cubins(force: bool = False) -> bool:
     return True
 
 
+def build_hlsl_ref(force: bool = False) -> bool:
+    """Compile the reference's dependency-marking shader functions as C++ (build_hlsl_ref.sh)
+    when the reference checkout is present."""
+    src = os.path.join(REFERENCE, "windows", "patch", "rtxgi_bench.patch")
+    out = os.path.join(HERE, "_ref", "libhlsl_dep.so")
+    if not os.path.exists(src):
+        return os.path.exists(out)
+    deps = [src, os.path.join(HERE, "build_hlsl_ref.sh"), os.path.join(HERE, "hlsl_compat.h"), os.path.join(HERE, "hlsl_dep_ref.cpp")]
+    if force or _stale(out, deps):
+        subprocess.check_call(["sh", os.path.join(HERE, "build_hlsl_ref.sh"), REFERENCE])
+    return True
+
+
 def build(force: bool = False) -> None:
     from oracle import pyoracle
     pyoracle.build(force)
     build_refrun(force)
     build_reference_cubins(force)
+    build_hlsl_ref(force)
 
 
 if __name__ == "__main__":
