@@ -5,8 +5,9 @@
 * ``_ref/ref_l{3,8,16,32}.cubin`` -- the reference's cuda/poc_gpu.cu compiled for sm_103a by
   build_ref.sh, only where the reference checkout is present (the cubins are device code,
   so the copies built here are used unchanged on the GPU machine);
-* ``_ref/libhlsl_dep.so`` -- the reference's dependency-marking shader functions compiled as
-  C++ by build_hlsl_ref.sh, where the reference checkout is present (CPU tests only).
+* ``_ref/libpatch_ref.so`` -- pieces of the reference's bench patch (the dependency-marking
+  shader functions, the host function of an object's event zones) compiled as C++ by
+  build_patch_ref.sh, where the reference checkout is present (CPU tests only).
 """
 from __future__ import annotations
 
@@ -50,16 +51,16 @@ def build_reference_cubins(force: bool = False) -> bool:
     return True
 
 
-def build_hlsl_ref(force: bool = False) -> bool:
-    """Compile the reference's dependency-marking shader functions as C++ (build_hlsl_ref.sh)
-    when the reference checkout is present."""
+def build_patch_ref(force: bool = False) -> bool:
+    """Compile pieces of the reference's bench patch as C++ (build_patch_ref.sh) when the
+    reference checkout is present."""
     src = os.path.join(REFERENCE, "windows", "patch", "rtxgi_bench.patch")
-    out = os.path.join(HERE, "_ref", "libhlsl_dep.so")
+    out = os.path.join(HERE, "_ref", "libpatch_ref.so")
     if not os.path.exists(src):
         return os.path.exists(out)
-    deps = [src, os.path.join(HERE, "build_hlsl_ref.sh"), os.path.join(HERE, "hlsl_compat.h"), os.path.join(HERE, "hlsl_dep_ref.cpp")]
+    deps = [src, os.path.join(HERE, "build_patch_ref.sh"), os.path.join(HERE, "hlsl_compat.h"), os.path.join(HERE, "patch_ref.cpp")]
     if force or _stale(out, deps):
-        subprocess.check_call(["sh", os.path.join(HERE, "build_hlsl_ref.sh"), REFERENCE])
+        subprocess.check_call(["sh", os.path.join(HERE, "build_patch_ref.sh"), REFERENCE])
     return True
 
 
@@ -68,7 +69,7 @@ def build(force: bool = False) -> None:
     pyoracle.build(force)
     build_refrun(force)
     build_reference_cubins(force)
-    build_hlsl_ref(force)
+    build_patch_ref(force)
 
 
 if __name__ == "__main__":

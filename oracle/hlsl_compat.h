@@ -2,7 +2,7 @@
 //
 // Just enough of HLSL's float3 / uint3 / uint4 / bool3 arithmetic and of its intrinsics (any,
 // all, min, max, abs, ceil, length, lerp) to compile the bench's dependency-marking functions,
-// taken unchanged from the reference's shader patch by oracle/build_hlsl_ref.sh, as C++ on the
+// taken unchanged from the reference's shader patch by oracle/build_patch_ref.sh, as C++ on the
 // CPU.  Every operation is the IEEE single-precision one, component by component, in HLSL's
 // definition order (lerp(x, y, s) = x + s * (y - x); length(v) = sqrt(dot(v, v)), the dot
 // product summed x, y, z in that order); the recipe compiles without contraction.

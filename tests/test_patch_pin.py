@@ -1,11 +1,17 @@
-"""Pins the restatement of the bench's dependency marking (oracle/hg_oracle.c: hgo_mark_point,
-hgo_mark_segment, the checker of the GPU kernels in csrc/rc_hashgrid.cu) to the reference's own
-shader functions DepMarkPoint and DepMarkSegment (rtxgi_bench.patch:825-858), extracted unchanged
-from a reference checkout and compiled as C++ by oracle/build_hlsl_ref.sh (HLSL's vector types
-from oracle/hlsl_compat.h, IEEE single precision, no contraction).  The masks must be equal bit
-for bit on random points and segments, on points on the zone boundaries, on axis-aligned and
-degenerate segments, on segments that miss the box and on long ones (the 48-step cap).  Skipped
-without a reference checkout (the shader source is read from there)."""
+"""Pins the restatement of the bench's dependency encoding to the reference's own code, extracted
+unchanged from a reference checkout and compiled as C++ by oracle/build_patch_ref.sh:
+
+* the shader functions DepMarkPoint and DepMarkSegment (rtxgi_bench.patch:825-858; HLSL's vector
+  types from oracle/hlsl_compat.h, IEEE single precision, no contraction) against oracle/
+  hg_oracle.c's hgo_mark_point / hgo_mark_segment, the checker of the GPU kernels in
+  csrc/rc_hashgrid.cu: masks equal bit for bit on random points and segments, on points on the
+  zone boundaries, on axis-aligned and degenerate segments, on segments that miss the box and on
+  long ones (the 48-step cap);
+* the host function Pathtracer::BenchObjVoxels (patch:592-615, the zones an object invalidates)
+  against the oracle's event mask and the library's own rc_hg_event_mask (host code, no GPU):
+  equal zone words for random objects, objects on zone edges and objects outside the box.
+
+Skipped without a reference checkout (the patch is read from there)."""
 import ctypes
 import os
 
@@ -15,17 +21,18 @@ import pytest
 from oracle import build as OB
 from oracle import pyhg
 
-LIB = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "libhlsl_dep.so")
+LIB = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "libpatch_ref.so")
 
 
 @pytest.fixture(scope="module")
 def href():
-    if not OB.build_hlsl_ref():
-        pytest.skip("no reference checkout (the shader functions are read from there)")
+    if not OB.build_patch_ref():
+        pytest.skip("no reference checkout (the patch is read from there)")
     L = ctypes.CDLL(LIB)
     vp = ctypes.c_void_p
     L.href_mark_point.argtypes = [vp, vp, vp, vp]
     L.href_mark_segment.argtypes = [vp, vp, vp, vp, vp]
+    L.href_obj_voxels.argtypes = [vp, vp, vp, vp]
     return L
 
 
@@ -85,3 +92,34 @@ def test_mark_segment_equals_the_shader(href, box):
         href.href_mark_segment(_p(lo), _p(hi), _p(m1), _p(a), _p(b))
         m2[:] = pyhg.mark_segment(cfg, a, b)
         assert np.array_equal(m1, m2), (a, b, m1, m2)
+
+
+@pytest.mark.parametrize("box", BOXES)
+def test_object_zones_equal_the_reference(href, box):
+    from render_engine_gb300 import hashgrid as H
+    lo, hi = np.array(box[0], np.float32), np.array(box[1], np.float32)
+    cfg = pyhg.Config()
+    cfg.zone_lo[:], cfg.zone_hi[:] = lo.tolist(), hi.tolist()
+    lib_cfg = H.make_config(zone_lo=tuple(lo.tolist()), zone_hi=tuple(hi.tolist()))
+    rng = np.random.default_rng(7)
+    ext = hi - lo
+    cs = ext / np.array([6, 4, 4], np.float32)
+    objs = []
+    for _ in range(3000):
+        c = rng.uniform(lo - 0.2 * ext, hi + 0.2 * ext)
+        size = rng.uniform(0.01, 0.5, 3) * ext
+        objs.append(np.concatenate([c, size]).astype(np.float32))
+    for _ in range(500):   # faces 0.25 (the margin) away from a zone edge, exactly
+        k = int(rng.integers(0, 3))
+        z = int(rng.integers(0, (6, 4, 4)[k] + 1))
+        c = rng.uniform(lo, hi)
+        size = rng.uniform(0.05, 0.3, 3) * ext
+        c[k] = lo[k] + cs[k] * z - 0.25 - 0.5 * size[k]
+        objs.append(np.concatenate([c, size]).astype(np.float32))
+    for o in objs:
+        want = np.zeros(4, np.uint32)
+        href.href_obj_voxels(_p(lo), _p(hi), _p(o), _p(want))
+        got_oracle = pyhg.event_mask(cfg, obj_a=o)
+        got_lib = H.event_mask(lib_cfg, obj_a=o)
+        assert np.array_equal(want[:3], got_oracle[:3]), (o, want, got_oracle)
+        assert np.array_equal(want[:3], got_lib[:3]), (o, want, got_lib)
