@@ -7,7 +7,7 @@
 # and compiles them as C++ with oracle/patch_ref.cpp (HLSL's types from oracle/hlsl_compat.h, a
 # stand-in for the members BenchObjVoxels reads) into oracle/_ref/libpatch_ref.so, without FP
 # contraction.
-# Usage: oracle/build_hlsl_ref.sh [reference checkout]; default $RC_REFERENCE_DIR, else the
+# Usage: oracle/build_patch_ref.sh [reference checkout]; default $RC_REFERENCE_DIR, else the
 # directory "reference" beside this repository
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
