@@ -1,9 +1,9 @@
 // HLSL vector types and intrinsics as plain C++ — TEST INFRASTRUCTURE ONLY.
 //
-// Just enough of HLSL's float3 / uint3 / uint4 / bool3 arithmetic and of its intrinsics (any,
-// all, min, max, abs, ceil, length, lerp) to compile the bench's dependency-marking functions,
-// taken unchanged from the reference's shader patch by oracle/build_patch_ref.sh, as C++ on the
-// CPU.  Every operation is the IEEE single-precision one, component by component, in HLSL's
+// Just enough of HLSL's float3 / uint2 / uint3 / uint4 / bool3 arithmetic, of its intrinsics
+// (any, all, min, max, abs, ceil, length, lerp, InterlockedAdd) and of its compute-shader
+// resources to compile the bench's dependency-marking functions and snapshot shaders, taken
+// from the reference's patch by oracle/build_patch_ref.sh, as C++ on the CPU.  Every operation is the IEEE single-precision one, component by component, in HLSL's
 // definition order (lerp(x, y, s) = x + s * (y - x); length(v) = sqrt(dot(v, v)), the dot
 // product summed x, y, z in that order); the recipe compiles without contraction.
 #pragma once
@@ -39,9 +39,38 @@ struct uint3 {
     uint3(uint a, uint b, uint c) : x(a), y(b), z(c) {}
     explicit uint3(float3 f) : x((uint)f.x), y((uint)f.y), z((uint)f.z) {}   // truncation, as HLSL's conversion
 };
-struct uint4 {
-    uint x, y, z, w;
+struct uint2 {
+    uint x, y;
 };
+struct uint4 {
+    union {
+        struct {
+            uint x, y, z, w;
+        };
+        struct {
+            uint2 xy, zw;
+        };
+    };
+    uint4() : x(0u), y(0u), z(0u), w(0u) {}
+    uint4(uint a, uint b, uint c, uint d) : x(a), y(b), z(c), w(d) {}
+    uint4(uint2 a, uint c, uint d) : x(a.x), y(a.y), z(c), w(d) {}
+};
+
+// resources of a compute shader: a structured buffer is an array the harness points at, a
+// constant buffer the struct itself; InterlockedAdd on one thread at a time (the harness runs
+// the dispatch's threads in order)
+template <class T>
+struct RWStructuredBuffer {
+    T* p = nullptr;
+    T& operator[](uint i) const { return p[i]; }
+};
+template <class T>
+using ConstantBuffer = T;
+inline void InterlockedAdd(uint& dst, uint v) { dst += v; }
+inline void InterlockedAdd(uint& dst, uint v, uint& original) {
+    original = dst;
+    dst += v;
+}
 
 inline float abs(float v) { return std::fabs(v); }
 inline float min(float a, float b) { return std::fmin(a, b); }

@@ -5,7 +5,9 @@
 //     pass; HLSL's `inout` parameter becomes a C++ reference), with HLSL's vector types from
 //     oracle/hlsl_compat.h;
 //   * Pathtracer::BenchObjVoxels (patch:592-615, host code: the event zones of an object), with a
-//     stand-in for the members of the sample's Pathtracer class it reads.
+//     stand-in for the members of the sample's Pathtracer class it reads;
+//   * the snapshot compute shaders snapCount, snapPack, snapRestore of BenchSnap.hlsl
+//     (patch:1283-1345), dispatched here one thread after another.
 // Used by tests/test_patch_pin.py to pin oracle/hg_oracle.c and the library's rc_hg_event_mask.
 #include <array>
 #include <cstdint>
@@ -32,6 +34,8 @@ struct Pathtracer {
 };
 
 #include "bench_obj.inc"
+
+#include "bench_snap.inc"
 
 static void set_box(const float lo[3], const float hi[3]) {
     g_Global.benchGridMin.xyz = float3(lo[0], lo[1], lo[2]);
@@ -65,4 +69,32 @@ extern "C" void href_obj_voxels(const float lo[3], const float hi[3], const floa
     }
     pt.m_bench.objPos.push_back({obj[0], obj[1], obj[2], obj[3], obj[4], obj[5]});
     pt.BenchObjVoxels(0, inv);
+}
+
+// snapCount then snapPack over a table of `cap` entries (keys as the shader's uint2: low word,
+// high word; resolved as uint4), records into `recs` (at most rec_cap); returns the count
+extern "C" uint32_t href_snapshot(uint64_t* keys, uint32_t* resolved, uint32_t cap, void* recs, uint32_t rec_cap) {
+    static_assert(sizeof(SnapRec) == 24 && sizeof(uint4) == 16 && sizeof(uint2) == 8, "record layout");
+    uint counter = 0;
+    u_Hash.p = reinterpret_cast<uint2*>(keys);
+    u_Resolved.p = reinterpret_cast<uint4*>(resolved);
+    u_Snap.p = reinterpret_cast<SnapRec*>(recs);
+    u_Counter.p = &counter;
+    g_Snap.capacity = cap;
+    g_Snap.count = rec_cap;
+    for (uint id = 0; id < cap; ++id) snapCount(id);
+    const uint n = counter;
+    counter = 0;
+    for (uint id = 0; id < cap; ++id) snapPack(id);
+    return n;
+}
+
+// snapRestore of `count` records into the table
+extern "C" void href_restore(uint64_t* keys, uint32_t* resolved, uint32_t cap, void* recs, uint32_t count) {
+    u_Hash.p = reinterpret_cast<uint2*>(keys);
+    u_Resolved.p = reinterpret_cast<uint4*>(resolved);
+    u_Snap.p = reinterpret_cast<SnapRec*>(recs);
+    g_Snap.capacity = cap;
+    g_Snap.count = count;
+    for (uint id = 0; id < count; ++id) snapRestore(id);
 }

@@ -9,7 +9,11 @@ unchanged from a reference checkout and compiled as C++ by oracle/build_patch_re
   long ones (the 48-step cap);
 * the host function Pathtracer::BenchObjVoxels (patch:592-615, the zones an object invalidates)
   against the oracle's event mask and the library's own rc_hg_event_mask (host code, no GPU):
-  equal zone words for random objects, objects on zone edges and objects outside the box.
+  equal zone words for random objects, objects on zone edges and objects outside the box;
+* the snapshot compute shaders of BenchSnap.hlsl (patch:1283-1345: count, pack, restore),
+  dispatched one thread after another, against the oracle's snapshot and restore (the checker
+  of rc_hg_snapshot / rc_hg_restore): the same records in the same (entry) order, and the same
+  table after a restore, on tables with empty, evicted, sample-less and live entries.
 
 Skipped without a reference checkout (the patch is read from there)."""
 import ctypes
@@ -33,6 +37,9 @@ def href():
     L.href_mark_point.argtypes = [vp, vp, vp, vp]
     L.href_mark_segment.argtypes = [vp, vp, vp, vp, vp]
     L.href_obj_voxels.argtypes = [vp, vp, vp, vp]
+    L.href_snapshot.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_uint32]
+    L.href_snapshot.restype = ctypes.c_uint32
+    L.href_restore.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_uint32]
     return L
 
 
@@ -123,3 +130,56 @@ def test_object_zones_equal_the_reference(href, box):
         got_lib = H.event_mask(lib_cfg, obj_a=o)
         assert np.array_equal(want[:3], got_oracle[:3]), (o, want, got_oracle)
         assert np.array_equal(want[:3], got_lib[:3]), (o, want, got_lib)
+
+
+SNAP = np.dtype([("index", "<u4"), ("sample_data", "<u4"), ("key", "<u4", 2), ("radiance", "<u4", 2)])
+
+
+def _table(rng, cap):
+    """A table in the states the cache leaves entries in: empty (key 0, all zero), evicted (key
+    all ones, resolved zero), live without samples (fp16 count 0) and live with samples."""
+    keys = np.zeros(cap, np.uint64)
+    res = np.zeros((cap, 4), np.uint32)
+    kind = rng.choice(4, cap, p=[0.4, 0.05, 0.1, 0.45])
+    live = kind >= 2
+    keys[kind == 1] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    keys[live] = rng.integers(1, 2**63, live.sum(), dtype=np.int64).astype(np.uint64)
+    n = live.sum()
+    rgb = rng.random((n, 3)).astype(np.float16).view(np.uint16).astype(np.uint32)
+    cnt = np.where(kind[live] == 3, rng.integers(1, 64, n), 0).astype(np.float16).view(np.uint16).astype(np.uint32)
+    res[live, 0] = rgb[:, 0] | rgb[:, 1] << 16
+    res[live, 1] = rgb[:, 2] | cnt << 16
+    res[live, 2] = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    return keys, res
+
+
+def test_snapshot_shaders_equal_the_oracle(href):
+    rng = np.random.default_rng(11)
+    cap = 1 << 16
+    cfg = pyhg.Config()
+    cfg.capacity = cap
+    for trial in range(4):
+        keys, res = _table(rng, cap)
+        cache = pyhg.Cache(cfg)
+        cache.keys[:] = keys
+        cache.resolved[:] = res
+        mine = cache.snapshot(SNAP)
+        theirs = np.zeros(cap, SNAP)
+        k2, r2 = keys.copy(), res.copy()
+        n = href.href_snapshot(_p(k2), _p(r2), cap, _p(theirs), cap)
+        assert n == len(mine) and n > 0
+        assert np.array_equal(mine.view(np.uint32), theirs[:n].view(np.uint32))
+        # a capacity below the count: both keep the first records and report the full count
+        short = np.zeros(n // 2, SNAP)
+        assert href.href_snapshot(_p(k2), _p(r2), cap, _p(short), n // 2) == n
+        assert np.array_equal(short.view(np.uint32), mine[: n // 2].view(np.uint32))
+        # restore into a table whose restored entries hold something else
+        k_a, r_a = _table(rng, cap)
+        cache2 = pyhg.Cache(cfg)
+        cache2.keys[:] = k_a
+        cache2.resolved[:] = r_a
+        cache2.restore(mine)
+        k_b, r_b = k_a.copy(), r_a.copy()
+        href.href_restore(_p(k_b), _p(r_b), cap, _p(theirs), n)
+        assert np.array_equal(cache2.keys, k_b)
+        assert np.array_equal(cache2.resolved, r_b)
