@@ -39,3 +39,14 @@ def golden_main():
 def golden_stress():
     import json
     return json.load(open(os.path.join(GOLDEN, "golden_scen_stress.json")))
+
+
+@pytest.fixture(scope="session")
+def scene_holdout_bytes():
+    return golden_bytes("scene_holdout.bin")
+
+
+@pytest.fixture(scope="session")
+def golden_holdout():
+    import json
+    return json.load(open(os.path.join(GOLDEN, "golden_scen_holdout.json")))

@@ -2,10 +2,14 @@
 
 Reads, from the reference (falcon123212/render_engine):
   cuda/scenes/scene_main.bin, cuda/scenes/scene_stress.bin     (its box-scene fixtures)
+  cuda/scenes/scene_holdout.bin                                (its validation box scene)
+  cuda/scenes/scene_scale_43k.bin                              (its smallest timing scene)
   cuda/scenes/scene_scale_1M.bin.gz                            (its 1,082,802-point timing scene)
-  reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl    (its published RTX 4060
-      per-frame error curves: `poc_gpu_l3 scen scene_main.bin 10` and
-      `poc_gpu_l8 scenf scene_stress.bin 10 scenarios_stress.txt`)
+  reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl,
+      scen_holdout.jsonl                                       (its published RTX 4060
+      per-frame error curves: `poc_gpu_l3 scen scene_main.bin 10`,
+      `poc_gpu_l8 scenf scene_stress.bin 10 scenarios_stress.txt` and
+      `poc_gpu_l3 scen scene_holdout.bin 10`)
   cuda/scenes/scenarios_stress.txt, cuda/scenes/scenarios_main.txt
 and writes gzip copies of the scenes and the curves as JSON next to this script.
 
@@ -34,7 +38,7 @@ def curves(path):
     return out
 
 
-for name in ("scene_main.bin", "scene_stress.bin"):
+for name in ("scene_main.bin", "scene_stress.bin", "scene_holdout.bin", "scene_scale_43k.bin"):
     with open(os.path.join(REF, "cuda", "scenes", name), "rb") as f, gzip.open(os.path.join(HERE, name + ".gz"), "wb", 9) as g:
         shutil.copyfileobj(f, g)
 shutil.copy(os.path.join(REF, "cuda", "scenes", "scenarios_stress.txt"), os.path.join(HERE, "scenarios_stress.txt"))
@@ -45,4 +49,6 @@ json.dump({"mode": "scen", "seed0": 2000, "nseeds": 10, "rows": curves(os.path.j
           open(os.path.join(HERE, "golden_scen_main.json"), "w"))
 json.dump({"mode": "scenf", "seed0": 3000, "nseeds": 10, "rows": curves(os.path.join(REF, "reference", "cuda_rtx4060", "scen_stress.jsonl"))},
           open(os.path.join(HERE, "golden_scen_stress.json"), "w"))
+json.dump({"mode": "scen", "seed0": 2000, "nseeds": 10, "rows": curves(os.path.join(REF, "reference", "cuda_rtx4060", "scen_holdout.jsonl"))},
+          open(os.path.join(HERE, "golden_scen_holdout.json"), "w"))
 print("golden fixtures written to", HERE)

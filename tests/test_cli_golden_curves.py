@@ -1,10 +1,12 @@
 """Every error curve the drop-in binaries printed on a GB300 against the reference's published ones.
 
-tests/golden/cli/scen_main.jsonl and scen_stress.jsonl are the JSONL that poc_gpu_l3 / poc_gpu_l8
-printed on a GB300 (tests/golden/make_cli_fixtures.sh: the published files' own commands, 10 seeds);
-tests/golden/golden_scen_main.json and golden_scen_stress.json hold the curves the reference's
-binary printed on an RTX 4060 (reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl, 10-seed
-means, 5 decimals).  Each of the 126 + 112 (scenario, method) curves must be there, frame for frame
+tests/golden/cli/scen_main.jsonl, scen_stress.jsonl and scen_holdout.jsonl are the JSONL that
+poc_gpu_l3 / poc_gpu_l8 printed on a GB300 (tests/golden/make_cli_fixtures.sh: the published files'
+own commands, 10 seeds); tests/golden/golden_scen_main.json, golden_scen_stress.json and
+golden_scen_holdout.json hold the curves the reference's binary printed on an RTX 4060
+(reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl, scen_holdout.jsonl, 10-seed means,
+5 decimals; the holdout scene is the validation box scene the reference never tuned on).  Each of
+the 126 + 112 + 126 (scenario, method) curves must be there, frame for frame
 within 1e-3 relative: the GPU path's frames equal the reference kernels' bit for bit except where the
 reference itself sums with float atomics, so what is left is that run-to-run spread and the
 published files' rounding.  The GPU run itself is in the -m gpu tests (test_gpu_parity.py, three
@@ -37,7 +39,8 @@ def _printed(name):
 
 
 @pytest.mark.parametrize("printed,published,count", [("scen_main.jsonl", "golden_scen_main.json", 126),
-                                                     ("scen_stress.jsonl", "golden_scen_stress.json", 112)])
+                                                     ("scen_stress.jsonl", "golden_scen_stress.json", 112),
+                                                     ("scen_holdout.jsonl", "golden_scen_holdout.json", 126)])
 def test_every_printed_curve_matches_the_published_one(printed, published, count):
     ours, theirs = _printed(printed), _published(published)
     assert len(theirs) == count

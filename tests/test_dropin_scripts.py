@@ -3,7 +3,8 @@
 commands and file names) goes through the unmodified cuda/analyse_cuda.py and cuda/budget.py of
 a reference checkout ($RC_REFERENCE_DIR, else a directory named "reference" beside this
 repository; the test is skipped without one).  The scripts must exit 0 and read every table, and
-the gains G that analyse_cuda.py computes from our scen_main.jsonl / scen_stress.jsonl must match
+the gains G that analyse_cuda.py computes from our scen_main.jsonl / scen_stress.jsonl /
+scen_holdout.jsonl must match
 those it computes from the reference's published RTX 4060 files (same commands, same seeds) within
 the curves' tolerance."""
 import os
@@ -19,6 +20,7 @@ CLI = os.path.join(ROOT, "tests", "golden", "cli")
 REF = os.environ.get("RC_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 SCRIPTS = os.path.join(REF, "cuda")
 PUBLISHED = os.path.join(REF, "reference", "cuda_rtx4060")
+HOLDOUT = "Scene de validation (jamais vue pendant la mise au point)"
 
 pytestmark = pytest.mark.skipif(not os.path.exists(os.path.join(SCRIPTS, "analyse_cuda.py")),
                                 reason="no reference checkout (its analysis scripts are read from there)")
@@ -43,28 +45,34 @@ def _gains(md, title):
 
 
 def test_analyse_and_budget_accept_our_jsonl(tmp_path):
-    for f in ("scen_main.jsonl", "scen_stress.jsonl", "timing_1M.jsonl", "res_1M.jsonl"):
+    for f in ("scen_main.jsonl", "scen_holdout.jsonl", "scen_stress.jsonl", "timing_43k.jsonl", "timing_1M.jsonl", "res_1M.jsonl"):
         shutil.copy(os.path.join(CLI, f), tmp_path / f)
     md = _analyse(tmp_path)
-    assert "## Scene principale" in md and "## Scene stress" in md
+    assert "## Scene principale" in md and "## Scene stress" in md and "## " + HOLDOUT in md
+    assert "Temps GPU par image (timing_43k.jsonl, 43526 points, NVIDIA GB300)" in md
     assert "Temps GPU par image (timing_1M.jsonl, 1082802 points, NVIDIA GB300)" in md
     assert "VRAM : contexte" in md
-    r = subprocess.run([sys.executable, os.path.join(SCRIPTS, "budget.py"), str(tmp_path / "timing_1M.jsonl")], capture_output=True,
-                       text=True, timeout=60)
-    assert r.returncode == 0, r.stderr
-    assert 1.0 <= float(r.stdout.strip()) <= 4.0
+    for t in ("timing_43k.jsonl", "timing_1M.jsonl"):
+        r = subprocess.run([sys.executable, os.path.join(SCRIPTS, "budget.py"), str(tmp_path / t)], capture_output=True,
+                           text=True, timeout=60)
+        assert r.returncode == 0, r.stderr
+        assert 1.0 <= float(r.stdout.strip()) <= 4.0, t
 
 
-def test_run_cuda_scenf_output_reads(tmp_path):
-    """run_cuda.sh's own scenf command on scene_main (scenarios_main.txt, 10 seeds)."""
-    shutil.copy(os.path.join(CLI, "scenf_main.jsonl"), tmp_path / "scen_main.jsonl")
+@pytest.mark.parametrize("ours,theirs,title", [("scenf_main.jsonl", "scen_main.jsonl", "Scene principale"),
+                                               ("scenf_holdout.jsonl", "scen_holdout.jsonl", HOLDOUT)])
+def test_run_cuda_scenf_output_reads(tmp_path, ours, theirs, title):
+    """run_cuda.sh's own scenf commands on scene_main and scene_holdout (scenarios_main.txt, 10
+    seeds), under the file names run_cuda.sh gives them."""
+    shutil.copy(os.path.join(CLI, ours), tmp_path / theirs)
     md = _analyse(tmp_path)
-    g = _gains(md, "Scene principale")
+    g = _gains(md, title)
     assert "v4-A2C memoire verifiee+rampe" in g and all(x > 0 for v in g.values() for x in v)
 
 
 @pytest.mark.parametrize("name,title", [("scen_main.jsonl", "Scene principale"),
-                                        ("scen_stress.jsonl", "Scene stress (8 lampes, mur mobile, boites)")])
+                                        ("scen_stress.jsonl", "Scene stress (8 lampes, mur mobile, boites)"),
+                                        ("scen_holdout.jsonl", HOLDOUT)])
 def test_gains_match_the_published_ones(tmp_path, name, title):
     if not os.path.exists(os.path.join(PUBLISHED, name)):
         pytest.skip("published results absent")

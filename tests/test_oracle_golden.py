@@ -1,8 +1,9 @@
 """The CPU oracle against the reference's published golden error curves.
 
 The reference ships, for its box scenes, the per-frame error curves that its own binary
-printed on an RTX 4060 (reference/cuda_rtx4060/scen_main.jsonl and scen_stress.jsonl, means
-over 10 seeds, 5 decimals).  The oracle restates the reference in C; it must reproduce those
+printed on an RTX 4060 (reference/cuda_rtx4060/scen_main.jsonl, scen_stress.jsonl and, for the
+validation scene scene_holdout the reference never tuned on, scen_holdout.jsonl; means over 10
+seeds, 5 decimals).  The oracle restates the reference in C; it must reproduce those
 curves.  The only differences allowed are those of the C library's cosf/sinf/rsqrt against
 CUDA's (a few ulp on ray directions), which move the 10-seed means by less than 2e-3
 relative.
@@ -60,6 +61,23 @@ def test_oracle_matches_rtx4060_curves_main(main_run, golden_main, scen, method)
     last = gold["last"]
     post = ours[last:last + 30].mean()
     assert abs(post - gold["post"]) / gold["post"] < TOL
+
+
+@pytest.mark.parametrize("scen,method", [("R1 allumee-eteinte-rallumee", "v4-A2C memoire verifiee+rampe"),
+                                         ("I4 boite", "v5-AB instantanes+projection")])
+def test_oracle_matches_rtx4060_curves_holdout(scene_holdout_bytes, golden_holdout, scen, method):
+    sc = po.Scene(data=scene_holdout_bytes)
+    sc.build()
+    run = po.Run(sc)
+    seq = M.sequence(dict(M.SCEN_SCENARIOS)[scen])
+    m = M.by_name(M.scen_methods(), method)
+    gold = [r for r in golden_holdout["rows"] if r["scen"] == scen and r["name"] == method][0]
+    ours = _curve(run, m, seq, golden_holdout["seed0"], golden_holdout["nseeds"])
+    g = np.asarray(gold["curve"])
+    rel = np.abs(ours - g) / np.maximum(g, 1e-6)
+    assert rel.max() < TOL, (scen, method, rel.max())
+    last = gold["last"]
+    assert abs(ours[last:last + 30].mean() - gold["post"]) / gold["post"] < TOL
 
 
 def _stress_scenarios():
