@@ -28,21 +28,35 @@ def _published(name):
     return {(r["scen"], r["name"]): r for r in g["rows"]}
 
 
-def _printed(name):
+def scen_rows(lines):
+    """{(scenario, method): row} of the `scen` lines of a JSONL text."""
     rows = {}
-    with open(os.path.join(GOLDEN, "cli", name)) as f:
-        for line in f:
+    for line in lines:
+        if line.startswith("{"):
             r = json.loads(line)
             if r.get("type") == "scen":
                 rows[(r["scen"], r["name"])] = r
     return rows
 
 
-@pytest.mark.parametrize("printed,published,count", [("scen_main.jsonl", "golden_scen_main.json", 126),
-                                                     ("scen_stress.jsonl", "golden_scen_stress.json", 112),
-                                                     ("scen_holdout.jsonl", "golden_scen_holdout.json", 126)])
+def _printed(name):
+    with open(os.path.join(GOLDEN, "cli", name)) as f:
+        return scen_rows(f)
+
+
+CASES = [("scen_main.jsonl", "golden_scen_main.json", 126), ("scen_stress.jsonl", "golden_scen_stress.json", 112),
+         ("scen_holdout.jsonl", "golden_scen_holdout.json", 126)]
+
+
+@pytest.mark.parametrize("printed,published,count", CASES)
 def test_every_printed_curve_matches_the_published_one(printed, published, count):
-    ours, theirs = _printed(printed), _published(published)
+    assert_curves_match(_printed(printed), published, count, printed)
+
+
+def assert_curves_match(ours, published, count, label):
+    """Every published (scenario, method) curve of `published` is in `ours`, frame for frame
+    within TOL relative, with the same `last` frame and pre/post means."""
+    theirs = _published(published)
     assert len(theirs) == count
     assert set(ours) == set(theirs)
     worst = 0.0
@@ -56,7 +70,7 @@ def test_every_printed_curve_matches_the_published_one(printed, published, count
         assert r["last"] == g["last"], k
         for key in ("pre", "post"):
             assert abs(r[key] - g[key]) <= TOL * max(abs(g[key]), 1e-3) + 1e-5, (k, key, r[key], g[key])
-    print("%s: %d curves, worst relative difference %.2e" % (printed, len(theirs), worst))
+    print("%s: %d curves, worst relative difference %.2e" % (label, len(theirs), worst))
 
 
 def test_scene_line_names_the_gpu():
