@@ -35,6 +35,11 @@ R scen_holdout.jsonl $B/poc_gpu_l3 scen $T/scene_holdout.bin 10
 # the timing scenes
 R scenf_main.jsonl $B/poc_gpu_l3 scenf $T/scene_main.bin 10 $G/scenarios_main.txt
 R scenf_holdout.jsonl $B/poc_gpu_l3 scenf $T/scene_holdout.bin 10 $G/scenarios_main.txt
+# the modes the reference publishes nothing for, with the commands of
+# tests/golden/make_ref_main_fixtures.sh (which runs the reference's own binary)
+R quality_main.jsonl $B/poc_gpu_l3 quality $T/scene_main.bin 4 1,1.5
+R recon_main.jsonl $B/poc_gpu_l3 recon $T/scene_main.bin 4
+R taa_main.jsonl $B/poc_gpu_l3 taa $T/scene_main.bin 10 $G/scenarios_main.txt
 R timing_43k.jsonl $B/poc_gpu_l3 timing $T/scene_scale_43k.bin
 R timing_1M.jsonl $B/poc_gpu_l3 timing $T/scene_scale_1M.bin
 R res_1M.jsonl $B/poc_gpu_l3 res $T/scene_scale_1M.bin

@@ -1,0 +1,118 @@
+"""The drop-in binary against the reference's own binary, for the modes the reference publishes
+no output of.
+
+tests/golden/ref_main/ holds what the reference's `poc_gpu_l3` (cuda/poc_gpu.cu, unmodified,
+built with build.sh's flags on a GB300 by tests/golden/make_ref_main_fixtures.sh) printed for
+`quality scene_main.bin 4 1,1.5` (75 methods x 4 events: the accumulation, SHaRC and DDGI
+variants of methods_quality, poc_gpu.cu:1019-1045), `recon scene_main.bin 4` (per-seed curves and
+the bias / variance split by reference-change category, :1489-1548), `taa scene_main.bin 10
+scenarios_main.txt` (the screen-space TAA variants, :1047-1282) and run_cuda.sh's two `scenf`
+lines (scene_main and scene_holdout, scenarios_main.txt, 10 seeds).  tests/golden/cli/ holds what
+this repository's `poc_gpu_l3` printed for the same commands on a GB300
+(tests/golden/make_cli_fixtures.sh).  Every row must be there on both sides and agree: curves and
+pre/post means within 1e-3 relative (3e-3 for the DDGI rows of `quality`), the same `last` frame,
+the recon statistics as far as the reference's own float-atomic sums let two of its runs agree.
+On the GB300 the worst differences were 8.7e-4 (one DDGI row; 2.1e-4 for every other quality
+row), 2.9e-4 (recon curves), 0 (taa: identical) and 3.3e-4 / 1.3e-4 (scenf)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+REF_MAIN = os.path.join(GOLDEN, "ref_main")
+TOL = 1e-3
+
+
+def rows(lines, kind, key):
+    """{key(row): row} of the JSON lines of type `kind`."""
+    out = {}
+    for line in lines:
+        if line.startswith("{"):
+            r = json.loads(line)
+            if r.get("type") == kind:
+                k = key(r)
+                assert k not in out, k
+                out[k] = r
+    return out
+
+
+def _close(a, b, tol=TOL, floor=1e-6):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    assert a.shape == b.shape
+    return float((np.abs(a - b) / np.maximum(np.abs(b), floor)).max()) if a.size else 0.0
+
+
+def compare(mode, ours_lines, ref_lines):
+    """Asserts that the lines our binary printed for `mode` match the reference binary's; returns
+    (rows compared, worst relative difference of the curves or means)."""
+    worst = 0.0
+    if mode in ("scenf", "taa"):
+        kind = "scen" if mode == "scenf" else "taa"
+        a, b = rows(ours_lines, kind, lambda r: (r["scen"], r["name"])), rows(ref_lines, kind, lambda r: (r["scen"], r["name"]))
+        assert set(a) == set(b) and b
+        for k in b:
+            w = _close(a[k]["curve"], b[k]["curve"])
+            assert w < TOL, (k, w)
+            assert a[k]["last"] == b[k]["last"], k
+            for m in ("pre", "post"):
+                assert abs(a[k][m] - b[k][m]) <= TOL * abs(b[k][m]) + 1e-5, (k, m, a[k][m], b[k][m])
+            worst = max(worst, w)
+    elif mode == "quality":
+        key = lambda r: (r["name"], round(r["budget"], 3), r["event"])
+        a, b = rows(ours_lines, "quality", key), rows(ref_lines, "quality", key)
+        assert set(a) == set(b) and b
+        for k in b:
+            # DDGI's region irradiance sums are float atomics in the reference (k_trace2's dstat),
+            # added in an undefined order: its 4-seed means move by up to about 1e-3 between runs
+            tol = 3 * TOL if k[0].startswith("DDGI") else TOL
+            for m in ("pre", "post"):
+                w = abs(a[k][m] - b[k][m]) / max(abs(b[k][m]), 1e-3)
+                assert abs(a[k][m] - b[k][m]) <= tol * abs(b[k][m]) + 1e-5, (k, m, a[k][m], b[k][m])
+                worst = max(worst, w)
+    elif mode == "recon":
+        key = lambda r: (r["name"], r["event"])
+        a, b = rows(ours_lines, "recon_seeds", key), rows(ref_lines, "recon_seeds", key)
+        assert set(a) == set(b) and b
+        for k in b:
+            w = _close(a[k]["curves"], b[k]["curves"])
+            assert w < TOL, (k, w)
+            worst = max(worst, w)
+        a, b = rows(ours_lines, "recon_bv", key), rows(ref_lines, "recon_bv", key)
+        assert set(a) == set(b) and b
+        for k in b:
+            assert a[k]["f0"] == b[k]["f0"]
+            assert a[k]["mref"] == pytest.approx(b[k]["mref"], rel=1e-5)
+            for ca, cb in zip(a[k]["cats"], b[k]["cats"]):
+                assert ca["n"] == cb["n"], k
+                # bias^2 and the variance come from per-point float sums over the seeds
+                assert np.allclose(ca["bias2"], cb["bias2"], rtol=2e-3, atol=1e-9), k
+                assert np.allclose(ca["var"], cb["var"], rtol=2e-2, atol=1e-7), k
+    else:
+        raise ValueError(mode)
+    return len(b), worst
+
+
+CASES = [("quality", "quality_main.jsonl"), ("recon", "recon_main.jsonl"), ("taa", "taa_main.jsonl"),
+         ("scenf", "scenf_main.jsonl"), ("scenf", "scenf_holdout.jsonl")]
+
+
+def _lines(path):
+    with open(path) as f:
+        return f.read().splitlines()
+
+
+@pytest.mark.parametrize("mode,name", CASES)
+def test_drop_in_output_matches_the_reference_binary(mode, name):
+    ref = os.path.join(REF_MAIN, name)
+    ours = os.path.join(GOLDEN, "cli", name)
+    n, worst = compare(mode, _lines(ours), _lines(ref))
+    print("%s: %d rows, worst relative difference %.2e" % (name, n, worst))
+
+
+def test_reference_binary_fixtures_name_the_gpu():
+    for _, name in CASES:
+        head = json.loads(_lines(os.path.join(REF_MAIN, name))[0])
+        assert head["type"] == "scene" and head["np"] == 10728 and "GB300" in head["gpu"], name
