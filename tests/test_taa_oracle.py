@@ -1,14 +1,23 @@
 """The taa mode's CPU restatement (oracle/rc_oracle.c, run_taa_mode of poc_gpu.cu:1175-1282).
 
-The reference ships no taa outputs, so the mode's parity is pinned on the GPU against the
-reference's own k_taa_* kernels (tests/test_gpu_taa.py); here the restatement's own invariants:
-reproducible runs, history bounds, the reactive mask sources, and that every mask helps after
-an event on the golden scene.
+The reference publishes no taa outputs.  Its own binary's, printed on a GB300
+(tests/golden/ref_main/taa_main.jsonl: `poc_gpu_l3 taa scene_main.bin 10 scenarios_main.txt`,
+made by tests/golden/make_ref_main_fixtures.sh), pin the restatement: its 10-seed error curves
+must match to 2e-4 relative (the printed 5 decimals and the C library's cosf/sinf against
+CUDA's).  On the GPU the library's taa kernels are pinned against the reference's own k_taa_*
+kernels (tests/test_gpu_taa.py).  Here also the restatement's own invariants: reproducible runs,
+history bounds, the reactive mask sources, and that every mask helps after an event on the
+golden scene.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
 from oracle import pyoracle as po
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.fixture(scope="module")
@@ -67,3 +76,41 @@ def test_history_within_clamp(taa):
     H, mu, sg = taa.array(1), taa.array(2), taa.array(3)
     x = taa.array(0)
     assert (H >= np.minimum(mu - sg, x) - 1e-4).all() and (H <= np.maximum(mu + sg, x) + 1e-4).all()
+
+
+# run_taa_mode's methods (poc_gpu.cu:1219-1228): name -> (alpha, gamma, mask)
+TAA_METHODS = {"TAA borne alpha=0.05": (0.05, 1.0, 0), "TAA simple alpha=0.10 (sans bornage)": (0.1, 0.0, 0),
+               "TAA + detection aveugle": (0.1, 1.0, 1), "TAA + masque dependances verifie": (0.1, 1.0, 3),
+               "TAA + masque oracle": (0.1, 1.0, 4)}
+
+
+@pytest.mark.parametrize("scen,method", [("R1 allumee-eteinte-rallumee", "TAA + masque dependances verifie"),
+                                         ("I4 boite", "TAA borne alpha=0.05"),
+                                         ("R2 allumee-eteinte-porte-rallumee", "TAA + detection aveugle"),
+                                         ("I2 porte", "TAA simple alpha=0.10 (sans bornage)"),
+                                         ("I1 lampe eteinte", "TAA + masque oracle")])
+def test_matches_the_reference_binary(taa, scen, method):
+    gold = None
+    with open(os.path.join(GOLDEN, "ref_main", "taa_main.jsonl")) as f:
+        for line in f:
+            r = json.loads(line)
+            if r.get("type") == "taa" and r["scen"] == scen and r["name"] == method:
+                gold = r
+    parts = None
+    with open(os.path.join(GOLDEN, "scenarios_main.txt")) as f:
+        for line in f:
+            name, rest = line.strip().split(";", 1)
+            if name == scen:
+                parts = [tuple(int(x) for x in t.split(":")) for t in rest.split(",")]
+    seq = [s for s, n in parts for _ in range(n)]
+    alpha, gamma, mask = TAA_METHODS[method]
+    curve = np.zeros(len(seq))
+    for sd in range(10):                     # the reference's seeds 5000 + sd, 10 seeds
+        taa.begin(alpha, gamma, mask, seq[0], 5000 + sd)
+        for f, s in enumerate(seq):
+            curve[f] += taa.frame(s)[0] / 10
+    g = np.asarray(gold["curve"])
+    rel = np.abs(curve - g) / g
+    assert rel.max() < 2e-4, (scen, method, rel.max())
+    last = gold["last"]
+    assert abs(curve[last:last + 30].mean() - gold["post"]) <= 2e-4 * gold["post"] + 1e-5
