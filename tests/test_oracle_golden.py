@@ -149,3 +149,26 @@ def test_oracle_matches_the_reference_binary_quality(main_run, name, budget, eve
         post += er[50:80].mean() / 4
     assert abs(pre - gold["pre"]) <= TOL * gold["pre"] + 1e-5, (pre, gold["pre"])
     assert abs(post - gold["post"]) <= TOL * gold["post"] + 1e-5, (post, gold["post"])
+
+
+def test_oracle_matches_the_reference_binary_recon_curves(main_run):
+    """`recon scene_main.bin 4` (poc_gpu.cu:1489-1512): every per-seed error curve of its four
+    methods over the four events, seeds 1000 + sd, single runs rather than means (worst 5.2e-4)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_main", "recon_main.jsonl")
+    gold = {}
+    with open(path) as f:
+        for line in f:
+            r = json.loads(line)
+            if r.get("type") == "recon_seeds":
+                gold[(r["name"], r["event"])] = np.asarray(r["curves"])
+    checked = 0
+    for m in M.recon_methods():
+        for e in range(4):
+            seq = [e] * 50 + [e + 1] * 50
+            g = gold[(m.name, e)]
+            for sd in range(len(g)):
+                er = np.asarray(main_run.run(m, seq, 1000 + sd))
+                rel = np.abs(er - g[sd]) / np.maximum(g[sd], 1e-6)
+                assert rel.max() < TOL, (m.name, e, sd, rel.max())
+                checked += 1
+    assert checked == 4 * 4 * 4
