@@ -16,7 +16,7 @@ The network's inputs per point are its position and normal in the state's geomet
 (albedo, direct light of lights 0..2) of that state, each light's direct light divided by a
 constant, so a light switched off reaches the network through its input at once.  The value the cache serves (and whose error is measured) is the
 network's output of step 1.  There is no counterpart in the reference: its bench A calls the
-closed NRC library; this cache is judged against the reference's own per-point cache methods.
+closed NRC library; this cache is compared with the reference's own per-point cache methods.
 """
 from __future__ import annotations
 

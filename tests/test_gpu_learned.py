@@ -7,7 +7,7 @@ scene_main (10,728 points, 3 lights, converged references stored in the file):
   frame loop without it (the uncached one-bounce estimate, where the light beyond the first
   hit is missing), before and after a light is switched off;
 * against the per-point cache (the reference's Classique 1.0x, the hash-grid-style cache the
-  learned one is judged by): near it before the event, and its 30-frame post-event error far
+  learned one is compared with): near it before the event, and its 30-frame post-event error far
   below it (the switched-off light reaches the network through its direct-light input);
 * loss scaling: a step whose gradient is not finite is skipped (weights untouched) and the scale
   halved."""
