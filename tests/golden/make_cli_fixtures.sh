@@ -40,6 +40,9 @@ R scenf_holdout.jsonl $B/poc_gpu_l3 scenf $T/scene_holdout.bin 10 $G/scenarios_m
 R quality_main.jsonl $B/poc_gpu_l3 quality $T/scene_main.bin 4 1,1.5
 R recon_main.jsonl $B/poc_gpu_l3 recon $T/scene_main.bin 4
 R taa_main.jsonl $B/poc_gpu_l3 taa $T/scene_main.bin 10 $G/scenarios_main.txt
+R quality_stress.jsonl $B/poc_gpu_l8 quality $T/scene_stress.bin 4 1,1.5
+R recon_stress.jsonl $B/poc_gpu_l8 recon $T/scene_stress.bin 4
+R taa_stress.jsonl $B/poc_gpu_l8 taa $T/scene_stress.bin 10 $G/scenarios_stress.txt
 R timing_43k.jsonl $B/poc_gpu_l3 timing $T/scene_scale_43k.bin
 R timing_1M.jsonl $B/poc_gpu_l3 timing $T/scene_scale_1M.bin
 R res_1M.jsonl $B/poc_gpu_l3 res $T/scene_scale_1M.bin

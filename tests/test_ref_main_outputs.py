@@ -7,13 +7,16 @@ built with build.sh's flags on a GB300 by tests/golden/make_ref_main_fixtures.sh
 variants of methods_quality, poc_gpu.cu:1019-1045), `recon scene_main.bin 4` (per-seed curves and
 the bias / variance split by reference-change category, :1489-1548), `taa scene_main.bin 10
 scenarios_main.txt` (the screen-space TAA variants, :1047-1282) and run_cuda.sh's two `scenf`
-lines (scene_main and scene_holdout, scenarios_main.txt, 10 seeds).  tests/golden/cli/ holds what
-this repository's `poc_gpu_l3` printed for the same commands on a GB300
+lines (scene_main and scene_holdout, scenarios_main.txt, 10 seeds), and what its `poc_gpu_l8`
+printed for `quality`, `recon` and `taa` (scenarios_stress.txt) on the 8-light scene_stress.
+tests/golden/cli/ holds what this repository's `poc_gpu_l3` / `poc_gpu_l8` printed for the same
+commands on a GB300
 (tests/golden/make_cli_fixtures.sh).  Every row must be there on both sides and agree: curves and
 pre/post means within 1e-3 relative (3e-3 for the DDGI rows of `quality`), the same `last` frame,
 the recon statistics as far as the reference's own float-atomic sums let two of its runs agree.
 On the GB300 the worst differences were 8.7e-4 (one DDGI row; 2.1e-4 for every other quality
-row), 2.9e-4 (recon curves), 0 (taa: identical) and 3.3e-4 / 1.3e-4 (scenf)."""
+row), 2.9e-4 (recon curves), 0 (taa: identical) and 3.3e-4 / 1.3e-4 (scenf) with 3 lights, and
+2.2e-4 (quality, 375 rows), 4.5e-4 (recon) and 0 (taa) with 8."""
 import json
 import os
 
@@ -96,7 +99,8 @@ def compare(mode, ours_lines, ref_lines):
 
 
 CASES = [("quality", "quality_main.jsonl"), ("recon", "recon_main.jsonl"), ("taa", "taa_main.jsonl"),
-         ("scenf", "scenf_main.jsonl"), ("scenf", "scenf_holdout.jsonl")]
+         ("scenf", "scenf_main.jsonl"), ("scenf", "scenf_holdout.jsonl"),
+         ("quality", "quality_stress.jsonl"), ("recon", "recon_stress.jsonl"), ("taa", "taa_stress.jsonl")]
 
 
 def _lines(path):
@@ -115,4 +119,4 @@ def test_drop_in_output_matches_the_reference_binary(mode, name):
 def test_reference_binary_fixtures_name_the_gpu():
     for _, name in CASES:
         head = json.loads(_lines(os.path.join(REF_MAIN, name))[0])
-        assert head["type"] == "scene" and head["np"] == 10728 and "GB300" in head["gpu"], name
+        assert head["type"] == "scene" and head["np"] == (11268 if "stress" in name else 10728) and "GB300" in head["gpu"], name
