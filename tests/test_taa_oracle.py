@@ -79,9 +79,44 @@ def test_history_within_clamp(taa):
 
 
 # run_taa_mode's methods (poc_gpu.cu:1219-1228): name -> (alpha, gamma, mask)
-TAA_METHODS = {"TAA borne alpha=0.05": (0.05, 1.0, 0), "TAA simple alpha=0.10 (sans bornage)": (0.1, 0.0, 0),
-               "TAA + detection aveugle": (0.1, 1.0, 1), "TAA + masque dependances verifie": (0.1, 1.0, 3),
+TAA_METHODS = {"TAA borne alpha=0.05": (0.05, 1.0, 0), "TAA borne alpha=0.20": (0.2, 1.0, 0),
+               "TAA simple alpha=0.10 (sans bornage)": (0.1, 0.0, 0), "TAA + detection aveugle": (0.1, 1.0, 1),
+               "TAA + masque dependances": (0.1, 1.0, 2), "TAA + masque dependances verifie": (0.1, 1.0, 3),
                "TAA + masque oracle": (0.1, 1.0, 4)}
+
+
+@pytest.fixture(scope="module")
+def taa_stress(scene_stress_bytes):
+    return po.Taa(po.Scene(data=scene_stress_bytes))
+
+
+def _reference_curve(fixture, scenarios, scen, method):
+    gold = None
+    with open(os.path.join(GOLDEN, "ref_main", fixture)) as f:
+        for line in f:
+            r = json.loads(line)
+            if r.get("type") == "taa" and r["scen"] == scen and r["name"] == method:
+                gold = r
+    parts = None
+    with open(os.path.join(GOLDEN, scenarios)) as f:
+        for line in f:
+            line = line.strip()
+            if not line or line.startswith("#"):
+                continue
+            name, rest = line.split(";", 1)
+            if name == scen:
+                parts = [tuple(int(x) for x in t.split(":")) for t in rest.split(",")]
+    return gold, parts
+
+
+@pytest.mark.parametrize("scen,method", [("L2 quatre lampes eteintes puis rallumees", "TAA + masque dependances verifie"),
+                                         ("G3 quatre objets deplaces", "TAA + masque dependances"),
+                                         ("M1 extinction, mur effondre dans le noir, rallumage", "TAA borne alpha=0.20")])
+def test_matches_the_reference_binary_8_lights(taa_stress, scen, method):
+    """The same against the reference's poc_gpu_l8 on the 8-light scene_stress
+    (tests/golden/ref_main/taa_stress.jsonl, scenarios_stress.txt)."""
+    gold, parts = _reference_curve("taa_stress.jsonl", "scenarios_stress.txt", scen, method)
+    _check(taa_stress, gold, parts, method)
 
 
 @pytest.mark.parametrize("scen,method", [("R1 allumee-eteinte-rallumee", "TAA + masque dependances verifie"),
@@ -90,18 +125,11 @@ TAA_METHODS = {"TAA borne alpha=0.05": (0.05, 1.0, 0), "TAA simple alpha=0.10 (s
                                          ("I2 porte", "TAA simple alpha=0.10 (sans bornage)"),
                                          ("I1 lampe eteinte", "TAA + masque oracle")])
 def test_matches_the_reference_binary(taa, scen, method):
-    gold = None
-    with open(os.path.join(GOLDEN, "ref_main", "taa_main.jsonl")) as f:
-        for line in f:
-            r = json.loads(line)
-            if r.get("type") == "taa" and r["scen"] == scen and r["name"] == method:
-                gold = r
-    parts = None
-    with open(os.path.join(GOLDEN, "scenarios_main.txt")) as f:
-        for line in f:
-            name, rest = line.strip().split(";", 1)
-            if name == scen:
-                parts = [tuple(int(x) for x in t.split(":")) for t in rest.split(",")]
+    gold, parts = _reference_curve("taa_main.jsonl", "scenarios_main.txt", scen, method)
+    _check(taa, gold, parts, method)
+
+
+def _check(taa, gold, parts, method):
     seq = [s for s, n in parts for _ in range(n)]
     alpha, gamma, mask = TAA_METHODS[method]
     curve = np.zeros(len(seq))
@@ -111,6 +139,6 @@ def test_matches_the_reference_binary(taa, scen, method):
             curve[f] += taa.frame(s)[0] / 10
     g = np.asarray(gold["curve"])
     rel = np.abs(curve - g) / g
-    assert rel.max() < 2e-4, (scen, method, rel.max())
+    assert rel.max() < 2e-4, (method, rel.max())
     last = gold["last"]
     assert abs(curve[last:last + 30].mean() - gold["post"]) <= 2e-4 * gold["post"] + 1e-5
