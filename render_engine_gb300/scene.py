@@ -17,7 +17,6 @@ them on the transit grid directly.
 from __future__ import annotations
 
 import io
-import struct
 from dataclasses import dataclass, field
 
 import numpy as np

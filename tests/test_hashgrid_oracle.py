@@ -6,7 +6,6 @@ Known answers worked by hand from the HLSL of windows/patch/rtxgi_bench.patch
 BenchObjVoxels / BenchSnap), and numpy's float16 as the independent check of the fp16
 rounding.  No GPU needed."""
 import numpy as np
-import pytest
 
 from oracle import pyhg
 from render_engine_gb300 import hashgrid as H
