@@ -1280,7 +1280,7 @@ rc_status taa_alloc(rc_ctx* ctx) {
             v.erase(std::unique(v.begin(), v.end()), v.end());
             t.nV[(size_t)a * NS + b] = (int)v.size();
             const int* dv = nullptr;
-            if ((s = dput(ctx, pool, &dv, v.empty() ? std::vector<int>{0} : v))) return s;
+            if ((s = dput(ctx, pool, &dv, v.empty() ? std::vector<int>{0} : v)) != RC_OK) return s;
             t.dV[(size_t)a * NS + b] = dv;
         }
     return RC_OK;
@@ -1370,7 +1370,7 @@ rc_status rc_device_info_get(rc_ctx* ctx, rc_device_info* out) {
     cudaDeviceProp pr;
     CKR(cudaGetDeviceProperties(&pr, ctx->cfg.device));
     memset(out, 0, sizeof *out);
-    strncpy(out->name, pr.name, sizeof out->name - 1);
+    snprintf(out->name, sizeof out->name, "%s", pr.name);
     out->sm_count = pr.multiProcessorCount;
     out->cc_major = pr.major;
     out->cc_minor = pr.minor;
