@@ -12,8 +12,11 @@ The quality mode's outputs are not published; the reference's own binary printed
 GB300 (tests/golden/ref_main/quality_main.jsonl: `poc_gpu_l3 quality scene_main.bin 4 1,1.5`, made
 by tests/golden/make_ref_main_fixtures.sh), and the oracle's 4-seed pre/post means must match
 them to 2e-3 on a sample of its rows across the method families.  Over all 300 rows 282 agree to
-1e-3; the rest are DDGI rows, up to 5.8e-3 with the 0.25 irradiance threshold, where the region
-sums the reference adds with float atomics decide the per-region threshold tests.
+1e-3.  The rest are DDGI rows, up to 5.8e-3 with the 0.25 threshold.  With one ray per point,
+a region's frame-to-frame relative change is about 1/sqrt(15) for its ~15 points, which is the
+threshold itself.  So the per-region test flips on the last-ulp differences of the C library's
+cosf/sinf against CUDA's, and the runs drift apart.  The GPU path uses CUDA's functions and
+stays within 2.1e-4 of the reference binary on those rows.
 """
 import json
 import os
